@@ -1,0 +1,247 @@
+"""ctypes binding to the oracle (test infrastructure only).
+
+The oracle is the FP64 CPU restatement of the reference's alignment path in
+oracle/*.cpp. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg use this module, as the checker; the product never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libsoft_ref.so")
+
+
+class OracleParams(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int), ("B", ctypes.c_int),
+        ("mask_x", ctypes.c_float), ("mask_y", ctypes.c_float), ("mask_z", ctypes.c_float),
+        ("mask_sigma", ctypes.c_float), ("square_mask_size", ctypes.c_float),
+        ("bp_low", ctypes.c_float), ("bp_high", ctypes.c_float),
+        ("bp_low_sigma", ctypes.c_float), ("bp_high_sigma", ctypes.c_float),
+        ("bfactor", ctypes.c_float),
+        ("restrict_translation", ctypes.c_float), ("restrict_rotation", ctypes.c_float),
+        ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
+        ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
+    ]
+
+
+class OracleVolume(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.POINTER(ctypes.c_float)), ("dims", ctypes.c_int * 3),
+        ("lwedge", ctypes.c_float), ("uwedge", ctypes.c_float),
+        ("normal", ctypes.c_float * 3), ("matrix", ctypes.c_double * 16),
+        ("position", ctypes.c_float * 3), ("cut_offset", ctypes.c_float),
+    ]
+
+
+class OracleResult(ctypes.Structure):
+    _fields_ = [
+        ("distance", ctypes.c_float), ("matrix", ctypes.c_double * 16),
+        ("n_candidates", ctypes.c_int), ("cand_distance", ctypes.c_float * 8),
+        ("cand_matrix", (ctypes.c_double * 16) * 8), ("n_ccf", ctypes.c_int),
+        ("n_peaks_q1", ctypes.c_int), ("n_peaks_q2", ctypes.c_int),
+        ("use_window1", ctypes.c_int), ("use_window2", ctypes.c_int),
+        ("best_cell", ctypes.c_int * 3),
+    ]
+
+
+def build():
+    """Compile the oracle library (and, when the reference tree is present, SOFT under _ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
+    if os.path.isdir(os.environ.get("ETTK_REFERENCE_ROOT", "/root/reference")):
+        subprocess.run([os.path.join(HERE, "build_ref.sh")], check=True,
+                       stdout=subprocess.DEVNULL)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+        fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+        P = ctypes.POINTER(OracleParams)
+        V = ctypes.POINTER(OracleVolume)
+        L.oracle_align.argtypes = [P, V, V, ctypes.POINTER(OracleResult)]
+        L.oracle_get_image.argtypes = [P, V, ctypes.c_void_p, dp]
+        L.oracle_spherical_projection.argtypes = [P, V, fp]
+        L.oracle_spherical_wedge.argtypes = [P, V, fp]
+        L.oracle_wedge_half.argtypes = [P, V, ctypes.c_void_p, fp]
+        L.oracle_masks.argtypes = [P, fp, fp, fp]
+        L.oracle_soft.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.oracle_soft_scaled.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.oracle_rotate.argtypes = [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
+        L.oracle_sht.argtypes = [ctypes.c_int, dp, dp]
+        L.oracle_ccf.argtypes = [P, V, V, dp]
+        L.oracle_ccf.restype = ctypes.c_float
+        L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
+        L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
+        _lib = L
+    return _lib
+
+
+def make_params(p):
+    """OracleParams from the alignment parameter dict used across the repo."""
+    return OracleParams(
+        N=p["N"], B=p["B"], mask_x=p["mask_radius"], mask_y=p["mask_radius"], mask_z=p["mask_radius"],
+        mask_sigma=p["mask_sigma"], square_mask_size=p["square_mask_size"],
+        bp_low=p["bp_low"], bp_high=p["bp_high"], bp_low_sigma=p["bp_low_sigma"],
+        bp_high_sigma=p["bp_high_sigma"], bfactor=p.get("bfactor", 0.0),
+        restrict_translation=p["restrict_translation"], restrict_rotation=p["restrict_rotation"],
+        candidate_peaks=p["candidate_peaks"], number_of_candidates=p["number_of_candidates"],
+        wedge_compensation=int(p["wedge_compensation"]), overlap_normalized=int(p["overlap_normalized"]))
+
+
+def make_volume(data, meta):
+    """OracleVolume for a fixed image `data` ([z][y][x] numpy, i.e. x fastest) and its metadata."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    v = OracleVolume()
+    v.data = data.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    v._keep = data
+    nz, ny, nx = data.shape
+    v.dims[:] = [nx, ny, nz]
+    v.lwedge, v.uwedge = meta["lwedge"], meta["uwedge"]
+    v.normal[:] = list(meta.get("normal", (0.0, 0.0, 0.0)))
+    v.matrix[:] = list(np.asarray(meta.get("matrix", np.eye(4)), dtype=np.float64).reshape(16))
+    v.position[:] = list(meta.get("position", (nx / 2.0, ny / 2.0, nz / 2.0)))
+    v.cut_offset = meta.get("cut_offset", 0.0)
+    return v
+
+
+def align(params, ref, ref_meta, part, part_meta):
+    P = make_params(params)
+    r = make_volume(ref, ref_meta)
+    q = make_volume(part, part_meta)
+    out = OracleResult()
+    lib().oracle_align(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), ctypes.byref(out))
+    return {
+        "distance": out.distance,
+        "matrix": np.array(out.matrix[:]).reshape(4, 4),
+        "n_ccf": out.n_ccf, "n_peaks_q1": out.n_peaks_q1, "n_peaks_q2": out.n_peaks_q2,
+        "use_window1": out.use_window1, "use_window2": out.use_window2,
+        "best_cell": tuple(out.best_cell[:]),
+        "cand_distance": list(out.cand_distance[:out.n_candidates]),
+    }
+
+
+def ccf(params, ref, ref_meta, part, part_meta, T):
+    P = make_params(params)
+    r = make_volume(ref, ref_meta)
+    q = make_volume(part, part_meta)
+    t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16)).copy()
+    d = lib().oracle_ccf(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t)
+    return float(d), t.reshape(4, 4)
+
+
+def get_image(params, vol, meta, T=None):
+    P = make_params(params)
+    v = make_volume(vol, meta)
+    N = params["N"]
+    out = np.zeros(N ** 3, dtype=np.float64)
+    t = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(16))
+    lib().oracle_get_image(ctypes.byref(P), ctypes.byref(v), None if t is None else t.ctypes.data, out)
+    return out.reshape(N, N, N)  # [x][y][z]
+
+
+def spherical_projection(params, vol, meta):
+    P = make_params(params)
+    v = make_volume(vol, meta)
+    n = 2 * params["B"]
+    out = np.zeros(n * n, dtype=np.float32)
+    lib().oracle_spherical_projection(ctypes.byref(P), ctypes.byref(v), out)
+    return out.reshape(n, n)
+
+
+def spherical_wedge(params, meta, N):
+    P = make_params(params)
+    v = make_volume(np.zeros((N, N, N), np.float32), meta)
+    n = 2 * params["B"]
+    out = np.zeros(n * n, dtype=np.float32)
+    lib().oracle_spherical_wedge(ctypes.byref(P), ctypes.byref(v), out)
+    return out.reshape(n, n)
+
+
+def wedge_half(params, meta, T=None):
+    N = params["N"]
+    P = make_params(params)
+    v = make_volume(np.zeros((N, N, N), np.float32), meta)
+    out = np.zeros(N * N * (N // 2 + 1), dtype=np.float32)
+    t = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(16))
+    lib().oracle_wedge_half(ctypes.byref(P), ctypes.byref(v), None if t is None else t.ctypes.data, out)
+    return out.reshape(N, N, N // 2 + 1)
+
+
+def masks(params):
+    N = params["N"]
+    P = make_params(params)
+    m = np.zeros(N ** 3, np.float32)
+    mf = np.zeros(N ** 3, np.float32)
+    f = np.zeros(N * N * (N // 2 + 1), np.float32)
+    lib().oracle_masks(ctypes.byref(P), m, mf, f)
+    return m.reshape(N, N, N), mf.reshape(N, N, N), f.reshape(N, N, N // 2 + 1)
+
+
+def soft(B, F1, F2, scaled=False):
+    n = 2 * B
+    C = np.zeros(n ** 3, np.float64)
+    fn = lib().oracle_soft_scaled if scaled else lib().oracle_soft
+    fn(B, np.ascontiguousarray(F1, np.float64), np.ascontiguousarray(F2, np.float64), C)
+    return C.reshape(n, n, n)
+
+
+def rotate(B, F, a, b, g):
+    n = 2 * B
+    R = np.zeros(n * n, np.float64)
+    lib().oracle_rotate(B, np.ascontiguousarray(F, np.float64), a, b, g, R)
+    return R.reshape(n, n)
+
+
+def sht(B, F):
+    out = np.zeros(B * 2 * B * 2, np.float64)
+    lib().oracle_sht(B, np.ascontiguousarray(F, np.float64), out)
+    c = out.reshape(B, 2 * B, 2)
+    return c[..., 0] + 1j * c[..., 1]
+
+
+def rfft3d(x):
+    x = np.ascontiguousarray(x, np.float64)
+    n0, n1, n2 = x.shape
+    out = np.zeros((n0, n1, n2 // 2 + 1, 2), np.float64)
+    lib().oracle_rfft3d(n0, n1, n2, x, out)
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def irfft3d(X, n2):
+    n0, n1, h = X.shape
+    inp = np.ascontiguousarray(np.stack([X.real, X.imag], -1), np.float64)
+    out = np.zeros((n0, n1, n2), np.float64)
+    lib().oracle_irfft3d(n0, n1, n2, inp, out)
+    return out
+
+
+# ---------------------------------------------------------------- SOFT reference library (this container only)
+
+_ref = None
+
+
+def ref_lib():
+    """The reference's SOFT 1.0 compiled from its own sources (None when absent)."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            return None
+        L = ctypes.CDLL(REF_PATH)
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+        L.ref_soft.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.ref_fst.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.ref_rotate.argtypes = [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
+        _ref = L
+    return _ref
