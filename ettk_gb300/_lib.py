@@ -1,0 +1,120 @@
+"""Build and load libettk_gpu.so (the CUDA implementation behind include/ettk_gpu.h).
+
+The library is built in-tree under ettk_gb300/_build for sm_103a. Loading fails loudly when
+it is missing: there is no CPU fallback for the alignment path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(BUILD, "libettk_gpu.so")
+SRC = os.path.join(PKG, "csrc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+ETTK_OK, ETTK_ERR_ARG, ETTK_ERR_OOM, ETTK_ERR_CUDA, ETTK_ERR_TIMEOUT, ETTK_ERR_NAN, ETTK_ERR_STATE = range(7)
+
+
+def build(verbose=False):
+    """Compile the CUDA library (nvcc, sm_103a). Returns the library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(SRC, "ettk_gpu.cu")]
+    deps = srcs + [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(ROOT, "include", "ettk_gpu.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    cmd = ["nvcc", *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-shared",
+           "-o", LIB + ".tmp", *srcs]
+    subprocess.run(cmd, check=True, stdout=None if verbose else subprocess.DEVNULL)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int), ("B", ctypes.c_int),
+        ("mask_radius", ctypes.c_float), ("mask_sigma", ctypes.c_float), ("square_mask_size", ctypes.c_float),
+        ("bp_low", ctypes.c_float), ("bp_high", ctypes.c_float),
+        ("bp_low_sigma", ctypes.c_float), ("bp_high_sigma", ctypes.c_float), ("bfactor", ctypes.c_float),
+        ("restrict_translation", ctypes.c_float), ("restrict_rotation", ctypes.c_float),
+        ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
+        ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
+        ("mutual_correlation", ctypes.c_int), ("max_batch", ctypes.c_int),
+    ]
+
+
+class VolumeMeta(ctypes.Structure):
+    _fields_ = [
+        ("lwedge", ctypes.c_float), ("uwedge", ctypes.c_float), ("normal", ctypes.c_float * 3),
+        ("matrix", ctypes.c_double * 16), ("position", ctypes.c_float * 3), ("cut_offset", ctypes.c_float),
+    ]
+
+
+SYMBOLS = [
+    "ettk_gpu_create", "ettk_gpu_destroy", "ettk_gpu_set_references", "ettk_gpu_set_particles",
+    "ettk_gpu_set_particles_device", "ettk_gpu_align_pairs", "ettk_gpu_ccf", "ettk_gpu_spherical_projection",
+    "ettk_gpu_soft", "ettk_gpu_kernel_launches", "ettk_gpu_last_error", "ettk_gpu_stream", "ettk_gpu_profile",
+    "ettk_gpu_profile_read",
+]
+
+_lib = None
+
+
+def load(path=None):
+    """Load the library (building it first when absent). Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        build()
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    P = ctypes.POINTER
+    L.ettk_gpu_create.argtypes = [ctypes.c_int, P(Params), P(vp)]
+    L.ettk_gpu_destroy.argtypes = [vp]
+    L.ettk_gpu_set_references.argtypes = [vp, ctypes.c_int, vp, P(VolumeMeta)]
+    L.ettk_gpu_set_particles.argtypes = [vp, ctypes.c_int, vp, P(VolumeMeta)]
+    L.ettk_gpu_set_particles_device.argtypes = [vp, ctypes.c_int, vp, P(VolumeMeta)]
+    L.ettk_gpu_align_pairs.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int]
+    L.ettk_gpu_ccf.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, P(ctypes.c_float)]
+    L.ettk_gpu_spherical_projection.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+    L.ettk_gpu_soft.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    L.ettk_gpu_kernel_launches.argtypes = [vp]
+    L.ettk_gpu_kernel_launches.restype = ctypes.c_longlong
+    L.ettk_gpu_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+    L.ettk_gpu_stream.argtypes = [vp]
+    L.ettk_gpu_stream.restype = ctypes.c_void_p
+    L.ettk_gpu_profile.argtypes = [vp, ctypes.c_int]
+    L.ettk_gpu_profile_read.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_longlong),
+                                        P(ctypes.c_double), P(ctypes.c_double)]
+    for name in SYMBOLS:
+        getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
+    _lib = L
+    return L
+
+
+def make_params(p):
+    return Params(
+        N=int(p["N"]), B=int(p["B"]), mask_radius=p["mask_radius"], mask_sigma=p["mask_sigma"],
+        square_mask_size=p["square_mask_size"], bp_low=p["bp_low"], bp_high=p["bp_high"],
+        bp_low_sigma=p["bp_low_sigma"], bp_high_sigma=p["bp_high_sigma"], bfactor=p.get("bfactor", 0.0),
+        restrict_translation=p["restrict_translation"], restrict_rotation=p["restrict_rotation"],
+        candidate_peaks=int(p["candidate_peaks"]), number_of_candidates=int(p["number_of_candidates"]),
+        wedge_compensation=int(bool(p["wedge_compensation"])), overlap_normalized=int(bool(p["overlap_normalized"])),
+        mutual_correlation=int(bool(p.get("mutual_correlation", False))), max_batch=int(p.get("max_batch", 0)))
+
+
+def make_meta(metas):
+    arr = (VolumeMeta * len(metas))()
+    for i, m in enumerate(metas):
+        v = arr[i]
+        v.lwedge, v.uwedge = m["lwedge"], m["uwedge"]
+        v.normal[:] = [float(x) for x in m.get("normal", (0.0, 0.0, 0.0))]
+        v.matrix[:] = [float(x) for x in np.asarray(m.get("matrix", np.eye(4)), np.float64).reshape(16)]
+        v.position[:] = [float(x) for x in m["position"]]
+        v.cut_offset = float(m.get("cut_offset", 0.0))
+    return arr

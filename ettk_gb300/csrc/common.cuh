@@ -1,0 +1,93 @@
+// Shared device helpers for the GB300 alignment kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cfloat>
+
+#define ETTK_DEV __device__ __forceinline__
+
+namespace ettk {
+
+ETTK_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+ETTK_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+ETTK_DEV float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+ETTK_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+ETTK_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+ETTK_DEV float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+
+// (-1)^(i+j+k): the reference's centring "shift" arrays (inc/em/nbfFourierFilter.h:307-319)
+ETTK_DEV float parity_sign(int i, int j, int k) { return ((i + j + k) & 1) ? -1.0f : 1.0f; }
+
+// Order-preserving map of a float to uint32 (for packed atomic max of (value, index)).
+ETTK_DEV uint32_t float_to_ordered(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+ETTK_DEV float ordered_to_float(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+// Larger value wins; on equal values the smaller index wins (first occurrence in scan order).
+ETTK_DEV unsigned long long pack_max(float v, uint32_t idx) {
+  return ((unsigned long long)float_to_ordered(v) << 32) | (unsigned long long)(0xffffffffu - idx);
+}
+ETTK_DEV unsigned long long pack_min(float v, uint32_t idx) {
+  // smaller value wins -> negate ordering; smaller index wins
+  return ((unsigned long long)(~float_to_ordered(v)) << 32) | (unsigned long long)(0xffffffffu - idx);
+}
+
+template <typename T>
+ETTK_DEV T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of a double; result valid in thread 0. `sh` needs blockDim/32 doubles.
+ETTK_DEV double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0;
+  if (w == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    r = (lane < nw) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+ETTK_DEV unsigned long long warp_max_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+    v = t > v ? t : v;
+  }
+  return v;
+}
+
+// vtkInterpolationMath::Floor (64-bit x86 branch): integer part of x + 2^-17 and the fraction
+// rounded to the 2^-16 grid that the reference's double arithmetic produces
+// (Filtering/vtkImageInterpolatorInternals.h:96-108). Computed from an FP32 coordinate.
+ETTK_DEV int vtk_floor(float x, float &f) {
+  float xt = x + 7.62939453125e-06f;
+  float fi = floorf(xt);
+  float fr = xt - fi;
+  fr = rintf(fr * 65536.0f) * (1.0f / 65536.0f);
+  if (fr >= 1.0f) {
+    fr -= 1.0f;
+    fi += 1.0f;
+  }
+  f = fr;
+  return (int)fi;
+}
+
+// Tricubic weights of vtkImageInterpolator (Filtering/vtkImageInterpolator.cxx:313-325).
+ETTK_DEV void cubic_weights(float F[4], float f) {
+  float fm1 = f - 1.0f, fd2 = f * 0.5f, ft3 = f * 3.0f;
+  F[0] = -fd2 * fm1 * fm1;
+  F[1] = ((ft3 - 2.0f) * fd2 - 1.0f) * fm1;
+  F[2] = -((ft3 - 4.0f) * f - 1.0f) * fd2;
+  F[3] = f * fd2 * fm1;
+}
+
+}  // namespace ettk

@@ -1,0 +1,1595 @@
+// libettk_gpu: GB300 implementation of ETTK's pairwise sub-volume alignment
+// (nbfProjectionRotationMetric3D<float>::execute, alignment_mode 3) behind the C ABI of
+// include/ettk_gpu.h. Host orchestration: batches of (reference, particle) pairs go through
+//   1. |FFT| spherical projection of each particle (cartesianToSpherical),
+//   2. SO(3) correlations on the GPU (S^2 transform, Wigner-d synthesis, alpha/gamma FFT,
+//      softScaled rescaling) and 3x3x3 local-maximum extraction,
+//   3. per-pair candidate queues on the host (getTrueLocalMaximaPositions,
+//      eliminateEquivalentAngles, the mirror test and its counting rule),
+//   4. batched translational CCF evaluations (executeFourierNewHalf) in rounds until every
+//      pair's queues are exhausted or have counted candidatePeaks peaks,
+//   5. final candidate selection (eliminateEquivalentAngles with tolerance 2.5).
+#include "../../include/ettk_gpu.h"
+#include "geometry.hpp"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <array>
+#include <map>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <queue>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace ettk;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+  int code;
+  CudaError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                     \
+  do {                                                                                            \
+    cudaError_t e_ = (x);                                                                         \
+    if (e_ != cudaSuccess)                                                                        \
+      throw CudaError(e_ == cudaErrorMemoryAllocation ? ETTK_ERR_OOM : ETTK_ERR_CUDA,             \
+                      std::string(#x) + ": " + cudaGetErrorString(e_));                           \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void ensure(size_t count) {
+    if (count <= n) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    CK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// Rotation search bookkeeping (TinyVector<float,4>: alpha, beta, gamma, value) with an index that
+// rides along without taking part in comparisons, so heap order matches the reference's
+// PriorityQueue<TinyVector<Pixel,4>, greaterPD> (inc/fm/nbfFastMarching.h:18-35).
+struct Cand {
+  float v[4];
+  int ref;  // eval slot of the direct CCF (combined list) or -1
+};
+struct GreaterPD {
+  bool operator()(const Cand &a, const Cand &b) const { return a.v[3] > b.v[3]; }
+};
+typedef std::priority_queue<Cand, std::vector<Cand>, GreaterPD> PQ;
+
+enum SigKind {
+  K_PP1, K_PP2, K_W1, K_W2, K_PP1SQ_W1, K_PP2SQ_W2, K_PP1_W1, K_PP2_W2, K_PP2SQ, K_W1_PP1, K_PP1SQ, K_W2_PP2
+};
+
+struct SigDesc {
+  int pair, kind;
+};
+
+// per-pair signal assembly: Pp normalised by the common maximum (execute, 468-470), then the float
+// products the reference forms before each soft call (526-584).
+__global__ void k_build_signals(const SigDesc *__restrict__ sd, const int *__restrict__ pair_ref,
+                                const int *__restrict__ pair_pp2, const float *__restrict__ Pp1,
+                                const float *__restrict__ Pp2, const float *__restrict__ W1, const float *__restrict__ W2,
+                                const int *__restrict__ pair_part, int nn, float *__restrict__ out) {
+  __shared__ float smax[2][32];
+  const SigDesc d = sd[blockIdx.x];
+  const float *p1 = Pp1 + (long)pair_ref[d.pair] * nn;
+  const float *p2 = Pp2 + (long)pair_pp2[d.pair] * nn;
+  const float *w1 = W1 + (long)pair_ref[d.pair] * nn;
+  const float *w2 = W2 + (long)pair_part[d.pair] * nn;
+  float m1 = -FLT_MAX, m2 = -FLT_MAX;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+    m1 = fmaxf(m1, p1[i]);
+    m2 = fmaxf(m2, p2[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    smax[0][threadIdx.x >> 5] = m1;
+    smax[1][threadIdx.x >> 5] = m2;
+  }
+  __syncthreads();
+  float M = -FLT_MAX;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) M = fmaxf(M, fmaxf(smax[0][w], smax[1][w]));
+  float *o = out + (long)blockIdx.x * nn;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+    float a = p1[i] / M, b = p2[i] / M, wa = w1[i], wb = w2[i], v;
+    switch (d.kind) {
+      case K_PP1: v = a; break;
+      case K_PP2: v = b; break;
+      case K_W1: v = wa; break;
+      case K_W2: v = wb; break;
+      case K_PP1SQ_W1: v = a * a * wa; break;
+      case K_PP2SQ_W2: v = b * b * wb; break;
+      case K_PP1_W1: v = a * wa; break;
+      case K_PP2_W2: v = b * wb; break;
+      case K_PP2SQ: v = b * b; break;
+      case K_W1_PP1: v = wa * a; break;
+      case K_PP1SQ: v = a * a; break;
+      default: v = wb * b; break;
+    }
+    o[i] = v;
+  }
+}
+
+// softScaled rescale + branch combination + beta restriction (execute 526-602):
+// out[pair] = combination of the pair's correlation jobs; slot 4 (unwindowed) restricted in place.
+struct PairPlan {
+  int branch;   // 1 both windows, 2 only window 1, 3 only window 2, 4 none
+  int job[5];   // correlation job per slot (-1 unused)
+  int scaled[5];
+  int sjob[5];  // scaled-job index for weights (-1 if unscaled)
+};
+__global__ void k_combine(const PairPlan *__restrict__ plans, float *__restrict__ C, const unsigned long long *__restrict__ mm,
+                          const double *__restrict__ w, int n, int rstart, float *__restrict__ q1, float *__restrict__ q2) {
+  const PairPlan P = plans[blockIdx.y];
+  const long n3 = (long)n * n * n;
+  float lo[5], sc[5], wl[5];
+  for (int s = 0; s < 5; ++s) {
+    lo[s] = 0.f;
+    sc[s] = 1.f;
+    wl[s] = 0.f;
+    if (P.job[s] >= 0 && P.scaled[s]) {
+      float mn = ordered_to_float(~(uint32_t)(mm[2 * P.job[s]] >> 32));
+      float mx = ordered_to_float((uint32_t)(mm[2 * P.job[s] + 1] >> 32));
+      double wmin = w[2 * P.sjob[s]], wmax = w[2 * P.sjob[s] + 1];
+      lo[s] = mn;
+      sc[s] = (float)((wmax - wmin) / ((double)mx - (double)mn));
+      wl[s] = (float)wmin;
+    }
+  }
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    int b = (int)((id / n) % n);
+    float c[5];
+    for (int s = 0; s < 5; ++s) c[s] = P.job[s] >= 0 ? (C[(long)P.job[s] * n3 + id] - lo[s]) * sc[s] + wl[s] : 0.f;
+    float r;
+    if (P.branch == 1) {
+      float c1 = sqrtf(c[0]) * sqrtf(c[1]);
+      c1 = 2.0f * (1.0f - c[2] / c1);
+      r = -c1 / c[3];
+    } else if (P.branch == 2 || P.branch == 3) {
+      r = c[1] / sqrtf(c[0]);
+    } else {
+      r = c[0];
+    }
+    if (b >= rstart) r = -FLT_MAX;
+    q1[(long)blockIdx.y * n3 + id] = r;
+    if (P.job[4] >= 0) q2[(long)blockIdx.y * n3 + id] = (b >= rstart) ? -FLT_MAX : c[4];
+  }
+}
+
+// 3x3x3 ">=" local maxima with a -FLT_MAX border (localMaxima3D3x3, inc/em/nbfProjectionRotationMetric3D.h:67-79,
+// BordStrategyConst inc/bs/nbfBordStrategyConst.h:67-83); entries with |value| > 0 appended to the
+// item's list (order fixed on the host by sorting on the cell index).
+__global__ void k_local_max(const float *__restrict__ C, int n, const int *__restrict__ active, int cap, int *counts,
+                            int2 *lists) {
+  const long n3 = (long)n * n * n;
+  const int item = blockIdx.y;
+  if (!active[item]) return;
+  const float *c = C + (long)item * n3;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    int a = (int)(id / ((long)n * n)), b = (int)((id / n) % n), g = (int)(id % n);
+    float v = c[id];
+    bool ismax = true;
+    for (int da = -1; da <= 1 && ismax; ++da)
+      for (int db = -1; db <= 1 && ismax; ++db)
+        for (int dg = -1; dg <= 1; ++dg) {
+          if (!da && !db && !dg) continue;
+          int aa = a + da, bb = b + db, gg = g + dg;
+          float nb = (aa < 0 || bb < 0 || gg < 0 || aa >= n || bb >= n || gg >= n) ? -FLT_MAX
+                                                                                      : c[((long)aa * n + bb) * n + gg];
+          if (!(v >= nb)) {
+            ismax = false;
+            break;
+          }
+        }
+    if (ismax && fabsf(v) > 0.f) {
+      int slot = atomicAdd(&counts[item], 1);
+      if (slot < cap) lists[(long)item * cap + slot] = make_int2((int)id, __float_as_int(v));
+    }
+  }
+}
+
+template <class F>
+inline int nblocks(long n, int threads, int maxb = 1 << 16) {
+  long b = (n + threads - 1) / threads;
+  return (int)std::max(1L, std::min<long>(b, maxb));
+}
+
+// small-d^l_{m1 m2}(beta) for l in [max(|m1|,|m2|), B): closed form at the lowest degree and the
+// three-term recurrence in l (the L2-normalised version is what SOFT's genWigTrans_L2 tabulates,
+// external/soft-1.0/makeWigner.c:531-607).
+void small_d(int B, int m1, int m2, double beta, double *out) {
+  double c = cos(beta / 2), s = sin(beta / 2), cb = cos(beta);
+  int J = std::max(std::abs(m1), std::abs(m2));
+  double acc = 0;
+  for (int k = 0; k <= 2 * J; ++k) {
+    if (J + m2 - k < 0 || J - k - m1 < 0 || k - m2 + m1 < 0) continue;
+    double lg = 0.5 * (lgamma(J + m2 + 1.0) + lgamma(J - m2 + 1.0) + lgamma(J + m1 + 1.0) + lgamma(J - m1 + 1.0)) -
+                (lgamma(J + m2 - k + 1.0) + lgamma(k + 1.0) + lgamma(J - k - m1 + 1.0) + lgamma(k - m2 + m1 + 1.0));
+    acc += (((k - m2 + m1) % 2) ? -1.0 : 1.0) * exp(lg) * pow(c, 2 * J - 2 * k + m2 - m1) * pow(s, 2 * k - m2 + m1);
+  }
+  double prev = 0, cur = acc;
+  out[J] = cur;
+  for (int l = J; l < B - 1; ++l) {
+    double a = (l + 1) * (2.0 * l + 1) / sqrt(((l + 1.0) * (l + 1) - m1 * m1) * ((l + 1.0) * (l + 1) - m2 * m2));
+    double nx = (l == 0) ? a * cb * cur
+                         : a * ((cb - (double)m1 * m2 / (l * (l + 1.0))) * cur -
+                                (sqrt(((double)l * l - m1 * m1) * ((double)l * l - m2 * m2)) / (l * (2.0 * l + 1))) * prev);
+    prev = cur;
+    cur = nx;
+    out[l + 1] = cur;
+  }
+}
+
+struct EvalReq {
+  int ref, part;
+  Mat4 t;
+};
+struct EvalRes {
+  float dist;
+  Mat4 t;  // t * Translate(-shift)
+};
+
+}  // namespace
+
+struct ettk_ctx {
+  int device = 0;
+  ettk_params p{};
+  cudaStream_t st = nullptr;
+  int N = 0, H = 0, B = 0, n = 0;
+  long n3 = 0, h3 = 0, nn = 0, nso3 = 0;
+  std::string err;
+  long long launches = 0;
+  // constant tables
+  DevBuf<float> mask, maskfft, filter, lw, plm, dtab, sinth;
+  DevBuf<int> doff;
+  DevBuf<float4> dirs;
+  DevBuf<float2> Fm1;
+  double sum_filter = 0;
+  Smooth3 smooth{};
+  int bandL = 0, bandU = 0, rstart = 0, W = 0, lo = 0;
+  float rr2 = 0;
+  // references
+  int R = 0;
+  DevBuf<float> refvol, W1half, Pp1, W1sph;
+  DevBuf<float2> FI1;
+  std::vector<VolumeGeom> refg;
+  std::vector<int> useW1;
+  // particles
+  int V = 0;
+  DevBuf<float> partvol, W2sph, Pp2;
+  const float *partptr = nullptr;
+  std::vector<VolumeGeom> partg;
+  std::vector<int> useW2, pp2_ready;
+  // work buffers
+  DevBuf<float> w_r, w_v, w_fw, w_tmp, w_tmp2, w_C, w_q1, w_q2, w_sig, w_norm, w_norm2, sp_v, sp_M, sp_padc, sp_Pp;
+  DevBuf<float2> w_cA, w_cB, w_cC, w_p1, w_p2, w_coef, w_S, sp_F;
+  DevBuf<double> w_acc, w_w, sp_acc;
+  DevBuf<unsigned long long> w_peak, w_mm;
+  DevBuf<ResliceItem> w_items;
+  DevBuf<WedgeVecs> w_wv;
+  DevBuf<int> w_idx, w_idx2, w_cnt, w_active, w_pair_ref, w_pair_pp2, w_pair_part;
+  DevBuf<int2> w_lists;
+  DevBuf<EvalOut> w_out;
+  DevBuf<SigDesc> w_sd;
+  DevBuf<SynthJob> w_jobs;
+  DevBuf<ScaledJob> w_sjobs;
+  DevBuf<PairPlan> w_plans;
+
+  // ---- optional per-kernel-family timing with CUDA events on the library stream
+  bool prof = false;
+  struct ProfRec {
+    const char *name;
+    double bytes;
+    cudaEvent_t a, b;
+  };
+  struct ProfAgg {
+    long long n = 0;
+    double ms = 0, bytes = 0;
+  };
+  std::vector<ProfRec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  std::map<std::string, ProfAgg> prof_agg;
+  cudaEvent_t ev_get() {
+    if (ev_pool.empty()) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      return e;
+    }
+    cudaEvent_t e = ev_pool.back();
+    ev_pool.pop_back();
+    return e;
+  }
+  void prof_flush() {
+    for (auto &r : prof_pending) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, r.a, r.b));
+      ProfAgg &g = prof_agg[r.name];
+      g.n += 1;
+      g.ms += ms;
+      g.bytes += r.bytes;
+      ev_pool.push_back(r.a);
+      ev_pool.push_back(r.b);
+    }
+    prof_pending.clear();
+  }
+  struct Scope {
+    ettk_ctx *c;
+    const char *name;
+    double bytes;
+    cudaEvent_t a = nullptr;
+    Scope(ettk_ctx *c_, const char *n_, double b_) : c(c_), name(n_), bytes(b_) {
+      if (c->prof) {
+        a = c->ev_get();
+        CK(cudaEventRecord(a, c->st));
+      }
+    }
+    ~Scope() {
+      if (c->prof) {
+        cudaEvent_t b = c->ev_get();
+        cudaEventRecord(b, c->st);
+        c->prof_pending.push_back({name, bytes, a, b});
+      }
+    }
+  };
+
+  void sync() {
+    CK(cudaStreamSynchronize(st));
+    if (prof) prof_flush();
+  }
+  void post_launch() {
+    ++launches;
+    CK(cudaGetLastError());
+  }
+
+  // ---------------------------------------------------------------- FFT drivers
+  template <int NN>
+  void fft_strided_t(float2 *d, LineMap m, int sign, const float *scale, long scale_div) {
+    constexpr int L = (NN >= 128) ? 8 : 16;
+    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    int blocks = (int)((m.n_lines + L - 1) / L);
+    Scope sc(this, "fft_strided", 16.0 * m.n_lines * NN);
+    k_fft_strided<NN, L><<<blocks, 256, sm, st>>>(d, m, sign, scale, scale_div);
+    post_launch();
+  }
+  void fft_strided(int len, float2 *d, LineMap m, int sign, const float *scale = nullptr, long scale_div = 1) {
+    switch (len) {
+      case 16: fft_strided_t<16>(d, m, sign, scale, scale_div); break;
+      case 32: fft_strided_t<32>(d, m, sign, scale, scale_div); break;
+      case 64: fft_strided_t<64>(d, m, sign, scale, scale_div); break;
+      case 128: fft_strided_t<128>(d, m, sign, scale, scale_div); break;
+      case 256: fft_strided_t<256>(d, m, sign, scale, scale_div); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
+    }
+  }
+  template <int NN, class Pre>
+  void r2c_z_t(Pre pre, float2 *out, long lines) {
+    constexpr int L = (NN >= 128) ? 8 : 16;
+    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    int blocks = (int)((lines + 2 * L - 1) / (2 * L));
+    Scope sc(this, "fft_r2c_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
+    k_r2c_z<NN, L, Pre><<<blocks, 256, sm, st>>>(pre, out, lines);
+    post_launch();
+  }
+  template <class Pre>
+  void r2c_z(int len, Pre pre, float2 *out, long lines) {
+    switch (len) {
+      case 16: r2c_z_t<16>(pre, out, lines); break;
+      case 32: r2c_z_t<32>(pre, out, lines); break;
+      case 64: r2c_z_t<64>(pre, out, lines); break;
+      case 128: r2c_z_t<128>(pre, out, lines); break;
+      case 256: r2c_z_t<256>(pre, out, lines); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
+    }
+  }
+  static int lines_per_block(int len) { return 2 * ((len >= 128) ? 8 : 16); }
+  template <int NN, class Post>
+  void c2r_z_t(const float2 *in, Post post, long lines) {
+    constexpr int L = (NN >= 128) ? 8 : 16;
+    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    int blocks = (int)((lines + 2 * L - 1) / (2 * L));
+    Scope sc(this, "fft_c2r_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
+    k_c2r_z<NN, L, Post><<<blocks, 256, sm, st>>>(in, post, lines);
+    post_launch();
+  }
+  template <class Post>
+  void c2r_z(int len, const float2 *in, Post post, long lines) {
+    switch (len) {
+      case 16: c2r_z_t<16>(in, post, lines); break;
+      case 32: c2r_z_t<32>(in, post, lines); break;
+      case 64: c2r_z_t<64>(in, post, lines); break;
+      case 128: c2r_z_t<128>(in, post, lines); break;
+      case 256: c2r_z_t<256>(in, post, lines); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
+    }
+  }
+  // y and x passes of a 3-D transform of `items` arrays [len][len][len/2+1]
+  void xy_passes(int len, float2 *d, long items, int sign, bool x_first, const float *scale = nullptr) {
+    long h = len / 2 + 1;
+    LineMap my{items * len * h, (int)h, (long)len * h, 1, h};
+    LineMap mx{items * len * h, (int)(len * h), (long)len * len * h, 1, (long)len * h};
+    long per_item_lines = (long)len * h;
+    if (x_first) {
+      fft_strided(len, d, mx, sign, scale, per_item_lines);
+      fft_strided(len, d, my, sign);
+    } else {
+      fft_strided(len, d, my, sign, scale, per_item_lines);
+      fft_strided(len, d, mx, sign);
+    }
+  }
+
+  // ---------------------------------------------------------------- setup
+  void init_tables();
+  void spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out /*device, items*nn*/);
+  void eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> &res);
+  // executeFourierNewHalf for any number of requests, in device chunks of at most 1024 evaluations
+  void eval_batch(const std::vector<EvalReq> &req, std::vector<EvalRes> &res) {
+    res.resize(req.size());
+    const size_t chunk = 1024;
+    for (size_t c0 = 0; c0 < req.size(); c0 += chunk) {
+      size_t c1 = std::min(req.size(), c0 + chunk);
+      std::vector<EvalReq> sub(req.begin() + c0, req.begin() + c1);
+      std::vector<EvalRes> out;
+      eval_chunk(sub, out);
+      std::copy(out.begin(), out.end(), res.begin() + c0);
+    }
+  }
+  void align(int npairs, const int *pairs, float *D, int cols, int ncand);
+  void soft_diag(const float *F1, const float *F2, int scaled, float *C);
+};
+
+void ettk_ctx::init_tables() {
+  N = p.N;
+  H = N / 2 + 1;
+  B = p.B;
+  n = 2 * B;
+  n3 = (long)N * N * N;
+  h3 = (long)N * N * H;
+  nn = (long)n * n;
+  nso3 = (long)n * n * n;
+  // real-space mask (nbfImageFilter::buildMask, spherical raised cosine, inc/em/nbfImageFilter.h:383-472)
+  std::vector<float> m(n3, 1.0f), mf(n3, 0.0f), f(h3, 1.0f);
+  if (p.mask_radius != 0) {
+    float center = (float)(N / 2.0);
+    float r2 = std::min((float)(N - 1), (float)(p.mask_radius + p.mask_sigma / 2.0));
+    float r1 = (float)std::max(0.0, (double)(p.mask_radius - p.mask_sigma / 2.0));
+    float kappa = (float)(M_PI / (r2 - r1));
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        for (int k = 0; k < N; ++k) {
+          float di = i - center, dj = j - center, dk = k - center;
+          float v = sqrtf(di * di + dj * dj + dk * dk);
+          if (v <= r1) v = 1;
+          if (v >= r2) v = 0;
+          if (v > r1 && v <= r2) v = (float)((1 + cosf(kappa * (v - r1))) / 2.0);
+          m[((long)i * N + j) * N + k] = v;
+        }
+  }
+  // maskfft: soft box (nbfFourierImageMetric::reinitializeHalf, inc/em/nbfFourierImageMetric.h:640-662)
+  int sq = (int)p.square_mask_size;
+  if (sq > 0 && sq < floor(N / 2.0)) {
+    for (int i = sq; i <= N - 1 - sq; ++i)
+      for (int j = sq; j <= N - 1 - sq; ++j)
+        for (int k = sq; k <= N - 1 - sq; ++k) mf[((long)i * N + j) * N + k] = 1;
+  } else {
+    std::fill(mf.begin(), mf.end(), 1.0f);
+  }
+  {
+    // softenMask(maskfft, 2.5) operates on the blitz array with VTK x = first index
+    std::vector<float> t(n3);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        for (int k = 0; k < N; ++k) t[i + (long)N * (j + (long)N * k)] = mf[((long)i * N + j) * N + k];
+    int dims[3] = {N, N, N};
+    gaussian_smooth(t, dims, 2.5, (double)(2.5f * .75f));
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        for (int k = 0; k < N; ++k) mf[((long)i * N + j) * N + k] = t[i + (long)N * (j + (long)N * k)];
+  }
+  // filter on the centred half grid (nbfFourierFilter::updateFilterHalf, buildBandPassHalf, buildBFactorHalf)
+  int c = N / 2;
+  f[((long)c * N + c) * H + (H - 1)] = 0;
+  bool band = (p.bp_low > 0.0f) || (p.bp_high < 1.0f);
+  double blo = p.bp_low, bhi = p.bp_high, lv = p.bp_low_sigma, hv = p.bp_high_sigma;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < H; ++k) {
+        float t0 = (float)((1.0 * i - c) / c), t1 = (float)((1.0 * j - c) / c), t2 = (float)((1.0 * k - c) / c);
+        float rad = sqrtf(t0 * t0 + t1 * t1 + t2 * t2);
+        long id = ((long)i * N + j) * H + k;
+        if (band) {
+          float bp = (rad < blo) ? (float)exp(-((blo - rad) * (blo - rad)) / 2.0 / lv / lv) : 1.0f;
+          if (rad > bhi) bp = (float)exp(-((rad - bhi) * (rad - bhi)) / 2.0 / hv / hv);
+          f[id] *= bp;
+        }
+        if (p.bfactor != 0) f[id] *= (float)exp(-(double)p.bfactor * (double)(rad * rad));
+      }
+  sum_filter = 0;
+  for (float v : f) sum_filter += v;
+  mask.ensure(n3);
+  maskfft.ensure(n3);
+  filter.ensure(h3);
+  CK(cudaMemcpy(mask.p, m.data(), n3 * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(maskfft.p, mf.data(), n3 * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(filter.p, f.data(), h3 * 4, cudaMemcpyHostToDevice));
+  // wedge smoothing weights: std 2, radius int(2*0.5)=1, clipped renormalised kernels
+  {
+    double e1 = exp(-1.0 / 8.0), s3 = 1 + 2 * e1, s2 = 1 + e1;
+    smooth.w_int[0] = (float)(e1 / s3);
+    smooth.w_int[1] = (float)(1 / s3);
+    smooth.w_int[2] = (float)(e1 / s3);
+    smooth.w_lo[0] = (float)(1 / s2);
+    smooth.w_lo[1] = (float)(e1 / s2);
+    smooth.w_hi[0] = (float)(e1 / s2);
+    smooth.w_hi[1] = (float)(1 / s2);
+  }
+  // SO(3) tables: quadrature x Legendre (forward), Legendre (inverse), L2-normalised small-d per cell
+  std::vector<double> th(n), wq(n);
+  for (int j = 0; j < n; ++j) {
+    th[j] = M_PI * (2.0 * j + 1.0) / (4.0 * B);
+    double a = 0;
+    for (int k = 0; k < B; ++k) a += sin((2.0 * k + 1.0) * th[j]) / (2.0 * k + 1.0);
+    wq[j] = (2.0 / B) * sin(th[j]) * a;
+  }
+  std::vector<double> P((size_t)B * B * n, 0.0);  // [m][l][j]
+  for (int mm = 0; mm < B; ++mm) {
+    double cc = sqrt((2.0 * mm + 1.0) / 2.0);
+    for (int i = 1; i <= mm; ++i) cc *= sqrt((2.0 * i - 1.0) / (2.0 * i));
+    if (mm % 2) cc = -cc;
+    for (int j = 0; j < n; ++j) {
+      double x = cos(th[j]), s = sin(th[j]);
+      double pmm = cc * pow(s, mm);
+      P[((size_t)mm * B + mm) * n + j] = pmm;
+      if (mm + 1 < B) P[((size_t)mm * B + mm + 1) * n + j] = x * sqrt(2.0 * mm + 3.0) * pmm;
+      for (int l = mm + 2; l < B; ++l) {
+        double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)mm * mm));
+        double b = sqrt(((l - 1.0) * (l - 1.0) - (double)mm * mm) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+        P[((size_t)mm * B + l) * n + j] = a * (x * P[((size_t)mm * B + l - 1) * n + j] - b * P[((size_t)mm * B + l - 2) * n + j]);
+      }
+    }
+  }
+  std::vector<float> hlw((size_t)B * B * n), hplm((size_t)B * B * n);
+  double nrm = sqrt(2.0 * M_PI) / n;
+  for (size_t i = 0; i < hlw.size(); ++i) {
+    int j = (int)(i % n);
+    hlw[i] = (float)(nrm * wq[j] * P[i]);
+    hplm[i] = (float)P[i];
+  }
+  lw.ensure(hlw.size());
+  plm.ensure(hplm.size());
+  CK(cudaMemcpy(lw.p, hlw.data(), hlw.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(plm.p, hplm.data(), hplm.size() * 4, cudaMemcpyHostToDevice));
+  int ncell = (2 * B - 1) * (2 * B - 1);
+  std::vector<int> off(ncell);
+  long total = 0;
+  for (int cell = 0; cell < ncell; ++cell) {
+    int m1 = cell / (2 * B - 1) - (B - 1), m2 = cell % (2 * B - 1) - (B - 1);
+    off[cell] = (int)total;
+    total += (long)(B - std::max(std::abs(m1), std::abs(m2))) * n;
+  }
+  std::vector<float> hd(total);
+  std::vector<double> col(B);
+  for (int cell = 0; cell < ncell; ++cell) {
+    int m1 = cell / (2 * B - 1) - (B - 1), m2 = cell % (2 * B - 1) - (B - 1);
+    int l0 = std::max(std::abs(m1), std::abs(m2));
+    for (int j = 0; j < n; ++j) {
+      small_d(B, m1, m2, th[j], col.data());
+      for (int l = l0; l < B; ++l) hd[off[cell] + (size_t)(l - l0) * n + j] = (float)(sqrt((2.0 * l + 1.0) / 2.0) * col[l]);
+    }
+  }
+  dtab.ensure(total);
+  doff.ensure(ncell);
+  CK(cudaMemcpy(dtab.p, hd.data(), total * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(doff.p, off.data(), ncell * 4, cudaMemcpyHostToDevice));
+  std::vector<float> hs(n);
+  for (int j = 0; j < n; ++j) hs[j] = (float)sin(M_PI * (2 * j + 1) / 4 / (double)(float)B);
+  sinth.ensure(n);
+  CK(cudaMemcpy(sinth.p, hs.data(), n * 4, cudaMemcpyHostToDevice));
+  // spherical sampling directions (vtkSphericalTransform, origin pi/4B, spacing 2pi/4B and pi/B)
+  std::vector<float4> dv(nn);
+  double oy = M_PI / 4.0 / (double)(float)B, sy = 2.0 * M_PI / 4.0 / (double)(float)B, sz = M_PI / (double)(float)B;
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < n; ++k) {
+      double ph = oy + j * sy, t2 = 0.0 + k * sz;
+      dv[(size_t)j * n + k] = make_float4((float)(sin(ph) * cos(t2)), (float)(sin(ph) * sin(t2)), (float)cos(ph), 0.f);
+    }
+  dirs.ensure(nn);
+  CK(cudaMemcpy(dirs.p, dv.data(), nn * sizeof(float4), cudaMemcpyHostToDevice));
+  int N2 = 2 * N;
+  float lowCut = band ? p.bp_low : 0.0f, highCut = band ? p.bp_high : 1.0f;
+  bandL = std::max(4, (int)ceilf(lowCut * (float)(N2 - 1)));
+  bandU = (int)ceil(std::min(.5, (double)highCut) * (N2 - 1));
+  double rs = floor((double)(p.restrict_rotation * (float)B) / 90.0 - 1.0);
+  rstart = (int)std::max(1.0, std::min(rs, (double)(n - 1)));
+  // translational search window on the upsampled grid (nbfFourierImageMetric.h:1216-1232)
+  float center = (float)(N2 / 2.0);
+  float restriction = center;
+  if (p.restrict_translation < FLT_MAX) restriction = (float)std::max((double)p.restrict_translation * 2.0f, 1.0);
+  lo = (int)std::max(0.0, (double)center - floor(restriction));
+  int hi = (int)std::min((double)center + floor(restriction), (double)(N2 - 1));
+  W = hi - lo + 1;
+  rr2 = restriction * restriction;
+  // F(m1*shift)
+  Fm1.ensure(h3);
+  PreProductShift pre{mask.p, nullptr, N};
+  pre.src = nullptr;
+  pre.aux = mask.p;
+  r2c_z(N, pre, Fm1.p, (long)N * N);
+  xy_passes(N, Fm1.p, 1, -1, false);
+  sync();
+}
+
+// cartesianToSpherical for a batch of volumes (inc/em/nbfProjectionRotationMetric3D.h:264-413)
+void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out) {
+  long P = (long)items.size();
+  if (P == 0) return;
+  int N2 = 2 * N;
+  long big_h = (long)N2 * N2 * (N + 1);
+  w_items.ensure(P);
+  sp_v.ensure(P * n3);
+  sp_acc.ensure(P * 4);
+  sp_F.ensure(P * big_h);
+  sp_M.ensure(P * big_h);
+  sp_padc.ensure(P);
+  CK(cudaMemcpyAsync(w_items.p, items.data(), P * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
+  {
+    Scope sc(this, "reslice", 8.0 * P * n3);
+    k_reslice<<<dim3(nblocks<int>(n3, 256, 512), P), 256, 0, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
+  }
+  post_launch();
+  k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
+  post_launch();
+  PrePadded pre{sp_v.p, mask.p, sp_acc.p, 4, N};
+  k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
+  post_launch();
+  r2c_z(N2, pre, sp_F.p, P * N2 * N2);
+  xy_passes(N2, sp_F.p, P, -1, false);
+  k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
+  post_launch();
+  Scope sc_ss(this, "sphere_sample", 4.0 * P * big_h + 4.0 * P * nn);
+  k_sphere_sample<<<dim3(nblocks<int>(nn, 128), P), 128, 0, st>>>(sp_M.p, dirs.p, (int)nn, N, bandL, bandU, sp_padc.p,
+                                                                  Pp_out);
+  post_launch();
+}
+
+// executeFourierNewHalf for a batch of (reference, particle, transform) requests.
+void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> &res) {
+  long E = (long)req.size();
+  res.resize(E);
+  if (E == 0) return;
+  const int ACC = 8;  // 0,1 reslice sums; 2,3 norm1; 4 k1_m; 5 unused; 6 sum(w*f); 7 unused
+  w_items.ensure(E);
+  w_wv.ensure(E);
+  w_idx.ensure(E);
+  w_fw.ensure(E * h3);
+  w_tmp.ensure(E * h3);
+  w_cA.ensure(E * h3);
+  w_cB.ensure(E * h3);
+  w_cC.ensure(E * h3);
+  w_r.ensure(E * n3);
+  w_v.ensure(E * n3);
+  w_acc.ensure(E * ACC * 2);
+  w_norm.ensure(E);
+  w_norm2.ensure(E);
+  w_peak.ensure(E);
+  w_out.ensure(E);
+  w_p1.ensure(E * W * N * H);
+  w_p2.ensure(E * W * W * H);
+  std::vector<ResliceItem> items(E);
+  std::vector<WedgeVecs> wv(E);
+  std::vector<int> refidx(E);
+  for (long e = 0; e < E; ++e) {
+    const EvalReq &r = req[e];
+    const VolumeGeom &g = partg[r.part];
+    double m12[12];
+    reslice_index(g, N, &r.t, m12);
+    ResliceItem it;
+    it.vol = partptr + (long)r.part * n3;
+    it.dims[0] = it.dims[1] = it.dims[2] = N;
+    for (int i = 0; i < 12; ++i) it.m[i] = (float)m12[i];
+    items[e] = it;
+    WedgeVecs w{};
+    w.full = g.full_wedge() ? 1 : 0;
+    if (!w.full) wedge_vectors(g, &r.t, w.v1, w.v2);
+    wv[e] = w;
+    refidx[e] = r.ref;
+  }
+  CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_wv.p, wv.data(), E * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_idx.p, refidx.data(), E * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, E * ACC * 2 * sizeof(double), st));
+  CK(cudaMemsetAsync(w_peak.p, 0, E * sizeof(unsigned long long), st));
+  double *acc = w_acc.p;
+  double *acc2 = w_acc.p + E * ACC;  // second set: particle reslice sums + norm2
+  dim3 gh(nblocks<int>(h3, 256, 256), E), gn(nblocks<int>(n3, 256, 256), E);
+  bool useWedge = p.wedge_compensation != 0;
+  // wedge (W1 * W2(T)) * filter and its sum
+  if (useWedge) {
+    Scope sc_w(this, "wedge", 4.0 * E * h3 * 7);
+    k_wedge_binary<<<gh, 256, 0, st>>>(w_wv.p, N, w_fw.p);
+    post_launch();
+    k_wedge_smooth<<<gh, 256, 0, st>>>(w_fw.p, w_tmp.p, N, 2, smooth, nullptr, nullptr, nullptr, nullptr, 0, 0);
+    post_launch();
+    k_wedge_smooth<<<gh, 256, 0, st>>>(w_tmp.p, w_fw.p, N, 1, smooth, nullptr, nullptr, nullptr, nullptr, 0, 0);
+    post_launch();
+    k_wedge_smooth<<<gh, 256, 0, st>>>(w_fw.p, w_tmp.p, N, 0, smooth, W1half.p, w_idx.p, filter.p, acc, ACC, 6);
+    post_launch();
+    std::swap(w_fw, w_tmp);
+  } else {
+    for (long e = 0; e < E; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  // I1 branch: F1 = R2C(I1 maskfft shift) * fw, normalised, C2R, k1_m and R2C(I1' m1)
+  {
+  Scope sc_f(this, "spec_filter", 20.0 * E * h3);
+  k_spec_filter<<<gh, 256, 0, st>>>(FI1.p, w_idx.p, w_fw.p, w_cA.p, N, acc, ACC, 2);
+  post_launch();
+  }
+  k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)E, w_norm.p, nullptr);
+  post_launch();
+  xy_passes(N, w_cA.p, E, +1, true, w_norm.p);
+  c2r_z(N, w_cA.p, PostStore{w_r.p, N}, E * N * N);
+  PreY1M1 py{w_r.p, mask.p, N, acc, ACC, 4, 0.0, (long)lines_per_block(N)};
+  r2c_z(N, py, w_cA.p, E * N * N);
+  xy_passes(N, w_cA.p, E, -1, false);
+  // I2 branch: reslice under T, R2C((I2-mean) maskfft shift) * fw, normalised
+  {
+    Scope sc(this, "reslice", 8.0 * E * n3);
+    k_reslice<<<gn, 256, 0, st>>>(w_items.p, N, w_v.p, acc2, ACC);
+  }
+  post_launch();
+  PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
+  r2c_z(N, pp, w_cB.p, E * N * N);
+  xy_passes(N, w_cB.p, E, -1, false);
+  k_spec_filter<<<gh, 256, 0, st>>>(w_cB.p, nullptr, w_fw.p, w_cB.p, N, acc2, ACC, 2);
+  post_launch();
+  k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc2, ACC, 2, N, (int)E, w_norm2.p, nullptr);
+  post_launch();
+  k_fft2re<<<gh, 256, 0, st>>>(w_cA.p, w_cB.p, w_norm2.p, N);
+  post_launch();
+  xy_passes(N, w_cB.p, E, +1, true, w_norm2.p);
+  c2r_z(N, w_cB.p, PostStore{w_r.p, N}, E * N * N);
+  r2c_z(N, PreSquareShift{w_r.p, N}, w_cC.p, E * N * N);
+  xy_passes(N, w_cC.p, E, -1, false);
+  k_cross<<<gh, 256, 0, st>>>(w_cC.p, Fm1.p, w_cA.p, N, 8.0f);
+  post_launch();
+  int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
+  {
+  Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
+  k_pruned_x<<<dim3(nblocks<int>((long)W * N * H, 256, 1024), E), 256, 0, st>>>(w_cC.p, w_p1.p, N, W, lo, o0);
+  post_launch();
+  k_pruned_y<<<dim3(nblocks<int>((long)W * W * H, 256, 1024), E), 256, 0, st>>>(w_p1.p, w_p2.p, N, W, lo, o0);
+  post_launch();
+  k_pruned_z_peak<<<dim3(nblocks<int>((long)W * W * W, 256, 1024), E), 256, 0, st>>>(w_p2.p, N, W, lo, o2, rr2,
+                                                                                      w_peak.p);
+  post_launch();
+  }
+  k_score<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, w_peak.p, (int)E, W, sum_filter, p.overlap_normalized,
+                                                useWedge ? 1 : 0, N, w_out.p);
+  post_launch();
+  std::vector<EvalOut> out(E);
+  CK(cudaMemcpyAsync(out.data(), w_out.p, E * sizeof(EvalOut), cudaMemcpyDeviceToHost, st));
+  sync();
+  for (long e = 0; e < E; ++e) {
+    res[e].dist = out[e].dist;
+    Mat4 tr = Mat4::eye();
+    if (!(out[e].shift[0] == 0 && out[e].shift[1] == 0 && out[e].shift[2] == 0)) {
+      tr.e[3] = -(double)out[e].shift[0];
+      tr.e[7] = -(double)out[e].shift[1];
+      tr.e[11] = -(double)out[e].shift[2];
+    }
+    res[e].t = mul(req[e].t, tr);
+  }
+}
+
+namespace {
+
+// nbfImageMetric::isTransformValid (inc/em/nbfImageMetric.h:415-459)
+bool transform_valid(const ettk_params &p, const Mat4 &t) {
+  double sh[3] = {t.e[3], t.e[7], t.e[11]};
+  if (fabs(sh[0]) > p.restrict_translation || fabs(sh[1]) > p.restrict_translation || fabs(sh[2]) > p.restrict_translation)
+    return false;
+  double po[3];
+  for (int i = 0; i < 3; ++i) po[i] = t.e[4 * i + 2] + t.e[4 * i + 3] - sh[i];
+  double d = sqrt(po[0] * po[0] + po[1] * po[1] + po[2] * po[2]);
+  if (d != 0)
+    for (int i = 0; i < 3; ++i) po[i] /= d;
+  double ang = po[2];
+  ang = (ang >= 1) ? 0 : fabs(acos(ang) * 57.29577951308232);
+  return ang <= p.restrict_rotation;
+}
+
+// eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
+// matrices can be closer than `tol` in L1 are compared (each entry must differ by < tol); visiting only
+// those pairs in increasing j order is equivalent to the reference's full double loop.
+void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
+  size_t K = pos.size();
+  std::vector<Mat4> mats(K);
+  for (size_t i = 0; i < K; ++i) mats[i] = euler_candidate(pos[i].v[0], pos[i].v[1], pos[i].v[2]);
+  // bucket on the third column of the rotation (entries 2, 6, 10)
+  double cell = std::max((double)tol, 1e-3);
+  int nc = (int)ceil(2.0 / cell) + 3;
+  auto key = [&](double v) { return std::min(nc - 1, std::max(0, (int)floor((v + 1.0) / cell) + 1)); };
+  std::vector<std::vector<int>> grid((size_t)nc * nc * nc);
+  std::vector<int> kx(K), ky(K), kz(K);
+  for (size_t i = 0; i < K; ++i) {
+    kx[i] = key(mats[i].e[2]);
+    ky[i] = key(mats[i].e[6]);
+    kz[i] = key(mats[i].e[10]);
+    grid[((size_t)kx[i] * nc + ky[i]) * nc + kz[i]].push_back((int)i);
+  }
+  const float dead = -FLT_MAX;
+  std::vector<int> nb;
+  for (size_t i = 0; i < K; ++i) {
+    nb.clear();
+    for (int a = kx[i] - 1; a <= kx[i] + 1; ++a)
+      for (int b = ky[i] - 1; b <= ky[i] + 1; ++b)
+        for (int c = kz[i] - 1; c <= kz[i] + 1; ++c) {
+          if (a < 0 || b < 0 || c < 0 || a >= nc || b >= nc || c >= nc) continue;
+          for (int j : grid[((size_t)a * nc + b) * nc + c]) nb.push_back(j);
+        }
+    std::sort(nb.begin(), nb.end());
+    for (int j : nb) {
+      if (pos[i].v[3] == dead) break;
+      if ((size_t)j != i && pos[j].v[3] > dead) {
+        double err = 0;
+        for (int m = 0; m < 16; ++m) err += fabs(mats[i].e[m] - mats[j].e[m]);
+        if (err < tol) {
+          if (pos[i].v[3] > pos[j].v[3]) pos[i].v[3] = dead;
+          else pos[j].v[3] = dead;
+        }
+      }
+    }
+  }
+  for (size_t i = 0; i < K; ++i)
+    if (pos[i].v[3] > dead) pq.push(pos[i]);
+}
+
+}  // namespace
+
+void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand) {
+  int maxb = p.max_batch > 0 ? p.max_batch : 512;
+  std::vector<int> todo;
+  for (int i = 0; i < npairs; ++i)
+    if (D[(long)i * cols * ncand] == -1) todo.push_back(i);
+  for (size_t b0 = 0; b0 < todo.size(); b0 += maxb) {
+    int P = (int)std::min<size_t>(maxb, todo.size() - b0);
+    std::vector<int> pr(P), pp(P);
+    for (int i = 0; i < P; ++i) {
+      pr[i] = pairs[2 * todo[b0 + i]];
+      pp[i] = pairs[2 * todo[b0 + i] + 1];
+      if (pr[i] < 0 || pr[i] >= R || pp[i] < 0 || pp[i] >= V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+    }
+    // 1. spherical projections of particles not yet projected
+    {
+      std::vector<ResliceItem> items;
+      std::vector<int> ids;
+      for (int i = 0; i < P; ++i)
+        if (!pp2_ready[pp[i]] && std::find(ids.begin(), ids.end(), pp[i]) == ids.end()) ids.push_back(pp[i]);
+      const int chunk = 256;
+      for (size_t c0 = 0; c0 < ids.size(); c0 += chunk) {
+        items.clear();
+        size_t c1 = std::min(ids.size(), c0 + chunk);
+        for (size_t c = c0; c < c1; ++c) {
+          ResliceItem it;
+          it.vol = partptr + (long)ids[c] * n3;
+          it.dims[0] = it.dims[1] = it.dims[2] = N;
+          double m12[12];
+          reslice_index(partg[ids[c]], N, nullptr, m12);
+          for (int k = 0; k < 12; ++k) it.m[k] = (float)m12[k];
+          items.push_back(it);
+        }
+        w_sig.ensure(items.size() * nn);
+        spherical_projection(items, w_sig.p);
+        for (size_t c = c0; c < c1; ++c) {
+          CK(cudaMemcpyAsync(Pp2.p + (long)ids[c] * nn, w_sig.p + (c - c0) * nn, nn * 4, cudaMemcpyDeviceToDevice, st));
+          pp2_ready[ids[c]] = 1;
+        }
+      }
+    }
+    // 2. SO(3) plans: signals, correlation jobs, scaled jobs
+    std::vector<SigDesc> sd;
+    std::vector<SynthJob> jobs;
+    std::vector<ScaledJob> sjobs;
+    std::vector<PairPlan> plans(P);
+    std::vector<int> jscaled;
+    auto sig = [&](int pair, int kind) {
+      sd.push_back({pair, kind});
+      return (int)sd.size() - 1;
+    };
+    auto corr = [&](PairPlan &pl, int slot, int pair, int k1, int k2, bool scaled) {
+      int f = sig(pair, k1), h = sig(pair, k2);
+      jobs.push_back({f, h});
+      pl.job[slot] = (int)jobs.size() - 1;
+      pl.scaled[slot] = scaled;
+      pl.sjob[slot] = -1;
+      if (scaled) {
+        sjobs.push_back({h, f, (int)jobs.size() - 1});
+        pl.sjob[slot] = (int)sjobs.size() - 1;
+      }
+    };
+    for (int i = 0; i < P; ++i) {
+      PairPlan &pl = plans[i];
+      for (int s = 0; s < 5; ++s) pl.job[s] = -1, pl.scaled[s] = 0, pl.sjob[s] = -1;
+      bool u1 = p.wedge_compensation && useW1[pr[i]], u2 = p.wedge_compensation && useW2[pp[i]];
+      if (u1 && u2) {
+        pl.branch = 1;
+        corr(pl, 0, i, K_PP1SQ_W1, K_W2, true);
+        corr(pl, 1, i, K_W1, K_PP2SQ_W2, true);
+        corr(pl, 2, i, K_PP1_W1, K_PP2_W2, true);
+        corr(pl, 3, i, K_W1, K_W2, true);
+      } else if (u1) {
+        pl.branch = 2;
+        corr(pl, 0, i, K_W1, K_PP2SQ, true);
+        corr(pl, 1, i, K_W1_PP1, K_PP2, true);
+      } else if (u2) {
+        pl.branch = 3;
+        corr(pl, 0, i, K_PP1SQ, K_W2, true);
+        corr(pl, 1, i, K_PP1, K_W2_PP2, true);
+      } else {
+        pl.branch = 4;
+        corr(pl, 0, i, K_PP1, K_PP2, false);
+      }
+      if (u1 || u2) corr(pl, 4, i, K_PP1, K_PP2, false);
+    }
+    long NS = (long)sd.size(), NJ = (long)jobs.size(), NSJ = (long)sjobs.size();
+    w_sd.ensure(NS);
+    w_jobs.ensure(NJ);
+    w_sjobs.ensure(std::max(1L, NSJ));
+    w_plans.ensure(P);
+    w_pair_ref.ensure(P);
+    w_pair_pp2.ensure(P);
+    w_pair_part.ensure(P);
+    w_sig.ensure(NS * nn);
+    w_coef.ensure(NS * B * B);
+    w_S.ensure(NJ * nso3);
+    w_C.ensure(NJ * nso3);
+    w_mm.ensure(NJ * 2);
+    w_w.ensure(std::max(1L, NSJ) * 2);
+    w_q1.ensure((long)P * nso3);
+    w_q2.ensure((long)P * nso3);
+    CK(cudaMemcpyAsync(w_sd.p, sd.data(), NS * sizeof(SigDesc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_jobs.p, jobs.data(), NJ * sizeof(SynthJob), cudaMemcpyHostToDevice, st));
+    if (NSJ) CK(cudaMemcpyAsync(w_sjobs.p, sjobs.data(), NSJ * sizeof(ScaledJob), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_plans.p, plans.data(), P * sizeof(PairPlan), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_pair_ref.p, pr.data(), P * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_pair_pp2.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_pair_part.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
+    k_build_signals<<<NS, 256, 0, st>>>(w_sd.p, w_pair_ref.p, w_pair_pp2.p, Pp1.p, Pp2.p, W1sph.p, W2sph.p,
+                                        w_pair_part.p, (int)nn, w_sig.p);
+    post_launch();
+    size_t smem_sht = (n / 2 + (size_t)n * n) * sizeof(float2);
+    switch (B) {
+#define SO3_CASE(BB)                                                                                          \
+  case BB: {                                                                                                  \
+    if (smem_sht > 48 * 1024)                                                                                 \
+      CK(cudaFuncSetAttribute(k_sht<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sht));        \
+    k_sht<BB><<<NS, 256, smem_sht, st>>>(w_sig.p, lw.p, w_coef.p);                                            \
+    post_launch();                                                                                            \
+    CK(cudaMemsetAsync(w_S.p, 0, NJ * nso3 * sizeof(float2), st));                                           \
+    {                                                                                                         \
+    Scope sc_s(this, "so3_synth", 8.0 * NJ * nso3 + 4.0 * dtab.n);                                           \
+    k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(64, (NJ + 7) / 8)), 256, 0,  \
+                      st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab.p, doff.p, w_S.p);                              \
+    post_launch();                                                                                            \
+    }                                                                                                         \
+    fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, 1, (long)n, 0, 1}, -1);                                    \
+    fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n, (long)n * n, 1, (long)n}, -1);                          \
+    CK(cudaMemsetAsync(w_mm.p, 0, NJ * 2 * sizeof(unsigned long long), st));                                  \
+    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), NJ), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);            \
+    post_launch();                                                                                            \
+    if (NSJ) {                                                                                                \
+      k_so3_weights<BB><<<dim3(NSJ, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p,    \
+                                                      plm.p, sinth.p, w_w.p);                                 \
+      post_launch();                                                                                          \
+    }                                                                                                         \
+  } break;
+      SO3_CASE(8)
+      SO3_CASE(16)
+      SO3_CASE(32)
+      SO3_CASE(64)
+#undef SO3_CASE
+      default:
+        throw CudaError(ETTK_ERR_ARG, "unsupported bandwidth");
+    }
+    {
+    Scope sc_c(this, "combine", 4.0 * (NJ + 2.0 * P) * nso3);
+    k_combine<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_plans.p, w_C.p, w_mm.p, w_w.p, n, rstart,
+                                                                        w_q1.p, w_q2.p);
+    post_launch();
+    }
+    // 3. local maxima -> host queues
+    const int cap = 8192;
+    w_cnt.ensure(2 * P);
+    w_active.ensure(2 * P);
+    w_lists.ensure((long)2 * P * cap);
+    std::vector<int> act(2 * P);
+    for (int i = 0; i < P; ++i) {
+      act[i] = 1;
+      act[P + i] = plans[i].job[4] >= 0;
+    }
+    CK(cudaMemcpyAsync(w_active.p, act.data(), 2 * P * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w_cnt.p, 0, 2 * P * 4, st));
+    // q1 and q2 buffers are contiguous when allocated back to back; launch separately
+    {
+    Scope sc_lm(this, "local_max", 8.0 * P * nso3);
+    k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q1.p, n, w_active.p, cap, w_cnt.p, w_lists.p);
+    post_launch();
+    k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q2.p, n, w_active.p + P, cap, w_cnt.p + P,
+                                                                       w_lists.p + (long)P * cap);
+    post_launch();
+    }
+    std::vector<int> cnt(2 * P);
+    CK(cudaMemcpyAsync(cnt.data(), w_cnt.p, 2 * P * 4, cudaMemcpyDeviceToHost, st));
+    sync();
+    std::vector<int2> lists((long)2 * P * cap);
+    for (int q = 0; q < 2 * P; ++q) {
+      int c = std::min(cnt[q], cap);
+      if (cnt[q] > cap) throw CudaError(ETTK_ERR_ARG, "too many SO(3) local maxima");
+      if (c) CK(cudaMemcpyAsync(lists.data() + (long)q * cap, w_lists.p + (long)q * cap, c * sizeof(int2),
+                                cudaMemcpyDeviceToHost, st));
+    }
+    sync();
+    std::vector<PQ> q1(P), q2(P);
+    for (int q = 0; q < 2 * P; ++q) {
+      int c = std::min(cnt[q], cap);
+      std::vector<int2> L(lists.begin() + (long)q * cap, lists.begin() + (long)q * cap + c);
+      std::sort(L.begin(), L.end(), [](const int2 &a, const int2 &b) { return a.x < b.x; });
+      std::vector<Cand> pos;
+      for (auto &e : L) {
+        int a = e.x / (n * n), bb = (e.x / n) % n, g = e.x % n;
+        float val = __builtin_bit_cast(float, e.y);
+        float alpha = (float)(a / (double)B * 180.0);
+        float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
+        if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
+        float gamma = (float)(g / (double)B * 180.0);
+        if (transform_valid(p, euler_candidate(alpha, beta, gamma))) pos.push_back({{alpha, beta, gamma, -val}, -1});
+      }
+      eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f);
+    }
+    // 4. candidate rounds (execute 678-776): direct and mirror CCF per popped candidate
+    struct PairState {
+      int index[2] = {0, 0};
+      bool done[2] = {false, false};
+      std::vector<Cand> combined[2];
+    };
+    std::vector<PairState> ps(P);
+    std::vector<EvalRes> store;  // direct results referenced by combined entries
+    int nqueues_max = 2;
+    for (int round = 0;; ++round) {
+      std::vector<EvalReq> req;
+      struct Pend {
+        int pair, q;
+        Cand c;
+        int e_direct, e_mirror;
+      };
+      std::vector<Pend> pend;
+      for (int i = 0; i < P; ++i) {
+        int nq = plans[i].job[4] >= 0 ? 2 : 1;
+        for (int q = 0; q < nq && q < nqueues_max; ++q) {
+          PairState &S = ps[i];
+          if (S.done[q]) continue;
+          PQ &Q = q == 0 ? q1[i] : q2[i];
+          int peaks = p.candidate_peaks;
+          if (q == 1) peaks = (int)std::max(1.0, floor(p.candidate_peaks / 3.0));
+          int need = peaks - S.index[q];
+          if (need <= 0 || Q.empty()) {
+            S.done[q] = true;
+            continue;
+          }
+          for (int t = 0; t < need && !Q.empty(); ++t) {
+            Cand c = Q.top();
+            if (c.v[3] == FLT_MAX) {
+              // reference breaks out of this queue; leave the entry for the check below
+              break;
+            }
+            Q.pop();
+            Mat4 t1 = euler_candidate(c.v[0], c.v[1], c.v[2]);
+            Mat4 mir = Mat4::eye();
+            mir.e[0] = mir.e[5] = mir.e[10] = -1.0;
+            mir = mul(mir, t1);
+            Pend pd{i, q, c, (int)req.size(), (int)req.size() + 1};
+            req.push_back({pr[i], pp[i], t1});
+            req.push_back({pr[i], pp[i], mir});
+            pend.push_back(pd);
+          }
+        }
+      }
+      if (req.empty()) break;
+      std::vector<EvalRes> res;
+      eval_batch(req, res);
+      // apply in the reference's sequential order per (pair, queue)
+      for (auto &pd : pend) {
+        PairState &S = ps[pd.pair];
+        int peaks = p.candidate_peaks;
+        if (pd.q == 1) peaks = (int)std::max(1.0, floor(p.candidate_peaks / 3.0));
+        if (S.index[pd.q] >= peaks) continue;  // cannot happen: need bounded the pops
+        const EvalRes &d = res[pd.e_direct];
+        if (transform_valid(p, d.t)) {
+          if (res[pd.e_mirror].dist >= d.dist) S.index[pd.q]++;
+          store.push_back(d);
+          Cand c = pd.c;
+          c.v[3] = d.dist;
+          c.ref = (int)store.size() - 1;
+          S.combined[pd.q].push_back(c);
+        }
+      }
+      // queues whose top is the sentinel stop (execute 699-701)
+      for (int i = 0; i < P; ++i)
+        for (int q = 0; q < 2; ++q) {
+          PQ &Q = q == 0 ? q1[i] : q2[i];
+          if (!Q.empty() && Q.top().v[3] == FLT_MAX) ps[i].done[q] = true;
+        }
+    }
+    // 5. final selection (execute 786-907) and output rows (getDistances 1962-2002)
+    std::vector<EvalReq> fallback;
+    std::vector<int> fb_pair;
+    for (int i = 0; i < P; ++i) {
+      std::vector<Cand> comb = ps[i].combined[0];
+      comb.insert(comb.end(), ps[i].combined[1].begin(), ps[i].combined[1].end());
+      if (comb.empty()) {
+        comb.push_back({{0, 0, 0, 1.0f}, -2});
+      }
+      PQ pc;
+      eliminate_equivalent(comb, pc, 2.5f);
+      float best = FLT_MAX;
+      int row = todo[b0 + i];
+      for (int k = 0; k < ncand; ++k) D[((long)row * cols + 0) * ncand + k] = FLT_MAX;
+      int index = 0;
+      Mat4 bestT = Mat4::eye();
+      while (!pc.empty() && index < p.number_of_candidates) {
+        Cand c = pc.top();
+        pc.pop();
+        EvalRes r;
+        if (c.ref >= 0) {
+          r = store[c.ref];  // refine(t,0) repeats the direct evaluation at the same rotation
+        } else {
+          std::vector<EvalRes> rr;
+          eval_batch({{pr[i], pp[i], euler_candidate(c.v[0], c.v[1], c.v[2])}}, rr);
+          r = rr[0];
+        }
+        if (r.dist < best) {
+          best = r.dist;
+          bestT = r.t;
+        }
+        if (index < ncand && ncand > 1) {
+          int off = 1;
+          D[((long)row * cols + 0) * ncand + index] = r.dist;
+          if (cols > 17) D[((long)row * cols + 1) * ncand + index] = 1.0f, off = 2;
+          if (cols > 18) D[((long)row * cols + 2) * ncand + index] = 1.0f, off = 3;
+          for (int m = 0; m < 16; ++m) D[((long)row * cols + m + off) * ncand + index] = (float)r.t.e[m];
+        }
+        ++index;
+      }
+      if (ncand == 1 || p.number_of_candidates == 1) {
+        int off = 1;
+        D[((long)row * cols + 0) * ncand + 0] = best;
+        if (cols > 17) D[((long)row * cols + 1) * ncand + 0] = 1.0f, off = 2;
+        if (cols > 18) D[((long)row * cols + 2) * ncand + 0] = 1.0f, off = 3;
+        for (int m = 0; m < 16; ++m) D[((long)row * cols + m + off) * ncand + 0] = (float)bestT.e[m];
+      }
+    }
+  }
+}
+
+void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C) {
+  // one pair-like job on two user signals: reuse the SO(3) kernels with a single correlation
+  w_sig.ensure(2 * nn);
+  w_coef.ensure(2 * B * B);
+  w_S.ensure(nso3);
+  w_C.ensure(nso3);
+  w_mm.ensure(2);
+  w_w.ensure(2);
+  w_jobs.ensure(1);
+  w_sjobs.ensure(1);
+  CK(cudaMemcpyAsync(w_sig.p, F1, nn * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_sig.p + nn, F2, nn * 4, cudaMemcpyHostToDevice, st));
+  SynthJob j{0, 1};
+  ScaledJob sj{1, 0, 0};
+  CK(cudaMemcpyAsync(w_jobs.p, &j, sizeof(j), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_sjobs.p, &sj, sizeof(sj), cudaMemcpyHostToDevice, st));
+  size_t smem_sht = (n / 2 + (size_t)n * n) * sizeof(float2);
+  switch (B) {
+#define SO3D(BB)                                                                                          \
+  case BB:                                                                                                \
+    if (smem_sht > 48 * 1024)                                                                             \
+      CK(cudaFuncSetAttribute(k_sht<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sht));    \
+    k_sht<BB><<<2, 256, smem_sht, st>>>(w_sig.p, lw.p, w_coef.p);                                         \
+    post_launch();                                                                                        \
+    CK(cudaMemsetAsync(w_S.p, 0, nso3 * sizeof(float2), st));                                            \
+    k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), 1), 256, 0, st>>>(w_coef.p, w_jobs.p, 1, dtab.p,  \
+                                                                          doff.p, w_S.p);                 \
+    post_launch();                                                                                        \
+    fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, 1, (long)n, 0, 1}, -1);                               \
+    fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, n, (long)n * n, 1, (long)n}, -1);                     \
+    CK(cudaMemsetAsync(w_mm.p, 0, 2 * sizeof(unsigned long long), st));                                   \
+    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), 1), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);         \
+    post_launch();                                                                                        \
+    if (scaled) {                                                                                         \
+      k_so3_weights<BB><<<dim3(1, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p, \
+                                                    plm.p, sinth.p, w_w.p);                               \
+      post_launch();                                                                                      \
+    }                                                                                                     \
+    break;
+    SO3D(8)
+    SO3D(16)
+    SO3D(32)
+    SO3D(64)
+#undef SO3D
+    default:
+      throw CudaError(ETTK_ERR_ARG, "unsupported bandwidth");
+  }
+  std::vector<float> hc(nso3);
+  CK(cudaMemcpyAsync(hc.data(), w_C.p, nso3 * 4, cudaMemcpyDeviceToHost, st));
+  unsigned long long mm[2];
+  double w[2];
+  CK(cudaMemcpyAsync(mm, w_mm.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(w, w_w.p, sizeof(w), cudaMemcpyDeviceToHost, st));
+  sync();
+  if (scaled) {
+    auto unpack = [](unsigned long long k, bool isMin) {
+      uint32_t u = (uint32_t)(k >> 32);
+      if (isMin) u = ~u;
+      return __builtin_bit_cast(float, (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+    };
+    float mn = unpack(mm[0], true), mx = unpack(mm[1], false);
+    float sc = (float)((w[1] - w[0]) / ((double)mx - (double)mn));
+    for (long i = 0; i < nso3; ++i) hc[i] = (hc[i] - mn) * sc + (float)w[0];
+  }
+  memcpy(C, hc.data(), nso3 * 4);
+}
+
+// ------------------------------------------------------------------------------------- C ABI
+
+namespace {
+int fail(ettk_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+VolumeGeom to_geom(const ettk_volume_meta &m) {
+  VolumeGeom g;
+  g.lwedge = m.lwedge;
+  g.uwedge = m.uwedge;
+  for (int i = 0; i < 3; ++i) {
+    g.normal[i] = m.normal[i];
+    g.position[i] = m.position[i];
+  }
+  g.cut_offset = m.cut_offset;
+  memcpy(g.matrix, m.matrix, sizeof(g.matrix));
+  return g;
+}
+
+// nbfWedge3D::getSphericalImage + conditionSphericalWindow on the host (double arithmetic as the reference)
+void spherical_wedge_host(const VolumeGeom &g, int B, std::vector<float> &W, int &use) {
+  int n = 2 * B;
+  W.assign((size_t)n * n, 1.0f);
+  if (!g.full_wedge()) {
+    double v1[3], v2[3];
+    wedge_vectors(g, nullptr, v1, v2);
+    float phiK = (float)(M_PI / (n - 1)), thetaK = (float)(2.0 * M_PI / (n - 1));
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        float cj = cosf(j * thetaK), sj = sinf(j * thetaK), si = sinf(i * phiK), ci = cosf(i * phiK);
+        double a = v1[0] * cj * si + v1[1] * sj * si + v1[2] * ci;
+        double b = v2[0] * cj * si + v2[1] * sj * si + v2[2] * ci;
+        W[(size_t)i * n + j] = (a * b <= 0.0) ? 1.0f : 0.0f;
+      }
+  }
+  std::vector<float> t((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) t[i + (size_t)n * j] = W[(size_t)i * n + j];
+  int dims[3] = {n, n, 1};
+  gaussian_smooth(t, dims, 2.0, 1.0);
+  double s = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      W[(size_t)i * n + j] = t[i + (size_t)n * j];
+      s += W[(size_t)i * n + j];
+    }
+  use = s <= (double)(.95f * (float)(n * n));
+}
+
+// nbfWedge3D::getImageHalf for the reference (no transform), host side
+void wedge_half_host(const VolumeGeom &g, int N, std::vector<float> &W) {
+  int H = N / 2 + 1;
+  W.assign((size_t)N * N * H, 1.0f);
+  if (g.full_wedge()) return;
+  double v1[3], v2[3];
+  wedge_vectors(g, nullptr, v1, v2);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < H; ++k) {
+        double a = v1[0] * (i - N / 2) + v1[1] * (j - N / 2) + v1[2] * (k - (H - 1));
+        double b = v2[0] * (i - N / 2) + v2[1] * (j - N / 2) + v2[2] * (k - (H - 1));
+        W[((size_t)i * N + j) * H + k] = (a * b <= 0.0) ? 1.0f : 0.0f;
+      }
+  std::vector<float> t(W.size());
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < H; ++k) t[i + (size_t)N * (j + (size_t)N * k)] = W[((size_t)i * N + j) * H + k];
+  int dims[3] = {N, N, H};
+  gaussian_smooth(t, dims, 2.0, 0.5);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < H; ++k) W[((size_t)i * N + j) * H + k] = t[i + (size_t)N * (j + (size_t)N * k)];
+}
+
+bool finite_volume(const float *v, long n) {
+  for (long i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+template <class F>
+int guarded(ettk_ctx *c, F fn) {
+  try {
+    if (c) CK(cudaSetDevice(c->device));
+    fn();
+    return ETTK_OK;
+  } catch (const CudaError &e) {
+    return fail(c, e.code, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(c, ETTK_ERR_OOM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(c, ETTK_ERR_CUDA, e.what());
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **out) {
+  if (!params || !out) return ETTK_ERR_ARG;
+  *out = nullptr;
+  const ettk_params &p = *params;
+  if (!pow2(p.N) || p.N < 16 || p.N > 128 || !(p.B == 8 || p.B == 16 || p.B == 32 || p.B == 64) ||
+      p.mutual_correlation != 0 || p.candidate_peaks < 1 || p.number_of_candidates < 1)
+    return ETTK_ERR_ARG;
+  ettk_ctx *c = new (std::nothrow) ettk_ctx;
+  if (!c) return ETTK_ERR_OOM;
+  c->device = device;
+  c->p = p;
+  int rc = guarded(c, [&] {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    c->init_tables();
+  });
+  if (rc != ETTK_OK) {
+    ettk_gpu_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return ETTK_OK;
+}
+
+int ettk_gpu_destroy(ettk_ctx *c) {
+  if (!c) return ETTK_OK;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
+                         &c->W1half, &c->Pp1, &c->W1sph, &c->partvol, &c->W2sph, &c->Pp2, &c->w_r, &c->w_v,
+                         &c->w_fw, &c->w_tmp, &c->w_tmp2, &c->w_C, &c->w_q1, &c->w_q2, &c->w_sig, &c->w_norm,
+                         &c->w_norm2, &c->sp_v, &c->sp_M, &c->sp_padc, &c->sp_Pp};
+  for (auto b : fb) b->release();
+  DevBuf<float2> *cb[] = {&c->Fm1, &c->FI1, &c->w_cA, &c->w_cB, &c->w_cC, &c->w_p1, &c->w_p2, &c->w_coef, &c->w_S, &c->sp_F};
+  for (auto b : cb) b->release();
+  c->w_acc.release();
+  c->w_w.release();
+  c->sp_acc.release();
+  c->w_peak.release();
+  c->w_mm.release();
+  c->doff.release();
+  c->dirs.release();
+  c->w_items.release();
+  c->w_wv.release();
+  c->w_idx.release();
+  c->w_idx2.release();
+  c->w_cnt.release();
+  c->w_active.release();
+  c->w_pair_ref.release();
+  c->w_pair_pp2.release();
+  c->w_pair_part.release();
+  c->w_lists.release();
+  c->w_out.release();
+  c->w_sd.release();
+  c->w_jobs.release();
+  c->w_sjobs.release();
+  c->w_plans.release();
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return ETTK_OK;
+}
+
+int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_volume_meta *meta) {
+  if (!c || R <= 0 || !vols || !meta) return fail(c, ETTK_ERR_ARG, "invalid reference arguments");
+  if (!finite_volume(vols, (long)R * c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite reference volume");
+  return guarded(c, [&] {
+    long n3 = c->n3, h3 = c->h3;
+    c->R = R;
+    c->refg.resize(R);
+    c->useW1.resize(R);
+    c->refvol.ensure(R * n3);
+    CK(cudaMemcpy(c->refvol.p, vols, R * n3 * 4, cudaMemcpyHostToDevice));
+    std::vector<ResliceItem> items(R);
+    std::vector<float> w1h((size_t)R * h3), w1s((size_t)R * c->nn);
+    for (int r = 0; r < R; ++r) {
+      c->refg[r] = to_geom(meta[r]);
+      double m12[12];
+      reslice_index(c->refg[r], c->N, nullptr, m12);
+      items[r].vol = c->refvol.p + (long)r * n3;
+      items[r].dims[0] = items[r].dims[1] = items[r].dims[2] = c->N;
+      for (int k = 0; k < 12; ++k) items[r].m[k] = (float)m12[k];
+      std::vector<float> w;
+      wedge_half_host(c->refg[r], c->N, w);
+      std::copy(w.begin(), w.end(), w1h.begin() + (size_t)r * h3);
+      int use = 0;
+      spherical_wedge_host(c->refg[r], c->B, w, use);
+      std::copy(w.begin(), w.end(), w1s.begin() + (size_t)r * c->nn);
+      c->useW1[r] = use;
+    }
+    c->W1half.ensure(R * h3);
+    c->W1sph.ensure(R * c->nn);
+    CK(cudaMemcpy(c->W1half.p, w1h.data(), R * h3 * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->W1sph.p, w1s.data(), R * c->nn * 4, cudaMemcpyHostToDevice));
+    // I1 = getImage(reference): reslice, mean of valid voxels removed; F_I1 = R2C(I1 maskfft shift)
+    c->w_v.ensure(R * n3);
+    c->w_acc.ensure(R * 2);
+    c->w_items.ensure(R);
+    CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
+    k_reslice<<<dim3(nblocks<int>(n3, 256, 512), R), 256, 0, c->st>>>(c->w_items.p, c->N, c->w_v.p, c->w_acc.p, 2);
+    c->post_launch();
+    c->FI1.ensure(R * h3);
+    PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
+    c->r2c_z(c->N, pre, c->FI1.p, (long)R * c->N * c->N);
+    c->xy_passes(c->N, c->FI1.p, R, -1, false);
+    // Pp1 = cartesianToSpherical(I1)
+    c->Pp1.ensure(R * c->nn);
+    c->spherical_projection(items, c->Pp1.p);
+    c->sync();
+  });
+}
+
+static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_volume_meta *meta, bool device) {
+  if (!c || V <= 0 || !vols || !meta) return fail(c, ETTK_ERR_ARG, "invalid particle arguments");
+  if (!device && !finite_volume(vols, (long)V * c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite particle volume");
+  return guarded(c, [&] {
+    long n3 = c->n3;
+    c->V = V;
+    c->partg.resize(V);
+    c->useW2.resize(V);
+    c->pp2_ready.assign(V, 0);
+    if (device) {
+      c->partptr = vols;
+    } else {
+      c->partvol.ensure(V * n3);
+      CK(cudaMemcpyAsync(c->partvol.p, vols, V * n3 * 4, cudaMemcpyHostToDevice, c->st));
+      c->partptr = c->partvol.p;
+    }
+    std::vector<float> w2s((size_t)V * c->nn);
+    for (int v = 0; v < V; ++v) {
+      c->partg[v] = to_geom(meta[v]);
+      std::vector<float> w;
+      int use = 0;
+      spherical_wedge_host(c->partg[v], c->B, w, use);
+      std::copy(w.begin(), w.end(), w2s.begin() + (size_t)v * c->nn);
+      c->useW2[v] = use;
+    }
+    c->W2sph.ensure(V * c->nn);
+    CK(cudaMemcpyAsync(c->W2sph.p, w2s.data(), V * c->nn * 4, cudaMemcpyHostToDevice, c->st));
+    c->Pp2.ensure(V * c->nn);
+    c->sync();
+  });
+}
+
+int ettk_gpu_set_particles(ettk_ctx *c, int V, const float *vols, const ettk_volume_meta *meta) {
+  return set_particles_impl(c, V, vols, meta, false);
+}
+int ettk_gpu_set_particles_device(ettk_ctx *c, int V, const float *d_vols, const ettk_volume_meta *meta) {
+  return set_particles_impl(c, V, d_vols, meta, true);
+}
+
+int ettk_gpu_align_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, int cols, int ncand) {
+  if (!c || npairs < 0 || (npairs && (!pairs || !D)) || cols < 17 || ncand < 1)
+    return fail(c, ETTK_ERR_ARG, "invalid align arguments");
+  if (c->R == 0 || c->V == 0) return fail(c, ETTK_ERR_STATE, "references and particles must be set first");
+  return guarded(c, [&] { c->align(npairs, pairs, D, cols, ncand); });
+}
+
+int ettk_gpu_ccf(ettk_ctx *c, int r, int p, double *t, float *dist) {
+  if (!c || !t || !dist) return fail(c, ETTK_ERR_ARG, "invalid ccf arguments");
+  if (r < 0 || r >= c->R || p < 0 || p >= c->V) return fail(c, ETTK_ERR_STATE, "volume index out of range");
+  return guarded(c, [&] {
+    EvalReq q;
+    q.ref = r;
+    q.part = p;
+    memcpy(q.t.e, t, sizeof(q.t.e));
+    std::vector<EvalRes> res;
+    c->eval_batch({q}, res);
+    *dist = res[0].dist;
+    memcpy(t, res[0].t.e, sizeof(res[0].t.e));
+  });
+}
+
+int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
+  if (!c || !Pp) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] {
+    ResliceItem it;
+    double m12[12];
+    if (p >= 0) {
+      if (p >= c->V) throw CudaError(ETTK_ERR_STATE, "particle index out of range");
+      it.vol = c->partptr + (long)p * c->n3;
+      reslice_index(c->partg[p], c->N, nullptr, m12);
+    } else {
+      if (r < 0 || r >= c->R) throw CudaError(ETTK_ERR_STATE, "reference index out of range");
+      it.vol = c->refvol.p + (long)r * c->n3;
+      reslice_index(c->refg[r], c->N, nullptr, m12);
+    }
+    it.dims[0] = it.dims[1] = it.dims[2] = c->N;
+    for (int k = 0; k < 12; ++k) it.m[k] = (float)m12[k];
+    c->w_sig.ensure(c->nn);
+    c->spherical_projection({it}, c->w_sig.p);
+    CK(cudaMemcpyAsync(Pp, c->w_sig.p, c->nn * 4, cudaMemcpyDeviceToHost, c->st));
+    c->sync();
+  });
+}
+
+int ettk_gpu_soft(ettk_ctx *c, const float *F1, const float *F2, int scaled, float *C) {
+  if (!c || !F1 || !F2 || !C) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] { c->soft_diag(F1, F2, scaled, C); });
+}
+
+long long ettk_gpu_kernel_launches(ettk_ctx *c) { return c ? c->launches : 0; }
+
+void *ettk_gpu_stream(ettk_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+int ettk_gpu_profile(ettk_ctx *c, int enable) {
+  if (!c) return ETTK_ERR_ARG;
+  return guarded(c, [&] {
+    c->sync();
+    c->prof = enable != 0;
+    c->prof_agg.clear();
+  });
+}
+
+int ettk_gpu_profile_read(ettk_ctx *c, int index, char *name, int name_size, long long *launches, double *total_ms,
+                          double *bytes) {
+  if (!c || index < 0) return ETTK_ERR_ARG;
+  if (index >= (int)c->prof_agg.size()) return ETTK_ERR_ARG;
+  auto it = c->prof_agg.begin();
+  std::advance(it, index);
+  if (name && name_size > 0) snprintf(name, name_size, "%s", it->first.c_str());
+  if (launches) *launches = it->second.n;
+  if (total_ms) *total_ms = it->second.ms;
+  if (bytes) *bytes = it->second.bytes;
+  return ETTK_OK;
+}
+
+int ettk_gpu_last_error(ettk_ctx *c, char *buf, int size) {
+  if (!buf || size <= 0) return ETTK_ERR_ARG;
+  const char *m = c ? c->err.c_str() : "no context";
+  snprintf(buf, size, "%s", m);
+  return ETTK_OK;
+}
+
+}  // extern "C"

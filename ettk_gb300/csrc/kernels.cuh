@@ -1,0 +1,697 @@
+// Device kernels of the alignment path (FP32 arithmetic, FP64 reductions).
+// Each kernel names the reference step it computes.
+#pragma once
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace ettk {
+
+// Per-item reslice input: the fixed image, its dims and the output-index -> input-index map.
+struct ResliceItem {
+  const float *vol;
+  int dims[3];
+  float m[12];  // origin[3], x axis[3], y axis[3], z axis[3]
+};
+
+// nbfWedgedSubImage3D::getImage (inc/em/nbfWedgedSubImage3D.h:602-828): tricubic reslice of the
+// fixed image under Euler*matrix*t into an N^3 box (output [x][y][z], z fastest), background
+// -FLT_MAX outside [-0.5, dim-0.5] (vtkImageReslice border 1, clamp mode), plus per-item sums
+// of valid values and their count into acc[item*acc_stride + 0/1].
+__global__ void k_reslice(const ResliceItem *__restrict__ items, int N, float *__restrict__ out, double *acc,
+                          int acc_stride) {
+  __shared__ double sh[32];
+  const ResliceItem it = items[blockIdx.y];
+  long n3 = (long)N * N * N;
+  double s = 0, c = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    int a = (int)(id / ((long)N * N)), b = (int)((id / N) % N), cz = (int)(id % N);
+    float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
+    p0 = p0 + b * it.m[6];
+    p1 = p1 + b * it.m[7];
+    p2 = p2 + b * it.m[8];
+    p0 = p0 + a * it.m[3];
+    p1 = p1 + a * it.m[4];
+    p2 = p2 + a * it.m[5];
+    float val = -FLT_MAX;
+    const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
+    if (!(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f)) {
+      float fx, fy, fz;
+      int ix = vtk_floor(p0, fx), iy = vtk_floor(p1, fy), iz = vtk_floor(p2, fz);
+      float wx[4], wy[4], wz[4];
+      cubic_weights(wx, fx);
+      cubic_weights(wy, fy);
+      cubic_weights(wz, fz);
+      int mY = (dy > 1) && (fy != 0.f), mZ = (dz > 1) && (fz != 0.f);
+      int j1 = 1 - mY, j2 = 1 + 2 * mY, k1 = 1 - mZ, k2 = 1 + 2 * mZ;
+      if (!mY) wy[1] = 1.f;
+      if (!mZ) wz[1] = 1.f;
+      int xs[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) xs[t] = min(max(ix - 1 + t, 0), dx - 1);
+      float acc2 = 0.f;
+      for (int k = k1; k <= k2; ++k) {
+        int zz = min(max(iz - 1 + k, 0), dz - 1);
+        for (int j = j1; j <= j2; ++j) {
+          int yy = min(max(iy - 1 + j, 0), dy - 1);
+          const float *row = it.vol + ((long)zz * dy + yy) * dx;
+          acc2 += (wz[k] * wy[j]) * (wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
+                                     wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]));
+        }
+      }
+      val = acc2;
+      s += val;
+      c += 1;
+    }
+    out[(long)blockIdx.y * n3 + id] = val;
+  }
+  if (acc) {
+    double bs = block_sum(s, sh), bc = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 0], bs);
+      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 1], bc);
+    }
+  }
+}
+
+// Binary wedge on the centred half grid (nbfWedge3D::getImageHalf, inc/em/nbfWedge3D.h:312-356):
+// ((v1.d)(v2.d) <= 0) with d = (i-N/2, j-N/2, k-N/2). Near the planes the test is redone in FP64
+// with the reference's operation order (no FMA) so exact-zero cases resolve as they do there.
+struct WedgeVecs {
+  double v1[3], v2[3];
+  int full;
+};
+__global__ void k_wedge_binary(const WedgeVecs *__restrict__ wv, int N, float *__restrict__ out) {
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H;
+  const WedgeVecs w = wv[blockIdx.y];
+  float f1[3] = {(float)w.v1[0], (float)w.v1[1], (float)w.v1[2]}, f2[3] = {(float)w.v2[0], (float)w.v2[1], (float)w.v2[2]};
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    float r = 1.f;
+    if (!w.full) {
+      int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+      float di = (float)(i - N / 2), dj = (float)(j - N / 2), dk = (float)(k - (H - 1));
+      float a = f1[0] * di + f1[1] * dj + f1[2] * dk, b = f2[0] * di + f2[1] * dj + f2[2] * dk;
+      if (fabsf(a) > 1e-3f && fabsf(b) > 1e-3f) {
+        r = (a * b <= 0.f) ? 1.f : 0.f;
+      } else {
+        double ad = __dadd_rn(__dadd_rn(__dmul_rn(w.v1[0], (double)di), __dmul_rn(w.v1[1], (double)dj)),
+                              __dmul_rn(w.v1[2], (double)dk));
+        double bd = __dadd_rn(__dadd_rn(__dmul_rn(w.v2[0], (double)di), __dmul_rn(w.v2[1], (double)dj)),
+                              __dmul_rn(w.v2[2], (double)dk));
+        r = (__dmul_rn(ad, bd) <= 0.0) ? 1.f : 0.f;
+      }
+    }
+    out[(long)blockIdx.y * h3 + id] = r;
+  }
+}
+
+// One axis of vtkImageGaussianSmooth with std 2 and radius 1 (nbfWedge3D::smoothWedgeImage,
+// inc/em/nbfWedge3D.h:431-445) on [item][N][N][H] arrays; axis 2 = k (VTK z, first pass),
+// 1 = j, 0 = i. The final pass (axis 0) multiplies by the reference wedge and the filter
+// (wedge2 *= wedge1; filter*wedge, inc/em/nbfFourierImageMetric.h:1101-1113, nbfFourierFilter.h:586-606)
+// and accumulates sum(wedge*filter) for the overlap normalisation.
+struct Smooth3 {
+  float w_int[3];   // interior weights (-1, 0, +1)
+  float w_lo[2];    // at index 0: (0, +1)
+  float w_hi[2];    // at last index: (-1, 0)
+};
+__global__ void k_wedge_smooth(const float *__restrict__ in, float *__restrict__ out, int N, int axis, Smooth3 sw,
+                               const float *__restrict__ w1, const int *__restrict__ w1_index,
+                               const float *__restrict__ filter, double *acc, int acc_stride, int acc_slot) {
+  __shared__ double sh[32];
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H;
+  const float *src = in + (long)blockIdx.y * h3;
+  double s = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+    int pos = axis == 2 ? k : (axis == 1 ? j : i);
+    int n = axis == 2 ? H : N;
+    long st = axis == 2 ? 1 : (axis == 1 ? H : (long)N * H);
+    float v;
+    if (n == 1) v = src[id];
+    else if (pos == 0) v = sw.w_lo[0] * src[id] + sw.w_lo[1] * src[id + st];
+    else if (pos == n - 1) v = sw.w_hi[0] * src[id - st] + sw.w_hi[1] * src[id];
+    else v = sw.w_int[0] * src[id - st] + sw.w_int[1] * src[id] + sw.w_int[2] * src[id + st];
+    if (axis == 0) {
+      float wedge = v * w1[(long)w1_index[blockIdx.y] * h3 + id];
+      float fw = filter[id] * wedge;
+      s += (double)fw;
+      v = fw;
+    }
+    out[(long)blockIdx.y * h3 + id] = v;
+  }
+  if (axis == 0) {
+    double b = block_sum(s, sh);
+    if (threadIdx.x == 0) atomicAdd(&acc[(long)blockIdx.y * acc_stride + acc_slot], b);
+  }
+}
+
+// executeHalf + normalizeFourierHalf accumulation (inc/em/nbfFourierFilter.h:586-606,
+// inc/em/nbfCorrelationImageMetric.h:497-530): out = src * fw, DC zeroed, sums of |F|^2 for
+// k < H-1 (slot) and k = H-1 (slot+1). src item index through src_index (nullptr = same item).
+__global__ void k_spec_filter(const float2 *__restrict__ src, const int *__restrict__ src_index,
+                              const float *__restrict__ fw, float2 *__restrict__ out, int N, double *acc,
+                              int acc_stride, int slot) {
+  __shared__ double sh[32];
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H;
+  long sidx = src_index ? (long)src_index[blockIdx.y] : (long)blockIdx.y;
+  const float2 *S = src + sidx * h3;
+  long dc = ((long)(N / 2) * N + N / 2) * H + (H - 1);
+  double s1 = 0, s2 = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    float2 v = cscale(S[id], fw[(long)blockIdx.y * h3 + id]);
+    if (id == dc) v = make_float2(0.f, 0.f);
+    out[(long)blockIdx.y * h3 + id] = v;
+    double m = (double)v.x * v.x + (double)v.y * v.y;
+    if ((id % H) < H - 1) s1 += m; else s2 += m;
+  }
+  double b1 = block_sum(s1, sh), b2 = block_sum(s2, sh);
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot], b1);
+    atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot + 1], b2);
+  }
+}
+
+// norm of normalizeFourierHalf with its float roundings: norm = float(2*s1);
+// norm = float(sqrt((norm + s2) / (N*N*2*(H-1)))). Writes 1/norm (and norm) per item.
+__global__ void k_norms(const double *acc, int acc_stride, int slot, int N, int n_items, float *inv_norm,
+                        float *norm_out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_items) return;
+  const int H = N / 2 + 1;
+  double s1 = acc[(long)e * acc_stride + slot], s2 = acc[(long)e * acc_stride + slot + 1];
+  float nrm = (float)(2.0 * s1);
+  nrm = (float)sqrt(((double)nrm + s2) / (1.0 * N * N * 2 * (H - 1)));
+  inv_norm[e] = nrm > 0.f ? 1.0f / nrm : 0.f;
+  if (norm_out) norm_out[e] = nrm;
+}
+
+// ---- R2C z-pass input functors ------------------------------------------------------------
+
+// y1 * m1 with the accumulation k1_m = sum(y1^2 m1) (inc/em/nbfFourierImageMetric.h:1143-1153).
+struct PreY1M1 {
+  const float *y;
+  const float *m1;
+  int N;
+  double *acc;
+  int acc_stride, slot;
+  double s;
+  ETTK_DEV void begin() { s = 0; }
+  ETTK_DEV float operator()(long line, int k) {
+    long n2 = (long)N * N;
+    long e = line / n2, r = line - e * n2;
+    float v = y[line * N + k];
+    float m = m1[r * N + k];
+    s += (double)v * (double)v * (double)m;
+    return v * m;
+  }
+  ETTK_DEV void end() {
+    __shared__ double shm[32];
+    double b = block_sum(s, shm);
+    if (threadIdx.x == 0) atomicAdd(&acc[item_of_block() * acc_stride + slot], b);
+  }
+  long lines_per_block;  // real lines handled by one CTA (never straddles two items)
+  ETTK_DEV long item_of_block() const { return ((long)blockIdx.x * lines_per_block) / ((long)N * N); }
+};
+
+// Resliced particle: (valid ? v - meanInside : 0) * maskfft * shift
+// (nbfWedgedSubImage3D.h:794-802 then nbfFourierImageMetric.h:1165-1166).
+struct PreParticle {
+  const float *v;
+  const float *maskfft;
+  const double *acc;
+  int acc_stride, N;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV float operator()(long line, int k) {
+    long n2 = (long)N * N;
+    long e = line / n2, r = line - e * n2;
+    float val = v[line * N + k];
+    float out = 0.f;
+    if (val > -FLT_MAX) {
+      float cnt = (float)acc[e * acc_stride + 1];
+      float mean = (float)(acc[e * acc_stride + 0] / (double)cnt);
+      out = val - mean;
+    }
+    int i = (int)(r / N), j = (int)(r % N);
+    return out * maskfft[r * N + k] * parity_sign(i, j, k);
+  }
+};
+
+// y2^2 * shift (nbfFourierImageMetric.h:1188-1190)
+struct PreSquareShift {
+  const float *y;
+  int N;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV float operator()(long line, int k) {
+    long r = line % ((long)N * N);
+    int i = (int)(r / N), j = (int)(r % N);
+    float v = y[line * N + k];
+    return v * v * parity_sign(i, j, k);
+  }
+};
+
+// Generic: src * aux * shift over one N^3 volume per item (the constant transforms of the
+// reference and of the mask: R2C(I1*maskfft*shift), R2C(m1*shift)).
+struct PreProductShift {
+  const float *src;  // per item N^3 (nullptr -> 1)
+  const float *aux;  // shared N^3 (nullptr -> 1)
+  int N;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV float operator()(long line, int k) {
+    long r = line % ((long)N * N);
+    int i = (int)(r / N), j = (int)(r % N);
+    float a = src ? src[line * N + k] : 1.f;
+    float b = aux ? aux[r * N + k] : 1.f;
+    return a * b * parity_sign(i, j, k);
+  }
+};
+
+// Store real output of a C2R z-pass.
+struct PostStore {
+  float *y;
+  int N;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v; }
+};
+
+// FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3), stored over FFT1re (nbfFourierImageMetric.h:1174-1177).
+__global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict__ f2, const float *__restrict__ inv_norm2,
+                         int N) {
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H;
+  float sc = inv_norm2[blockIdx.y] * (float)((long)N * N * N);
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    long g = (long)blockIdx.y * h3 + id;
+    float2 b = cscale(f2[g], sc);
+    a[g] = cscale(cmul(a[g], cconj(b)), 2.0f);
+  }
+}
+
+// FFTre = (-F(m1) conj(F(I2'^2)) + FFT2re) * shiftr, times the zero-padding factor 8
+// (nbfFourierImageMetric.h:1192-1210: FFTre holds F(m1) and FFT1re holds F(I2'^2) there). In place over q.
+__global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict__ fm1, const float2 *__restrict__ fft2re, int N,
+                        float factor) {
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    long g = (long)blockIdx.y * h3 + id;
+    int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+    float2 v = cadd(cscale(cmul(fm1[id], cconj(q[g])), -1.f), fft2re[g]);
+    q[g] = cscale(v, parity_sign(i, j, k) * factor);
+  }
+}
+
+// Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
+// [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
+// and reads only this window). Same FFTW order: complex inverse along x, then y, then the
+// half-complex-to-real sum along z (real parts only for the kz=N term).
+// Stage x: q1[e][X][ky][kz] = sum_kx q[e][kx][ky][kz] exp(+2 pi i (kx+o0) (lo+X) / 2N)
+__global__ void k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N, int W, int lo, int o0) {
+  const int H = N / 2 + 1;
+  long nrow = (long)N * H;  // (ky,kz) per X
+  long total = (long)W * nrow;
+  const float2 *Q = q + (long)blockIdx.y * N * nrow;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+    int X = (int)(id / nrow);
+    long r = id - (long)X * nrow;
+    int XX = lo + X;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int kx = 0; kx < N; ++kx) {
+      int ph = ((kx + o0) * XX) % (2 * N);
+      float s, c;
+      sincospif((float)ph / (float)N, &s, &c);
+      acc = cadd(acc, cmul(Q[(long)kx * nrow + r], make_float2(c, s)));
+    }
+    q1[(long)blockIdx.y * total + id] = acc;
+  }
+}
+// Stage y: q2[e][X][Y][kz] = sum_ky q1[e][X][ky][kz] exp(+2 pi i (ky+o0)(lo+Y)/2N)
+__global__ void k_pruned_y(const float2 *__restrict__ q1, float2 *__restrict__ q2, int N, int W, int lo, int o0) {
+  const int H = N / 2 + 1;
+  long total = (long)W * W * H;
+  const float2 *Q = q1 + (long)blockIdx.y * W * N * H;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+    int X = (int)(id / ((long)W * H)), Y = (int)((id / H) % W), kz = (int)(id % H);
+    int YY = lo + Y;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int ky = 0; ky < N; ++ky) {
+      int ph = ((ky + o0) * YY) % (2 * N);
+      float s, c;
+      sincospif((float)ph / (float)N, &s, &c);
+      acc = cadd(acc, cmul(Q[((long)X * N + ky) * H + kz], make_float2(c, s)));
+    }
+    q2[(long)blockIdx.y * total + id] = acc;
+  }
+}
+// Stage z + peak: T = out * shift / (2N)^3 inside the sphere radius^2 < r^2 (else -max);
+// packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
+__global__ void k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo, int o2, float rr2,
+                                unsigned long long *peak) {
+  const int H = N / 2 + 1;
+  long total = (long)W * W * W;
+  const float2 *Q = q2 + (long)blockIdx.y * W * W * H;
+  const float inv = 1.0f / (float)(8L * N * N * N);
+  unsigned long long best = 0;
+  int half = (W - 1) / 2;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+    int X = (int)(id / ((long)W * W)), Y = (int)((id / W) % W), Z = (int)(id % W);
+    int ZZ = lo + Z;
+    const float2 *row = Q + ((long)X * W + Y) * H;
+    float acc = 0.f;
+    for (int kz = 0; kz < H; ++kz) {
+      int KZ = kz + o2;
+      int ph = (KZ * ZZ) % (2 * N);
+      float s, c;
+      sincospif((float)ph / (float)N, &s, &c);
+      float2 v = row[kz];
+      float re = v.x * c - v.y * s;
+      acc += (KZ == N || KZ == 0) ? re : 2.f * re;
+    }
+    float T = acc * parity_sign(lo + X, lo + Y, ZZ) * inv;
+    float rad = (float)((half - X) * (half - X) + (half - Y) * (half - Y) + (half - Z) * (half - Z));
+    if (!(rad < rr2)) T = -FLT_MAX;
+    unsigned long long key = pack_max(T, (uint32_t)id);
+    best = key > best ? key : best;
+  }
+  best = warp_max_u64(best);
+  if ((threadIdx.x & 31) == 0) atomicMax(&peak[blockIdx.y], best);
+}
+
+// Final CCF distance and half-voxel shift (nbfFourierImageMetric.h:1249-1264).
+struct EvalOut {
+  float dist;
+  float shift[3];
+};
+__global__ void k_score(const double *acc, int acc_stride, const unsigned long long *peak, int n_items, int W,
+                        double sum_filter, int overlap, int use_wedge, int N, EvalOut *out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_items) return;
+  unsigned long long key = peak[e];
+  float T = ordered_to_float((uint32_t)(key >> 32));
+  uint32_t idx = 0xffffffffu - (uint32_t)(key & 0xffffffffu);
+  const double *a = acc + (long)e * acc_stride;
+  float k1_m = (float)a[4];
+  double big = 8.0 * N * N * N;
+  double pk;
+  if (overlap && use_wedge) pk = fmax(0.0, (double)k1_m - (double)T) / a[6] * sum_filter;
+  else pk = fmax(0.0, (double)k1_m - (double)T);
+  EvalOut o;
+  o.dist = (float)(pk / big / big);
+  int X = idx / (W * W), Y = (idx / W) % W, Z = idx % W;
+  o.shift[0] = (float)((X - (W - 1) / 2.0) / 2.0f);
+  o.shift[1] = (float)((Y - (W - 1) / 2.0) / 2.0f);
+  o.shift[2] = (float)((Z - (W - 1) / 2.0) / 2.0f);
+  out[e] = o;
+}
+
+// ---- spherical projection ------------------------------------------------------------------
+
+// mean over all voxels of the mean-subtracted particle (nbfImageFilter::execute meanValue,
+// inc/em/nbfImageFilter.h:255) -> acc[slot]
+__global__ void k_mean_all(const float *__restrict__ v, const double *acc_in, int acc_stride, int N, double *acc_out,
+                           int slot) {
+  __shared__ double sh[32];
+  long n3 = (long)N * N * N;
+  const double *a = acc_in + (long)blockIdx.y * acc_stride;
+  float mean = (float)(a[0] / (double)(float)a[1]);
+  double s = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    float x = v[(long)blockIdx.y * n3 + id];
+    s += (x > -FLT_MAX) ? (double)(x - mean) : 0.0;
+  }
+  double b = block_sum(s, sh);
+  if (threadIdx.x == 0) atomicAdd(&acc_out[(long)blockIdx.y * acc_stride + slot], b);
+}
+
+// Padded, windowed, shifted (2N)^3 input of cartesianToSpherical (inc/em/nbfProjectionRotationMetric3D.h:271-318):
+// x<N,y<N,z<N: (img - meanAll)*mask + meanAll; elsewhere the corner value; times (-1)^(x+y+z).
+struct PrePadded {
+  const float *v;
+  const float *mask;
+  const double *acc;
+  int acc_stride, N;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV float windowed(long e, long id) const {
+    const double *a = acc + e * acc_stride;
+    float mean = (float)(a[0] / (double)(float)a[1]);
+    float meanAll = (float)(a[2] / (double)((long)N * N * N));
+    float x = v[e * (long)N * N * N + id];
+    float img = (x > -FLT_MAX) ? x - mean : 0.f;
+    return (img - meanAll) * mask[id] + meanAll;
+  }
+  ETTK_DEV float operator()(long line, int z) {
+    const int N2 = 2 * N;
+    long per = (long)N2 * N2;
+    long e = line / per, r = line - e * per;
+    int x = (int)(r / N2), y = (int)(r % N2);
+    float val = (x < N && y < N && z < N) ? windowed(e, ((long)x * N + y) * N + z) : windowed(e, 0);
+    return val * parity_sign(x, y, z);
+  }
+};
+
+// |F| of the (2N)^3 half spectrum (inc/em/nbfProjectionRotationMetric3D.h:321-325)
+__global__ void k_magnitude(const float2 *__restrict__ F, float *__restrict__ M, long n) {
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+    float2 f = F[id];
+    M[id] = sqrtf(f.x * f.x + f.y * f.y);
+  }
+}
+
+// Virtual Hermitian-completed magnitude cube (lines 327-338): z <= N from the half spectrum,
+// x = 0 plane zero, z > N mirrored through (N,N,N) except the y = 0 plane which keeps the
+// padded real-space value (the corner value).
+ETTK_DEV float mag_at(const float *Mh, int N, int x, int y, int z, float padc) {
+  const int N2 = 2 * N, H = N + 1;
+  if (x == 0) return 0.f;
+  if (z <= N) return Mh[((long)x * N2 + y) * H + z];
+  if (y == 0) return padc;
+  return Mh[((long)(N2 - x) * N2 + (N2 - y)) * H + (N2 - z)];
+}
+
+// Cubic resampling on radial shells through vtkSphericalTransform with wrap, summed over the
+// radii [bandL, bandU] (lines 359-406): Pp[e][j][k] for polar j, azimuth k.
+__global__ void k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs, int n_dirs, int N,
+                                int bandL, int bandU, const float *__restrict__ padc, float *__restrict__ Pp) {
+  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= n_dirs) return;
+  const int e = blockIdx.y, N2 = 2 * N;
+  const float *M = Mh + (long)e * N2 * N2 * (N + 1);
+  float4 u = dirs[d];
+  float pc = padc[e];
+  float acc = 0.f;
+  for (int r = bandL; r <= bandU; ++r) {
+    float p[3] = {r * u.x + (float)N, r * u.y + (float)N, r * u.z + (float)N};
+    float f[3];
+    int ii[3];
+    for (int t = 0; t < 3; ++t) ii[t] = vtk_floor(p[t], f[t]);
+    float wx[4], wy[4], wz[4];
+    cubic_weights(wx, f[0]);
+    cubic_weights(wy, f[1]);
+    cubic_weights(wz, f[2]);
+    int mY = f[1] != 0.f, mZ = f[2] != 0.f;
+    int j1 = 1 - mY, j2 = 1 + 2 * mY, k1 = 1 - mZ, k2 = 1 + 2 * mZ;
+    if (!mY) wy[1] = 1.f;
+    if (!mZ) wz[1] = 1.f;
+    int xs[4];
+    for (int t = 0; t < 4; ++t) xs[t] = ((ii[0] - 1 + t) % N2 + N2) % N2;
+    float v = 0.f;
+    for (int k = k1; k <= k2; ++k) {
+      int zz = ((ii[2] - 1 + k) % N2 + N2) % N2;
+      for (int j = j1; j <= j2; ++j) {
+        int yy = ((ii[1] - 1 + j) % N2 + N2) % N2;
+        v += (wz[k] * wy[j]) * (wx[0] * mag_at(M, N, xs[0], yy, zz, pc) + wx[1] * mag_at(M, N, xs[1], yy, zz, pc) +
+                                wx[2] * mag_at(M, N, xs[2], yy, zz, pc) + wx[3] * mag_at(M, N, xs[3], yy, zz, pc));
+      }
+    }
+    acc += v;
+  }
+  Pp[(long)e * n_dirs + d] = acc;
+}
+
+// Corner value of the windowed image (the pad constant).
+__global__ void k_pad_constant(PrePadded pre, int n_items, float *padc) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n_items) padc[e] = pre.windowed(e, 0);
+}
+
+// ---- SO(3) stage ---------------------------------------------------------------------------
+
+// Forward S^2 transform of real signals [J][2B][2B] -> coef[J][l][m] (m >= 0), one CTA per signal:
+// phi-FFT of each polar row then the quadrature sum with lw[m][l][j] = sqrt(2pi)/2B w_j P~_l^m(theta_j)
+// (SOFT FST_semi_memo, external/soft-1.0/FST_semi_memo.c:134-357).
+template <int B>
+__global__ void k_sht(const float *__restrict__ sig, const float *__restrict__ lw, float2 *__restrict__ coef) {
+  constexpr int n = 2 * B;
+  extern __shared__ float2 smem[];
+  float2 *tw = smem;
+  float2 *s = smem + n / 2;
+  load_twiddles<n>(tw);
+  const float *x = sig + (long)blockIdx.x * n * n;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    int j = idx / n, k = idx - j * n;
+    s[j * n + bitrev<n>(k)] = make_float2(x[idx], 0.f);
+  }
+  block_fft<n>(s, n, -1, tw);
+  float2 *out = coef + (long)blockIdx.x * B * B;
+  for (int idx = threadIdx.x; idx < B * B; idx += blockDim.x) {
+    int l = idx / B, m = idx - l * B;
+    float2 acc = make_float2(0.f, 0.f);
+    if (m <= l) {
+      const float *w = lw + ((long)m * B + l) * n;
+      for (int j = 0; j < n; ++j) acc = cadd(acc, cscale(s[j * n + m], w[j]));
+    }
+    out[idx] = acc;
+  }
+}
+
+ETTK_DEV float2 coef_at(const float2 *c, int B, int l, int m) {
+  // real-signal symmetry f(l,-m) = (-1)^m conj f(l,m)
+  if (m >= 0) return c[l * B + m];
+  float2 v = cconj(c[l * B - m]);
+  return ((-m) & 1) ? cscale(v, -1.f) : v;
+}
+
+// Wigner-d synthesis of the SO(3) correlation (so3CombineCoef_fftw, so3_correlate_fftw.c:103-162, and the
+// inverse Wigner transform of Inverse_SO3_Naive_fftw, soft_fftw.c:1045-1840):
+// S[job][b][m1][m2] = sum_l F^l_{m1 m2} dt^l_{m1 m2}(beta_b), F = f(l,-m1) conj(h(l,-m2)) (-1)^(m1+m2).
+// One CTA per (m1,m2) cell and block of jobs; the d table slice lives in shared memory.
+struct SynthJob {
+  int f, h;  // signal indices of the two coefficient sets
+};
+template <int B>
+__global__ void k_so3_synth(const float2 *__restrict__ coef, const SynthJob *__restrict__ jobs, int n_jobs,
+                            const float *__restrict__ dtab, const int *__restrict__ doff, float2 *__restrict__ S) {
+  constexpr int n = 2 * B;
+  __shared__ float sd[B * n];
+  __shared__ float2 sF[8][B];
+  int cell = blockIdx.x;
+  int m1 = cell / (2 * B - 1) - (B - 1), m2 = cell % (2 * B - 1) - (B - 1);
+  int l0 = max(abs(m1), abs(m2));
+  int L = B - l0;
+  const float *d = dtab + doff[cell];
+  for (int i = threadIdx.x; i < L * n; i += blockDim.x) sd[i] = d[i];
+  int sgn = ((m1 + m2) & 1) ? -1 : 1;
+  for (int j0 = blockIdx.y * 8; j0 < n_jobs; j0 += gridDim.y * 8) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * L; i += blockDim.x) {
+      int jl = i / L, l = l0 + (i - jl * L);
+      float2 F = make_float2(0.f, 0.f);
+      if (j0 + jl < n_jobs) {
+        SynthJob jb = jobs[j0 + jl];
+        float2 a = coef_at(coef + (long)jb.f * B * B, B, l, -m1);
+        float2 b = coef_at(coef + (long)jb.h * B * B, B, l, -m2);
+        F = cscale(cmul(a, cconj(b)), (float)sgn);
+      }
+      sF[jl][l - l0] = F;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * n; i += blockDim.x) {
+      int jl = i / n, b = i - jl * n;
+      if (j0 + jl >= n_jobs) continue;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int t = 0; t < L; ++t) acc = cadd(acc, cscale(sF[jl][t], sd[t * n + b]));
+      int mm1 = (m1 + n) % n, mm2 = (m2 + n) % n;
+      S[(((long)(j0 + jl) * n + b) * n + mm1) * n + mm2] = acc;
+    }
+  }
+}
+
+// Real part and scale (1/2B)(B/pi) of the alpha/gamma-transformed synthesis into C[job][a][b][g]
+// (soft_fftw.c:1913-1920; nbfProjectionRotationMetric3D.h:1254-1265), with packed min/max per job
+// in memory order (rotatedSphericalImageMinMax, 1557-1589).
+template <int B>
+__global__ void k_so3_real(const float2 *__restrict__ S, float *__restrict__ C, unsigned long long *mm) {
+  constexpr int n = 2 * B;
+  const long n3 = (long)n * n * n;
+  const int job = blockIdx.y;
+  const float scale = (1.0f / n) * ((float)B / 3.14159265358979f);
+  unsigned long long bmax = 0, bmin = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    int a = (int)(id / ((long)n * n)), b = (int)((id / n) % n), g = (int)(id % n);
+    float v = S[(((long)job * n + b) * n + a) * n + g].x * scale;
+    C[(long)job * n3 + id] = v;
+    unsigned long long kx = pack_max(v, (uint32_t)id), kn = pack_min(v, (uint32_t)id);
+    bmax = kx > bmax ? kx : bmax;
+    bmin = kn > bmin ? kn : bmin;
+  }
+  if (mm) {
+    bmax = warp_max_u64(bmax);
+    bmin = warp_max_u64(bmin);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&mm[2 * job + 0], bmin);
+      atomicMax(&mm[2 * job + 1], bmax);
+    }
+  }
+}
+
+// softScaled weights (nbfProjectionRotationMetric3D.h:1297-1319): rotate the pattern (coefficients h) to the
+// Euler angles of the min (which=0) / max (which=1) cell, synthesise it on the grid and return
+// sum(F1 * R * sin(theta)). Rotation: g(l,m) = sum_m' e^{-i m alpha} d^l_{m m'}(beta) e^{-i m' gamma} h(l,m')
+// (rotateFct, rotate_so3.c:695-741); R = (1/sqrt(2pi)) Re sum_{l,m} g(l,m) P~_l^m(theta_j) e^{i m phi_k}.
+struct ScaledJob {
+  int h;      // coefficient index of the pattern
+  int f1sig;  // signal index of F1
+  int job;    // correlation job (for the min/max cells)
+};
+template <int B>
+__global__ void k_so3_weights(const ScaledJob *__restrict__ sj, const unsigned long long *__restrict__ mm,
+                              const float2 *__restrict__ coef, const float *__restrict__ sig,
+                              const float *__restrict__ dtab, const int *__restrict__ doff, const float *__restrict__ plm,
+                              const float *__restrict__ sinth, double *w) {
+  constexpr int n = 2 * B;
+  __shared__ float2 g[B * B];
+  __shared__ double sh[32];
+  const ScaledJob J = sj[blockIdx.x];
+  const int which = blockIdx.y;
+  unsigned long long key = mm[2 * J.job + which];
+  uint32_t pos = 0xffffffffu - (uint32_t)(key & 0xffffffffu);
+  int a = pos / (n * n), b = (pos / n) % n, gg = pos % n;
+  float alpha = (float)(a / (double)B * 3.141592653589793), gamma = (float)(gg / (double)B * 3.141592653589793);
+  const float2 *h = coef + (long)J.h * B * B;
+  for (int idx = threadIdx.x; idx < B * B; idx += blockDim.x) {
+    int l = idx / B, m = idx - l * B;
+    float2 acc = make_float2(0.f, 0.f);
+    if (m <= l) {
+      float nl = rsqrtf((2.0f * l + 1.0f) * 0.5f);
+      for (int mp = -l; mp <= l; ++mp) {
+        int cell = (m + B - 1) * (2 * B - 1) + (mp + B - 1);
+        int l0 = max(abs(m), abs(mp));
+        float dv = dtab[doff[cell] + (l - l0) * n + b] * nl;
+        float s1, c1;
+        sincosf(-(m * alpha + mp * gamma), &s1, &c1);
+        acc = cadd(acc, cscale(cmul(make_float2(c1, s1), coef_at(h, B, l, mp)), dv));
+      }
+    }
+    g[idx] = acc;
+  }
+  __syncthreads();
+  const float *F1 = sig + (long)J.f1sig * n * n;
+  double s = 0;
+  const float inv = 0.3989422804014327f;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    int j = idx / n, k = idx - j * n;
+    float phi = 2.0f * 3.14159265358979f * k / n;
+    float r = 0.f;
+    for (int m = 0; m < B; ++m) {
+      float2 hm = make_float2(0.f, 0.f);
+      for (int l = m; l < B; ++l) hm = cadd(hm, cscale(g[l * B + m], plm[((long)m * B + l) * n + j]));
+      float sn, cs;
+      sincosf(m * phi, &sn, &cs);
+      float re = hm.x * cs - hm.y * sn;
+      r += (m == 0) ? re : 2.f * re;
+    }
+    r *= inv;
+    s += (double)F1[idx] * (double)r * (double)sinth[j];
+  }
+  double bsum = block_sum(s, sh);
+  if (threadIdx.x == 0) w[2 * blockIdx.x + which] = bsum;
+}
+
+}  // namespace ettk

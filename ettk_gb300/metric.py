@@ -1,0 +1,168 @@
+"""Host-side mirror of the reference's metric classes for the alignment path.
+
+`ProjectionRotationMetric3D` keeps the method names and argument meaning of
+nbfProjectionRotationMetric3D<float> / nbfCorrelationImageMetric<float,3> / nbfImageMetric<float,3>
+(inc/em/nbfProjectionRotationMetric3D.h:90-196, inc/em/nbfCorrelationImageMetric.h:50-121,
+inc/em/nbfImageMetric.h:33-99) and computes on the GPU through the C ABI of include/ettk_gpu.h.
+Volumes are `WedgedSubImage3D` objects (fixed images plus volume-list metadata).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+class EttkError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ettk_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class WedgedSubImage3D:
+    """A fixed-image particle with the metadata of one volume-list row
+    (nbfWedgedSubImage3D, inc/em/nbfWedgedSubImage3D.h:17-185)."""
+
+    def __init__(self, image, lwedge=-90.0, uwedge=90.0, normal=(0.0, 0.0, 0.0), matrix=None, position=None,
+                 cut_offset=0.0, filename="NA"):
+        self.image = np.ascontiguousarray(image, dtype=np.float32)  # [z][y][x]
+        n = self.image.shape[0]
+        self.lwedge, self.uwedge = float(lwedge), float(uwedge)
+        self.normal = tuple(float(x) for x in normal)
+        self.matrix = np.eye(4) if matrix is None else np.asarray(matrix, np.float64).reshape(4, 4)
+        self.position = tuple(position) if position is not None else (n / 2.0,) * 3
+        self.cut_offset = float(cut_offset)
+        self.filename = filename
+
+    def meta(self):
+        return {"lwedge": self.lwedge, "uwedge": self.uwedge, "normal": self.normal, "matrix": self.matrix,
+                "position": self.position, "cut_offset": self.cut_offset}
+
+
+class ProjectionRotationMetric3D:
+    """GPU drop-in for nbfProjectionRotationMetric3D<float> in alignment_mode 3."""
+
+    def __init__(self, params, device=0):
+        self.L = _lib.load()
+        self.params = dict(params)
+        self._ctx = ctypes.c_void_p()
+        P = _lib.make_params(self.params)
+        self._check(self.L.ettk_gpu_create(device, ctypes.byref(P), ctypes.byref(self._ctx)), "create")
+        self._refs = None
+        self._parts = None
+        self.input1 = self.input2 = None
+        self.transform = np.eye(4)
+        self.correlationPeak = None
+
+    def close(self):
+        if self._ctx:
+            self.L.ettk_gpu_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != _lib.ETTK_OK:
+            buf = ctypes.create_string_buffer(512)
+            if self._ctx:
+                self.L.ettk_gpu_last_error(self._ctx, buf, 512)
+            raise EttkError(rc, "%s: %s" % (what, buf.value.decode(errors="replace")))
+
+    # -- volume sets (getDistances' list1 / list2) -------------------------------------------
+    def set_references(self, volumes):
+        vols = np.ascontiguousarray(np.stack([v.image for v in volumes]), np.float32)
+        meta = _lib.make_meta([v.meta() for v in volumes])
+        self._check(self.L.ettk_gpu_set_references(self._ctx, len(volumes), vols.ctypes.data, meta), "set_references")
+        self._refs = volumes
+
+    def set_particles(self, volumes, stacked=None):
+        vols = stacked if stacked is not None else np.stack([v.image for v in volumes])
+        vols = np.ascontiguousarray(vols, np.float32)
+        meta = _lib.make_meta([v.meta() for v in volumes])
+        self._check(self.L.ettk_gpu_set_particles(self._ctx, len(volumes), vols.ctypes.data, meta), "set_particles")
+        self._parts = volumes
+
+    def set_particles_device(self, dev_ptr, metas):
+        meta = _lib.make_meta(metas)
+        self._check(self.L.ettk_gpu_set_particles_device(self._ctx, len(metas), ctypes.c_void_p(dev_ptr), meta),
+                    "set_particles_device")
+
+    # -- nbfImageMetric interface (single pair) ------------------------------------------------
+    def setInput1(self, v):
+        self.set_references([v])
+        self.input1 = v
+
+    def setInput2(self, v):
+        self.set_particles([v])
+        self.input2 = v
+
+    def getDistance(self):
+        D = self.getDistances([(0, 0)])
+        self.correlationPeak = float(D[0, 0, 0])
+        self.transform = D[0, 1:17, 0].astype(np.float64).reshape(4, 4)
+        return self.correlationPeak
+
+    def getTransform(self):
+        return self.transform
+
+    # -- nbfCorrelationImageMetric::getDistances (core overload) ---------------------------------
+    def getDistances(self, indexes, D=None, cols=17, ncand=1):
+        """indexes: sequence of (reference index, particle index). D: float32 (npairs, cols, ncand),
+        rows pre-filled with -1 are computed (others skipped)."""
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        n = idx.shape[0]
+        if D is None:
+            D = -np.ones((n, cols, ncand), np.float32)
+        assert D.dtype == np.float32 and D.flags.c_contiguous and D.shape[0] == n
+        self._check(self.L.ettk_gpu_align_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1], D.shape[2]),
+                    "align_pairs")
+        return D
+
+    # -- diagnostics ---------------------------------------------------------------------------
+    def ccf(self, r, p, T):
+        t = np.ascontiguousarray(np.asarray(T, np.float64).reshape(16)).copy()
+        d = ctypes.c_float()
+        self._check(self.L.ettk_gpu_ccf(self._ctx, r, p, t.ctypes.data, ctypes.byref(d)), "ccf")
+        return float(d.value), t.reshape(4, 4)
+
+    def spherical_projection(self, r=0, p=-1):
+        n = 2 * self.params["B"]
+        out = np.zeros((n, n), np.float32)
+        self._check(self.L.ettk_gpu_spherical_projection(self._ctx, r, p, out.ctypes.data), "spherical_projection")
+        return out
+
+    def soft(self, F1, F2, scaled=False):
+        n = 2 * self.params["B"]
+        a = np.ascontiguousarray(F1, np.float32)
+        b = np.ascontiguousarray(F2, np.float32)
+        C = np.zeros((n, n, n), np.float32)
+        self._check(self.L.ettk_gpu_soft(self._ctx, a.ctypes.data, b.ctypes.data, int(scaled), C.ctypes.data), "soft")
+        return C
+
+    def stream(self):
+        """cudaStream_t of this context (for CUDA-event timing)."""
+        return int(self.L.ettk_gpu_stream(self._ctx) or 0)
+
+    def profile(self, enable=True):
+        self._check(self.L.ettk_gpu_profile(self._ctx, int(enable)), "profile")
+
+    def profile_read(self):
+        out = {}
+        i = 0
+        while True:
+            name = ctypes.create_string_buffer(64)
+            n = ctypes.c_longlong()
+            ms = ctypes.c_double()
+            b = ctypes.c_double()
+            if self.L.ettk_gpu_profile_read(self._ctx, i, name, 64, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)):
+                break
+            out[name.value.decode()] = {"launches": n.value, "ms": ms.value, "bytes": b.value}
+            i += 1
+        return out
+
+    def kernel_launches(self):
+        return int(self.L.ettk_gpu_kernel_launches(self._ctx))

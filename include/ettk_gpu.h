@@ -1,0 +1,125 @@
+/* ettk_gpu.h — C ABI of the GB300 sub-volume alignment library (libettk_gpu.so).
+ *
+ * Drop-in for the pairwise particle x reference alignment of ETTK's MPI_Classification:
+ * nbfProjectionRotationMetric3D<float>::execute (inc/em/nbfProjectionRotationMetric3D.h:415-1052)
+ * driven by nbfCorrelationImageMetric::getDistances (inc/em/nbfCorrelationImageMetric.h:1873-2288),
+ * alignment_mode 3 (SO(3) grid hit + translational CCF, no Powell refinement).
+ *
+ * Conventions
+ *  - Every call returns an int status (ETTK_OK = 0); no exception crosses the ABI.
+ *    ettk_gpu_last_error() returns a description of the last failure on a context.
+ *  - Host buffers are caller-owned and only read/written during the call (synchronous API).
+ *  - Volumes are float32 fixed images of edge N stored x-fastest (MRC / VTK order),
+ *    i.e. element (x,y,z) at x + N*(y + N*z).
+ *  - Matrices are 4x4 row-major doubles (vtkMatrix4x4::DeepCopy order).
+ *  - One context = one GPU = one CUDA stream; contexts are independent (re-entrant across contexts,
+ *    not thread-safe within one context).
+ */
+#ifndef ETTK_GPU_H
+#define ETTK_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  ETTK_OK = 0,
+  ETTK_ERR_ARG = 1,      /* invalid argument or unsupported configuration */
+  ETTK_ERR_OOM = 2,      /* device or host allocation failed (the reference exit(1)s instead,
+                            inc/em/nbfProjectionRotationMetric3D.h:1093-1104) */
+  ETTK_ERR_CUDA = 3,     /* a CUDA runtime call failed */
+  ETTK_ERR_TIMEOUT = 4,  /* reserved: a bounded device wait gave up */
+  ETTK_ERR_NAN = 5,      /* non-finite input volume */
+  ETTK_ERR_STATE = 6     /* references or particles not set */
+};
+
+typedef struct ettk_ctx ettk_ctx;
+
+/* Alignment parameters. Each field names the reference setting it replaces. */
+typedef struct {
+  int N;                        /* box edge, power of two 16..128 (nbfWedgedSubImage3D geometry) */
+  int B;                        /* SH bandwidth, power of two 8..64 (nbfProjectionRotationMetric3D::B) */
+  float mask_radius;            /* nbfImageFilter::setMaskSize(x=y=z=mask_radius, sigma) */
+  float mask_sigma;
+  float square_mask_size;       /* nbfImageFilter::squareMaskSize */
+  float bp_low, bp_high;        /* nbfFourierFilter::bandPassOn(lowCut, highCut, lowVar, highVar) */
+  float bp_low_sigma, bp_high_sigma;
+  float bfactor;                /* nbfFourierFilter::bfactorOn (0 = off) */
+  float restrict_translation;   /* nbfImageMetric::setTranslationSearchRestriction */
+  float restrict_rotation;      /* nbfImageMetric::setRotationSearchRestriction (degrees) */
+  int candidate_peaks;          /* nbfProjectionRotationMetric3D::setNumberOfCandidatePeaksToSearch */
+  int number_of_candidates;     /* nbfCorrelationImageMetric::setNumberOfCandidates */
+  int wedge_compensation;       /* nbfImageMetric::setMissingWedgeCompensation */
+  int overlap_normalized;       /* nbfImageMetric::setToComputeOverlapNormalizedDistances */
+  int mutual_correlation;       /* nbfImageMetric::setToUseMutualCorrelation (must be 0) */
+  int max_batch;                /* pairs aligned per device batch (0 = automatic) */
+} ettk_params;
+
+/* Per-volume metadata: the columns of the reference's 33-column volume list
+ * (nbfWedgedSubImage3D::serialize, inc/em/nbfWedgedSubImage3D.h:387-421). */
+typedef struct {
+  float lwedge, uwedge;         /* missing wedge limits (degrees, about Y) */
+  float normal[3];              /* Euler angles applied as RotateZ(-n2) RotateX(-n0) RotateZ(-n1) */
+  double matrix[16];            /* alignment matrix */
+  float position[3];            /* centre of the box in the fixed image (N/2 for fixed images) */
+  float cut_offset;             /* extra Z offset of the box */
+} ettk_volume_meta;
+
+/* Replaces constructing nbfProjectionRotationMetric3D<float>(imageFilter, fourierFilter) and its
+ * setters (src/MPI_Classification.cpp:594-653). */
+int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **ctx);
+int ettk_gpu_destroy(ettk_ctx *ctx);
+
+/* Replaces the list1 side of getDistances(list1, list2, ...) (inc/em/nbfCorrelationImageMetric.h:1873):
+ * R reference volumes (R*N^3 floats) and their metadata. */
+int ettk_gpu_set_references(ettk_ctx *ctx, int R, const float *volumes, const ettk_volume_meta *meta);
+
+/* Replaces the list2 side: V particle volumes and metadata (host memory). */
+int ettk_gpu_set_particles(ettk_ctx *ctx, int V, const float *volumes, const ettk_volume_meta *meta);
+
+/* Same as ettk_gpu_set_particles with `volumes` already in device memory of the context's GPU. */
+int ettk_gpu_set_particles_device(ettk_ctx *ctx, int V, const float *d_volumes, const ettk_volume_meta *meta);
+
+/* Replaces nbfCorrelationImageMetric::getDistances(list1, list2, indexes, D, type=3)
+ * (inc/em/nbfCorrelationImageMetric.h:1873-2009): pairs[2*i] = reference index, pairs[2*i+1] =
+ * particle index. D is the reference's Array<float,3> D(npairs, cols, ncand) in C order:
+ * D[(i*cols + c)*ncand + k]. Column 0 = distance (getDistance), then correlation scale when
+ * cols > 17, wedge overlap when cols > 18, then the 16 entries of the final transform.
+ * Rows whose D[i][0][0] != -1 on entry are skipped (the reference's resume convention). */
+int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand);
+
+/* Diagnostics (staged parity checks; no counterpart in the reference API):
+ * one executeFourierNewHalf call (inc/em/nbfFourierImageMetric.h:1077-1323) of particle p against
+ * reference r at transform t (updated in place with the found shift); returns the distance in *dist. */
+int ettk_gpu_ccf(ettk_ctx *ctx, int r, int p, double *t, float *dist);
+
+/* Diagnostics: the |FFT| spherical projection Pp (cartesianToSpherical, [2B][2B]) of particle p,
+ * or of reference r when p < 0. */
+int ettk_gpu_spherical_projection(ettk_ctx *ctx, int r, int p, float *Pp);
+
+/* Diagnostics: SO(3) correlation of two real S^2 signals ([2B][2B]) on the (2B)^3 grid,
+ * C[alpha][beta][gamma] (nbfProjectionRotationMetric3D::soft, 1136-1295); scaled != 0 applies
+ * softScaled's min/max rescaling (1297-1319). */
+int ettk_gpu_soft(ettk_ctx *ctx, const float *F1, const float *F2, int scaled, float *C);
+
+/* Number of kernels this library launched since the context was created. */
+long long ettk_gpu_kernel_launches(ettk_ctx *ctx);
+
+/* The CUDA stream (cudaStream_t) all of this context's work is issued on, for timing with events. */
+void *ettk_gpu_stream(ettk_ctx *ctx);
+
+/* Per-kernel-family timing: enable != 0 records CUDA events around each kernel family on the
+ * context stream (and clears earlier totals); ettk_gpu_profile_read returns family `index`
+ * (0-based, ETTK_ERR_ARG past the end): its name, launch count, summed device time and the
+ * algorithmic bytes those launches must move (one read of each input, one write of each output). */
+int ettk_gpu_profile(ettk_ctx *ctx, int enable);
+int ettk_gpu_profile_read(ettk_ctx *ctx, int index, char *name, int name_size, long long *launches,
+                          double *total_ms, double *bytes);
+
+/* Copies a description of the last error (NUL-terminated) into buf. */
+int ettk_gpu_last_error(ettk_ctx *ctx, char *buf, int size);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ETTK_GPU_H */

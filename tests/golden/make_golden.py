@@ -1,0 +1,59 @@
+"""Regenerates the golden fixtures in this directory (run in a tree where the reference is present).
+
+soft_bw8.npz   SOFT 1.0's own bandwidth-8 test signals (external/soft-1.0/randomS2sig_bw8.dat and
+               randomS2sigA_bw8.dat, real parts) pushed through the reference's SOFT library built from
+               its sources (oracle/_ref): the SO(3) correlation as nbfProjectionRotationMetric3D::soft
+               computes it, and an S^2 rotation as ::harmonics does.
+align32_b16.npz  oracle alignments of the first particles of the 32^3 B=16 workload (a regression pin
+               of the oracle itself), with a checksum of the generated particles.
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import pyoracle  # noqa: E402
+from ettk_gb300 import synthetic  # noqa: E402
+
+REF = os.environ.get("ETTK_REFERENCE_ROOT", "/root/reference")
+
+
+def read_s2(path):
+    v = np.loadtxt(path)
+    return v[0::2].reshape(16, 16)
+
+
+def main():
+    R = pyoracle.ref_lib()
+    if R is None:
+        raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+    soft_dir = os.path.join(REF, "external", "soft-1.0")
+    sig = read_s2(os.path.join(soft_dir, "randomS2sig_bw8.dat"))
+    pat = read_s2(os.path.join(soft_dir, "randomS2sigA_bw8.dat"))
+    B = 8
+    C = np.zeros((16, 16, 16))
+    R.ref_soft(B, np.ascontiguousarray(sig), np.ascontiguousarray(pat), C)
+    angles = np.array([0.3, 1.2, 2.0])
+    Rr = np.zeros((16, 16))
+    R.ref_rotate(B, np.ascontiguousarray(sig), *angles, Rr)
+    np.savez_compressed(os.path.join(HERE, "soft_bw8.npz"), sig=sig, pat=pat, C=C, R=Rr, angles=angles)
+
+    n = 4
+    ds = synthetic.generate("align32_b16", n_particles=n)
+    dist, mats = [], []
+    for i in range(n):
+        o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
+        dist.append(o["distance"])
+        mats.append(o["matrix"])
+    np.savez_compressed(os.path.join(HERE, "align32_b16.npz"), n=n, distance=np.array(dist), matrix=np.array(mats),
+                        particles_sha256=hashlib.sha256(ds.particles.tobytes()).hexdigest())
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,80 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same seeded inputs.
+
+Tolerances: distances within 1e-4 relative, same SO(3) grid cell (rotation matrices equal to
+1e-5, they are built from the same grid angles), same half-voxel shift; staged quantities
+(spherical projections, SO(3) correlations) to 1e-4 relative of their range (FP32 vs FP64).
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from ettk_gb300 import synthetic
+from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+
+pytestmark = pytest.mark.gpu
+
+KW = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+
+
+def vol(img, meta):
+    return WedgedSubImage3D(img, **{k: meta[k] for k in KW})
+
+
+@pytest.fixture(scope="module")
+def ds32():
+    return synthetic.generate("align32_b16", n_particles=6)
+
+
+@pytest.fixture(scope="module")
+def metric32(ds32):
+    m = ProjectionRotationMetric3D(ds32.params)
+    m.set_references([vol(ds32.references[0], ds32.ref_meta[0])])
+    m.set_particles([vol(ds32.particles[i], ds32.meta[i]) for i in range(len(ds32.meta))])
+    yield m
+    m.close()
+
+
+def test_spherical_projection(ds32, metric32):
+    for p in range(2):
+        g = metric32.spherical_projection(0, p)
+        o = pyoracle.spherical_projection(ds32.params, ds32.particles[p], ds32.meta[p])
+        assert np.abs(g - o).max() <= 1e-4 * np.abs(o).max()
+    g = metric32.spherical_projection(0, -1)
+    o = pyoracle.spherical_projection(ds32.params, ds32.references[0], ds32.ref_meta[0])
+    assert np.abs(g - o).max() <= 1e-4 * np.abs(o).max()
+
+
+@pytest.mark.parametrize("scaled", [False, True])
+def test_soft(metric32, scaled):
+    B = 16
+    rng = np.random.default_rng(11)
+    F1 = rng.random((2 * B, 2 * B)).astype(np.float32)
+    F2 = rng.random((2 * B, 2 * B)).astype(np.float32)
+    g = metric32.soft(F1, F2, scaled=scaled)
+    o = pyoracle.soft(B, F1.astype(np.float64), F2.astype(np.float64), scaled=scaled)
+    rng_ = o.max() - o.min()
+    assert np.abs(g - o).max() <= 1e-4 * rng_
+    assert np.unravel_index(g.argmax(), g.shape) == np.unravel_index(o.argmax(), o.shape)
+
+
+def test_ccf(ds32, metric32):
+    rng = np.random.default_rng(5)
+    for p in range(3):
+        R = synthetic.random_rotation(rng)
+        T = np.eye(4)
+        T[:3, :3] = R
+        dg, Tg = metric32.ccf(0, p, T)
+        do, To = pyoracle.ccf(ds32.params, ds32.references[0], ds32.ref_meta[0], ds32.particles[p], ds32.meta[p], T)
+        assert abs(dg - do) <= 1e-4 * abs(do)
+        assert np.allclose(Tg[:3, 3], To[:3, 3], atol=1e-6)
+
+
+def test_align_pairs(ds32, metric32):
+    P = len(ds32.meta)
+    D = metric32.getDistances([(0, i) for i in range(P)])
+    for i in range(P):
+        o = pyoracle.align(ds32.params, ds32.references[0], ds32.ref_meta[0], ds32.particles[i], ds32.meta[i])
+        T = D[i, 1:17, 0].reshape(4, 4)
+        assert abs(D[i, 0, 0] - o["distance"]) <= 1e-4 * abs(o["distance"])
+        assert np.allclose(T[:3, :3], o["matrix"][:3, :3], atol=1e-5)
+        assert np.allclose(T[:3, 3], o["matrix"][:3, 3], atol=1e-4)

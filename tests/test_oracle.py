@@ -1,0 +1,93 @@
+"""Oracle checks (CPU): the FP64 restatement against the reference's own SOFT 1.0 (compiled from
+the reference sources under oracle/_ref when the reference tree is present), against numpy's FFT,
+and against the committed golden fixtures (tests/golden, made by tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_fft_matches_numpy():
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((8, 16, 32))
+    X = pyoracle.rfft3d(x)
+    assert np.abs(X - np.fft.rfftn(x)).max() < 1e-10
+    y = pyoracle.irfft3d(X, 32)
+    assert np.abs(y - x * x.size).max() < 1e-8
+
+
+def test_c2r_ignores_imaginary_nyquist_terms():
+    # FFTW hc2r semantics on the last axis: Im of the k=0 and k=n/2 terms (after the leading-axis
+    # inverse transforms) does not reach the output
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((4, 4, 5)) + 1j * rng.standard_normal((4, 4, 5))
+    y = pyoracle.irfft3d(X, 8)
+    Z = np.fft.ifft(np.fft.ifft(X, axis=0), axis=1) * 16
+    Z[..., 0] = Z[..., 0].real
+    Z[..., 4] = Z[..., 4].real
+    ref = np.fft.irfft(Z, 8, axis=2) * 8
+    assert np.abs(y - ref).max() < 1e-9
+
+
+@pytest.mark.parametrize("B", [4, 8, 16])
+def test_so3_against_soft_library(B):
+    R = pyoracle.ref_lib()
+    if R is None:
+        pytest.skip("SOFT reference library not built (reference tree absent)")
+    n = 2 * B
+    rng = np.random.default_rng(B)
+    F1 = rng.standard_normal((n, n))
+    F2 = rng.standard_normal((n, n))
+    C = pyoracle.soft(B, F1, F2)
+    Cr = np.zeros((n, n, n))
+    R.ref_soft(B, F1, F2, Cr)
+    assert np.abs(C - Cr).max() <= 1e-9 * np.abs(Cr).max()
+    Rm = pyoracle.rotate(B, F1, 0.4, 1.1, 2.3)
+    Rr = np.zeros((n, n))
+    R.ref_rotate(B, F1, 0.4, 1.1, 2.3, Rr)
+    assert np.abs(Rm - Rr).max() <= 1e-9 * np.abs(Rr).max()
+    cR = np.zeros(B * B)
+    cI = np.zeros(B * B)
+    R.ref_fst(B, F1, cR, cI)
+    c = pyoracle.sht(B, F1)
+    idx = 0
+    for m in range(B):
+        for l in range(m, B):
+            assert abs(c[l, m + B] - (cR[idx] + 1j * cI[idx])) < 1e-9 * (1 + abs(c[l, m + B]))
+            idx += 1
+
+
+def _golden(name):
+    p = os.path.join(GOLD, name)
+    if not os.path.exists(p):
+        pytest.skip("golden fixture %s missing" % name)
+    return np.load(p, allow_pickle=False)
+
+
+def test_soft_fixture_vectors():
+    """SOFT's own S^2 test signal (randomS2sig_bw8.dat) through the reference SOFT build: the oracle
+    reproduces the stored correlation and rotation outputs."""
+    g = _golden("soft_bw8.npz")
+    B = 8
+    C = pyoracle.soft(B, g["sig"], g["pat"])
+    assert np.abs(C - g["C"]).max() <= 1e-9 * np.abs(g["C"]).max()
+    Rm = pyoracle.rotate(B, g["sig"], *g["angles"])
+    assert np.abs(Rm - g["R"]).max() <= 1e-9 * np.abs(g["R"]).max()
+
+
+def test_alignment_golden():
+    """Frozen oracle outputs for the 32^3 B=16 workload (first particles); pins the oracle against
+    accidental changes."""
+    g = _golden("align32_b16.npz")
+    from ettk_gb300 import synthetic
+    ds = synthetic.generate("align32_b16", n_particles=int(g["n"]))
+    import hashlib
+    assert hashlib.sha256(ds.particles.tobytes()).hexdigest() == str(g["particles_sha256"])
+    for i in range(int(g["n"])):
+        o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
+        assert abs(o["distance"] - g["distance"][i]) <= 1e-6 * abs(g["distance"][i])
+        assert np.allclose(o["matrix"], g["matrix"][i], atol=1e-9)
