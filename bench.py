@@ -1,0 +1,268 @@
+"""Benchmark: alignments/s of the sub-volume alignment path at 64^3, B=32.
+
+One step = aligning a batch of particle x reference pairs (the plain method: SO(3) grid search plus
+translational CCF candidates, alignment_mode 3) through the library's getDistances entry point.
+
+  value : pairs/s with the particle volumes already resident in HBM (set_particles_device + align)
+  e2e   : pairs/s through the host-buffer API: pinned host volumes copied in every step
+          (ettk_gpu_set_particles) and the result rows read back (ettk_gpu_align_pairs)
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank aligns its own batch on its own GPU (independent replicas, no collective
+on the data path); rank 0 prints one JSON line with the max time over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "align64_b32"
+METRIC = "alignments/s at 64^3 bw=32: plain GPU vs batched+adjoint form at <=0.5deg/0.1 vox"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--pairs", type=int, default=256, help="pairs aligned per step (per GPU)")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="pairs in the CPU baseline sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------- CPU (oracle) arm
+
+def _cpu_worker(args):
+    idx, n = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from ettk_gb300 import synthetic
+    ds = synthetic.generate(WORKLOAD, n_particles=n)
+    t0 = time.perf_counter()
+    for i in idx:
+        pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
+    return time.perf_counter() - t0, len(idx)
+
+
+def cpu_baseline(n_pairs):
+    """The oracle (FP64 port of the reference path) on all host cores: one single-threaded process per
+    core on a disjoint shard, as the reference runs one MPI worker per core. Returns pairs/s."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    cores = os.cpu_count() or 1
+    n_pairs = max(n_pairs, cores)
+    shards = [list(range(k, n_pairs, cores)) for k in range(cores)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(s, n_pairs) for s in shards if s])
+    wall = time.perf_counter() - t0
+    busy = max(r[0] for r in res)
+    return {"value": n_pairs / busy, "unit": "alignments/s", "cores": cores, "kind": "port",
+            "sample": "%d pairs of the %s workload (64^3, B=32), one oracle process per core, %.1f s wall"
+                      % (n_pairs, WORKLOAD, wall)}
+
+
+# ------------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------- GPU arm
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        # The reference's CPU path (C++ on VTK 5.10 + FFTW3 + MPI) cannot be built here (FFTW3, MPI and a
+        # VTK build are absent); its FP64 restatement (the oracle) is timed on all host cores instead.
+        n = a.cpu_sample or 2 * (os.cpu_count() or 1)
+        vals = [cpu_baseline(n) for _ in range(a.steps)]  # a process pool has no warm state to prime
+        v = vals[-1]
+        per = [x["value"] for x in vals]
+        value = statistics.median(per)
+        out = {"metric": METRIC, "value": value, "unit": "alignments/s", "n_gpus": a.gpus, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": 1000.0 * n / value, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+               "config": {"workload": WORKLOAD, "N": 64, "B": 32, "pairs_per_step": n, "method": "alignment_mode 3"},
+               "cpu_baseline": {"value": value, "unit": "alignments/s", "cores": v["cores"], "kind": "port",
+                                "sample": v["sample"]},
+               "e2e": {"value": value, "unit": "alignments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a.cpu_sample or 2 * (os.cpu_count() or 1))
+
+    import numpy as np
+    import torch
+    from ettk_gb300 import synthetic
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    ds = synthetic.generate(WORKLOAD, n_particles=a.pairs)
+    P = a.pairs
+    N = ds.params["N"]
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    metas = [{k: m[k] for k in kw} for m in ds.meta]
+    m = ProjectionRotationMetric3D(ds.params, device=local)
+    m.set_references([WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})])
+    parts_dev = torch.from_numpy(ds.particles).to("cuda")
+    parts_host = torch.from_numpy(ds.particles).pin_memory()
+    vols = [WedgedSubImage3D(ds.particles[i], **metas[i]) for i in range(P)]
+    pairs = [(0, i) for i in range(P)]
+    stream = torch.cuda.ExternalStream(m.stream())
+
+    def step_device():
+        m.set_particles_device(parts_dev.data_ptr(), metas)
+        return m.getDistances(pairs)
+
+    def step_e2e():
+        m.set_particles(vols, stacked=parts_host.numpy())
+        return m.getDistances(pairs)
+
+    def timed(fn, steps):
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    for _ in range(a.warmup):
+        step_device()
+    clocks = ClockSampler(local)
+    clocks.start()
+    m.profile(True)
+    launches0 = m.kernel_launches()
+    ms = timed(step_device, a.steps)
+    launches = m.kernel_launches() - launches0
+    prof = m.profile_read()
+    m.profile(False)
+    ms_e2e = timed(step_e2e, a.steps)
+    clk = clocks.stop()
+
+    hbm, tflops, peak_kind = peaks()
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+    total_prof_ms = sum(v["ms"] for v in prof.values())
+    value = world * P * a.steps / (ms * 1e-3)
+    e2e = world * P * a.steps / (ms_e2e * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "alignments/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "N": N, "B": ds.params["B"], "pairs_per_step_per_gpu": P,
+                   "method": "alignment_mode 3 (SO(3) grid + CCF candidates), FP32",
+                   "l2": "inputs larger than L2 (%.0f MB of particle volumes per step)" % (P * N ** 3 * 4 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "alignments/s", "h2d_bytes_per_step": P * N ** 3 * 4,
+                "d2h_bytes_per_step": P * 17 * 4},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                     "kernel_share": dom["ms"] / total_prof_ms if total_prof_ms else None,
+                     "families": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                                      "GBps": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None}
+                                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}},
+        "clocks": clk,
+    }
+    if cpu:
+        out["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    m.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

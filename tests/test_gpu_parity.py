@@ -78,3 +78,23 @@ def test_align_pairs(ds32, metric32):
         assert abs(D[i, 0, 0] - o["distance"]) <= 1e-4 * abs(o["distance"])
         assert np.allclose(T[:3, :3], o["matrix"][:3, :3], atol=1e-5)
         assert np.allclose(T[:3, 3], o["matrix"][:3, 3], atol=1e-4)
+
+
+@pytest.fixture(scope="module")
+def ds64():
+    return synthetic.generate("align64_b32", n_particles=2)
+
+
+def test_align_pairs_64(ds64):
+    """The benchmark shape (64^3, B=32, per-particle wedges rotated in-plane)."""
+    m = ProjectionRotationMetric3D(ds64.params)
+    m.set_references([vol(ds64.references[0], ds64.ref_meta[0])])
+    m.set_particles([vol(ds64.particles[i], ds64.meta[i]) for i in range(2)])
+    D = m.getDistances([(0, 0), (0, 1)])
+    for i in range(2):
+        o = pyoracle.align(ds64.params, ds64.references[0], ds64.ref_meta[0], ds64.particles[i], ds64.meta[i])
+        T = D[i, 1:17, 0].reshape(4, 4)
+        assert abs(D[i, 0, 0] - o["distance"]) <= 1e-4 * abs(o["distance"])
+        assert np.allclose(T[:3, :3], o["matrix"][:3, :3], atol=1e-5)
+        assert np.allclose(T[:3, 3], o["matrix"][:3, 3], atol=1e-4)
+    m.close()
