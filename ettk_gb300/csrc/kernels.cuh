@@ -17,7 +17,7 @@ struct ResliceItem {
 // fixed image under Euler*matrix*t into an N^3 box (output [x][y][z], z fastest), background
 // -FLT_MAX outside [-0.5, dim-0.5] (vtkImageReslice border 1, clamp mode), plus per-item sums
 // of valid values and their count into acc[item*acc_stride + 0/1].
-__global__ void k_reslice(const ResliceItem *__restrict__ items, int N, float *__restrict__ out, double *acc,
+static __global__ void k_reslice(const ResliceItem *__restrict__ items, int N, float *__restrict__ out, double *acc,
                           int acc_stride) {
   __shared__ double sh[32];
   const ResliceItem it = items[blockIdx.y];
@@ -80,7 +80,7 @@ struct WedgeVecs {
   double v1[3], v2[3];
   int full;
 };
-__global__ void k_wedge_binary(const WedgeVecs *__restrict__ wv, int N, float *__restrict__ out) {
+static __global__ void k_wedge_binary(const WedgeVecs *__restrict__ wv, int N, float *__restrict__ out) {
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
   const WedgeVecs w = wv[blockIdx.y];
@@ -115,7 +115,7 @@ struct Smooth3 {
   float w_lo[2];    // at index 0: (0, +1)
   float w_hi[2];    // at last index: (-1, 0)
 };
-__global__ void k_wedge_smooth(const float *__restrict__ in, float *__restrict__ out, int N, int axis, Smooth3 sw,
+static __global__ void k_wedge_smooth(const float *__restrict__ in, float *__restrict__ out, int N, int axis, Smooth3 sw,
                                const float *__restrict__ w1, const int *__restrict__ w1_index,
                                const float *__restrict__ filter, double *acc, int acc_stride, int acc_slot) {
   __shared__ double sh[32];
@@ -150,7 +150,7 @@ __global__ void k_wedge_smooth(const float *__restrict__ in, float *__restrict__
 // executeHalf + normalizeFourierHalf accumulation (inc/em/nbfFourierFilter.h:586-606,
 // inc/em/nbfCorrelationImageMetric.h:497-530): out = src * fw, DC zeroed, sums of |F|^2 for
 // k < H-1 (slot) and k = H-1 (slot+1). src item index through src_index (nullptr = same item).
-__global__ void k_spec_filter(const float2 *__restrict__ src, const int *__restrict__ src_index,
+static __global__ void k_spec_filter(const float2 *__restrict__ src, const int *__restrict__ src_index,
                               const float *__restrict__ fw, float2 *__restrict__ out, int N, double *acc,
                               int acc_stride, int slot) {
   __shared__ double sh[32];
@@ -176,7 +176,7 @@ __global__ void k_spec_filter(const float2 *__restrict__ src, const int *__restr
 
 // norm of normalizeFourierHalf with its float roundings: norm = float(2*s1);
 // norm = float(sqrt((norm + s2) / (N*N*2*(H-1)))). Writes 1/norm (and norm) per item.
-__global__ void k_norms(const double *acc, int acc_stride, int slot, int N, int n_items, float *inv_norm,
+static __global__ void k_norms(const double *acc, int acc_stride, int slot, int N, int n_items, float *inv_norm,
                         float *norm_out) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_items) return;
@@ -281,7 +281,7 @@ struct PostStore {
 };
 
 // FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3), stored over FFT1re (nbfFourierImageMetric.h:1174-1177).
-__global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict__ f2, const float *__restrict__ inv_norm2,
+static __global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict__ f2, const float *__restrict__ inv_norm2,
                          int N) {
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
@@ -295,7 +295,7 @@ __global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict__ f2, 
 
 // FFTre = (-F(m1) conj(F(I2'^2)) + FFT2re) * shiftr, times the zero-padding factor 8
 // (nbfFourierImageMetric.h:1192-1210: FFTre holds F(m1) and FFT1re holds F(I2'^2) there). In place over q.
-__global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict__ fm1, const float2 *__restrict__ fft2re, int N,
+static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict__ fm1, const float2 *__restrict__ fft2re, int N,
                         float factor) {
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
@@ -312,7 +312,7 @@ __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict__ fm1, 
 // and reads only this window). Same FFTW order: complex inverse along x, then y, then the
 // half-complex-to-real sum along z (real parts only for the kz=N term).
 // Stage x: q1[e][X][ky][kz] = sum_kx q[e][kx][ky][kz] exp(+2 pi i (kx+o0) (lo+X) / 2N)
-__global__ void k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N, int W, int lo, int o0) {
+static __global__ void k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N, int W, int lo, int o0) {
   const int H = N / 2 + 1;
   long nrow = (long)N * H;  // (ky,kz) per X
   long total = (long)W * nrow;
@@ -332,7 +332,7 @@ __global__ void k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1
   }
 }
 // Stage y: q2[e][X][Y][kz] = sum_ky q1[e][X][ky][kz] exp(+2 pi i (ky+o0)(lo+Y)/2N)
-__global__ void k_pruned_y(const float2 *__restrict__ q1, float2 *__restrict__ q2, int N, int W, int lo, int o0) {
+static __global__ void k_pruned_y(const float2 *__restrict__ q1, float2 *__restrict__ q2, int N, int W, int lo, int o0) {
   const int H = N / 2 + 1;
   long total = (long)W * W * H;
   const float2 *Q = q1 + (long)blockIdx.y * W * N * H;
@@ -351,7 +351,7 @@ __global__ void k_pruned_y(const float2 *__restrict__ q1, float2 *__restrict__ q
 }
 // Stage z + peak: T = out * shift / (2N)^3 inside the sphere radius^2 < r^2 (else -max);
 // packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
-__global__ void k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo, int o2, float rr2,
+static __global__ void k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo, int o2, float rr2,
                                 unsigned long long *peak) {
   const int H = N / 2 + 1;
   long total = (long)W * W * W;
@@ -388,7 +388,7 @@ struct EvalOut {
   float dist;
   float shift[3];
 };
-__global__ void k_score(const double *acc, int acc_stride, const unsigned long long *peak, int n_items, int W,
+static __global__ void k_score(const double *acc, int acc_stride, const unsigned long long *peak, int n_items, int W,
                         double sum_filter, int overlap, int use_wedge, int N, EvalOut *out) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_items) return;
@@ -414,7 +414,7 @@ __global__ void k_score(const double *acc, int acc_stride, const unsigned long l
 
 // mean over all voxels of the mean-subtracted particle (nbfImageFilter::execute meanValue,
 // inc/em/nbfImageFilter.h:255) -> acc[slot]
-__global__ void k_mean_all(const float *__restrict__ v, const double *acc_in, int acc_stride, int N, double *acc_out,
+static __global__ void k_mean_all(const float *__restrict__ v, const double *acc_in, int acc_stride, int N, double *acc_out,
                            int slot) {
   __shared__ double sh[32];
   long n3 = (long)N * N * N;
@@ -457,7 +457,7 @@ struct PrePadded {
 };
 
 // |F| of the (2N)^3 half spectrum (inc/em/nbfProjectionRotationMetric3D.h:321-325)
-__global__ void k_magnitude(const float2 *__restrict__ F, float *__restrict__ M, long n) {
+static __global__ void k_magnitude(const float2 *__restrict__ F, float *__restrict__ M, long n) {
   for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
     float2 f = F[id];
     M[id] = sqrtf(f.x * f.x + f.y * f.y);
@@ -477,7 +477,7 @@ ETTK_DEV float mag_at(const float *Mh, int N, int x, int y, int z, float padc) {
 
 // Cubic resampling on radial shells through vtkSphericalTransform with wrap, summed over the
 // radii [bandL, bandU] (lines 359-406): Pp[e][j][k] for polar j, azimuth k.
-__global__ void k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs, int n_dirs, int N,
+static __global__ void k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs, int n_dirs, int N,
                                 int bandL, int bandU, const float *__restrict__ padc, float *__restrict__ Pp) {
   int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= n_dirs) return;
@@ -516,7 +516,7 @@ __global__ void k_sphere_sample(const float *__restrict__ Mh, const float4 *__re
 }
 
 // Corner value of the windowed image (the pad constant).
-__global__ void k_pad_constant(PrePadded pre, int n_items, float *padc) {
+static __global__ void k_pad_constant(PrePadded pre, int n_items, float *padc) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < n_items) padc[e] = pre.windowed(e, 0);
 }
@@ -527,7 +527,7 @@ __global__ void k_pad_constant(PrePadded pre, int n_items, float *padc) {
 // phi-FFT of each polar row then the quadrature sum with lw[m][l][j] = sqrt(2pi)/2B w_j P~_l^m(theta_j)
 // (SOFT FST_semi_memo, external/soft-1.0/FST_semi_memo.c:134-357).
 template <int B>
-__global__ void k_sht(const float *__restrict__ sig, const float *__restrict__ lw, float2 *__restrict__ coef) {
+static __global__ void k_sht(const float *__restrict__ sig, const float *__restrict__ lw, float2 *__restrict__ coef) {
   constexpr int n = 2 * B;
   extern __shared__ float2 smem[];
   float2 *tw = smem;
@@ -566,7 +566,7 @@ struct SynthJob {
   int f, h;  // signal indices of the two coefficient sets
 };
 template <int B>
-__global__ void k_so3_synth(const float2 *__restrict__ coef, const SynthJob *__restrict__ jobs, int n_jobs,
+static __global__ void k_so3_synth(const float2 *__restrict__ coef, const SynthJob *__restrict__ jobs, int n_jobs,
                             const float *__restrict__ dtab, const int *__restrict__ doff, float2 *__restrict__ S) {
   constexpr int n = 2 * B;
   __shared__ float sd[B * n];
@@ -607,7 +607,7 @@ __global__ void k_so3_synth(const float2 *__restrict__ coef, const SynthJob *__r
 // (soft_fftw.c:1913-1920; nbfProjectionRotationMetric3D.h:1254-1265), with packed min/max per job
 // in memory order (rotatedSphericalImageMinMax, 1557-1589).
 template <int B>
-__global__ void k_so3_real(const float2 *__restrict__ S, float *__restrict__ C, unsigned long long *mm) {
+static __global__ void k_so3_real(const float2 *__restrict__ S, float *__restrict__ C, unsigned long long *mm) {
   constexpr int n = 2 * B;
   const long n3 = (long)n * n * n;
   const int job = blockIdx.y;
@@ -641,7 +641,7 @@ struct ScaledJob {
   int job;    // correlation job (for the min/max cells)
 };
 template <int B>
-__global__ void k_so3_weights(const ScaledJob *__restrict__ sj, const unsigned long long *__restrict__ mm,
+static __global__ void k_so3_weights(const ScaledJob *__restrict__ sj, const unsigned long long *__restrict__ mm,
                               const float2 *__restrict__ coef, const float *__restrict__ sig,
                               const float *__restrict__ dtab, const int *__restrict__ doff, const float *__restrict__ plm,
                               const float *__restrict__ sinth, double *w) {

@@ -102,6 +102,18 @@ int ettk_gpu_spherical_projection(ettk_ctx *ctx, int r, int p, float *Pp);
  * softScaled's min/max rescaling (1297-1319). */
 int ettk_gpu_soft(ettk_ctx *ctx, const float *F1, const float *F2, int scaled, float *C);
 
+/* SO(3) correlation of two real S^2 signals that allocates no memory. No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc where they need the correlation,
+ * e.g. an application whose memory pool already owns the device memory or a process under a
+ * fixed memory budget. d_F1, d_F2 ([2B][2B] floats) and d_C ([2B]^3 floats, C[alpha][beta][gamma]
+ * as ettk_gpu_soft without scaling) are device buffers; the work is queued on `stream`
+ * (a cudaStream_t, NULL = default stream) and the call returns without waiting for it.
+ * Every intermediate lives in one 2 MiB file-scope device array of the library, so only B = 8 and
+ * B = 16 are accepted (ETTK_ERR_ARG otherwise). The first call on a device sets that device's array
+ * up (address and tables); make it before any stream capture on the device. All calls share the
+ * array: calls whose GPU work overlaps race, so serialise them. */
+int ettk_gpu_soft_noalloc(int B, const float *d_F1, const float *d_F2, float *d_C, void *stream);
+
 /* Number of kernels this library launched since the context was created. */
 long long ettk_gpu_kernel_launches(ettk_ctx *ctx);
 
