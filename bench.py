@@ -231,9 +231,10 @@ def main():
     clk = clocks.stop()
 
     hbm, tflops, peak_kind = peaks()
-    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    kernels = {k: v for k, v in prof.items() if not k.startswith("host_")}
+    dom_name, dom = max(kernels.items(), key=lambda kv: kv[1]["ms"])
     achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
-    total_prof_ms = sum(v["ms"] for v in prof.values())
+    total_prof_ms = sum(v["ms"] for v in kernels.values())
     value = world * P * a.steps / (ms * 1e-3)
     e2e = world * P * a.steps / (ms_e2e * 1e-3)
     out = {

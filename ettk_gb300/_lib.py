@@ -26,7 +26,7 @@ def build(verbose=False):
     deps = srcs + [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(ROOT, "include", "ettk_gpu.h")]
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
-    cmd = ["nvcc", *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-shared",
+    cmd = ["nvcc", *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "-shared",
            "-o", LIB + ".tmp", *srcs]
     subprocess.run(cmd, check=True, stdout=None if verbose else subprocess.DEVNULL)
     os.replace(LIB + ".tmp", LIB)
@@ -57,7 +57,7 @@ SYMBOLS = [
     "ettk_gpu_create", "ettk_gpu_destroy", "ettk_gpu_set_references", "ettk_gpu_set_particles",
     "ettk_gpu_set_particles_device", "ettk_gpu_align_pairs", "ettk_gpu_ccf", "ettk_gpu_spherical_projection",
     "ettk_gpu_soft", "ettk_gpu_kernel_launches", "ettk_gpu_last_error", "ettk_gpu_stream", "ettk_gpu_profile",
-    "ettk_gpu_profile_read", "ettk_gpu_soft_noalloc",
+    "ettk_gpu_profile_read", "ettk_gpu_soft_noalloc", "ettk_gpu_average",
 ]
 
 _lib = None
@@ -90,6 +90,7 @@ def load(path=None):
     L.ettk_gpu_stream.restype = ctypes.c_void_p
     L.ettk_gpu_profile.argtypes = [vp, ctypes.c_int]
     L.ettk_gpu_soft_noalloc.argtypes = [ctypes.c_int, vp, vp, vp, vp]
+    L.ettk_gpu_average.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
     L.ettk_gpu_profile_read.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_longlong),
                                         P(ctypes.c_double), P(ctypes.c_double)]
     for name in SYMBOLS:

@@ -65,20 +65,14 @@ ETTK_DEV unsigned long long warp_max_u64(unsigned long long v) {
   return v;
 }
 
-// vtkInterpolationMath::Floor (64-bit x86 branch): integer part of x + 2^-17 and the fraction
-// rounded to the 2^-16 grid that the reference's double arithmetic produces
-// (Filtering/vtkImageInterpolatorInternals.h:96-108). Computed from an FP32 coordinate.
+// vtkInterpolationMath::Floor (64-bit x86 branch, Filtering/vtkImageInterpolatorInternals.h:96-108):
+// x + (103079215104.0 + 2^-17) in double, where the constant is 1.5*2^36 and the 2^-17 tolerance term is
+// half an ulp of it and rounds away (ties to even), so the sum rounds x to the nearest multiple of 2^-16
+// (ties to even); the integer part and the fraction come from that rounded value. Exact for |x| < 128.
 ETTK_DEV int vtk_floor(float x, float &f) {
-  float xt = x + 7.62939453125e-06f;
-  float fi = floorf(xt);
-  float fr = xt - fi;
-  fr = rintf(fr * 65536.0f) * (1.0f / 65536.0f);
-  if (fr >= 1.0f) {
-    fr -= 1.0f;
-    fi += 1.0f;
-  }
-  f = fr;
-  return (int)fi;
+  int q = __float2int_rn(x * 65536.0f);
+  f = (float)(q & 0xFFFF) * (1.0f / 65536.0f);
+  return q >> 16;
 }
 
 // Tricubic weights of vtkImageInterpolator (Filtering/vtkImageInterpolator.cxx:313-325).

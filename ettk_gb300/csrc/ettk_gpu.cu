@@ -12,10 +12,13 @@
 #include "../../include/ettk_gpu.h"
 #include "geometry.hpp"
 #include "kernels.cuh"
+#include "fft_reg.cuh"
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <map>
+#include <memory>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -32,6 +35,14 @@ struct CudaError : std::runtime_error {
   int code;
   CudaError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
+
+// Output-index -> input-index map of a reslice item, in FP32 (default kernels) and FP64 (exact variant).
+inline void set_map(ResliceItem &it, const double m12[12]) {
+  for (int k = 0; k < 12; ++k) {
+    it.m[k] = (float)m12[k];
+    it.md[k] = m12[k];
+  }
+}
 
 #define CK(x)                                                                                     \
   do {                                                                                            \
@@ -351,7 +362,23 @@ struct ettk_ctx {
     }
   };
 
+  // host-side phases (wall time), reported through the same profile table
+  struct HostScope {
+    ettk_ctx *c;
+    const char *name;
+    std::chrono::steady_clock::time_point t0;
+    HostScope(ettk_ctx *c_, const char *n_) : c(c_), name(n_), t0(std::chrono::steady_clock::now()) {}
+    ~HostScope() {
+      if (!c->prof) return;
+      double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      ProfAgg &g = c->prof_agg[name];
+      g.n += 1;
+      g.ms += ms;
+    }
+  };
+
   void sync() {
+    HostScope hs(this, "host_wait");
     CK(cudaStreamSynchronize(st));
     if (prof) prof_flush();
   }
@@ -361,13 +388,18 @@ struct ettk_ctx {
   }
 
   // ---------------------------------------------------------------- FFT drivers
+  // CTA shape of the register FFT kernels: 256 threads = LINES x max(A, B)
+  template <int NN>
+  static constexpr int reg_lines() { return 256 / MaxAB<NN>::v; }
   template <int NN>
   void fft_strided_t(float2 *d, LineMap m, int sign, const float *scale, long scale_div) {
-    constexpr int L = (NN >= 128) ? 8 : 16;
-    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    constexpr int L = reg_lines<NN>();
     int blocks = (int)((m.n_lines + L - 1) / L);
     Scope sc(this, "fft_strided", 16.0 * m.n_lines * NN);
-    k_fft_strided<NN, L><<<blocks, 256, sm, st>>>(d, m, sign, scale, scale_div);
+    if (m.elem_stride == 1)
+      k_fft_reg<NN, L, true><<<blocks, 256, 0, st>>>(d, m, sign, scale, scale_div);
+    else
+      k_fft_reg<NN, L, false><<<blocks, 256, 0, st>>>(d, m, sign, scale, scale_div);
     post_launch();
   }
   void fft_strided(int len, float2 *d, LineMap m, int sign, const float *scale = nullptr, long scale_div = 1) {
@@ -382,11 +414,10 @@ struct ettk_ctx {
   }
   template <int NN, class Pre>
   void r2c_z_t(Pre pre, float2 *out, long lines) {
-    constexpr int L = (NN >= 128) ? 8 : 16;
-    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    constexpr int L = reg_lines<NN>();
     int blocks = (int)((lines + 2 * L - 1) / (2 * L));
     Scope sc(this, "fft_r2c_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
-    k_r2c_z<NN, L, Pre><<<blocks, 256, sm, st>>>(pre, out, lines);
+    k_r2c_reg<NN, L, Pre><<<blocks, 256, 0, st>>>(pre, out, lines);
     post_launch();
   }
   template <class Pre>
@@ -400,14 +431,22 @@ struct ettk_ctx {
       default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
     }
   }
-  static int lines_per_block(int len) { return 2 * ((len >= 128) ? 8 : 16); }
+  // real lines handled by one CTA of the r2c/c2r passes
+  static int lines_per_block(int len) {
+    switch (len) {
+      case 16: return 2 * reg_lines<16>();
+      case 32: return 2 * reg_lines<32>();
+      case 64: return 2 * reg_lines<64>();
+      case 128: return 2 * reg_lines<128>();
+      default: return 2 * reg_lines<256>();
+    }
+  }
   template <int NN, class Post>
   void c2r_z_t(const float2 *in, Post post, long lines) {
-    constexpr int L = (NN >= 128) ? 8 : 16;
-    size_t sm = (NN / 2 + (size_t)L * NN) * sizeof(float2);
+    constexpr int L = reg_lines<NN>();
     int blocks = (int)((lines + 2 * L - 1) / (2 * L));
     Scope sc(this, "fft_c2r_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
-    k_c2r_z<NN, L, Post><<<blocks, 256, sm, st>>>(in, post, lines);
+    k_c2r_reg<NN, L, Post><<<blocks, 256, 0, st>>>(in, post, lines);
     post_launch();
   }
   template <class Post>
@@ -454,7 +493,75 @@ struct ettk_ctx {
   }
   void align(int npairs, const int *pairs, float *D, int cols, int ncand);
   void soft_diag(const float *F1, const float *F2, int scaled, float *C);
+  void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
 };
+
+// Class average (getImageMPI + getImage): members resliced under Euler(normal) * alignment with their
+// own matrix reset to identity (inc/em/nbfWedgedAverageImage3D.h:313-319), R2C, |F|-weighted FP64
+// accumulation in member order, normalised inverse, RMS scaling.
+void ettk_ctx::average(int M, const int *parts, const float *weights, const double *mats, float *avg) {
+  std::vector<int> idx;
+  for (int i = 0; i < M; ++i) {
+    if (parts[i] < 0 || parts[i] >= V) throw CudaError(ETTK_ERR_ARG, "member index out of range");
+    if (fabs(weights[i]) > 0) idx.push_back(i);
+  }
+  DevBuf<double> &ac = w_w;  // reused: acc, re, im, sumsq
+  ac.ensure(3 * h3 + 1);
+  CK(cudaMemsetAsync(ac.p, 0, (3 * h3 + 1) * sizeof(double), st));
+  const int chunk = 256;
+  for (size_t c0 = 0; c0 < idx.size(); c0 += chunk) {
+    int E = (int)std::min<size_t>(chunk, idx.size() - c0);
+    std::vector<ResliceItem> items(E);
+    std::vector<float> w(E);
+    for (int e = 0; e < E; ++e) {
+      int i = idx[c0 + e];
+      VolumeGeom g = partg[parts[i]];
+      for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+      Mat4 t;
+      memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
+      double m12[12];
+      reslice_index(g, N, &t, m12);
+      items[e].vol = partptr + (long)parts[i] * n3;
+      items[e].dims[0] = items[e].dims[1] = items[e].dims[2] = N;
+      set_map(items[e], m12);
+      w[e] = weights[i];
+    }
+    w_items.ensure(E);
+    w_v.ensure((long)E * n3);
+    w_cA.ensure((long)E * h3);
+    w_acc.ensure(2L * E);
+    w_norm.ensure(E);
+    CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w_norm.p, w.data(), E * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
+    {
+      Scope sc(this, "reslice", 8.0 * E * n3);
+      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, 0, st>>>(w_items.p, N, w_v.p, w_acc.p, 2);
+      post_launch();
+    }
+    PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
+    r2c_z(N, pre, w_cA.p, (long)E * N * N);
+    xy_passes(N, w_cA.p, E, -1, false);
+    {
+      Scope sc(this, "avg_accum", 8.0 * E * h3 + 48.0 * h3);
+      k_avg_accum<<<nblocks<int>(h3, 256, 4096), 256, 0, st>>>(w_cA.p, w_norm.p, E, h3, ac.p, ac.p + h3, ac.p + 2 * h3);
+      post_launch();
+    }
+  }
+  w_cB.ensure(h3);
+  w_r.ensure(n3);
+  k_avg_spectrum<<<nblocks<int>(h3, 256, 4096), 256, 0, st>>>(ac.p, ac.p + h3, ac.p + 2 * h3, N, w_cB.p);
+  post_launch();
+  xy_passes(N, w_cB.p, 1, +1, true);
+  c2r_z(N, w_cB.p, PostStore{w_r.p, N}, (long)N * N);
+  k_avg_shift_sumsq<<<nblocks<int>(n3, 256, 1024), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3);
+  post_launch();
+  w_tmp.ensure(n3);
+  k_avg_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3, w_tmp.p);
+  post_launch();
+  CK(cudaMemcpyAsync(avg, w_tmp.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+}
 
 void ettk_ctx::init_tables() {
   N = p.N;
@@ -653,7 +760,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
     Scope sc(this, "reslice", 8.0 * P * n3);
-    k_reslice<<<dim3(nblocks<int>(n3, 256, 512), P), 256, 0, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, 0, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
   }
   post_launch();
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
@@ -693,10 +800,11 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   w_peak.ensure(E);
   w_out.ensure(E);
   w_p1.ensure(E * W * N * H);
-  w_p2.ensure(E * W * W * H);
   std::vector<ResliceItem> items(E);
   std::vector<WedgeVecs> wv(E);
   std::vector<int> refidx(E);
+  {
+    HostScope hs_prep(this, "host_eval_prep");
   for (long e = 0; e < E; ++e) {
     const EvalReq &r = req[e];
     const VolumeGeom &g = partg[r.part];
@@ -705,7 +813,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     ResliceItem it;
     it.vol = partptr + (long)r.part * n3;
     it.dims[0] = it.dims[1] = it.dims[2] = N;
-    for (int i = 0; i < 12; ++i) it.m[i] = (float)m12[i];
+    set_map(it, m12);
     items[e] = it;
     WedgeVecs w{};
     w.full = g.full_wedge() ? 1 : 0;
@@ -713,6 +821,8 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     wv[e] = w;
     refidx[e] = r.ref;
   }
+  }
+  std::unique_ptr<HostScope> hs_launch(new HostScope(this, "host_eval_issue"));
   CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(w_wv.p, wv.data(), E * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(w_idx.p, refidx.data(), E * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -724,16 +834,11 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   bool useWedge = p.wedge_compensation != 0;
   // wedge (W1 * W2(T)) * filter and its sum
   if (useWedge) {
-    Scope sc_w(this, "wedge", 4.0 * E * h3 * 7);
-    k_wedge_binary<<<gh, 256, 0, st>>>(w_wv.p, N, w_fw.p);
+    Scope sc_w(this, "wedge", 4.0 * E * h3);
+    size_t smw = 6 * (size_t)N * H * sizeof(float);
+    if (smw > 48 * 1024) CK(cudaFuncSetAttribute(k_wedge_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw));
+    k_wedge_fused<<<dim3(N, E), 256, smw, st>>>(w_wv.p, N, smooth, W1half.p, w_idx.p, filter.p, w_fw.p, acc, ACC, 6);
     post_launch();
-    k_wedge_smooth<<<gh, 256, 0, st>>>(w_fw.p, w_tmp.p, N, 2, smooth, nullptr, nullptr, nullptr, nullptr, 0, 0);
-    post_launch();
-    k_wedge_smooth<<<gh, 256, 0, st>>>(w_tmp.p, w_fw.p, N, 1, smooth, nullptr, nullptr, nullptr, nullptr, 0, 0);
-    post_launch();
-    k_wedge_smooth<<<gh, 256, 0, st>>>(w_fw.p, w_tmp.p, N, 0, smooth, W1half.p, w_idx.p, filter.p, acc, ACC, 6);
-    post_launch();
-    std::swap(w_fw, w_tmp);
   } else {
     for (long e = 0; e < E; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
   }
@@ -747,13 +852,20 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   xy_passes(N, w_cA.p, E, +1, true, w_norm.p);
   c2r_z(N, w_cA.p, PostStore{w_r.p, N}, E * N * N);
-  PreY1M1 py{w_r.p, mask.p, N, acc, ACC, 4, 0.0, (long)lines_per_block(N)};
+  PreY1M1 py;
+  py.y = w_r.p;
+  py.m1 = mask.p;
+  py.N = N;
+  py.acc = acc;
+  py.acc_stride = ACC;
+  py.slot = 4;
+  py.lines_per_block = lines_per_block(N);
   r2c_z(N, py, w_cA.p, E * N * N);
   xy_passes(N, w_cA.p, E, -1, false);
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift) * fw, normalised
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
-    k_reslice<<<gn, 256, 0, st>>>(w_items.p, N, w_v.p, acc2, ACC);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, 0, st>>>(w_items.p, N, w_v.p, acc2, ACC);
   }
   post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
@@ -773,18 +885,18 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
   {
-  Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
-  k_pruned_x<<<dim3(nblocks<int>((long)W * N * H, 256, 1024), E), 256, 0, st>>>(w_cC.p, w_p1.p, N, W, lo, o0);
+  Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H));
+  k_pruned_x<<<dim3((unsigned)((N * H + PX_R - 1) / PX_R), E), 256, 0, st>>>(w_cC.p, w_p1.p, N, W, lo, o0);
   post_launch();
-  k_pruned_y<<<dim3(nblocks<int>((long)W * W * H, 256, 1024), E), 256, 0, st>>>(w_p1.p, w_p2.p, N, W, lo, o0);
-  post_launch();
-  k_pruned_z_peak<<<dim3(nblocks<int>((long)W * W * W, 256, 1024), E), 256, 0, st>>>(w_p2.p, N, W, lo, o2, rr2,
-                                                                                      w_peak.p);
+  size_t smyz = ((size_t)N * H + (size_t)W * N + 2 * (size_t)W * H) * sizeof(float2);
+  if (smyz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_yz_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smyz));
+  k_pruned_yz_peak<<<dim3(W, E), 256, smyz, st>>>(w_p1.p, N, W, lo, o0, o2, rr2, w_peak.p);
   post_launch();
   }
   k_score<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, w_peak.p, (int)E, W, sum_filter, p.overlap_normalized,
                                                 useWedge ? 1 : 0, N, w_out.p);
   post_launch();
+  hs_launch.reset();
   std::vector<EvalOut> out(E);
   CK(cudaMemcpyAsync(out.data(), w_out.p, E * sizeof(EvalOut), cudaMemcpyDeviceToHost, st));
   sync();
@@ -894,7 +1006,7 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
           it.dims[0] = it.dims[1] = it.dims[2] = N;
           double m12[12];
           reslice_index(partg[ids[c]], N, nullptr, m12);
-          for (int k = 0; k < 12; ++k) it.m[k] = (float)m12[k];
+          set_map(it, m12);
           items.push_back(it);
         }
         w_sig.ensure(items.size() * nn);
@@ -1049,6 +1161,8 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
     }
     sync();
     std::vector<PQ> q1(P), q2(P);
+    {
+    HostScope hs_q(this, "host_queues");
     for (int q = 0; q < 2 * P; ++q) {
       int c = std::min(cnt[q], cap);
       std::vector<int2> L(lists.begin() + (long)q * cap, lists.begin() + (long)q * cap + c);
@@ -1064,6 +1178,7 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         if (transform_valid(p, euler_candidate(alpha, beta, gamma))) pos.push_back({{alpha, beta, gamma, -val}, -1});
       }
       eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f);
+    }
     }
     // 4. candidate rounds (execute 678-776): direct and mirror CCF per popped candidate
     struct PairState {
@@ -1438,7 +1553,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
       reslice_index(c->refg[r], c->N, nullptr, m12);
       items[r].vol = c->refvol.p + (long)r * n3;
       items[r].dims[0] = items[r].dims[1] = items[r].dims[2] = c->N;
-      for (int k = 0; k < 12; ++k) items[r].m[k] = (float)m12[k];
+      set_map(items[r], m12);
       std::vector<float> w;
       wedge_half_host(c->refg[r], c->N, w);
       std::copy(w.begin(), w.end(), w1h.begin() + (size_t)r * h3);
@@ -1457,7 +1572,8 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->w_items.ensure(R);
     CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
-    k_reslice<<<dim3(nblocks<int>(n3, 256, 512), R), 256, 0, c->st>>>(c->w_items.p, c->N, c->w_v.p, c->w_acc.p, 2);
+    k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, 0, c->st>>>(c->w_items.p, c->N, c->w_v.p,
+                                                                                          c->w_acc.p, 2);
     c->post_launch();
     c->FI1.ensure(R * h3);
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
@@ -1546,7 +1662,7 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
       reslice_index(c->refg[r], c->N, nullptr, m12);
     }
     it.dims[0] = it.dims[1] = it.dims[2] = c->N;
-    for (int k = 0; k < 12; ++k) it.m[k] = (float)m12[k];
+    set_map(it, m12);
     c->w_sig.ensure(c->nn);
     c->spherical_projection({it}, c->w_sig.p);
     CK(cudaMemcpyAsync(Pp, c->w_sig.p, c->nn * 4, cudaMemcpyDeviceToHost, c->st));
@@ -1557,6 +1673,13 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
 int ettk_gpu_soft(ettk_ctx *c, const float *F1, const float *F2, int scaled, float *C) {
   if (!c || !F1 || !F2 || !C) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   return guarded(c, [&] { c->soft_diag(F1, F2, scaled, C); });
+}
+
+int ettk_gpu_average(ettk_ctx *c, int M, const int *particles, const float *weights, const double *matrices,
+                     float *avg) {
+  if (!c || M < 0 || (M && (!particles || !weights || !matrices)) || !avg) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (c->V == 0) return fail(c, ETTK_ERR_STATE, "particles must be set first");
+  return guarded(c, [&] { c->average(M, particles, weights, matrices, avg); });
 }
 
 long long ettk_gpu_kernel_launches(ettk_ctx *c) { return c ? c->launches : 0; }

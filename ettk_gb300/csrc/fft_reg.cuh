@@ -1,0 +1,253 @@
+// Register-resident batched FFTs (four-step, N = A*B) for the alignment path.
+//
+// A line of N complex values x[n], n = B*j1 + j2, is transformed as
+//   y[k1][j2] = W_N^(j2*k1) * sum_j1 x[B*j1 + j2] W_A^(j1*k1)        (A-point DFT in registers per j2)
+//   X[k1 + A*k2] = sum_j2 y[k1][j2] W_B^(j2*k2)                         (B-point DFT in registers per k1)
+// with one shared-memory exchange of y in between. Thread t of a CTA owns (line = t % LINES, lane
+// = t / LINES) so that a warp touches the same element of 32 consecutive lines: global loads and
+// stores of strided axes are coalesced across lines. Conventions as fft.cuh (FFTW: forward
+// exp(-i...), unnormalised; the c2r pass uses only the real parts of the k=0 and k=N/2 inputs).
+#pragma once
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace ettk {
+
+template <int N>
+struct Split;
+template <> struct Split<16> { static const int A = 4, B = 4; };
+template <> struct Split<32> { static const int A = 8, B = 4; };
+template <> struct Split<64> { static const int A = 8, B = 8; };
+template <> struct Split<128> { static const int A = 16, B = 8; };
+template <> struct Split<256> { static const int A = 16, B = 16; };
+
+// cos/sin(2 pi k / 16), k < 16 (exact mathematical constants to float precision)
+__device__ __constant__ float kC16[16] = {1.0f, 0.92387953f, 0.70710678f, 0.38268343f, 0.0f, -0.38268343f,
+                                          -0.70710678f, -0.92387953f, -1.0f, -0.92387953f, -0.70710678f,
+                                          -0.38268343f, 0.0f, 0.38268343f, 0.70710678f, 0.92387953f};
+__device__ __constant__ float kS16[16] = {0.0f, 0.38268343f, 0.70710678f, 0.92387953f, 1.0f, 0.92387953f,
+                                          0.70710678f, 0.38268343f, 0.0f, -0.38268343f, -0.70710678f,
+                                          -0.92387953f, -1.0f, -0.92387953f, -0.70710678f, -0.38268343f};
+
+template <int R>
+struct Log2R;
+template <> struct Log2R<2> { static const int v = 1; };
+template <> struct Log2R<4> { static const int v = 2; };
+template <> struct Log2R<8> { static const int v = 3; };
+template <> struct Log2R<16> { static const int v = 4; };
+
+template <int R>
+ETTK_DEV constexpr int brev_c(int k) {
+  int r = 0;
+  for (int b = 0; b < Log2R<R>::v; ++b)
+    if (k & (1 << b)) r |= 1 << (Log2R<R>::v - 1 - b);
+  return r;
+}
+
+// In-register R-point DFT (natural order in and out), sign -1 forward, +1 inverse.
+template <int R>
+ETTK_DEV void dft_reg(float2 (&x)[R], int sign) {
+  float2 y[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) y[brev_c<R>(k)] = x[k];
+#pragma unroll
+  for (int half = 1; half < R; half <<= 1) {
+#pragma unroll
+    for (int s = 0; s < R; s += 2 * half) {
+#pragma unroll
+      for (int p = 0; p < half; ++p) {
+        const int idx = p * (16 / (2 * half));  // W_(2 half)^p = exp(-2 pi i p / (2 half)) on the 16-grid
+        // forward: exp(-i a) = (cos a, -sin a); inverse: (cos a, +sin a)
+        const float c = kC16[idx], sn = (sign < 0) ? -kS16[idx] : kS16[idx];
+        float2 a = y[s + p], b = y[s + p + half];
+        float2 bw = make_float2(b.x * c - b.y * sn, b.x * sn + b.y * c);
+        y[s + p] = make_float2(a.x + bw.x, a.y + bw.y);
+        y[s + p + half] = make_float2(a.x - bw.x, a.y - bw.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k) x[k] = y[k];
+}
+
+// Twiddle exp(sign * 2 pi i m / N) from the per-CTA table tw (forward values).
+template <int N>
+ETTK_DEV float2 twid(const float2 *tw, int m, int sign) {
+  float2 w = tw[m & (N - 1)];
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+template <int N>
+ETTK_DEV void load_full_twiddles(float2 *tw) {
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    float s, c;
+    sincospif(-2.0f * (float)k / (float)N, &s, &c);
+    tw[k] = make_float2(c, s);
+  }
+}
+
+// Core: thread (line, lane) with lane < B holds x[B*j1 + lane] (j1 < A) in `v`; after the call the
+// thread with lane < A holds X[lane + A*k2] (k2 < B) in `o`. ex is the CTA exchange buffer
+// [A*B][LINES+1] (index (k1*B + j2)*(LINES+1) + line; the pad keeps lane-strided accesses off one bank).
+template <int N>
+struct MaxAB {
+  static const int v = (Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B;
+};
+// Thread -> (line, lane). CONTIG (contiguous lines): lanes of one line are adjacent threads so that
+// element loads along the line coalesce; otherwise adjacent threads are adjacent lines.
+template <int N, int LINES, bool CONTIG>
+ETTK_DEV void thread_map(int &line, int &lane) {
+  if (CONTIG) {
+    line = threadIdx.x / MaxAB<N>::v;
+    lane = threadIdx.x % MaxAB<N>::v;
+  } else {
+    line = threadIdx.x % LINES;
+    lane = threadIdx.x / LINES;
+  }
+}
+template <int N, int LINES>
+ETTK_DEV void four_step(float2 (&v)[Split<N>::A], float2 (&o)[Split<N>::B], int line, int lane, int sign,
+                        const float2 *tw, float2 *ex) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  if (lane < B) {
+    dft_reg<A>(v, sign);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      float2 w = twid<N>(tw, lane * k1, sign);
+      float2 t = v[k1];
+      ex[(k1 * B + lane) * (LINES + 1) + line] = make_float2(t.x * w.x - t.y * w.y, t.x * w.y + t.y * w.x);
+    }
+  }
+  __syncthreads();
+  if (lane < A) {
+#pragma unroll
+    for (int j2 = 0; j2 < B; ++j2) o[j2] = ex[(lane * B + j2) * (LINES + 1) + line];
+    dft_reg<B>(o, sign);
+  }
+}
+
+// Strided complex pass (same LineMap as k_fft_strided); optional per-item scale on load.
+template <int N, int LINES, bool CONTIG>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_fft_reg(float2 *__restrict__ data, LineMap map, int sign, const float *__restrict__ line_scale, long scale_div) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  __shared__ float2 tw[N];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  load_full_twiddles<N>(tw);
+  int line, lane;
+  thread_map<N, LINES, CONTIG>(line, lane);
+  const long l = (long)blockIdx.x * LINES + line;
+  const bool ok = l < map.n_lines;
+  const long base = ok ? map.base(l) : 0;
+  float2 v[A], o[B];
+  float sc = 1.f;
+  if (ok && line_scale) sc = line_scale[l / scale_div];
+  if (lane < B) {
+#pragma unroll
+    for (int j1 = 0; j1 < A; ++j1) {
+      float2 t = ok ? data[base + (long)(B * j1 + lane) * map.elem_stride] : make_float2(0.f, 0.f);
+      v[j1] = make_float2(t.x * sc, t.y * sc);
+    }
+  }
+  __syncthreads();
+  four_step<N, LINES>(v, o, line, lane, sign, tw, ex);
+  if (lane < A && ok) {
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) data[base + (long)(lane + A * k2) * map.elem_stride] = o[k2];
+  }
+}
+
+// Real-to-complex pass along the contiguous axis: two real lines (2c, 2c+1) packed into one complex
+// FFT; Pre(line, k) supplies the real inputs; out has N/2+1 complex values per real line.
+template <int N, int LINES, class Pre>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_r2c_reg(Pre pre, float2 *__restrict__ out, long n_lines) {
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1;
+  __shared__ float2 tw[N];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  load_full_twiddles<N>(tw);
+  int line, lane;
+  thread_map<N, LINES, true>(line, lane);
+  const long c = (long)blockIdx.x * LINES + line;  // complex line = real lines 2c, 2c+1
+  const long l0 = 2 * c;
+  const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
+  float2 v[A], o[B];
+  pre.begin();
+  if (lane < B) {
+#pragma unroll
+    for (int j1 = 0; j1 < A; ++j1) {
+      int k = B * j1 + lane;
+      float a = ok0 ? pre(l0, k) : 0.f;
+      float b = ok1 ? pre(l0 + 1, k) : 0.f;
+      v[j1] = make_float2(a, b);
+    }
+  }
+  pre.end();
+  __syncthreads();
+  four_step<N, LINES>(v, o, line, lane, -1, tw, ex);
+  __syncthreads();
+  // full spectrum of the packed line back into the exchange buffer, [k][LINES]
+  if (lane < A) {
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
+  }
+  __syncthreads();
+  for (int k = lane; k < H; k += (A > B ? A : B)) {
+    float2 zk = ex[k * (LINES + 1) + line];
+    float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + line];
+    float2 x1 = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    float2 x2 = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+    if (ok0) out[l0 * H + k] = x1;
+    if (ok1) out[(l0 + 1) * H + k] = x2;
+  }
+}
+
+// Complex-to-real pass along the contiguous axis (two half spectra -> one packed complex inverse).
+template <int N, int LINES, class Post>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_c2r_reg(const float2 *__restrict__ in, Post post, long n_lines) {
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1;
+  __shared__ float2 tw[N];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  load_full_twiddles<N>(tw);
+  int line, lane;
+  thread_map<N, LINES, true>(line, lane);
+  const long c = (long)blockIdx.x * LINES + line;
+  const long l0 = 2 * c;
+  const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
+  float2 v[A], o[B];
+  if (lane < B) {
+#pragma unroll
+    for (int j1 = 0; j1 < A; ++j1) {
+      int k = B * j1 + lane;
+      float2 a, b;
+      if (k <= N / 2) {
+        a = ok0 ? in[l0 * H + k] : make_float2(0.f, 0.f);
+        b = ok1 ? in[(l0 + 1) * H + k] : make_float2(0.f, 0.f);
+        if (k == 0 || k == N / 2) {
+          a.y = 0.f;
+          b.y = 0.f;
+        }
+      } else {
+        a = ok0 ? cconj(in[l0 * H + (N - k)]) : make_float2(0.f, 0.f);
+        b = ok1 ? cconj(in[(l0 + 1) * H + (N - k)]) : make_float2(0.f, 0.f);
+      }
+      v[j1] = make_float2(a.x - b.y, a.y + b.x);
+    }
+  }
+  __syncthreads();
+  four_step<N, LINES>(v, o, line, lane, +1, tw, ex);
+  post.begin();
+  if (lane < A) {
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) {
+      int k = lane + A * k2;
+      if (ok0) post(l0, k, o[k2].x);
+      if (ok1) post(l0 + 1, k, o[k2].y);
+    }
+  }
+  post.end();
+}
+
+}  // namespace ettk

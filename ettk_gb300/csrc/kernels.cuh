@@ -10,7 +10,8 @@ namespace ettk {
 struct ResliceItem {
   const float *vol;
   int dims[3];
-  float m[12];  // origin[3], x axis[3], y axis[3], z axis[3]
+  float m[12];   // origin[3], x axis[3], y axis[3], z axis[3]
+  double md[12]; // the same in FP64 (used by the exact-coordinate variant)
 };
 
 // nbfWedgedSubImage3D::getImage (inc/em/nbfWedgedSubImage3D.h:602-828): tricubic reslice of the
@@ -73,6 +74,139 @@ static __global__ void k_reslice(const ResliceItem *__restrict__ items, int N, f
   }
 }
 
+// Same computation as k_reslice, one 8x8x8 output brick per CTA: the input footprint of the brick
+// (corner coordinates, widened by the cubic support and a rounding margin) is staged in shared memory
+// with clamped loads, so every tap of the brick reads shared memory. Bricks whose footprint exceeds the
+// staging buffer (strong scaling in the matrix) read global memory as k_reslice does.
+constexpr int RB = 8;                 // brick edge
+constexpr int RB_SMEM = 8192;         // staged floats (32 KiB)
+// PRECISE: the voxel coordinate follows the reference's FP64 sequence (origin + c*z) + b*y) + a*x without
+// FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5 output parity matters).
+template <bool PRECISE>
+__global__ void __launch_bounds__(256) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
+                                                       float *__restrict__ out, double *acc, int acc_stride) {
+  __shared__ float box[RB_SMEM];
+  __shared__ double sh[32];
+  const ResliceItem it = items[blockIdx.y];
+  const int nb = N / RB;
+  const int bx = blockIdx.x / (nb * nb), by = (blockIdx.x / nb) % nb, bz = blockIdx.x % nb;
+  const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
+  // footprint of the 8 corners (same affine map as the per-voxel coordinates)
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int c8 = 0; c8 < 8; ++c8) {
+    int a = bx * RB + ((c8 & 1) ? RB - 1 : 0), b = by * RB + ((c8 & 2) ? RB - 1 : 0), cz = bz * RB + ((c8 & 4) ? RB - 1 : 0);
+    for (int t = 0; t < 3; ++t) {
+      float p = it.m[t] + cz * it.m[9 + t];
+      p = p + b * it.m[6 + t];
+      p = p + a * it.m[3 + t];
+      lo[t] = fminf(lo[t], p);
+      hi[t] = fmaxf(hi[t], p);
+    }
+  }
+  int o[3], ext[3];
+  for (int t = 0; t < 3; ++t) {
+    o[t] = (int)floorf(lo[t]) - 2;
+    ext[t] = (int)floorf(hi[t]) + 4 - o[t] + 1;  // taps reach floor(p)+1+2, p may exceed hi by rounding
+  }
+  const long vol3 = (long)ext[0] * ext[1] * ext[2];
+  const bool staged = vol3 <= RB_SMEM;
+  if (staged) {
+    for (int i = threadIdx.x; i < vol3; i += blockDim.x) {
+      int ux = i % ext[0], uy = (i / ext[0]) % ext[1], uz = i / (ext[0] * ext[1]);
+      int x = min(max(o[0] + ux, 0), dx - 1), y = min(max(o[1] + uy, 0), dy - 1), z = min(max(o[2] + uz, 0), dz - 1);
+      box[i] = __ldg(it.vol + ((long)z * dy + y) * dx + x);
+    }
+  }
+  __syncthreads();
+  const long n3 = (long)N * N * N;
+  float s = 0.f;
+  int cnt = 0;
+  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
+    int a = bx * RB + v / (RB * RB), b = by * RB + (v / RB) % RB, cz = bz * RB + v % RB;
+    float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
+    p0 = p0 + b * it.m[6];
+    p1 = p1 + b * it.m[7];
+    p2 = p2 + b * it.m[8];
+    p0 = p0 + a * it.m[3];
+    p1 = p1 + a * it.m[4];
+    p2 = p2 + a * it.m[5];
+    float val = -FLT_MAX;
+    bool inside;
+    int ix, iy, iz;
+    float fx, fy, fz;
+    if (PRECISE) {
+      double q[3];
+      for (int t = 0; t < 3; ++t) {
+        double v = __dadd_rn(it.md[t], __dmul_rn((double)cz, it.md[9 + t]));
+        v = __dadd_rn(v, __dmul_rn((double)b, it.md[6 + t]));
+        q[t] = __dadd_rn(v, __dmul_rn((double)a, it.md[3 + t]));
+      }
+      inside = !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 || q[2] > dz - 0.5);
+      long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0), r2 = __double2ll_rn(q[2] * 65536.0);
+      ix = (int)(r0 >> 16); fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
+      iy = (int)(r1 >> 16); fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
+      iz = (int)(r2 >> 16); fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
+    } else {
+      inside = !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
+      ix = vtk_floor(p0, fx);
+      iy = vtk_floor(p1, fy);
+      iz = vtk_floor(p2, fz);
+    }
+    if (inside) {
+      float wx[4], wy[4], wz[4];
+      cubic_weights(wx, fx);
+      cubic_weights(wy, fy);
+      cubic_weights(wz, fz);
+      int mY = (dy > 1) && (fy != 0.f), mZ = (dz > 1) && (fz != 0.f);
+      if (!mY) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
+      if (!mZ) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
+      float acc2 = 0.f;
+      // The reference uses only the middle row/plane when fy/fz == 0; the full 4x4x4 sum with the
+      // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
+      if (staged) {
+        const float *b0 = box + ((long)(iz - 1 - o[2]) * ext[1] + (iy - 1 - o[1])) * ext[0] + (ix - 1 - o[0]);
+        const int ry = ext[0], rz = ext[0] * ext[1];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float *row = b0 + k * rz + j * ry;
+            acc2 += (wz[k] * wy[j]) * (wx[0] * row[0] + wx[1] * row[1] + wx[2] * row[2] + wx[3] * row[3]);
+          }
+        }
+      } else {
+        int xs[4], ys[4], zs[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          xs[t] = min(max(ix - 1 + t, 0), dx - 1);
+          ys[t] = min(max(iy - 1 + t, 0), dy - 1);
+          zs[t] = min(max(iz - 1 + t, 0), dz - 1);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float *row = it.vol + ((long)zs[k] * dy + ys[j]) * dx;
+            acc2 += (wz[k] * wy[j]) * (wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
+                                       wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]));
+          }
+        }
+      }
+      val = acc2;
+      s += val;
+      cnt += 1;
+    }
+    out[(long)blockIdx.y * n3 + ((long)a * N + b) * N + cz] = val;
+  }
+  if (acc) {
+    double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
+    if (threadIdx.x == 0) {
+      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 0], bs);
+      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 1], bc);
+    }
+  }
+}
+
 // Binary wedge on the centred half grid (nbfWedge3D::getImageHalf, inc/em/nbfWedge3D.h:312-356):
 // ((v1.d)(v2.d) <= 0) with d = (i-N/2, j-N/2, k-N/2). Near the planes the test is redone in FP64
 // with the reference's operation order (no FMA) so exact-zero cases resolve as they do there.
@@ -85,10 +219,11 @@ static __global__ void k_wedge_binary(const WedgeVecs *__restrict__ wv, int N, f
   long h3 = (long)N * N * H;
   const WedgeVecs w = wv[blockIdx.y];
   float f1[3] = {(float)w.v1[0], (float)w.v1[1], (float)w.v1[2]}, f2[3] = {(float)w.v2[0], (float)w.v2[1], (float)w.v2[2]};
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+  const int nh = N * H;
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
     float r = 1.f;
     if (!w.full) {
-      int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+      int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
       float di = (float)(i - N / 2), dj = (float)(j - N / 2), dk = (float)(k - (H - 1));
       float a = f1[0] * di + f1[1] * dj + f1[2] * dk, b = f2[0] * di + f2[1] * dj + f2[2] * dk;
       if (fabsf(a) > 1e-3f && fabsf(b) > 1e-3f) {
@@ -122,12 +257,13 @@ static __global__ void k_wedge_smooth(const float *__restrict__ in, float *__res
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
   const float *src = in + (long)blockIdx.y * h3;
-  double s = 0;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
-    int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+  float s = 0.f;
+  const int nh = N * H;
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
+    int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
     int pos = axis == 2 ? k : (axis == 1 ? j : i);
     int n = axis == 2 ? H : N;
-    long st = axis == 2 ? 1 : (axis == 1 ? H : (long)N * H);
+    int st = axis == 2 ? 1 : (axis == 1 ? H : nh);
     float v;
     if (n == 1) v = src[id];
     else if (pos == 0) v = sw.w_lo[0] * src[id] + sw.w_lo[1] * src[id + st];
@@ -136,15 +272,81 @@ static __global__ void k_wedge_smooth(const float *__restrict__ in, float *__res
     if (axis == 0) {
       float wedge = v * w1[(long)w1_index[blockIdx.y] * h3 + id];
       float fw = filter[id] * wedge;
-      s += (double)fw;
+      s += fw;
       v = fw;
     }
     out[(long)blockIdx.y * h3 + id] = v;
   }
   if (axis == 0) {
-    double b = block_sum(s, sh);
+    double b = block_sum((double)s, sh);
     if (threadIdx.x == 0) atomicAdd(&acc[(long)blockIdx.y * acc_stride + acc_slot], b);
   }
+}
+
+// Binary wedge + the three smoothing passes + (wedge2 * wedge1) * filter in one kernel: one CTA per
+// (x plane i, item) builds the binary wedge of planes i-1, i, i+1 in shared memory, smooths along k then j
+// (float rounding after each pass, as vtkImageGaussianSmooth stores its intermediates), then along i, and
+// writes fw = filter * (wedge2 * wedge1) for plane i plus the partial sum(fw). Dynamic shared memory:
+// 2 * 3 * N * (N/2+1) floats.
+ETTK_DEV float wedge_bit(const WedgeVecs &w, const float f1[3], const float f2[3], int i, int j, int k, int N, int H) {
+  if (w.full) return 1.f;
+  float di = (float)(i - N / 2), dj = (float)(j - N / 2), dk = (float)(k - (H - 1));
+  float a = f1[0] * di + f1[1] * dj + f1[2] * dk, b = f2[0] * di + f2[1] * dj + f2[2] * dk;
+  if (fabsf(a) > 1e-3f && fabsf(b) > 1e-3f) return (a * b <= 0.f) ? 1.f : 0.f;
+  double ad = __dadd_rn(__dadd_rn(__dmul_rn(w.v1[0], (double)di), __dmul_rn(w.v1[1], (double)dj)),
+                        __dmul_rn(w.v1[2], (double)dk));
+  double bd = __dadd_rn(__dadd_rn(__dmul_rn(w.v2[0], (double)di), __dmul_rn(w.v2[1], (double)dj)),
+                        __dmul_rn(w.v2[2], (double)dk));
+  return (__dmul_rn(ad, bd) <= 0.0) ? 1.f : 0.f;
+}
+ETTK_DEV float smooth3(const Smooth3 &sw, const float *p, int pos, int n, int st) {
+  if (n == 1) return p[0];
+  if (pos == 0) return sw.w_lo[0] * p[0] + sw.w_lo[1] * p[st];
+  if (pos == n - 1) return sw.w_hi[0] * p[-st] + sw.w_hi[1] * p[0];
+  return sw.w_int[0] * p[-st] + sw.w_int[1] * p[0] + sw.w_int[2] * p[st];
+}
+static __global__ void __launch_bounds__(256) k_wedge_fused(const WedgeVecs *__restrict__ wv, int N, Smooth3 sw,
+                                                            const float *__restrict__ w1, const int *__restrict__ w1_index,
+                                                            const float *__restrict__ filter, float *__restrict__ out,
+                                                            double *acc, int acc_stride, int acc_slot) {
+  extern __shared__ float wsm[];
+  __shared__ double sh[32];
+  const int H = N / 2 + 1, plane = N * H;
+  float *A = wsm, *Bf = wsm + 3 * plane;
+  const int i = blockIdx.x, e = blockIdx.y;
+  const WedgeVecs w = wv[e];
+  const float f1[3] = {(float)w.v1[0], (float)w.v1[1], (float)w.v1[2]};
+  const float f2[3] = {(float)w.v2[0], (float)w.v2[1], (float)w.v2[2]};
+  const int p0 = max(i - 1, 0), p1 = min(i + 1, N - 1), np = p1 - p0 + 1;
+  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
+    int q = t / plane, r = t - q * plane, j = r / H, k = r - j * H;
+    A[t] = wedge_bit(w, f1, f2, p0 + q, j, k, N, H);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
+    int r = t % plane, k = r % H;
+    Bf[t] = smooth3(sw, A + t, k, H, 1);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
+    int r = t % plane, j = r / H;
+    A[t] = smooth3(sw, Bf + t, j, N, H);
+  }
+  __syncthreads();
+  const long h3 = (long)plane * N;
+  const float *W1 = w1 + (long)w1_index[e] * h3 + (long)i * plane;
+  const float *F = filter + (long)i * plane;
+  float *o = out + (long)e * h3 + (long)i * plane;
+  float s = 0.f;
+  for (int r = threadIdx.x; r < plane; r += blockDim.x) {
+    float v = smooth3(sw, A + (i - p0) * plane + r, i, N, plane);
+    float wedge = v * W1[r];
+    float fw = F[r] * wedge;
+    o[r] = fw;
+    s += fw;
+  }
+  double b = block_sum((double)s, sh);
+  if (threadIdx.x == 0) atomicAdd(&acc[(long)e * acc_stride + acc_slot], b);
 }
 
 // executeHalf + normalizeFourierHalf accumulation (inc/em/nbfFourierFilter.h:586-606,
@@ -159,15 +361,15 @@ static __global__ void k_spec_filter(const float2 *__restrict__ src, const int *
   long sidx = src_index ? (long)src_index[blockIdx.y] : (long)blockIdx.y;
   const float2 *S = src + sidx * h3;
   long dc = ((long)(N / 2) * N + N / 2) * H + (H - 1);
-  double s1 = 0, s2 = 0;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+  float s1 = 0.f, s2 = 0.f;  // per-thread partials over a few elements; FP64 across threads
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
     float2 v = cscale(S[id], fw[(long)blockIdx.y * h3 + id]);
     if (id == dc) v = make_float2(0.f, 0.f);
     out[(long)blockIdx.y * h3 + id] = v;
-    double m = (double)v.x * v.x + (double)v.y * v.y;
+    float m = v.x * v.x + v.y * v.y;
     if ((id % H) < H - 1) s1 += m; else s2 += m;
   }
-  double b1 = block_sum(s1, sh), b2 = block_sum(s2, sh);
+  double b1 = block_sum((double)s1, sh), b2 = block_sum((double)s2, sh);
   if (threadIdx.x == 0) {
     atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot], b1);
     atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot + 1], b2);
@@ -197,22 +399,25 @@ struct PreY1M1 {
   int N;
   double *acc;
   int acc_stride, slot;
-  double s;
-  ETTK_DEV void begin() { s = 0; }
+  float s = 0.f;  // per-thread partial (a thread sees at most a few dozen elements); FP64 across threads
+  long lines_per_block = 0;  // real lines handled by one CTA (never straddles two items)
+  long cl = -1, cr = 0;      // per-thread cache of the last line's in-item row
+  ETTK_DEV void begin() { s = 0.f; }
   ETTK_DEV float operator()(long line, int k) {
-    long n2 = (long)N * N;
-    long e = line / n2, r = line - e * n2;
+    if (line != cl) {
+      cl = line;
+      cr = line % ((long)N * N);
+    }
     float v = y[line * N + k];
-    float m = m1[r * N + k];
-    s += (double)v * (double)v * (double)m;
+    float m = m1[cr * N + k];
+    s += v * v * m;
     return v * m;
   }
   ETTK_DEV void end() {
     __shared__ double shm[32];
-    double b = block_sum(s, shm);
+    double b = block_sum((double)s, shm);
     if (threadIdx.x == 0) atomicAdd(&acc[item_of_block() * acc_stride + slot], b);
   }
-  long lines_per_block;  // real lines handled by one CTA (never straddles two items)
   ETTK_DEV long item_of_block() const { return ((long)blockIdx.x * lines_per_block) / ((long)N * N); }
 };
 
@@ -223,20 +428,29 @@ struct PreParticle {
   const float *maskfft;
   const double *acc;
   int acc_stride, N;
+  long cached = -1;  // per-thread: item whose mean is in `mean`
+  float mean = 0.f;
+  long cl = -1;      // per-thread cache of the last line's decomposition
+  int cr = 0, cij = 0;
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV float operator()(long line, int k) {
-    long n2 = (long)N * N;
-    long e = line / n2, r = line - e * n2;
-    float val = v[line * N + k];
-    float out = 0.f;
-    if (val > -FLT_MAX) {
-      float cnt = (float)acc[e * acc_stride + 1];
-      float mean = (float)(acc[e * acc_stride + 0] / (double)cnt);
-      out = val - mean;
+    if (line != cl) {
+      long n2 = (long)N * N;
+      long e = line / n2;
+      cl = line;
+      cr = (int)(line - e * n2);
+      cij = cr / N + cr % N;
+      if (e != cached) {
+        float cnt = (float)acc[e * acc_stride + 1];
+        mean = (float)(acc[e * acc_stride + 0] / (double)cnt);
+        cached = e;
+      }
     }
-    int i = (int)(r / N), j = (int)(r % N);
-    return out * maskfft[r * N + k] * parity_sign(i, j, k);
+    float val = v[line * N + k];
+    float out = (val > -FLT_MAX) ? val - mean : 0.f;
+    float m = maskfft ? maskfft[(long)cr * N + k] : 1.f;
+    return out * m * (((cij + k) & 1) ? -1.f : 1.f);
   }
 };
 
@@ -244,13 +458,18 @@ struct PreParticle {
 struct PreSquareShift {
   const float *y;
   int N;
+  long cl = -1;
+  int cij = 0;
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV float operator()(long line, int k) {
-    long r = line % ((long)N * N);
-    int i = (int)(r / N), j = (int)(r % N);
+    if (line != cl) {
+      cl = line;
+      int r = (int)(line % ((long)N * N));
+      cij = r / N + r % N;
+    }
     float v = y[line * N + k];
-    return v * v * parity_sign(i, j, k);
+    return v * v * (((cij + k) & 1) ? -1.f : 1.f);
   }
 };
 
@@ -286,7 +505,7 @@ static __global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
   float sc = inv_norm2[blockIdx.y] * (float)((long)N * N * N);
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
     long g = (long)blockIdx.y * h3 + id;
     float2 b = cscale(f2[g], sc);
     a[g] = cscale(cmul(a[g], cconj(b)), 2.0f);
@@ -299,9 +518,10 @@ static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict_
                         float factor) {
   const int H = N / 2 + 1;
   long h3 = (long)N * N * H;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+  const int nh = N * H;
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
     long g = (long)blockIdx.y * h3 + id;
-    int i = (int)(id / ((long)N * H)), j = (int)((id / H) % N), k = (int)(id % H);
+    int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
     float2 v = cadd(cscale(cmul(fm1[id], cconj(q[g])), -1.f), fft2re[g]);
     q[g] = cscale(v, parity_sign(i, j, k) * factor);
   }
@@ -310,77 +530,130 @@ static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict_
 // Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
 // [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
 // and reads only this window). Same FFTW order: complex inverse along x, then y, then the
-// half-complex-to-real sum along z (real parts only for the kz=N term).
-// Stage x: q1[e][X][ky][kz] = sum_kx q[e][kx][ky][kz] exp(+2 pi i (kx+o0) (lo+X) / 2N)
-static __global__ void k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N, int W, int lo, int o0) {
+// half-complex-to-real sum along z (real parts only for the kz = N term).
+//
+// Stage x (a complex GEMM per item): q1[e][X][r] = sum_kx E[X][kx] q[e][kx][r], r = (ky,kz),
+// E[X][kx] = exp(+i pi ((kx+o0)(lo+X) mod 2N) / N). CTA = 64 consecutive r of one item; kx in chunks
+// of 32 staged in shared memory with the twiddle rows; each thread accumulates up to XPT outputs.
+constexpr int PX_R = 64, PX_K = 32, PX_XPT = 16;
+static __global__ void __launch_bounds__(256) k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N,
+                                                         int W, int lo, int o0) {
+  __shared__ float2 Qs[PX_K][PX_R];
+  __shared__ float2 Es[4 * PX_XPT][PX_K];
   const int H = N / 2 + 1;
-  long nrow = (long)N * H;  // (ky,kz) per X
-  long total = (long)W * nrow;
+  const long nrow = (long)N * H;
   const float2 *Q = q + (long)blockIdx.y * N * nrow;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
-    int X = (int)(id / nrow);
-    long r = id - (long)X * nrow;
-    int XX = lo + X;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int kx = 0; kx < N; ++kx) {
-      int ph = ((kx + o0) * XX) % (2 * N);
-      float s, c;
-      sincospif((float)ph / (float)N, &s, &c);
-      acc = cadd(acc, cmul(Q[(long)kx * nrow + r], make_float2(c, s)));
+  const long r0 = (long)blockIdx.x * PX_R;
+  const int tr = threadIdx.x & (PX_R - 1), tx = threadIdx.x >> 6;  // 4 X-lanes
+  for (int xb = 0; xb < W; xb += 4 * PX_XPT) {
+    float2 acc[PX_XPT];
+#pragma unroll
+    for (int t = 0; t < PX_XPT; ++t) acc[t] = make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < N; k0 += PX_K) {
+      int kc = min(PX_K, N - k0);
+      __syncthreads();
+      for (int i = threadIdx.x; i < kc * PX_R; i += blockDim.x) {
+        int kk = i / PX_R, rr = i - kk * PX_R;
+        long r = r0 + rr;
+        Qs[kk][rr] = (r < nrow) ? Q[(long)(k0 + kk) * nrow + r] : make_float2(0.f, 0.f);
+      }
+      for (int i = threadIdx.x; i < 4 * PX_XPT * kc; i += blockDim.x) {
+        int xx = i / kc, kk = i - xx * kc;
+        int X = xb + xx;
+        float2 e = make_float2(0.f, 0.f);
+        if (X < W) {
+          int ph = ((k0 + kk + o0) * (lo + X)) & (2 * N - 1);
+          float sn, cs;
+          sincospif((float)ph / (float)N, &sn, &cs);
+          e = make_float2(cs, sn);
+        }
+        Es[xx][kk] = e;
+      }
+      __syncthreads();
+      for (int kk = 0; kk < kc; ++kk) {
+        float2 v = Qs[kk][tr];
+#pragma unroll
+        for (int t = 0; t < PX_XPT; ++t) {
+          float2 e = Es[tx + 4 * t][kk];
+          acc[t].x += v.x * e.x - v.y * e.y;
+          acc[t].y += v.x * e.y + v.y * e.x;
+        }
+      }
     }
-    q1[(long)blockIdx.y * total + id] = acc;
+    long r = r0 + tr;
+    if (r < nrow) {
+#pragma unroll
+      for (int t = 0; t < PX_XPT; ++t) {
+        int X = xb + tx + 4 * t;
+        if (X < W) q1[((long)blockIdx.y * W + X) * nrow + r] = acc[t];
+      }
+    }
   }
 }
-// Stage y: q2[e][X][Y][kz] = sum_ky q1[e][X][ky][kz] exp(+2 pi i (ky+o0)(lo+Y)/2N)
-static __global__ void k_pruned_y(const float2 *__restrict__ q1, float2 *__restrict__ q2, int N, int W, int lo, int o0) {
+
+// Stages y and z plus the peak search, one CTA per (X, item):
+// q2[Y][kz] = sum_ky Ey[Y][ky] q1[X][ky][kz]; out[Y][Z] = sum_kz c_kz Re(q2[Y][kz] Ez[Z][kz]);
+// T = out * (-1)^(X+Y+Z) / (2N)^3 inside the sphere radius^2 < r^2 (else -max); packed argmax
+// (first occurrence in [X][Y][Z] order) into peak[e]. Dynamic shared memory:
+// q1 plane N*H, Ey W*N, q2 W*H, Ez W*H complex values.
+static __global__ void __launch_bounds__(256) k_pruned_yz_peak(const float2 *__restrict__ q1, int N, int W, int lo,
+                                                               int o0, int o2, float rr2,
+                                                               unsigned long long *peak) {
+  extern __shared__ float2 sm[];
   const int H = N / 2 + 1;
-  long total = (long)W * W * H;
-  const float2 *Q = q1 + (long)blockIdx.y * W * N * H;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
-    int X = (int)(id / ((long)W * H)), Y = (int)((id / H) % W), kz = (int)(id % H);
-    int YY = lo + Y;
+  float2 *P1 = sm;               // [N][H]
+  float2 *Ey = P1 + N * H;       // [W][N]
+  float2 *P2 = Ey + W * N;       // [W][H]
+  float2 *Ez = P2 + W * H;       // [W][H] (with the hc2r coefficient folded in)
+  const int X = blockIdx.x, e = blockIdx.y;
+  const float2 *src = q1 + ((long)e * W + X) * (long)N * H;
+  for (int i = threadIdx.x; i < N * H; i += blockDim.x) P1[i] = src[i];
+  for (int i = threadIdx.x; i < W * N; i += blockDim.x) {
+    int Y = i / N, ky = i - Y * N;
+    int ph = ((ky + o0) * (lo + Y)) & (2 * N - 1);
+    float sn, cs;
+    sincospif((float)ph / (float)N, &sn, &cs);
+    Ey[i] = make_float2(cs, sn);
+  }
+  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
+    int Z = i / H, kz = i - Z * H;
+    int KZ = kz + o2;
+    int ph = (KZ * (lo + Z)) & (2 * N - 1);
+    float sn, cs;
+    sincospif((float)ph / (float)N, &sn, &cs);
+    float c = (KZ == N || KZ == 0) ? 1.f : 2.f;
+    Ez[i] = make_float2(c * cs, c * sn);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
+    int Y = i / H, kz = i - Y * H;
     float2 acc = make_float2(0.f, 0.f);
     for (int ky = 0; ky < N; ++ky) {
-      int ph = ((ky + o0) * YY) % (2 * N);
-      float s, c;
-      sincospif((float)ph / (float)N, &s, &c);
-      acc = cadd(acc, cmul(Q[((long)X * N + ky) * H + kz], make_float2(c, s)));
+      float2 a = Ey[Y * N + ky], b = P1[ky * H + kz];
+      acc.x += a.x * b.x - a.y * b.y;
+      acc.y += a.x * b.y + a.y * b.x;
     }
-    q2[(long)blockIdx.y * total + id] = acc;
+    P2[i] = acc;
   }
-}
-// Stage z + peak: T = out * shift / (2N)^3 inside the sphere radius^2 < r^2 (else -max);
-// packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
-static __global__ void k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo, int o2, float rr2,
-                                unsigned long long *peak) {
-  const int H = N / 2 + 1;
-  long total = (long)W * W * W;
-  const float2 *Q = q2 + (long)blockIdx.y * W * W * H;
+  __syncthreads();
   const float inv = 1.0f / (float)(8L * N * N * N);
+  const int half = (W - 1) / 2;
   unsigned long long best = 0;
-  int half = (W - 1) / 2;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
-    int X = (int)(id / ((long)W * W)), Y = (int)((id / W) % W), Z = (int)(id % W);
-    int ZZ = lo + Z;
-    const float2 *row = Q + ((long)X * W + Y) * H;
+  for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+    int Y = i / W, Z = i - Y * W;
     float acc = 0.f;
     for (int kz = 0; kz < H; ++kz) {
-      int KZ = kz + o2;
-      int ph = (KZ * ZZ) % (2 * N);
-      float s, c;
-      sincospif((float)ph / (float)N, &s, &c);
-      float2 v = row[kz];
-      float re = v.x * c - v.y * s;
-      acc += (KZ == N || KZ == 0) ? re : 2.f * re;
+      float2 v = P2[Y * H + kz], t = Ez[Z * H + kz];
+      acc += v.x * t.x - v.y * t.y;
     }
-    float T = acc * parity_sign(lo + X, lo + Y, ZZ) * inv;
+    float T = acc * parity_sign(lo + X, lo + Y, lo + Z) * inv;
     float rad = (float)((half - X) * (half - X) + (half - Y) * (half - Y) + (half - Z) * (half - Z));
     if (!(rad < rr2)) T = -FLT_MAX;
-    unsigned long long key = pack_max(T, (uint32_t)id);
+    unsigned long long key = pack_max(T, (uint32_t)(((long)X * W + Y) * W + Z));
     best = key > best ? key : best;
   }
   best = warp_max_u64(best);
-  if ((threadIdx.x & 31) == 0) atomicMax(&peak[blockIdx.y], best);
+  if ((threadIdx.x & 31) == 0) atomicMax(&peak[e], best);
 }
 
 // Final CCF distance and half-voxel shift (nbfFourierImageMetric.h:1249-1264).
@@ -410,6 +683,66 @@ static __global__ void k_score(const double *acc, int acc_stride, const unsigned
   out[e] = o;
 }
 
+// ---- class average (nbfWedgedAverageImage3D::getImageMPI / getImage, inc/em/nbfWedgedAverageImage3D.h:216-356)
+
+// acc += |w| |F|, re += w |F| Re F, im += w |F| Im F over the chunk's members in order (deterministic, FP64).
+static __global__ void k_avg_accum(const float2 *__restrict__ F, const float *__restrict__ w, int n_members, long h3,
+                                   double *__restrict__ acc, double *__restrict__ re, double *__restrict__ im) {
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    double a = acc[id], r = re[id], m = im[id];
+    for (int i = 0; i < n_members; ++i) {
+      float2 f = F[(long)i * h3 + id];
+      double b = sqrt((double)f.x * f.x + (double)f.y * f.y);
+      double wi = w[i];
+      a += fabs(wi) * b;
+      r += wi * b * (double)f.x;
+      m += wi * b * (double)f.y;
+    }
+    acc[id] = a;
+    re[id] = r;
+    im[id] = m;
+  }
+}
+
+// F = (re, im) / acc where acc > 0, DC zeroed (getImage lines 224-228)
+static __global__ void k_avg_spectrum(const double *__restrict__ acc, const double *__restrict__ re,
+                                      const double *__restrict__ im, int N, float2 *__restrict__ F) {
+  const int H = N / 2 + 1;
+  long h3 = (long)N * N * H, dc = ((long)(N / 2) * N + N / 2) * H + (H - 1);
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
+    float2 v = make_float2(0.f, 0.f);
+    if (acc[id] > 0) v = make_float2((float)(re[id] / acc[id]), (float)(im[id] / acc[id]));
+    if (id == dc) v = make_float2(0.f, 0.f);
+    F[id] = v;
+  }
+}
+
+// average = C2R * shift / N^3 (already in y), sum of squares into acc_out[0]
+static __global__ void k_avg_shift_sumsq(float *__restrict__ y, int N, double *acc_out) {
+  __shared__ double sh[32];
+  long n3 = (long)N * N * N;
+  float s = 0.f;
+  const float inv = 1.0f / (float)n3;
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
+    int x = id / (N * N), yy = (id / N) % N, z = id % N;
+    float v = y[id] * inv * parity_sign(x, yy, z);
+    y[id] = v;
+    s += v * v;
+  }
+  double b = block_sum((double)s, sh);
+  if (threadIdx.x == 0) atomicAdd(acc_out, b);
+}
+
+// divide by the RMS (float, as varianceInside) and write x-fastest
+static __global__ void k_avg_finish(const float *__restrict__ y, int N, const double *sumsq, float *__restrict__ out) {
+  long n3 = (long)N * N * N;
+  float rms = (float)sqrt(sumsq[0] / (double)n3);
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
+    int x = id / (N * N), yy = (id / N) % N, z = id % N;
+    out[x + (long)N * (yy + (long)N * z)] = y[id] / rms;
+  }
+}
+
 // ---- spherical projection ------------------------------------------------------------------
 
 // mean over all voxels of the mean-subtracted particle (nbfImageFilter::execute meanValue,
@@ -420,12 +753,12 @@ static __global__ void k_mean_all(const float *__restrict__ v, const double *acc
   long n3 = (long)N * N * N;
   const double *a = acc_in + (long)blockIdx.y * acc_stride;
   float mean = (float)(a[0] / (double)(float)a[1]);
-  double s = 0;
+  float s = 0.f;
   for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
     float x = v[(long)blockIdx.y * n3 + id];
-    s += (x > -FLT_MAX) ? (double)(x - mean) : 0.0;
+    s += (x > -FLT_MAX) ? (x - mean) : 0.f;
   }
-  double b = block_sum(s, sh);
+  double b = block_sum((double)s, sh);
   if (threadIdx.x == 0) atomicAdd(&acc_out[(long)blockIdx.y * acc_stride + slot], b);
 }
 
@@ -436,23 +769,36 @@ struct PrePadded {
   const float *mask;
   const double *acc;
   int acc_stride, N;
+  long cached = -1;  // per-thread: item whose means are cached
+  float mean = 0.f, meanAll = 0.f;
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
-  ETTK_DEV float windowed(long e, long id) const {
+  ETTK_DEV void load(long e) {
     const double *a = acc + e * acc_stride;
-    float mean = (float)(a[0] / (double)(float)a[1]);
-    float meanAll = (float)(a[2] / (double)((long)N * N * N));
+    mean = (float)(a[0] / (double)(float)a[1]);
+    meanAll = (float)(a[2] / (double)((long)N * N * N));
+    cached = e;
+  }
+  ETTK_DEV float windowed(long e, long id) {
+    if (e != cached) load(e);
     float x = v[e * (long)N * N * N + id];
     float img = (x > -FLT_MAX) ? x - mean : 0.f;
     return (img - meanAll) * mask[id] + meanAll;
   }
+  long cl = -1, ce = 0;
+  int cx = 0, cy = 0;
   ETTK_DEV float operator()(long line, int z) {
-    const int N2 = 2 * N;
-    long per = (long)N2 * N2;
-    long e = line / per, r = line - e * per;
-    int x = (int)(r / N2), y = (int)(r % N2);
-    float val = (x < N && y < N && z < N) ? windowed(e, ((long)x * N + y) * N + z) : windowed(e, 0);
-    return val * parity_sign(x, y, z);
+    if (line != cl) {
+      const int N2 = 2 * N;
+      long per = (long)N2 * N2;
+      ce = line / per;
+      int r = (int)(line - ce * per);
+      cx = r / N2;
+      cy = r % N2;
+      cl = line;
+    }
+    float val = (cx < N && cy < N && z < N) ? windowed(ce, ((long)cx * N + cy) * N + z) : windowed(ce, 0);
+    return val * parity_sign(cx, cy, z);
   }
 };
 
@@ -613,8 +959,8 @@ static __global__ void k_so3_real(const float2 *__restrict__ S, float *__restric
   const int job = blockIdx.y;
   const float scale = (1.0f / n) * ((float)B / 3.14159265358979f);
   unsigned long long bmax = 0, bmin = 0;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
-    int a = (int)(id / ((long)n * n)), b = (int)((id / n) % n), g = (int)(id % n);
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
+    int a = id / (n * n), b = (id / n) & (n - 1), g = id & (n - 1);
     float v = S[(((long)job * n + b) * n + a) * n + g].x * scale;
     C[(long)job * n3 + id] = v;
     unsigned long long kx = pack_max(v, (uint32_t)id), kn = pack_min(v, (uint32_t)id);

@@ -122,6 +122,20 @@ class ProjectionRotationMetric3D:
                     "align_pairs")
         return D
 
+    # -- nbfWedgedAverageImage3D::setAlignments + getImage ----------------------------------------
+    def average(self, particles, weights, matrices):
+        """Class average of particles (indices into the particle set) with weights and 4x4 alignment
+        matrices; returns [z][y][x] float32 (RMS 1)."""
+        n = len(particles)
+        N = self.params["N"]
+        idx = np.ascontiguousarray(particles, np.int32)
+        w = np.ascontiguousarray(weights, np.float32)
+        M = np.ascontiguousarray(np.asarray(matrices, np.float64).reshape(n, 16))
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_average(self._ctx, n, idx.ctypes.data, w.ctypes.data, M.ctypes.data,
+                                            out.ctypes.data), "average")
+        return out
+
     # -- diagnostics ---------------------------------------------------------------------------
     def ccf(self, r, p, T):
         t = np.ascontiguousarray(np.asarray(T, np.float64).reshape(16)).copy()

@@ -88,6 +88,13 @@ int ettk_gpu_set_particles_device(ettk_ctx *ctx, int V, const float *d_volumes, 
  * Rows whose D[i][0][0] != -1 on entry are skipped (the reference's resume convention). */
 int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand);
 
+/* Replaces nbfWedgedAverageImage3D::setAlignments + getImage (getImageMPI and getImage with
+ * NBF_AVERAGE_IN_RECIPROCAL_SPACE, inc/em/nbfWedgedAverageImage3D.h:181-356): the wedge-weighted class
+ * average of M members of the particle set (particles[i] = particle index, weights[i] = alignment
+ * weight, matrices[16*i] = alignment matrix), written to avg (N^3 floats, x fastest, RMS 1). */
+int ettk_gpu_average(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
+                     float *avg);
+
 /* Diagnostics (staged parity checks; no counterpart in the reference API):
  * one executeFourierNewHalf call (inc/em/nbfFourierImageMetric.h:1077-1323) of particle p against
  * reference r at transform t (updated in place with the found shift); returns the distance in *dist. */

@@ -784,6 +784,56 @@ void align(const OracleParams &P, const OracleVolume &ref, const OracleVolume &p
   res.n_ccf = ccf.ncalls;
 }
 
+/* nbfWedgedAverageImage3D::getImageMPI + getImage with NBF_AVERAGE_IN_RECIPROCAL_SPACE
+ * (inc/em/nbfWedgedAverageImage3D.h:216-258, 260-356): every member with weight w != 0 is resliced
+ * under Euler(normal) * alignment (its own matrix reset to identity, line 313), transformed (R2C of
+ * image * shift), and accumulated acc += |w||F|, re += w|F|Re F, im += w|F|Im F; the average is
+ * IFFT((re, im)/acc where acc > 0, DC = 0) * shift / N^3, divided by its RMS. out is [x][y][z]. */
+void average(const OracleParams &P, int M, const OracleVolume *vols, const float *weights, const double *mats,
+             std::vector<double> &out) {
+  int N = P.N, H = N / 2 + 1;
+  long n3 = (long)N * N * N, h3 = (long)N * N * H;
+  std::vector<double> re(h3, 0.0), im(h3, 0.0), acc(h3, 0.0), R(n3);
+  std::vector<cplx> F(h3);
+  for (int i = 0; i < M; ++i) {
+    if (!(fabs(weights[i]) > 0)) continue;
+    OracleVolume v = vols[i];
+    for (int k = 0; k < 16; ++k) v.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    M4 t;
+    memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
+    std::vector<double> img;
+    get_image(v, N, &t, img);
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) {
+          long id = ((long)x * N + y) * N + z;
+          R[id] = img[id] * (double)(float)(((x + y + z) % 2) ? -1.0f : 1.0f);
+        }
+    rfft3d(R.data(), F.data(), N, N, N);
+    double w = weights[i];
+    for (long k = 0; k < h3; ++k) {
+      double b = sqrt((F[k] * std::conj(F[k])).real());
+      acc[k] += fabs(w) * b;
+      re[k] += w * b * F[k].real();
+      im[k] += w * b * F[k].imag();
+    }
+  }
+  for (long k = 0; k < h3; ++k) F[k] = (acc[k] > 0) ? cplx(re[k] / acc[k], im[k] / acc[k]) : cplx(0, 0);
+  F[((long)(N / 2) * N + N / 2) * H + (H - 1)] = 0;
+  irfft3d(F.data(), R.data(), N, N, N);
+  out.resize(n3);
+  double ss = 0;
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int z = 0; z < N; ++z) {
+        long id = ((long)x * N + y) * N + z;
+        out[id] = R[id] / (double)n3 * (double)(float)(((x + y + z) % 2) ? -1.0f : 1.0f);
+        ss += out[id] * out[id];
+      }
+  float rms = (float)sqrt(ss / (double)n3);
+  for (auto &o : out) o /= (double)rms;
+}
+
 } // namespace
 
 extern "C" {
@@ -873,6 +923,15 @@ float oracle_ccf(const OracleParams *P, const OracleVolume *ref, const OracleVol
   float d = ccf.execute(t);
   memcpy(t16, t.e, sizeof(t.e));
   return d;
+}
+
+/* Class average of M members (volumes + metadata, weights, 4x4 alignment matrices); out [x][y][z]. */
+int oracle_average(const OracleParams *P, int M, const OracleVolume *vols, const float *weights, const double *mats,
+                   double *out) {
+  std::vector<double> a;
+  average(*P, M, vols, weights, mats, a);
+  memcpy(out, a.data(), sizeof(double) * a.size());
+  return 0;
 }
 
 int oracle_rfft3d(int n0, int n1, int n2, const double *in, double *outRI) {

@@ -82,6 +82,7 @@ def lib():
         L.oracle_sht.argtypes = [ctypes.c_int, dp, dp]
         L.oracle_ccf.argtypes = [P, V, V, dp]
         L.oracle_ccf.restype = ctypes.c_float
+        L.oracle_average.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -209,6 +210,24 @@ def sht(B, F):
     lib().oracle_sht(B, np.ascontiguousarray(F, np.float64), out)
     c = out.reshape(B, 2 * B, 2)
     return c[..., 0] + 1j * c[..., 1]
+
+
+def average(params, vols, metas, weights, mats):
+    """Class average (getImageMPI + getImage), returned as [x][y][z]."""
+    P = make_params(params)
+    n = len(vols)
+    arr = (OracleVolume * n)()
+    keep = []
+    for i in range(n):
+        v = make_volume(vols[i], metas[i])
+        keep.append(v)
+        arr[i] = v
+    w = np.ascontiguousarray(weights, np.float32)
+    m = np.ascontiguousarray(np.asarray(mats, np.float64).reshape(n, 16))
+    N = params["N"]
+    out = np.zeros(N ** 3, np.float64)
+    lib().oracle_average(ctypes.byref(P), n, ctypes.addressof(arr), w.ctypes.data, m.ctypes.data, out)
+    return out.reshape(N, N, N)
 
 
 def rfft3d(x):

@@ -98,3 +98,21 @@ def test_align_pairs_64(ds64):
         assert np.allclose(T[:3, :3], o["matrix"][:3, :3], atol=1e-5)
         assert np.allclose(T[:3, 3], o["matrix"][:3, 3], atol=1e-4)
     m.close()
+
+
+def test_class_average(ds32, metric32):
+    """Wedge-weighted class average (getImageMPI + getImage) against the oracle: 1e-5 relative RMS."""
+    members = [0, 1, 2, 3, 4]
+    weights = [1.0, 1.0, 0.5, -0.25, 1.0]
+    mats = []
+    for i in members:
+        T = np.eye(4)
+        T[:3, :3] = ds32.truth[i]["rotation"]
+        T[:3, 3] = ds32.truth[i]["shift"]
+        mats.append(T)
+    g = metric32.average(members, weights, mats)  # [z][y][x]
+    o = pyoracle.average(ds32.params, [ds32.particles[i] for i in members], [ds32.meta[i] for i in members],
+                         weights, mats)  # [x][y][z]
+    o = o.transpose(2, 1, 0)
+    err = np.sqrt(np.mean((g - o) ** 2)) / np.sqrt(np.mean(o ** 2))
+    assert err <= 1e-5, err
