@@ -382,6 +382,13 @@ struct ettk_ctx {
     CK(cudaStreamSynchronize(st));
     if (prof) prof_flush();
   }
+  // Blocking read of device results (the host waits for the stream here; timed as host_wait).
+  void read_back(void *dst, const void *src, size_t bytes) {
+    HostScope hs(this, "host_wait");
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (prof) prof_flush();
+  }
   void post_launch() {
     ++launches;
     CK(cudaGetLastError());
@@ -536,7 +543,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
     CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
     {
       Scope sc(this, "reslice", 8.0 * E * n3);
-      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, 0, st>>>(w_items.p, N, w_v.p, w_acc.p, 2);
+      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2);
       post_launch();
     }
     PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
@@ -564,6 +571,10 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
 }
 
 void ettk_ctx::init_tables() {
+  CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   N = p.N;
   H = N / 2 + 1;
   B = p.B;
@@ -760,7 +771,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
     Scope sc(this, "reslice", 8.0 * P * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, 0, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
   }
   post_launch();
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
@@ -865,7 +876,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift) * fw, normalised
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, 0, st>>>(w_items.p, N, w_v.p, acc2, ACC);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, acc2, ACC);
   }
   post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
@@ -898,8 +909,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   hs_launch.reset();
   std::vector<EvalOut> out(E);
-  CK(cudaMemcpyAsync(out.data(), w_out.p, E * sizeof(EvalOut), cudaMemcpyDeviceToHost, st));
-  sync();
+  read_back(out.data(), w_out.p, E * sizeof(EvalOut));
   for (long e = 0; e < E; ++e) {
     res[e].dist = out[e].dist;
     Mat4 tr = Mat4::eye();
@@ -978,6 +988,7 @@ void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
 }  // namespace
 
 void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand) {
+  HostScope hs_all(this, "host_align_wall");
   int maxb = p.max_batch > 0 ? p.max_batch : 512;
   std::vector<int> todo;
   for (int i = 0; i < npairs; ++i)
@@ -1150,16 +1161,20 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
     post_launch();
     }
     std::vector<int> cnt(2 * P);
-    CK(cudaMemcpyAsync(cnt.data(), w_cnt.p, 2 * P * 4, cudaMemcpyDeviceToHost, st));
-    sync();
+    read_back(cnt.data(), w_cnt.p, 2 * P * 4);
     std::vector<int2> lists((long)2 * P * cap);
+    int maxc = 0;
     for (int q = 0; q < 2 * P; ++q) {
-      int c = std::min(cnt[q], cap);
       if (cnt[q] > cap) throw CudaError(ETTK_ERR_ARG, "too many SO(3) local maxima");
-      if (c) CK(cudaMemcpyAsync(lists.data() + (long)q * cap, w_lists.p + (long)q * cap, c * sizeof(int2),
-                                cudaMemcpyDeviceToHost, st));
+      maxc = std::max(maxc, cnt[q]);
     }
-    sync();
+    if (maxc) {
+      // one strided copy of the first maxc entries of every list
+      HostScope hs(this, "host_wait");
+      CK(cudaMemcpy2DAsync(lists.data(), cap * sizeof(int2), w_lists.p, cap * sizeof(int2), maxc * sizeof(int2),
+                           2 * P, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+    }
     std::vector<PQ> q1(P), q2(P);
     {
     HostScope hs_q(this, "host_queues");
@@ -1572,7 +1587,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->w_items.ensure(R);
     CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
-    k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, 0, c->st>>>(c->w_items.p, c->N, c->w_v.p,
+    k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, RS_SMEM, c->st>>>(c->w_items.p, c->N, c->w_v.p,
                                                                                           c->w_acc.p, 2);
     c->post_launch();
     c->FI1.ensure(R * h3);

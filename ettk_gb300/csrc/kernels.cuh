@@ -18,179 +18,164 @@ struct ResliceItem {
 // fixed image under Euler*matrix*t into an N^3 box (output [x][y][z], z fastest), background
 // -FLT_MAX outside [-0.5, dim-0.5] (vtkImageReslice border 1, clamp mode), plus per-item sums
 // of valid values and their count into acc[item*acc_stride + 0/1].
-static __global__ void k_reslice(const ResliceItem *__restrict__ items, int N, float *__restrict__ out, double *acc,
-                          int acc_stride) {
-  __shared__ double sh[32];
-  const ResliceItem it = items[blockIdx.y];
-  long n3 = (long)N * N * N;
-  double s = 0, c = 0;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
-    int a = (int)(id / ((long)N * N)), b = (int)((id / N) % N), cz = (int)(id % N);
-    float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
-    p0 = p0 + b * it.m[6];
-    p1 = p1 + b * it.m[7];
-    p2 = p2 + b * it.m[8];
-    p0 = p0 + a * it.m[3];
-    p1 = p1 + a * it.m[4];
-    p2 = p2 + a * it.m[5];
-    float val = -FLT_MAX;
-    const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
-    if (!(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f)) {
-      float fx, fy, fz;
-      int ix = vtk_floor(p0, fx), iy = vtk_floor(p1, fy), iz = vtk_floor(p2, fz);
-      float wx[4], wy[4], wz[4];
-      cubic_weights(wx, fx);
-      cubic_weights(wy, fy);
-      cubic_weights(wz, fz);
-      int mY = (dy > 1) && (fy != 0.f), mZ = (dz > 1) && (fz != 0.f);
-      int j1 = 1 - mY, j2 = 1 + 2 * mY, k1 = 1 - mZ, k2 = 1 + 2 * mZ;
-      if (!mY) wy[1] = 1.f;
-      if (!mZ) wz[1] = 1.f;
-      int xs[4];
+//
+// One 8x8x8 output brick per CTA. The input footprint of the brick (its corner coordinates widened by
+// the cubic support and a rounding margin) is staged in shared memory with 16-byte loads: the x range
+// starts at a multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge value
+// (the clamp border of the reference, exact because the x extent is a multiple of 4). For a rotation the
+// footprint is at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices,
+// unaligned volumes) read the taps from global memory.
+constexpr int RB = 8;             // brick edge
+constexpr int RS_MAX = 9600;      // staged floats (37.5 KiB of dynamic shared memory, five CTAs per SM)
+constexpr size_t RS_SMEM = RS_MAX * sizeof(float);
+
+// Tricubic sum with clamped taps read from global memory (bricks whose footprint is not staged).
+static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz, int ix, int iy, int iz,
+                                              float wx0, float wx1, float wx2, float wx3, float wy0, float wy1, float wy2,
+                                              float wy3, float wz0, float wz1, float wz2, float wz3) {
+  const float wy[4] = {wy0, wy1, wy2, wy3}, wz[4] = {wz0, wz1, wz2, wz3};
+  const int x_0 = min(max(ix - 1, 0), dx - 1), x_1 = min(max(ix, 0), dx - 1), x_2 = min(max(ix + 1, 0), dx - 1),
+            x_3 = min(max(ix + 2, 0), dx - 1);
+  float acc = 0.f;
 #pragma unroll
-      for (int t = 0; t < 4; ++t) xs[t] = min(max(ix - 1 + t, 0), dx - 1);
-      float acc2 = 0.f;
-      for (int k = k1; k <= k2; ++k) {
-        int zz = min(max(iz - 1 + k, 0), dz - 1);
-        for (int j = j1; j <= j2; ++j) {
-          int yy = min(max(iy - 1 + j, 0), dy - 1);
-          const float *row = it.vol + ((long)zz * dy + yy) * dx;
-          acc2 += (wz[k] * wy[j]) * (wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
-                                     wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]));
-        }
-      }
-      val = acc2;
-      s += val;
-      c += 1;
-    }
-    out[(long)blockIdx.y * n3 + id] = val;
-  }
-  if (acc) {
-    double bs = block_sum(s, sh), bc = block_sum(c, sh);
-    if (threadIdx.x == 0) {
-      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 0], bs);
-      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 1], bc);
+  for (int k = 0; k < 4; ++k) {
+    const int z = min(max(iz - 1 + k, 0), dz - 1);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int y = min(max(iy - 1 + j, 0), dy - 1);
+      const float *row = vol + ((long)z * dy + y) * dx;
+      acc += (wz[k] * wy[j]) * (wx0 * __ldg(row + x_0) + wx1 * __ldg(row + x_1) + wx2 * __ldg(row + x_2) + wx3 * __ldg(row + x_3));
     }
   }
+  return acc;
 }
 
-// Same computation as k_reslice, one 8x8x8 output brick per CTA: the input footprint of the brick
-// (corner coordinates, widened by the cubic support and a rounding margin) is staged in shared memory
-// with clamped loads, so every tap of the brick reads shared memory. Bricks whose footprint exceeds the
-// staging buffer (strong scaling in the matrix) read global memory as k_reslice does.
-constexpr int RB = 8;                 // brick edge
-constexpr int RB_SMEM = 8192;         // staged floats (32 KiB)
-// PRECISE: the voxel coordinate follows the reference's FP64 sequence (origin + c*z) + b*y) + a*x without
-// FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5 output parity matters).
+// PRECISE: the voxel coordinate follows the reference's FP64 sequence ((origin + c*z) + b*y) + a*x
+// without FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5 output parity
+// matters); otherwise the same sequence runs in FP32.
 template <bool PRECISE>
-__global__ void __launch_bounds__(256) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
-                                                       float *__restrict__ out, double *acc, int acc_stride) {
-  __shared__ float box[RB_SMEM];
+__global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
+                                                          float *__restrict__ out, double *acc, int acc_stride) {
+  extern __shared__ float4 box4[];
+  const float *box = reinterpret_cast<const float *>(box4);
   __shared__ double sh[32];
-  const ResliceItem it = items[blockIdx.y];
+  __shared__ int geo[6];  // o[3], ext[3]
+  const ResliceItem &it = items[blockIdx.y];
   const int nb = N / RB;
   const int bx = blockIdx.x / (nb * nb), by = (blockIdx.x / nb) % nb, bz = blockIdx.x % nb;
   const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
-  // footprint of the 8 corners (same affine map as the per-voxel coordinates)
-  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  for (int c8 = 0; c8 < 8; ++c8) {
-    int a = bx * RB + ((c8 & 1) ? RB - 1 : 0), b = by * RB + ((c8 & 2) ? RB - 1 : 0), cz = bz * RB + ((c8 & 4) ? RB - 1 : 0);
+  const float *vol = it.vol;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    // footprint of the 8 corners (same affine map as the per-voxel coordinates), lanes 0..7
+    const int c8 = lane & 7;
+    const int a = bx * RB + ((c8 & 1) ? RB - 1 : 0), b = by * RB + ((c8 & 2) ? RB - 1 : 0),
+              cz = bz * RB + ((c8 & 4) ? RB - 1 : 0);
+    float lo[3], hi[3];
     for (int t = 0; t < 3; ++t) {
-      float p = it.m[t] + cz * it.m[9 + t];
-      p = p + b * it.m[6 + t];
-      p = p + a * it.m[3 + t];
-      lo[t] = fminf(lo[t], p);
-      hi[t] = fmaxf(hi[t], p);
+      float q = it.m[t] + cz * it.m[9 + t];
+      q = q + b * it.m[6 + t];
+      q = q + a * it.m[3 + t];
+      lo[t] = hi[t] = q;
     }
+    for (int off = 4; off > 0; off >>= 1)
+      for (int t = 0; t < 3; ++t) {
+        lo[t] = fminf(lo[t], __shfl_xor_sync(0xffffffffu, lo[t], off));
+        hi[t] = fmaxf(hi[t], __shfl_xor_sync(0xffffffffu, hi[t], off));
+      }
+    if (lane == 0)
+      for (int t = 0; t < 3; ++t) {
+        int o = (int)floorf(lo[t]) - 2;
+        geo[t] = o;
+        geo[3 + t] = (int)floorf(hi[t]) + 4 - o + 1;  // taps reach floor(p)+1+2; p may exceed hi by rounding
+      }
   }
-  int o[3], ext[3];
-  for (int t = 0; t < 3; ++t) {
-    o[t] = (int)floorf(lo[t]) - 2;
-    ext[t] = (int)floorf(hi[t]) + 4 - o[t] + 1;  // taps reach floor(p)+1+2, p may exceed hi by rounding
-  }
-  const long vol3 = (long)ext[0] * ext[1] * ext[2];
-  const bool staged = vol3 <= RB_SMEM;
+  __syncthreads();
+  const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5];
+  const int x0 = o0 & ~3;                        // floor to a multiple of 4
+  const int w4 = (o0 + e0 - x0 + 3) >> 2;        // 16-byte groups per staged row
+  const int P = w4 * 4;                          // staged row pitch (floats)
+  const bool staged = e0 >= 5 && e0 <= 64 && e1 >= 5 && e1 <= 64 && e2 >= 5 && e2 <= 64 && e1 * e2 * P <= RS_MAX &&
+                      (dx & 3) == 0 && (((unsigned long long)vol) & 15) == 0;
   if (staged) {
-    for (int i = threadIdx.x; i < vol3; i += blockDim.x) {
-      int ux = i % ext[0], uy = (i / ext[0]) % ext[1], uz = i / (ext[0] * ext[1]);
-      int x = min(max(o[0] + ux, 0), dx - 1), y = min(max(o[1] + uy, 0), dy - 1), z = min(max(o[2] + uz, 0), dz - 1);
-      box[i] = __ldg(it.vol + ((long)z * dy + y) * dx + x);
+    // flat index -> (row, group) and row -> (y, z) by multiply-high (exact for divisors <= 64, index < 2^16)
+    const unsigned mw = 0xFFFFFFFFu / (unsigned)w4 + 1u, me = 0xFFFFFFFFu / (unsigned)e1 + 1u;
+    const int n4 = e1 * e2 * w4;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+      const int row = (int)__umulhi((unsigned)i, mw), c4 = i - row * w4;
+      const int uz = (int)__umulhi((unsigned)row, me), uy = row - uz * e1;
+      const int y = min(max(o1 + uy, 0), dy - 1), z = min(max(o2 + uz, 0), dz - 1);
+      const int xs = x0 + 4 * c4, xl = min(max(xs, 0), dx - 4);
+      float4 f = __ldg(reinterpret_cast<const float4 *>(vol + ((long)z * dy + y) * dx + xl));
+      if (xs < 0) f = make_float4(f.x, f.x, f.x, f.x);
+      else if (xs > dx - 4) f = make_float4(f.w, f.w, f.w, f.w);
+      box4[i] = f;
     }
   }
   __syncthreads();
   const long n3 = (long)N * N * N;
   float s = 0.f;
   int cnt = 0;
+#pragma unroll 1
   for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
-    int a = bx * RB + v / (RB * RB), b = by * RB + (v / RB) % RB, cz = bz * RB + v % RB;
-    float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
-    p0 = p0 + b * it.m[6];
-    p1 = p1 + b * it.m[7];
-    p2 = p2 + b * it.m[8];
-    p0 = p0 + a * it.m[3];
-    p1 = p1 + a * it.m[4];
-    p2 = p2 + a * it.m[5];
-    float val = -FLT_MAX;
+    const int a = bx * RB + v / (RB * RB), b = by * RB + (v / RB) % RB, cz = bz * RB + v % RB;
     bool inside;
     int ix, iy, iz;
     float fx, fy, fz;
     if (PRECISE) {
       double q[3];
       for (int t = 0; t < 3; ++t) {
-        double v = __dadd_rn(it.md[t], __dmul_rn((double)cz, it.md[9 + t]));
-        v = __dadd_rn(v, __dmul_rn((double)b, it.md[6 + t]));
-        q[t] = __dadd_rn(v, __dmul_rn((double)a, it.md[3 + t]));
+        double w = __dadd_rn(it.md[t], __dmul_rn((double)cz, it.md[9 + t]));
+        w = __dadd_rn(w, __dmul_rn((double)b, it.md[6 + t]));
+        q[t] = __dadd_rn(w, __dmul_rn((double)a, it.md[3 + t]));
       }
       inside = !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 || q[2] > dz - 0.5);
-      long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0), r2 = __double2ll_rn(q[2] * 65536.0);
-      ix = (int)(r0 >> 16); fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
-      iy = (int)(r1 >> 16); fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
-      iz = (int)(r2 >> 16); fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
+      const long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0),
+                      r2 = __double2ll_rn(q[2] * 65536.0);
+      ix = (int)(r0 >> 16);
+      fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
+      iy = (int)(r1 >> 16);
+      fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
+      iz = (int)(r2 >> 16);
+      fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
     } else {
+      float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
+      p0 = p0 + b * it.m[6];
+      p1 = p1 + b * it.m[7];
+      p2 = p2 + b * it.m[8];
+      p0 = p0 + a * it.m[3];
+      p1 = p1 + a * it.m[4];
+      p2 = p2 + a * it.m[5];
       inside = !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
       ix = vtk_floor(p0, fx);
       iy = vtk_floor(p1, fy);
       iz = vtk_floor(p2, fz);
     }
+    float val = -FLT_MAX;
     if (inside) {
       float wx[4], wy[4], wz[4];
       cubic_weights(wx, fx);
       cubic_weights(wy, fy);
       cubic_weights(wz, fz);
-      int mY = (dy > 1) && (fy != 0.f), mZ = (dz > 1) && (fz != 0.f);
-      if (!mY) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
-      if (!mZ) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
-      float acc2 = 0.f;
       // The reference uses only the middle row/plane when fy/fz == 0; the full 4x4x4 sum with the
       // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
+      if (!((dy > 1) && (fy != 0.f))) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
+      if (!((dz > 1) && (fz != 0.f))) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
+      float acc2 = 0.f;
       if (staged) {
-        const float *b0 = box + ((long)(iz - 1 - o[2]) * ext[1] + (iy - 1 - o[1])) * ext[0] + (ix - 1 - o[0]);
-        const int ry = ext[0], rz = ext[0] * ext[1];
+        const float *b0 = box + ((iz - 1 - o2) * e1 + (iy - 1 - o1)) * P + (ix - 1 - x0);
+        const int rz = e1 * P;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const float *row = b0 + k * rz + j * ry;
+            const float *row = b0 + k * rz + j * P;
             acc2 += (wz[k] * wy[j]) * (wx[0] * row[0] + wx[1] * row[1] + wx[2] * row[2] + wx[3] * row[3]);
           }
         }
       } else {
-        int xs[4], ys[4], zs[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          xs[t] = min(max(ix - 1 + t, 0), dx - 1);
-          ys[t] = min(max(iy - 1 + t, 0), dy - 1);
-          zs[t] = min(max(iz - 1 + t, 0), dz - 1);
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const float *row = it.vol + ((long)zs[k] * dy + ys[j]) * dx;
-            acc2 += (wz[k] * wy[j]) * (wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
-                                       wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]));
-          }
-        }
+        acc2 = tricubic_global(vol, dx, dy, dz, ix, iy, iz, wx[0], wx[1], wx[2], wx[3], wy[0], wy[1], wy[2], wy[3], wz[0],
+                               wz[1], wz[2], wz[3]);
       }
       val = acc2;
       s += val;
