@@ -15,6 +15,8 @@
 #include "fft_reg.cuh"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <array>
 #include <chrono>
 #include <map>
@@ -392,6 +394,17 @@ struct ettk_ctx {
   void post_launch() {
     ++launches;
     CK(cudaGetLastError());
+  }
+
+  // wedge * filter of E evaluations (missing-wedge compensation), rolling-window kernel
+  template <int NN>
+  void wedge_t(long E, double *acc, int acc_stride) {
+    constexpr int SLAB = wedge_slab<NN>();
+    constexpr size_t smem = wedge_smem<NN>();
+    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_wedge_roll<NN, SLAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_wedge_roll<NN, SLAB><<<dim3(NN / SLAB, (unsigned)E), 256, smem, st>>>(w_wv.p, smooth, W1half.p, w_idx.p, filter.p,
+                                                                            w_fw.p, acc, acc_stride, 6);
+    post_launch();
   }
 
   // ---------------------------------------------------------------- FFT drivers
@@ -846,10 +859,13 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   // wedge (W1 * W2(T)) * filter and its sum
   if (useWedge) {
     Scope sc_w(this, "wedge", 4.0 * E * h3);
-    size_t smw = 6 * (size_t)N * H * sizeof(float);
-    if (smw > 48 * 1024) CK(cudaFuncSetAttribute(k_wedge_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw));
-    k_wedge_fused<<<dim3(N, E), 256, smw, st>>>(w_wv.p, N, smooth, W1half.p, w_idx.p, filter.p, w_fw.p, acc, ACC, 6);
-    post_launch();
+    switch (N) {
+      case 16: wedge_t<16>(E, acc, ACC); break;
+      case 32: wedge_t<32>(E, acc, ACC); break;
+      case 64: wedge_t<64>(E, acc, ACC); break;
+      case 128: wedge_t<128>(E, acc, ACC); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+    }
   } else {
     for (long e = 0; e < E; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
   }
@@ -942,6 +958,24 @@ bool transform_valid(const ettk_params &p, const Mat4 &t) {
 // eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
 // matrices can be closer than `tol` in L1 are compared (each entry must differ by < tol); visiting only
 // those pairs in increasing j order is equivalent to the reference's full double loop.
+// Runs f(0..n-1) on up to 16 host threads (independent items; f must not throw).
+template <class F>
+void parallel_for(int n, F f) {
+  int nt = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+  nt = std::min(nt, n);
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&] {
+      for (int i; (i = next.fetch_add(1)) < n;) f(i);
+    });
+  for (auto &x : th) x.join();
+}
+
 void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
   size_t K = pos.size();
   std::vector<Mat4> mats(K);
@@ -1178,7 +1212,8 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
     std::vector<PQ> q1(P), q2(P);
     {
     HostScope hs_q(this, "host_queues");
-    for (int q = 0; q < 2 * P; ++q) {
+    // queues are independent: build them on the host cores
+    auto build_queue = [&](int q) {
       int c = std::min(cnt[q], cap);
       std::vector<int2> L(lists.begin() + (long)q * cap, lists.begin() + (long)q * cap + c);
       std::sort(L.begin(), L.end(), [](const int2 &a, const int2 &b) { return a.x < b.x; });
@@ -1193,7 +1228,8 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         if (transform_valid(p, euler_candidate(alpha, beta, gamma))) pos.push_back({{alpha, beta, gamma, -val}, -1});
       }
       eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f);
-    }
+    };
+    parallel_for(2 * P, build_queue);
     }
     // 4. candidate rounds (execute 678-776): direct and mirror CCF per popped candidate
     struct PairState {

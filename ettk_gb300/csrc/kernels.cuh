@@ -199,32 +199,6 @@ struct WedgeVecs {
   double v1[3], v2[3];
   int full;
 };
-static __global__ void k_wedge_binary(const WedgeVecs *__restrict__ wv, int N, float *__restrict__ out) {
-  const int H = N / 2 + 1;
-  long h3 = (long)N * N * H;
-  const WedgeVecs w = wv[blockIdx.y];
-  float f1[3] = {(float)w.v1[0], (float)w.v1[1], (float)w.v1[2]}, f2[3] = {(float)w.v2[0], (float)w.v2[1], (float)w.v2[2]};
-  const int nh = N * H;
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
-    float r = 1.f;
-    if (!w.full) {
-      int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
-      float di = (float)(i - N / 2), dj = (float)(j - N / 2), dk = (float)(k - (H - 1));
-      float a = f1[0] * di + f1[1] * dj + f1[2] * dk, b = f2[0] * di + f2[1] * dj + f2[2] * dk;
-      if (fabsf(a) > 1e-3f && fabsf(b) > 1e-3f) {
-        r = (a * b <= 0.f) ? 1.f : 0.f;
-      } else {
-        double ad = __dadd_rn(__dadd_rn(__dmul_rn(w.v1[0], (double)di), __dmul_rn(w.v1[1], (double)dj)),
-                              __dmul_rn(w.v1[2], (double)dk));
-        double bd = __dadd_rn(__dadd_rn(__dmul_rn(w.v2[0], (double)di), __dmul_rn(w.v2[1], (double)dj)),
-                              __dmul_rn(w.v2[2], (double)dk));
-        r = (__dmul_rn(ad, bd) <= 0.0) ? 1.f : 0.f;
-      }
-    }
-    out[(long)blockIdx.y * h3 + id] = r;
-  }
-}
-
 // One axis of vtkImageGaussianSmooth with std 2 and radius 1 (nbfWedge3D::smoothWedgeImage,
 // inc/em/nbfWedge3D.h:431-445) on [item][N][N][H] arrays; axis 2 = k (VTK z, first pass),
 // 1 = j, 0 = i. The final pass (axis 0) multiplies by the reference wedge and the filter
@@ -235,44 +209,9 @@ struct Smooth3 {
   float w_lo[2];    // at index 0: (0, +1)
   float w_hi[2];    // at last index: (-1, 0)
 };
-static __global__ void k_wedge_smooth(const float *__restrict__ in, float *__restrict__ out, int N, int axis, Smooth3 sw,
-                               const float *__restrict__ w1, const int *__restrict__ w1_index,
-                               const float *__restrict__ filter, double *acc, int acc_stride, int acc_slot) {
-  __shared__ double sh[32];
-  const int H = N / 2 + 1;
-  long h3 = (long)N * N * H;
-  const float *src = in + (long)blockIdx.y * h3;
-  float s = 0.f;
-  const int nh = N * H;
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
-    int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
-    int pos = axis == 2 ? k : (axis == 1 ? j : i);
-    int n = axis == 2 ? H : N;
-    int st = axis == 2 ? 1 : (axis == 1 ? H : nh);
-    float v;
-    if (n == 1) v = src[id];
-    else if (pos == 0) v = sw.w_lo[0] * src[id] + sw.w_lo[1] * src[id + st];
-    else if (pos == n - 1) v = sw.w_hi[0] * src[id - st] + sw.w_hi[1] * src[id];
-    else v = sw.w_int[0] * src[id - st] + sw.w_int[1] * src[id] + sw.w_int[2] * src[id + st];
-    if (axis == 0) {
-      float wedge = v * w1[(long)w1_index[blockIdx.y] * h3 + id];
-      float fw = filter[id] * wedge;
-      s += fw;
-      v = fw;
-    }
-    out[(long)blockIdx.y * h3 + id] = v;
-  }
-  if (axis == 0) {
-    double b = block_sum((double)s, sh);
-    if (threadIdx.x == 0) atomicAdd(&acc[(long)blockIdx.y * acc_stride + acc_slot], b);
-  }
-}
-
-// Binary wedge + the three smoothing passes + (wedge2 * wedge1) * filter in one kernel: one CTA per
-// (x plane i, item) builds the binary wedge of planes i-1, i, i+1 in shared memory, smooths along k then j
-// (float rounding after each pass, as vtkImageGaussianSmooth stores its intermediates), then along i, and
-// writes fw = filter * (wedge2 * wedge1) for plane i plus the partial sum(fw). Dynamic shared memory:
-// 2 * 3 * N * (N/2+1) floats.
+// Binary wedge (nbfWedge3D::getImageHalf, inc/em/nbfWedge3D.h:312-356): ((v1.d)(v2.d) <= 0) with
+// d = (i-N/2, j-N/2, k-N/2) on the centred half grid. Near the planes the test is redone in FP64 with the
+// reference's operation order (no FMA) so exact-zero cases resolve as they do there.
 ETTK_DEV float wedge_bit(const WedgeVecs &w, const float f1[3], const float f2[3], int i, int j, int k, int N, int H) {
   if (w.full) return 1.f;
   float di = (float)(i - N / 2), dj = (float)(j - N / 2), dk = (float)(k - (H - 1));
@@ -284,55 +223,76 @@ ETTK_DEV float wedge_bit(const WedgeVecs &w, const float f1[3], const float f2[3
                         __dmul_rn(w.v2[2], (double)dk));
   return (__dmul_rn(ad, bd) <= 0.0) ? 1.f : 0.f;
 }
-ETTK_DEV float smooth3(const Smooth3 &sw, const float *p, int pos, int n, int st) {
-  if (n == 1) return p[0];
-  if (pos == 0) return sw.w_lo[0] * p[0] + sw.w_lo[1] * p[st];
-  if (pos == n - 1) return sw.w_hi[0] * p[-st] + sw.w_hi[1] * p[0];
-  return sw.w_int[0] * p[-st] + sw.w_int[1] * p[0] + sw.w_int[2] * p[st];
+// One 3-tap pass of vtkImageGaussianSmooth at position pos of an axis of length n (clipped, renormalised
+// kernel at the ends); vm / vp are the neighbours (ignored where clipped).
+ETTK_DEV float smooth3v(const Smooth3 &sw, float vm, float v0, float vp, int pos, int n) {
+  if (n == 1) return v0;
+  if (pos == 0) return sw.w_lo[0] * v0 + sw.w_lo[1] * vp;
+  if (pos == n - 1) return sw.w_hi[0] * vm + sw.w_hi[1] * v0;
+  return sw.w_int[0] * vm + sw.w_int[1] * v0 + sw.w_int[2] * vp;
 }
-static __global__ void __launch_bounds__(256) k_wedge_fused(const WedgeVecs *__restrict__ wv, int N, Smooth3 sw,
-                                                            const float *__restrict__ w1, const int *__restrict__ w1_index,
-                                                            const float *__restrict__ filter, float *__restrict__ out,
-                                                            double *acc, int acc_stride, int acc_slot) {
+
+// Binary wedge + the three smoothing passes + (wedge2 * wedge1) * filter in one kernel. One CTA per
+// (slab of SLAB x planes, item) walks the planes i0-1 .. i0+SLAB: each plane's binary wedge is smoothed
+// along k then j (float rounding after each pass, as vtkImageGaussianSmooth stores its intermediates) into a
+// three-plane ring in shared memory; as soon as planes q-1, q, q+1 are in the ring, plane q is smoothed
+// along i, multiplied by the reference wedge and the filter, stored, and summed into acc[item][acc_slot]
+// (sum(wedge*filter) of the overlap normalisation).
+template <int N, int SLAB>
+__global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict__ wv, Smooth3 sw,
+                                                    const float *__restrict__ w1, const int *__restrict__ w1_index,
+                                                    const float *__restrict__ filter, float *__restrict__ out,
+                                                    double *acc, int acc_stride, int acc_slot) {
+  constexpr int H = N / 2 + 1, PL = N * H;
+  constexpr long h3 = (long)PL * N;
   extern __shared__ float wsm[];
+  float *Kp = wsm;            // k-smoothed plane
+  float *ring = wsm + PL;     // 3 j/k-smoothed planes, plane p in slot p % 3
   __shared__ double sh[32];
-  const int H = N / 2 + 1, plane = N * H;
-  float *A = wsm, *Bf = wsm + 3 * plane;
-  const int i = blockIdx.x, e = blockIdx.y;
+  const int e = blockIdx.y, i0 = blockIdx.x * SLAB;
   const WedgeVecs w = wv[e];
   const float f1[3] = {(float)w.v1[0], (float)w.v1[1], (float)w.v1[2]};
   const float f2[3] = {(float)w.v2[0], (float)w.v2[1], (float)w.v2[2]};
-  const int p0 = max(i - 1, 0), p1 = min(i + 1, N - 1), np = p1 - p0 + 1;
-  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
-    int q = t / plane, r = t - q * plane, j = r / H, k = r - j * H;
-    A[t] = wedge_bit(w, f1, f2, p0 + q, j, k, N, H);
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
-    int r = t % plane, k = r % H;
-    Bf[t] = smooth3(sw, A + t, k, H, 1);
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < np * plane; t += blockDim.x) {
-    int r = t % plane, j = r / H;
-    A[t] = smooth3(sw, Bf + t, j, N, H);
-  }
-  __syncthreads();
-  const long h3 = (long)plane * N;
-  const float *W1 = w1 + (long)w1_index[e] * h3 + (long)i * plane;
-  const float *F = filter + (long)i * plane;
-  float *o = out + (long)e * h3 + (long)i * plane;
+  const float *W1 = w1 + (long)w1_index[e] * h3;
+  float *o = out + (long)e * h3;
   float s = 0.f;
-  for (int r = threadIdx.x; r < plane; r += blockDim.x) {
-    float v = smooth3(sw, A + (i - p0) * plane + r, i, N, plane);
-    float wedge = v * W1[r];
-    float fw = F[r] * wedge;
-    o[r] = fw;
-    s += fw;
+  auto emit = [&](int q) {
+    const float *rm = ring + ((q + 2) % 3) * PL, *r0 = ring + (q % 3) * PL, *rp = ring + ((q + 1) % 3) * PL;
+    for (int r = threadIdx.x; r < PL; r += blockDim.x) {
+      const float vm = q > 0 ? rm[r] : 0.f, vp = q < N - 1 ? rp[r] : 0.f;
+      const float v = smooth3v(sw, vm, r0[r], vp, q, N);
+      const long g = (long)q * PL + r;
+      const float fw = filter[g] * (v * W1[g]);
+      o[g] = fw;
+      s += fw;
+    }
+  };
+  const int pstart = max(i0 - 1, 0), pend = min(i0 + SLAB, N - 1);
+  for (int p = pstart; p <= pend; ++p) {
+    for (int r = threadIdx.x; r < PL; r += blockDim.x) {
+      const int j = r / H, k = r - j * H;
+      const float b0 = wedge_bit(w, f1, f2, p, j, k, N, H);
+      const float bm = k > 0 ? wedge_bit(w, f1, f2, p, j, k - 1, N, H) : 0.f;
+      const float bp = k < H - 1 ? wedge_bit(w, f1, f2, p, j, k + 1, N, H) : 0.f;
+      Kp[r] = smooth3v(sw, bm, b0, bp, k, H);
+    }
+    __syncthreads();  // also orders the previous emit's ring reads before this plane's ring write
+    float *dst = ring + (p % 3) * PL;
+    for (int r = threadIdx.x; r < PL; r += blockDim.x) {
+      const int j = r / H;
+      dst[r] = smooth3v(sw, j > 0 ? Kp[r - H] : 0.f, Kp[r], j < N - 1 ? Kp[r + H] : 0.f, j, N);
+    }
+    __syncthreads();
+    if (p - 1 >= i0) emit(p - 1);
   }
-  double b = block_sum((double)s, sh);
+  if (pend == N - 1 && N - 1 < i0 + SLAB) emit(N - 1);
+  const double b = block_sum((double)s, sh);
   if (threadIdx.x == 0) atomicAdd(&acc[(long)e * acc_stride + acc_slot], b);
 }
+template <int N>
+constexpr int wedge_slab() { return N >= 32 ? 16 : 8; }
+template <int N>
+constexpr size_t wedge_smem() { return 4 * (size_t)N * (N / 2 + 1) * sizeof(float); }
 
 // executeHalf + normalizeFourierHalf accumulation (inc/em/nbfFourierFilter.h:586-606,
 // inc/em/nbfCorrelationImageMetric.h:497-530): out = src * fw, DC zeroed, sums of |F|^2 for
