@@ -407,6 +407,23 @@ struct ettk_ctx {
     post_launch();
   }
 
+  // one zero-padded 2N-point pruned inverse stage of the translational search window
+  template <int NN>
+  void pruned_fft_t(const float2 *in, float2 *out, const PrunedLines &pl, int off) {
+    constexpr int L = reg_lines<NN>();
+    k_pruned_fft<NN, L><<<(unsigned)((pl.n_lines + L - 1) / L), L * MaxAB<NN>::v, 0, st>>>(in, out, pl, N, W, lo, off);
+    post_launch();
+  }
+  void pruned_fft(const float2 *in, float2 *out, const PrunedLines &pl, int off) {
+    switch (2 * N) {
+      case 32: pruned_fft_t<32>(in, out, pl, off); break;
+      case 64: pruned_fft_t<64>(in, out, pl, off); break;
+      case 128: pruned_fft_t<128>(in, out, pl, off); break;
+      case 256: pruned_fft_t<256>(in, out, pl, off); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+    }
+  }
+
   // ---------------------------------------------------------------- FFT drivers
   // CTA shape of the register FFT kernels: 256 threads = LINES x max(A, B)
   template <int NN>
@@ -824,6 +841,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   w_peak.ensure(E);
   w_out.ensure(E);
   w_p1.ensure(E * W * N * H);
+  w_p2.ensure(E * W * W * H);
   std::vector<ResliceItem> items(E);
   std::vector<WedgeVecs> wv(E);
   std::vector<int> refidx(E);
@@ -912,12 +930,13 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
   {
-  Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H));
-  k_pruned_x<<<dim3((unsigned)((N * H + PX_R - 1) / PX_R), E), 256, 0, st>>>(w_cC.p, w_p1.p, N, W, lo, o0);
-  post_launch();
-  size_t smyz = ((size_t)N * H + (size_t)W * N + 2 * (size_t)W * H) * sizeof(float2);
-  if (smyz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_yz_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smyz));
-  k_pruned_yz_peak<<<dim3(W, E), 256, smyz, st>>>(w_p1.p, N, W, lo, o0, o2, rr2, w_peak.p);
+  Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
+  // x: lines (item, ky, kz), stride N*H; y: lines (item, X, kz), stride H
+  pruned_fft(w_cC.p, w_p1.p, PrunedLines{E * N * H, (long)N * H, (long)N * N * H, (long)W * N * H, (long)N * H}, o0);
+  pruned_fft(w_p1.p, w_p2.p, PrunedLines{E * W * H, (long)H, (long)N * H, (long)W * H, (long)H}, o0);
+  size_t smz = 2 * (size_t)W * H * sizeof(float2);
+  if (smz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_z_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
+  k_pruned_z_peak<<<dim3(W, E), 256, smz, st>>>(w_p2.p, N, W, lo, o2, rr2, w_peak.p);
   post_launch();
   }
   k_score<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, w_peak.p, (int)E, W, sum_filter, p.overlap_normalized,

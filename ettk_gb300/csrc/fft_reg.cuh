@@ -250,4 +250,50 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   post.end();
 }
 
+// Lines of a pruned, zero-padded inverse transform: line l = outer * inner_n + inner reads n_in complex
+// inputs at in + outer * in_outer + inner + n * stride and writes W outputs at
+// out + outer * out_outer + inner + X * stride.
+struct PrunedLines {
+  long n_lines, inner_n, in_outer, out_outer, stride;
+};
+
+// One axis of the upsampled (2N)^3 C2R restricted to the translational search window
+// (nbfFourierImageMetric::executeFourierNewHalf, inc/em/nbfFourierImageMetric.h:1203-1264): for each line,
+//   y[X] = sum_{k < n_in} x[k] exp(+2 pi i (k + off)(lo + X) / NN),  X < W,
+// computed as exp(+2 pi i off m / NN) * IFFT_NN(x zero-padded)[m] with m = (lo + X) mod NN.
+template <int NN, int LINES>
+__global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split<NN>::A : Split<NN>::B))
+    k_pruned_fft(const float2 *__restrict__ in, float2 *__restrict__ out, PrunedLines pl, int n_in, int W, int lo,
+                 int off) {
+  constexpr int A = Split<NN>::A, B = Split<NN>::B;
+  __shared__ float2 tw[NN];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  load_full_twiddles<NN>(tw);
+  int line, lane;
+  thread_map<NN, LINES, false>(line, lane);
+  const long l = (long)blockIdx.x * LINES + line;
+  const bool ok = l < pl.n_lines;
+  const long outer = ok ? l / pl.inner_n : 0, inner = ok ? l - outer * pl.inner_n : 0;
+  const float2 *src = in + outer * pl.in_outer + inner;
+  float2 *dst = out + outer * pl.out_outer + inner;
+  float2 v[A], o[B];
+  if (lane < B) {
+#pragma unroll
+    for (int j1 = 0; j1 < A; ++j1) {
+      const int n = B * j1 + lane;
+      v[j1] = (ok && n < n_in) ? src[(long)n * pl.stride] : make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  four_step<NN, LINES>(v, o, line, lane, +1, tw, ex);
+  if (lane < A && ok) {
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) {
+      const int m = lane + A * k2;
+      const int X = (m - lo) & (NN - 1);
+      if (X < W) dst[(long)X * pl.stride] = cmul(o[k2], twid<NN>(tw, off * m, +1));
+    }
+  }
+}
+
 }  // namespace ettk

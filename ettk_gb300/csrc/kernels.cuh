@@ -474,92 +474,23 @@ static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict_
 
 // Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
 // [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
-// and reads only this window). Same FFTW order: complex inverse along x, then y, then the
-// half-complex-to-real sum along z (real parts only for the kz = N term).
-//
-// Stage x (a complex GEMM per item): q1[e][X][r] = sum_kx E[X][kx] q[e][kx][r], r = (ky,kz),
-// E[X][kx] = exp(+i pi ((kx+o0)(lo+X) mod 2N) / N). CTA = 64 consecutive r of one item; kx in chunks
-// of 32 staged in shared memory with the twiddle rows; each thread accumulates up to XPT outputs.
-constexpr int PX_R = 64, PX_K = 32, PX_XPT = 16;
-static __global__ void __launch_bounds__(256) k_pruned_x(const float2 *__restrict__ q, float2 *__restrict__ q1, int N,
-                                                         int W, int lo, int o0) {
-  __shared__ float2 Qs[PX_K][PX_R];
-  __shared__ float2 Es[4 * PX_XPT][PX_K];
-  const int H = N / 2 + 1;
-  const long nrow = (long)N * H;
-  const float2 *Q = q + (long)blockIdx.y * N * nrow;
-  const long r0 = (long)blockIdx.x * PX_R;
-  const int tr = threadIdx.x & (PX_R - 1), tx = threadIdx.x >> 6;  // 4 X-lanes
-  for (int xb = 0; xb < W; xb += 4 * PX_XPT) {
-    float2 acc[PX_XPT];
-#pragma unroll
-    for (int t = 0; t < PX_XPT; ++t) acc[t] = make_float2(0.f, 0.f);
-    for (int k0 = 0; k0 < N; k0 += PX_K) {
-      int kc = min(PX_K, N - k0);
-      __syncthreads();
-      for (int i = threadIdx.x; i < kc * PX_R; i += blockDim.x) {
-        int kk = i / PX_R, rr = i - kk * PX_R;
-        long r = r0 + rr;
-        Qs[kk][rr] = (r < nrow) ? Q[(long)(k0 + kk) * nrow + r] : make_float2(0.f, 0.f);
-      }
-      for (int i = threadIdx.x; i < 4 * PX_XPT * kc; i += blockDim.x) {
-        int xx = i / kc, kk = i - xx * kc;
-        int X = xb + xx;
-        float2 e = make_float2(0.f, 0.f);
-        if (X < W) {
-          int ph = ((k0 + kk + o0) * (lo + X)) & (2 * N - 1);
-          float sn, cs;
-          sincospif((float)ph / (float)N, &sn, &cs);
-          e = make_float2(cs, sn);
-        }
-        Es[xx][kk] = e;
-      }
-      __syncthreads();
-      for (int kk = 0; kk < kc; ++kk) {
-        float2 v = Qs[kk][tr];
-#pragma unroll
-        for (int t = 0; t < PX_XPT; ++t) {
-          float2 e = Es[tx + 4 * t][kk];
-          acc[t].x += v.x * e.x - v.y * e.y;
-          acc[t].y += v.x * e.y + v.y * e.x;
-        }
-      }
-    }
-    long r = r0 + tr;
-    if (r < nrow) {
-#pragma unroll
-      for (int t = 0; t < PX_XPT; ++t) {
-        int X = xb + tx + 4 * t;
-        if (X < W) q1[((long)blockIdx.y * W + X) * nrow + r] = acc[t];
-      }
-    }
-  }
-}
-
-// Stages y and z plus the peak search, one CTA per (X, item):
-// q2[Y][kz] = sum_ky Ey[Y][ky] q1[X][ky][kz]; out[Y][Z] = sum_kz c_kz Re(q2[Y][kz] Ez[Z][kz]);
-// T = out * (-1)^(X+Y+Z) / (2N)^3 inside the sphere radius^2 < r^2 (else -max); packed argmax
-// (first occurrence in [X][Y][Z] order) into peak[e]. Dynamic shared memory:
-// q1 plane N*H, Ey W*N, q2 W*H, Ez W*H complex values.
-static __global__ void __launch_bounds__(256) k_pruned_yz_peak(const float2 *__restrict__ q1, int N, int W, int lo,
-                                                               int o0, int o2, float rr2,
-                                                               unsigned long long *peak) {
+// and reads only this window). Same FFTW order: complex inverse along x, then y (k_pruned_fft, 2N-point
+// register FFTs of the zero-padded lines), then the half-complex-to-real sum along z (real parts only for
+// the kz = N term) fused with the peak search.
+// Last axis of the windowed upsampled C2R plus the peak search, one CTA per (X, item):
+// out[Y][Z] = sum_kz c_KZ Re(q2[X][Y][kz] exp(+2 pi i KZ (lo + Z) / 2N)), KZ = kz + o2 (c = 1 at KZ = 0 and
+// KZ = N, else 2: the hc2r of the reference's (2N)^3 C2R); T = out * (-1)^(X+Y+Z) / (2N)^3 inside the sphere
+// radius^2 < r^2 (else -max); packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
+// Dynamic shared memory: q2 plane W*H and Ez W*H complex values.
+static __global__ void __launch_bounds__(256) k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo,
+                                                              int o2, float rr2, unsigned long long *peak) {
   extern __shared__ float2 sm[];
   const int H = N / 2 + 1;
-  float2 *P1 = sm;               // [N][H]
-  float2 *Ey = P1 + N * H;       // [W][N]
-  float2 *P2 = Ey + W * N;       // [W][H]
-  float2 *Ez = P2 + W * H;       // [W][H] (with the hc2r coefficient folded in)
+  float2 *P2 = sm;           // [W][H]
+  float2 *Ez = P2 + W * H;   // [W][H] (with the hc2r coefficient folded in)
   const int X = blockIdx.x, e = blockIdx.y;
-  const float2 *src = q1 + ((long)e * W + X) * (long)N * H;
-  for (int i = threadIdx.x; i < N * H; i += blockDim.x) P1[i] = src[i];
-  for (int i = threadIdx.x; i < W * N; i += blockDim.x) {
-    int Y = i / N, ky = i - Y * N;
-    int ph = ((ky + o0) * (lo + Y)) & (2 * N - 1);
-    float sn, cs;
-    sincospif((float)ph / (float)N, &sn, &cs);
-    Ey[i] = make_float2(cs, sn);
-  }
+  const float2 *src = q2 + ((long)e * W + X) * (long)W * H;
+  for (int i = threadIdx.x; i < W * H; i += blockDim.x) P2[i] = src[i];
   for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
     int Z = i / H, kz = i - Z * H;
     int KZ = kz + o2;
@@ -568,17 +499,6 @@ static __global__ void __launch_bounds__(256) k_pruned_yz_peak(const float2 *__r
     sincospif((float)ph / (float)N, &sn, &cs);
     float c = (KZ == N || KZ == 0) ? 1.f : 2.f;
     Ez[i] = make_float2(c * cs, c * sn);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
-    int Y = i / H, kz = i - Y * H;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int ky = 0; ky < N; ++ky) {
-      float2 a = Ey[Y * N + ky], b = P1[ky * H + kz];
-      acc.x += a.x * b.x - a.y * b.y;
-      acc.y += a.x * b.y + a.y * b.x;
-    }
-    P2[i] = acc;
   }
   __syncthreads();
   const float inv = 1.0f / (float)(8L * N * N * N);
