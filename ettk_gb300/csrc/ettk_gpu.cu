@@ -13,10 +13,12 @@
 #include "geometry.hpp"
 #include "kernels.cuh"
 #include "fft_reg.cuh"
+#include "fft2d.cuh"
 
 #include <algorithm>
 #include <atomic>
 #include <thread>
+#include <type_traits>
 #include <array>
 #include <chrono>
 #include <map>
@@ -53,6 +55,34 @@ inline void set_map(ResliceItem &it, const double m12[12]) {
       throw CudaError(e_ == cudaErrorMemoryAllocation ? ETTK_ERR_OOM : ETTK_ERR_CUDA,             \
                       std::string(#x) + ": " + cudaGetErrorString(e_));                           \
   } while (0)
+
+// Calls f(std::integral_constant<int, N>) for the supported volume sizes (kernels templated on N).
+template <class F>
+void with_n(int N, F f) {
+  switch (N) {
+    case 16: f(std::integral_constant<int, 16>{}); break;
+    case 32: f(std::integral_constant<int, 32>{}); break;
+    case 64: f(std::integral_constant<int, 64>{}); break;
+    case 128: f(std::integral_constant<int, 128>{}); break;
+    default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+  }
+}
+
+inline int ilog2(long v) {
+  int r = 0;
+  while ((1L << r) < v) ++r;
+  return r;
+}
+
+// Host table in [x][y][kz] order (kz < N/2+1) -> the kz-major order of the device spectra, [kz][x][y].
+inline std::vector<float> to_kz_major(const float *src, int N) {
+  const int H = N / 2 + 1;
+  std::vector<float> out((size_t)N * N * H);
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int k = 0; k < H; ++k) out[((size_t)k * N + x) * N + y] = src[((size_t)x * N + y) * H + k];
+  return out;
+}
 
 template <typename T>
 struct DevBuf {
@@ -408,18 +438,20 @@ struct ettk_ctx {
   }
 
   // one zero-padded 2N-point pruned inverse stage of the translational search window
-  template <int NN>
+  template <int NN, bool CONTIG>
   void pruned_fft_t(const float2 *in, float2 *out, const PrunedLines &pl, int off) {
     constexpr int L = reg_lines<NN>();
-    k_pruned_fft<NN, L><<<(unsigned)((pl.n_lines + L - 1) / L), L * MaxAB<NN>::v, 0, st>>>(in, out, pl, N, W, lo, off);
+    k_pruned_fft<NN, L, CONTIG><<<(unsigned)((pl.n_lines + L - 1) / L), L * MaxAB<NN>::v, 0, st>>>(in, out, pl, N, W,
+                                                                                                  lo, off);
     post_launch();
   }
+  template <bool CONTIG>
   void pruned_fft(const float2 *in, float2 *out, const PrunedLines &pl, int off) {
     switch (2 * N) {
-      case 32: pruned_fft_t<32>(in, out, pl, off); break;
-      case 64: pruned_fft_t<64>(in, out, pl, off); break;
-      case 128: pruned_fft_t<128>(in, out, pl, off); break;
-      case 256: pruned_fft_t<256>(in, out, pl, off); break;
+      case 32: pruned_fft_t<32, CONTIG>(in, out, pl, off); break;
+      case 64: pruned_fft_t<64, CONTIG>(in, out, pl, off); break;
+      case 128: pruned_fft_t<128, CONTIG>(in, out, pl, off); break;
+      case 256: pruned_fft_t<256, CONTIG>(in, out, pl, off); break;
       default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
     }
   }
@@ -493,22 +525,33 @@ struct ettk_ctx {
       case 32: c2r_z_t<32>(in, post, lines); break;
       case 64: c2r_z_t<64>(in, post, lines); break;
       case 128: c2r_z_t<128>(in, post, lines); break;
-      case 256: c2r_z_t<256>(in, post, lines); break;
       default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
     }
   }
-  // y and x passes of a 3-D transform of `items` arrays [len][len][len/2+1]
-  void xy_passes(int len, float2 *d, long items, int sign, bool x_first, const float *scale = nullptr) {
-    long h = len / 2 + 1;
-    LineMap my{items * len * h, (int)h, (long)len * h, 1, h};
-    LineMap mx{items * len * h, (int)(len * h), (long)len * len * h, 1, (long)len * h};
-    long per_item_lines = (long)len * h;
-    if (x_first) {
-      fft_strided(len, d, mx, sign, scale, per_item_lines);
-      fft_strided(len, d, my, sign);
-    } else {
-      fft_strided(len, d, my, sign, scale, per_item_lines);
-      fft_strided(len, d, mx, sign);
+  // (x, y) passes of a 3-D transform of `items` kz-major spectra [len/2+1][len][len]: one CTA per kz plane
+  // (k_fft2d) up to len = 128, two strided register passes beyond.
+  template <int NN, class Op>
+  void fft2d_t(Op op, long items, const char *family = "fft_xy", double bytes_per_elem = 16.0) {
+    constexpr size_t smem = fft2d_smem<NN>();
+    constexpr long H2 = NN / 2 + 1;
+    Scope sc(this, family, bytes_per_elem * items * H2 * NN * NN);
+    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_fft2d<NN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fft2d<NN, Op><<<dim3((unsigned)H2, (unsigned)items), 256, smem, st>>>(op);
+    post_launch();
+  }
+  void xy_kxy(int len, float2 *d, long items, int sign) {
+    switch (len) {
+      case 16: fft2d_t<16>(OpPlain<16>{d, sign}, items); break;
+      case 32: fft2d_t<32>(OpPlain<32>{d, sign}, items); break;
+      case 64: fft2d_t<64>(OpPlain<64>{d, sign}, items); break;
+      case 128: fft2d_t<128>(OpPlain<128>{d, sign}, items); break;
+      case 256: {
+        const long h = len / 2 + 1;
+        fft_strided(len, d, LineMap{items * h * len, 1, (long)len, 0, 1}, sign);                          // y lines
+        fft_strided(len, d, LineMap{items * h * len, len, (long)len * len, 1, (long)len}, sign);           // x lines
+        break;
+      }
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
     }
   }
 
@@ -578,7 +621,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
     }
     PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
     r2c_z(N, pre, w_cA.p, (long)E * N * N);
-    xy_passes(N, w_cA.p, E, -1, false);
+    xy_kxy(N, w_cA.p, E, -1);
     {
       Scope sc(this, "avg_accum", 8.0 * E * h3 + 48.0 * h3);
       k_avg_accum<<<nblocks<int>(h3, 256, 4096), 256, 0, st>>>(w_cA.p, w_norm.p, E, h3, ac.p, ac.p + h3, ac.p + 2 * h3);
@@ -589,7 +632,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
   w_r.ensure(n3);
   k_avg_spectrum<<<nblocks<int>(h3, 256, 4096), 256, 0, st>>>(ac.p, ac.p + h3, ac.p + 2 * h3, N, w_cB.p);
   post_launch();
-  xy_passes(N, w_cB.p, 1, +1, true);
+  xy_kxy(N, w_cB.p, 1, +1);
   c2r_z(N, w_cB.p, PostStore{w_r.p, N}, (long)N * N);
   k_avg_shift_sumsq<<<nblocks<int>(n3, 256, 1024), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3);
   post_launch();
@@ -677,7 +720,10 @@ void ettk_ctx::init_tables() {
   filter.ensure(h3);
   CK(cudaMemcpy(mask.p, m.data(), n3 * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(maskfft.p, mf.data(), n3 * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(filter.p, f.data(), h3 * 4, cudaMemcpyHostToDevice));
+  {
+    std::vector<float> fk = to_kz_major(f.data(), N);
+    CK(cudaMemcpy(filter.p, fk.data(), h3 * 4, cudaMemcpyHostToDevice));
+  }
   // wedge smoothing weights: std 2, radius int(2*0.5)=1, clipped renormalised kernels
   {
     double e1 = exp(-1.0 / 8.0), s3 = 1 + 2 * e1, s2 = 1 + e1;
@@ -781,7 +827,7 @@ void ettk_ctx::init_tables() {
   pre.src = nullptr;
   pre.aux = mask.p;
   r2c_z(N, pre, Fm1.p, (long)N * N);
-  xy_passes(N, Fm1.p, 1, -1, false);
+  xy_kxy(N, Fm1.p, 1, -1);
   sync();
 }
 
@@ -810,12 +856,23 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
   post_launch();
   r2c_z(N2, pre, sp_F.p, P * N2 * N2);
-  xy_passes(N2, sp_F.p, P, -1, false);
+  xy_kxy(N2, sp_F.p, P, -1);
   k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
   post_launch();
   Scope sc_ss(this, "sphere_sample", 4.0 * P * big_h + 4.0 * P * nn);
-  k_sphere_sample<<<dim3(nblocks<int>(nn, 128), P), 128, 0, st>>>(sp_M.p, dirs.p, (int)nn, N, bandL, bandU, sp_padc.p,
-                                                                  Pp_out);
+  switch (N) {
+#define SS_CASE(NN)                                                                                              \
+  case NN:                                                                                                       \
+    k_sphere_sample<NN><<<dim3(nblocks<int>(nn, 128), P), 128, 0, st>>>(sp_M.p, dirs.p, (int)nn, bandL, bandU,   \
+                                                                        sp_padc.p, Pp_out);                     \
+    break;
+    SS_CASE(16)
+    SS_CASE(32)
+    SS_CASE(64)
+    SS_CASE(128)
+#undef SS_CASE
+    default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+  }
   post_launch();
 }
 
@@ -887,16 +944,15 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   } else {
     for (long e = 0; e < E; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
   }
-  // I1 branch: F1 = R2C(I1 maskfft shift) * fw, normalised, C2R, k1_m and R2C(I1' m1)
-  {
-  Scope sc_f(this, "spec_filter", 20.0 * E * h3);
-  k_spec_filter<<<gh, 256, 0, st>>>(FI1.p, w_idx.p, w_fw.p, w_cA.p, N, acc, ACC, 2);
-  post_launch();
-  }
+  // I1 branch: F1 = FI1 * fw (DC zeroed) with its normalisation sums, inverse (x, y) passes, C2R scaled by
+  // 1/norm, then k1_m and R2C(I1' m1)
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, w_fw.p, w_cA.p, HalfSums<NN>{acc, ACC, 2}}, E, "fft_xy", 20.0);
+  });
   k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)E, w_norm.p, nullptr);
   post_launch();
-  xy_passes(N, w_cA.p, E, +1, true, w_norm.p);
-  c2r_z(N, w_cA.p, PostStore{w_r.p, N}, E * N * N);
+  c2r_z(N, w_cA.p, PostStoreScaled{w_r.p, N, w_norm.p, ilog2((long)N * N)}, E * N * N);
   PreY1M1 py;
   py.y = w_r.p;
   py.m1 = mask.p;
@@ -906,8 +962,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   py.slot = 4;
   py.lines_per_block = lines_per_block(N);
   r2c_z(N, py, w_cA.p, E * N * N);
-  xy_passes(N, w_cA.p, E, -1, false);
-  // I2 branch: reslice under T, R2C((I2-mean) maskfft shift) * fw, normalised
+  xy_kxy(N, w_cA.p, E, -1);
+  // I2 branch: reslice under T, R2C((I2-mean) maskfft shift), forward (x, y) passes then * fw with the
+  // normalisation sums
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
     k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, acc2, ACC);
@@ -915,25 +972,32 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
   r2c_z(N, pp, w_cB.p, E * N * N);
-  xy_passes(N, w_cB.p, E, -1, false);
-  k_spec_filter<<<gh, 256, 0, st>>>(w_cB.p, nullptr, w_fw.p, w_cB.p, N, acc2, ACC, 2);
-  post_launch();
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFwdFilter<NN>{w_cB.p, w_fw.p, HalfSums<NN>{acc2, ACC, 2}}, E, "fft_xy", 20.0);
+  });
   k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc2, ACC, 2, N, (int)E, w_norm2.p, nullptr);
   post_launch();
-  k_fft2re<<<gh, 256, 0, st>>>(w_cA.p, w_cB.p, w_norm2.p, N);
-  post_launch();
-  xy_passes(N, w_cB.p, E, +1, true, w_norm2.p);
+  // FFT2re over FFT1re, inverse (x, y) passes of F2/norm2, C2R, R2C(I2'^2 shift), forward passes + cross term
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFft2reInv<NN>{w_cA.p, w_cB.p, w_norm2.p}, E, "fft_xy", 32.0);
+  });
   c2r_z(N, w_cB.p, PostStore{w_r.p, N}, E * N * N);
   r2c_z(N, PreSquareShift{w_r.p, N}, w_cC.p, E * N * N);
-  xy_passes(N, w_cC.p, E, -1, false);
-  k_cross<<<gh, 256, 0, st>>>(w_cC.p, Fm1.p, w_cA.p, N, 8.0f);
-  post_launch();
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFwdCross<NN>{w_cC.p, Fm1.p, w_cA.p, 8.0f}, E, "fft_xy", 24.0);
+  });
   int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
   {
   Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
-  // x: lines (item, ky, kz), stride N*H; y: lines (item, X, kz), stride H
-  pruned_fft(w_cC.p, w_p1.p, PrunedLines{E * N * H, (long)N * H, (long)N * N * H, (long)W * N * H, (long)N * H}, o0);
-  pruned_fft(w_p1.p, w_p2.p, PrunedLines{E * W * H, (long)H, (long)N * H, (long)W * H, (long)H}, o0);
+  // x: lines (item, kz, ky) of the kz-major spectrum, stride N, into q1[item][X][kz][ky];
+  // y: lines (item, X, kz), contiguous, into q2[item][X][kz][Y]
+  pruned_fft<false>(w_cC.p, w_p1.p,
+                    PrunedLines{E * H * N, (long)H * N, (long)H * N * N, (long)N, (long)N * N, (long)N,
+                                (long)W * H * N, (long)H * N}, o0);
+  pruned_fft<true>(w_p1.p, w_p2.p, PrunedLines{E * W * H, 1, (long)N, 1, 0, 1, (long)W, 1}, o0);
   size_t smz = 2 * (size_t)W * H * sizeof(float2);
   if (smz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_z_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
   k_pruned_z_peak<<<dim3(W, E), 256, smz, st>>>(w_p2.p, N, W, lo, o2, rr2, w_peak.p);
@@ -1626,7 +1690,8 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
       set_map(items[r], m12);
       std::vector<float> w;
       wedge_half_host(c->refg[r], c->N, w);
-      std::copy(w.begin(), w.end(), w1h.begin() + (size_t)r * h3);
+      std::vector<float> wk = to_kz_major(w.data(), c->N);
+      std::copy(wk.begin(), wk.end(), w1h.begin() + (size_t)r * h3);
       int use = 0;
       spherical_wedge_host(c->refg[r], c->B, w, use);
       std::copy(w.begin(), w.end(), w1s.begin() + (size_t)r * c->nn);
@@ -1648,7 +1713,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->FI1.ensure(R * h3);
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
     c->r2c_z(c->N, pre, c->FI1.p, (long)R * c->N * c->N);
-    c->xy_passes(c->N, c->FI1.p, R, -1, false);
+    c->xy_kxy(c->N, c->FI1.p, R, -1);
     // Pp1 = cartesianToSpherical(I1)
     c->Pp1.ensure(R * c->nn);
     c->spherical_projection(items, c->Pp1.p);

@@ -1,0 +1,209 @@
+// (x, y) passes of the 3-D transforms on kz-major spectra.
+//
+// Every half spectrum of an N^3 volume is stored kz-major, [item][kz][x][y] (kz < N/2+1), so one kz plane
+// is a contiguous N x N complex tile. k_fft2d transforms one plane per CTA in shared memory: coalesced
+// load (with an optional fused prologue), the N-point register FFT of every row (y lines), then of every
+// column (x lines), and a coalesced store (with an optional fused epilogue). The prologues/epilogues are
+// the elementwise steps of executeFourierNewHalf that sit between the transforms (filter, normalisation
+// sums, the FFT2re update and the cross term), so each of them costs no extra pass over HBM.
+#pragma once
+#include "fft_reg.cuh"
+
+namespace ettk {
+
+// kz-major index of element i = x*N + y of plane kz of item e
+template <int N>
+struct KXY {
+  static constexpr int H = N / 2 + 1;
+  static constexpr long NN = (long)N * N;
+  static constexpr long h3 = NN * H;
+  ETTK_DEV static long at(long e, int kz, int i) { return (e * H + kz) * NN + i; }
+  // DC of the centred half spectrum: (x, y, kz) = (N/2, N/2, H-1)
+  static constexpr int dc_xy = (N / 2) * N + N / 2;
+};
+
+// FFT of one line of N complex values in shared memory (element n at line[n * stride]) by a group of
+// MaxAB<N> consecutive lanes of one warp (lane = index within the group; act = false for a group without a
+// line). Every lane of the warp must make the call (warp-synchronous exchange through the line itself).
+template <int N>
+ETTK_DEV void group_fft(float2 *line, int stride, int lane, bool act, int sign, const float2 *tw) {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  float2 v[A];
+  const bool s1 = act && lane < B, s2 = act && lane < A;
+  if (s1) {
+#pragma unroll
+    for (int j1 = 0; j1 < A; ++j1) v[j1] = line[(B * j1 + lane) * stride];
+    dft_reg<A>(v, sign);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) v[k1] = cmul(v[k1], twid<N>(tw, lane * k1, sign));
+  }
+  __syncwarp();
+  if (s1) {
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) line[(k1 * B + lane) * stride] = v[k1];
+  }
+  __syncwarp();
+  float2 o[B];
+  if (s2) {
+#pragma unroll
+    for (int j2 = 0; j2 < B; ++j2) o[j2] = line[(lane * B + j2) * stride];
+    dft_reg<B>(o, sign);
+  }
+  __syncwarp();
+  if (s2) {
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) line[(lane + A * k2) * stride] = o[k2];
+  }
+  __syncwarp();
+}
+
+// Shared memory of k_fft2d: the plane with a row pitch of N+1 complex values.
+template <int N>
+constexpr size_t fft2d_smem() { return (size_t)N * (N + 1) * sizeof(float2); }
+
+// One CTA per (kz plane, item) = (blockIdx.x, blockIdx.y). Op supplies sign, begin(), load(e, kz, i),
+// store(e, kz, i, x, y, v) and end(e, kz) (all threads call begin/end).
+template <int N, class Op>
+__global__ void __launch_bounds__(256) k_fft2d(Op op) {
+  constexpr int G = MaxAB<N>::v;      // lanes per line
+  constexpr int GROUPS = 256 / G;     // lines in flight
+  constexpr int WG = 32 / G;          // groups per warp
+  constexpr int P = N + 1;            // row pitch
+  extern __shared__ float2 pl[];
+  __shared__ float2 tw[N];
+  load_full_twiddles<N>(tw);
+  const int kz = blockIdx.x, e = blockIdx.y;
+  op.begin();
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    const int x = i / N, y = i - x * N;
+    pl[x * P + y] = op.load(e, kz, i);
+  }
+  __syncthreads();
+  // the groups of one warp take lines 8 apart, which puts their rows / columns 16 words apart in the banks
+  const int grp = threadIdx.x / G, lane = threadIdx.x % G;
+  const int sub = (grp % WG) * (GROUPS / WG) + grp / WG;
+  for (int r0 = 0; r0 < N; r0 += GROUPS) {
+    const int r = r0 + sub;
+    group_fft<N>(pl + (r < N ? r : 0) * P, 1, lane, r < N, op.sign, tw);
+  }
+  __syncthreads();
+  for (int c0 = 0; c0 < N; c0 += GROUPS) {
+    const int c = c0 + sub;
+    group_fft<N>(pl + (c < N ? c : 0), P, lane, c < N, op.sign, tw);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    const int x = i / N, y = i - x * N;
+    op.store(e, kz, i, x, y, pl[x * P + y]);
+  }
+  op.end(e, kz);
+}
+
+// In-place (x, y) transform.
+template <int N>
+struct OpPlain {
+  float2 *d;
+  int sign;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N>::at(e, kz, i)]; }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { d[KXY<N>::at(e, kz, i)] = v; }
+  ETTK_DEV void end(int, int) {}
+};
+
+// Sums of |v|^2 of a normalizeFourierHalf (inc/em/nbfCorrelationImageMetric.h:497-530): kz < H-1 into
+// acc[e][slot], the kz = H-1 plane into acc[e][slot+1]; per-thread FP32 partials, FP64 across threads.
+template <int N>
+struct HalfSums {
+  double *acc;
+  int acc_stride, slot;
+  float s = 0.f;
+  ETTK_DEV void add(float2 v) { s += v.x * v.x + v.y * v.y; }
+  ETTK_DEV void flush(int e, int kz) {
+    __shared__ double shm[32];
+    const double b = block_sum((double)s, shm);
+    if (threadIdx.x == 0) atomicAdd(&acc[(long)e * acc_stride + slot + (kz == KXY<N>::H - 1 ? 1 : 0)], b);
+  }
+};
+
+// I1 branch: F1 = FI1[ref] * fw with the DC zeroed (executeHalf, inc/em/nbfFourierFilter.h:586-606), its
+// normalisation sums, then the inverse (x, y) passes (the 1/norm scale is applied by the following C2R).
+template <int N>
+struct OpFilterInv {
+  const float2 *src;
+  const int *src_index;
+  const float *fw;
+  float2 *dst;
+  HalfSums<N> sums;
+  int sign = +1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) {
+    const long g = KXY<N>::at(e, kz, i);
+    float2 v = cscale(src[KXY<N>::at(src_index[e], kz, i)], fw[g]);
+    if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
+    sums.add(v);
+    return v;
+  }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { dst[KXY<N>::at(e, kz, i)] = v; }
+  ETTK_DEV void end(int e, int kz) { sums.flush(e, kz); }
+};
+
+// I2 branch: forward (x, y) passes, then * fw with the DC zeroed and the normalisation sums.
+template <int N>
+struct OpFwdFilter {
+  float2 *d;
+  const float *fw;
+  HalfSums<N> sums;
+  int sign = -1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N>::at(e, kz, i)]; }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
+    const long g = KXY<N>::at(e, kz, i);
+    v = cscale(v, fw[g]);
+    if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
+    sums.add(v);
+    d[g] = v;
+  }
+  ETTK_DEV void end(int e, int kz) { sums.flush(e, kz); }
+};
+
+// FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3) stored over FFT1re (nbfFourierImageMetric.h:1174-1177), then
+// the inverse (x, y) passes of F2 / norm2.
+template <int N>
+struct OpFft2reInv {
+  float2 *a;                 // FFT1re (updated in the prologue)
+  float2 *b;                 // F2 (transformed in place)
+  const float *inv_norm2;
+  int sign = +1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) {
+    const long g = KXY<N>::at(e, kz, i);
+    const float sc = inv_norm2[e];
+    const float2 bb = b[g];
+    const float2 bs = cscale(bb, sc * (float)((long)N * N * N));
+    a[g] = cscale(cmul(a[g], cconj(bs)), 2.0f);
+    return cscale(bb, sc);
+  }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { b[KXY<N>::at(e, kz, i)] = v; }
+  ETTK_DEV void end(int, int) {}
+};
+
+// Forward (x, y) passes of F(I2'^2), then FFTre = (-F(m1) conj(F(I2'^2)) + FFT2re) * shift * 8
+// (nbfFourierImageMetric.h:1192-1210, the 8 of the zero padding).
+template <int N>
+struct OpFwdCross {
+  float2 *q;
+  const float2 *fm1;         // one item
+  const float2 *fft2re;
+  float factor;
+  int sign = -1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) const { return q[KXY<N>::at(e, kz, i)]; }
+  ETTK_DEV void store(int e, int kz, int i, int x, int y, float2 v) {
+    const long g = KXY<N>::at(e, kz, i);
+    const float2 w = cadd(cscale(cmul(fm1[KXY<N>::at(0, kz, i)], cconj(v)), -1.f), fft2re[g]);
+    q[g] = cscale(w, parity_sign(x, y, kz) * factor);
+  }
+  ETTK_DEV void end(int, int) {}
+};
+
+}  // namespace ettk

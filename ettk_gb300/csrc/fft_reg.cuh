@@ -159,11 +159,14 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
 }
 
 // Real-to-complex pass along the contiguous axis: two real lines (2c, 2c+1) packed into one complex
-// FFT; Pre(line, k) supplies the real inputs; out has N/2+1 complex values per real line.
+// FFT; Pre(line, k) supplies the real inputs (line = item*N*N + x*N + y). The half spectra are written
+// kz-major, out[item][kz][x][y] (kz < N/2+1), through the exchange buffer so that consecutive threads
+// store consecutive lines of one kz plane.
 template <int N, int LINES, class Pre>
 __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
     k_r2c_reg(Pre pre, float2 *__restrict__ out, long n_lines) {
-  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1;
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES;
+  constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
   __shared__ float2 ex[A * B * (LINES + 1)];
   load_full_twiddles<N>(tw);
@@ -193,24 +196,38 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
   }
   __syncthreads();
-  for (int k = lane; k < H; k += (A > B ? A : B)) {
-    float2 zk = ex[k * (LINES + 1) + line];
-    float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + line];
-    float2 x1 = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
-    float2 x2 = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
-    if (ok0) out[l0 * H + k] = x1;
-    if (ok1) out[(l0 + 1) * H + k] = x2;
+  const long l_base = (long)blockIdx.x * RL;
+  for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+    const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
+    const long l = l_base + rl;
+    if (l < n_lines) {
+      const float2 zk = ex[k * (LINES + 1) + cl];
+      const float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + cl];
+      const float2 xv = (rl & 1) ? make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x))
+                                 : make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+      out[(l / NN) * H * NN + (long)k * NN + (l % NN)] = xv;
+    }
   }
 }
 
-// Complex-to-real pass along the contiguous axis (two half spectra -> one packed complex inverse).
+// Complex-to-real pass along the contiguous axis (two half spectra -> one packed complex inverse). The
+// kz-major input is staged in shared memory [kz][line] with consecutive threads loading consecutive lines.
 template <int N, int LINES, class Post>
 __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
     k_c2r_reg(const float2 *__restrict__ in, Post post, long n_lines) {
-  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1;
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES;
+  constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
   __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 hs[H * RL];
   load_full_twiddles<N>(tw);
+  const long l_base = (long)blockIdx.x * RL;
+  for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+    const int k = idx / RL, rl = idx - k * RL;
+    const long l = l_base + rl;
+    hs[idx] = (l < n_lines) ? in[(l / NN) * H * NN + (long)k * NN + (l % NN)] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
   int line, lane;
   thread_map<N, LINES, true>(line, lane);
   const long c = (long)blockIdx.x * LINES + line;
@@ -223,15 +240,15 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
       int k = B * j1 + lane;
       float2 a, b;
       if (k <= N / 2) {
-        a = ok0 ? in[l0 * H + k] : make_float2(0.f, 0.f);
-        b = ok1 ? in[(l0 + 1) * H + k] : make_float2(0.f, 0.f);
+        a = hs[k * RL + 2 * line];
+        b = hs[k * RL + 2 * line + 1];
         if (k == 0 || k == N / 2) {
           a.y = 0.f;
           b.y = 0.f;
         }
       } else {
-        a = ok0 ? cconj(in[l0 * H + (N - k)]) : make_float2(0.f, 0.f);
-        b = ok1 ? cconj(in[(l0 + 1) * H + (N - k)]) : make_float2(0.f, 0.f);
+        a = cconj(hs[(N - k) * RL + 2 * line]);
+        b = cconj(hs[(N - k) * RL + 2 * line + 1]);
       }
       v[j1] = make_float2(a.x - b.y, a.y + b.x);
     }
@@ -251,17 +268,17 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
 }
 
 // Lines of a pruned, zero-padded inverse transform: line l = outer * inner_n + inner reads n_in complex
-// inputs at in + outer * in_outer + inner + n * stride and writes W outputs at
-// out + outer * out_outer + inner + X * stride.
+// inputs at in + outer * in_outer + (inner / in_div) * in_mid + inner % in_div + n * in_stride and writes
+// W outputs at out + outer * out_outer + inner + X * out_stride.
 struct PrunedLines {
-  long n_lines, inner_n, in_outer, out_outer, stride;
+  long n_lines, inner_n, in_outer, in_div, in_mid, in_stride, out_outer, out_stride;
 };
 
 // One axis of the upsampled (2N)^3 C2R restricted to the translational search window
 // (nbfFourierImageMetric::executeFourierNewHalf, inc/em/nbfFourierImageMetric.h:1203-1264): for each line,
 //   y[X] = sum_{k < n_in} x[k] exp(+2 pi i (k + off)(lo + X) / NN),  X < W,
 // computed as exp(+2 pi i off m / NN) * IFFT_NN(x zero-padded)[m] with m = (lo + X) mod NN.
-template <int NN, int LINES>
+template <int NN, int LINES, bool CONTIG>
 __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split<NN>::A : Split<NN>::B))
     k_pruned_fft(const float2 *__restrict__ in, float2 *__restrict__ out, PrunedLines pl, int n_in, int W, int lo,
                  int off) {
@@ -270,18 +287,19 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
   __shared__ float2 ex[A * B * (LINES + 1)];
   load_full_twiddles<NN>(tw);
   int line, lane;
-  thread_map<NN, LINES, false>(line, lane);
+  thread_map<NN, LINES, CONTIG>(line, lane);
   const long l = (long)blockIdx.x * LINES + line;
   const bool ok = l < pl.n_lines;
   const long outer = ok ? l / pl.inner_n : 0, inner = ok ? l - outer * pl.inner_n : 0;
-  const float2 *src = in + outer * pl.in_outer + inner;
+  const long q = inner / pl.in_div;
+  const float2 *src = in + outer * pl.in_outer + q * pl.in_mid + (inner - q * pl.in_div);
   float2 *dst = out + outer * pl.out_outer + inner;
   float2 v[A], o[B];
   if (lane < B) {
 #pragma unroll
     for (int j1 = 0; j1 < A; ++j1) {
       const int n = B * j1 + lane;
-      v[j1] = (ok && n < n_in) ? src[(long)n * pl.stride] : make_float2(0.f, 0.f);
+      v[j1] = (ok && n < n_in) ? src[(long)n * pl.in_stride] : make_float2(0.f, 0.f);
     }
   }
   __syncthreads();
@@ -291,7 +309,7 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
     for (int k2 = 0; k2 < B; ++k2) {
       const int m = lane + A * k2;
       const int X = (m - lo) & (NN - 1);
-      if (X < W) dst[(long)X * pl.stride] = cmul(o[k2], twid<NN>(tw, off * m, +1));
+      if (X < W) dst[(long)X * pl.out_stride] = cmul(o[k2], twid<NN>(tw, off * m, +1));
     }
   }
 }

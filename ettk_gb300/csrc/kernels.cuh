@@ -237,7 +237,7 @@ ETTK_DEV float smooth3v(const Smooth3 &sw, float vm, float v0, float vp, int pos
 // along k then j (float rounding after each pass, as vtkImageGaussianSmooth stores its intermediates) into a
 // three-plane ring in shared memory; as soon as planes q-1, q, q+1 are in the ring, plane q is smoothed
 // along i, multiplied by the reference wedge and the filter, stored, and summed into acc[item][acc_slot]
-// (sum(wedge*filter) of the overlap normalisation).
+// (sum(wedge*filter) of the overlap normalisation). Filter, reference wedges and output are kz-major.
 template <int N, int SLAB>
 __global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict__ wv, Smooth3 sw,
                                                     const float *__restrict__ w1, const int *__restrict__ w1_index,
@@ -256,12 +256,15 @@ __global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict_
   const float *W1 = w1 + (long)w1_index[e] * h3;
   float *o = out + (long)e * h3;
   float s = 0.f;
+  // plane q of the output is written kz-major: element (q, j, k) at [k][q][j] (j fastest, coalesced)
   auto emit = [&](int q) {
     const float *rm = ring + ((q + 2) % 3) * PL, *r0 = ring + (q % 3) * PL, *rp = ring + ((q + 1) % 3) * PL;
-    for (int r = threadIdx.x; r < PL; r += blockDim.x) {
+    for (int t = threadIdx.x; t < PL; t += blockDim.x) {
+      const int k = t / N, j = t - k * N;
+      const int r = j * H + k;
       const float vm = q > 0 ? rm[r] : 0.f, vp = q < N - 1 ? rp[r] : 0.f;
       const float v = smooth3v(sw, vm, r0[r], vp, q, N);
-      const long g = (long)q * PL + r;
+      const long g = ((long)k * N + q) * N + j;
       const float fw = filter[g] * (v * W1[g]);
       o[g] = fw;
       s += fw;
@@ -294,33 +297,6 @@ constexpr int wedge_slab() { return N >= 32 ? 16 : 8; }
 template <int N>
 constexpr size_t wedge_smem() { return 4 * (size_t)N * (N / 2 + 1) * sizeof(float); }
 
-// executeHalf + normalizeFourierHalf accumulation (inc/em/nbfFourierFilter.h:586-606,
-// inc/em/nbfCorrelationImageMetric.h:497-530): out = src * fw, DC zeroed, sums of |F|^2 for
-// k < H-1 (slot) and k = H-1 (slot+1). src item index through src_index (nullptr = same item).
-static __global__ void k_spec_filter(const float2 *__restrict__ src, const int *__restrict__ src_index,
-                              const float *__restrict__ fw, float2 *__restrict__ out, int N, double *acc,
-                              int acc_stride, int slot) {
-  __shared__ double sh[32];
-  const int H = N / 2 + 1;
-  long h3 = (long)N * N * H;
-  long sidx = src_index ? (long)src_index[blockIdx.y] : (long)blockIdx.y;
-  const float2 *S = src + sidx * h3;
-  long dc = ((long)(N / 2) * N + N / 2) * H + (H - 1);
-  float s1 = 0.f, s2 = 0.f;  // per-thread partials over a few elements; FP64 across threads
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
-    float2 v = cscale(S[id], fw[(long)blockIdx.y * h3 + id]);
-    if (id == dc) v = make_float2(0.f, 0.f);
-    out[(long)blockIdx.y * h3 + id] = v;
-    float m = v.x * v.x + v.y * v.y;
-    if ((id % H) < H - 1) s1 += m; else s2 += m;
-  }
-  double b1 = block_sum((double)s1, sh), b2 = block_sum((double)s2, sh);
-  if (threadIdx.x == 0) {
-    atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot], b1);
-    atomicAdd(&acc[(long)blockIdx.y * acc_stride + slot + 1], b2);
-  }
-}
-
 // norm of normalizeFourierHalf with its float roundings: norm = float(2*s1);
 // norm = float(sqrt((norm + s2) / (N*N*2*(H-1)))). Writes 1/norm (and norm) per item.
 static __global__ void k_norms(const double *acc, int acc_stride, int slot, int N, int n_items, float *inv_norm,
@@ -346,15 +322,17 @@ struct PreY1M1 {
   int acc_stride, slot;
   float s = 0.f;  // per-thread partial (a thread sees at most a few dozen elements); FP64 across threads
   long lines_per_block = 0;  // real lines handled by one CTA (never straddles two items)
-  long cl = -1, cr = 0;      // per-thread cache of the last line's in-item row
+  // per-thread cache of the in-item row of the two real lines a thread alternates between (slot = line & 1)
+  long cl[2] = {-1, -1}, cr[2] = {0, 0};
   ETTK_DEV void begin() { s = 0.f; }
   ETTK_DEV float operator()(long line, int k) {
-    if (line != cl) {
-      cl = line;
-      cr = line % ((long)N * N);
+    const int sl = (int)(line & 1);
+    if (line != cl[sl]) {
+      cl[sl] = line;
+      cr[sl] = line % ((long)N * N);
     }
     float v = y[line * N + k];
-    float m = m1[cr * N + k];
+    float m = m1[cr[sl] * N + k];
     s += v * v * m;
     return v * m;
   }
@@ -375,27 +353,31 @@ struct PreParticle {
   int acc_stride, N;
   long cached = -1;  // per-thread: item whose mean is in `mean`
   float mean = 0.f;
-  long cl = -1;      // per-thread cache of the last line's decomposition
-  int cr = 0, cij = 0;
+  // per-thread cache of the decomposition of the two real lines a thread alternates between (slot = line & 1)
+  long cl[2] = {-1, -1};
+  int cr[2] = {0, 0}, cij[2] = {0, 0};
+  float cmean[2] = {0.f, 0.f};
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV float operator()(long line, int k) {
-    if (line != cl) {
+    const int sl = (int)(line & 1);
+    if (line != cl[sl]) {
       long n2 = (long)N * N;
       long e = line / n2;
-      cl = line;
-      cr = (int)(line - e * n2);
-      cij = cr / N + cr % N;
+      cl[sl] = line;
+      cr[sl] = (int)(line - e * n2);
+      cij[sl] = cr[sl] / N + cr[sl] % N;
       if (e != cached) {
         float cnt = (float)acc[e * acc_stride + 1];
         mean = (float)(acc[e * acc_stride + 0] / (double)cnt);
         cached = e;
       }
+      cmean[sl] = mean;
     }
     float val = v[line * N + k];
-    float out = (val > -FLT_MAX) ? val - mean : 0.f;
-    float m = maskfft ? maskfft[(long)cr * N + k] : 1.f;
-    return out * m * (((cij + k) & 1) ? -1.f : 1.f);
+    float out = (val > -FLT_MAX) ? val - cmean[sl] : 0.f;
+    float m = maskfft ? maskfft[(long)cr[sl] * N + k] : 1.f;
+    return out * m * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
 
@@ -403,18 +385,19 @@ struct PreParticle {
 struct PreSquareShift {
   const float *y;
   int N;
-  long cl = -1;
-  int cij = 0;
+  long cl[2] = {-1, -1};  // two-slot line cache (slot = line & 1)
+  int cij[2] = {0, 0};
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV float operator()(long line, int k) {
-    if (line != cl) {
-      cl = line;
+    const int sl = (int)(line & 1);
+    if (line != cl[sl]) {
+      cl[sl] = line;
       int r = (int)(line % ((long)N * N));
-      cij = r / N + r % N;
+      cij[sl] = r / N + r % N;
     }
     float v = y[line * N + k];
-    return v * v * (((cij + k) & 1) ? -1.f : 1.f);
+    return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
 
@@ -443,34 +426,17 @@ struct PostStore {
   ETTK_DEV void end() {}
   ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v; }
 };
-
-// FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3), stored over FFT1re (nbfFourierImageMetric.h:1174-1177).
-static __global__ void k_fft2re(float2 *__restrict__ a, const float2 *__restrict__ f2, const float *__restrict__ inv_norm2,
-                         int N) {
-  const int H = N / 2 + 1;
-  long h3 = (long)N * N * H;
-  float sc = inv_norm2[blockIdx.y] * (float)((long)N * N * N);
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
-    long g = (long)blockIdx.y * h3 + id;
-    float2 b = cscale(f2[g], sc);
-    a[g] = cscale(cmul(a[g], cconj(b)), 2.0f);
-  }
-}
-
-// FFTre = (-F(m1) conj(F(I2'^2)) + FFT2re) * shiftr, times the zero-padding factor 8
-// (nbfFourierImageMetric.h:1192-1210: FFTre holds F(m1) and FFT1re holds F(I2'^2) there). In place over q.
-static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict__ fm1, const float2 *__restrict__ fft2re, int N,
-                        float factor) {
-  const int H = N / 2 + 1;
-  long h3 = (long)N * N * H;
-  const int nh = N * H;
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)h3; id += gridDim.x * blockDim.x) {
-    long g = (long)blockIdx.y * h3 + id;
-    int i = id / nh, rem = id - i * nh, j = rem / H, k = rem - j * H;
-    float2 v = cadd(cscale(cmul(fm1[id], cconj(q[g])), -1.f), fft2re[g]);
-    q[g] = cscale(v, parity_sign(i, j, k) * factor);
-  }
-}
+// Same with a per-item scale (the 1/norm of normalizeFourierHalf, linear through the inverse passes);
+// item = line >> lg_nn (N*N lines per item).
+struct PostStoreScaled {
+  float *y;
+  int N;
+  const float *scale;
+  int lg_nn;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v * scale[line >> lg_nn]; }
+};
 
 // Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
 // [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
@@ -481,7 +447,7 @@ static __global__ void k_cross(float2 *__restrict__ q, const float2 *__restrict_
 // out[Y][Z] = sum_kz c_KZ Re(q2[X][Y][kz] exp(+2 pi i KZ (lo + Z) / 2N)), KZ = kz + o2 (c = 1 at KZ = 0 and
 // KZ = N, else 2: the hc2r of the reference's (2N)^3 C2R); T = out * (-1)^(X+Y+Z) / (2N)^3 inside the sphere
 // radius^2 < r^2 (else -max); packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
-// Dynamic shared memory: q2 plane W*H and Ez W*H complex values.
+// q2 is [item][X][kz][Y]; dynamic shared memory: the q2 plane as [Y][kz] (W*H) and Ez W*H complex values.
 static __global__ void __launch_bounds__(256) k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo,
                                                               int o2, float rr2, unsigned long long *peak) {
   extern __shared__ float2 sm[];
@@ -490,7 +456,10 @@ static __global__ void __launch_bounds__(256) k_pruned_z_peak(const float2 *__re
   float2 *Ez = P2 + W * H;   // [W][H] (with the hc2r coefficient folded in)
   const int X = blockIdx.x, e = blockIdx.y;
   const float2 *src = q2 + ((long)e * W + X) * (long)W * H;
-  for (int i = threadIdx.x; i < W * H; i += blockDim.x) P2[i] = src[i];
+  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
+    const int kz = i / W, Y = i - kz * W;
+    P2[Y * H + kz] = src[i];
+  }
   for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
     int Z = i / H, kz = i - Z * H;
     int KZ = kz + o2;
@@ -573,7 +542,7 @@ static __global__ void k_avg_accum(const float2 *__restrict__ F, const float *__
 static __global__ void k_avg_spectrum(const double *__restrict__ acc, const double *__restrict__ re,
                                       const double *__restrict__ im, int N, float2 *__restrict__ F) {
   const int H = N / 2 + 1;
-  long h3 = (long)N * N * H, dc = ((long)(N / 2) * N + N / 2) * H + (H - 1);
+  long h3 = (long)N * N * H, dc = (long)(H - 1) * N * N + (N / 2) * N + N / 2;  // kz-major DC
   for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < h3; id += (long)gridDim.x * blockDim.x) {
     float2 v = make_float2(0.f, 0.f);
     if (acc[id] > 0) v = make_float2((float)(re[id] / acc[id]), (float)(im[id] / acc[id]));
@@ -650,20 +619,22 @@ struct PrePadded {
     float img = (x > -FLT_MAX) ? x - mean : 0.f;
     return (img - meanAll) * mask[id] + meanAll;
   }
-  long cl = -1, ce = 0;
-  int cx = 0, cy = 0;
+  long cl[2] = {-1, -1}, ce[2] = {0, 0};  // two-slot line cache (slot = line & 1)
+  int cx[2] = {0, 0}, cy[2] = {0, 0};
   ETTK_DEV float operator()(long line, int z) {
-    if (line != cl) {
+    const int sl = (int)(line & 1);
+    if (line != cl[sl]) {
       const int N2 = 2 * N;
       long per = (long)N2 * N2;
-      ce = line / per;
-      int r = (int)(line - ce * per);
-      cx = r / N2;
-      cy = r % N2;
-      cl = line;
+      ce[sl] = line / per;
+      int r = (int)(line - ce[sl] * per);
+      cx[sl] = r / N2;
+      cy[sl] = r % N2;
+      cl[sl] = line;
     }
-    float val = (cx < N && cy < N && z < N) ? windowed(ce, ((long)cx * N + cy) * N + z) : windowed(ce, 0);
-    return val * parity_sign(cx, cy, z);
+    const int x = cx[sl], y = cy[sl];
+    float val = (x < N && y < N && z < N) ? windowed(ce[sl], ((long)x * N + y) * N + z) : windowed(ce[sl], 0);
+    return val * parity_sign(x, y, z);
   }
 };
 
@@ -675,50 +646,67 @@ static __global__ void k_magnitude(const float2 *__restrict__ F, float *__restri
   }
 }
 
-// Virtual Hermitian-completed magnitude cube (lines 327-338): z <= N from the half spectrum,
-// x = 0 plane zero, z > N mirrored through (N,N,N) except the y = 0 plane which keeps the
-// padded real-space value (the corner value).
-ETTK_DEV float mag_at(const float *Mh, int N, int x, int y, int z, float padc) {
-  const int N2 = 2 * N, H = N + 1;
-  if (x == 0) return 0.f;
-  if (z <= N) return Mh[((long)x * N2 + y) * H + z];
-  if (y == 0) return padc;
-  return Mh[((long)(N2 - x) * N2 + (N2 - y)) * H + (N2 - z)];
-}
-
 // Cubic resampling on radial shells through vtkSphericalTransform with wrap, summed over the
-// radii [bandL, bandU] (lines 359-406): Pp[e][j][k] for polar j, azimuth k.
-static __global__ void k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs, int n_dirs, int N,
-                                int bandL, int bandU, const float *__restrict__ padc, float *__restrict__ Pp) {
-  int d = blockIdx.x * blockDim.x + threadIdx.x;
+// radii [bandL, bandU] (lines 359-406): Pp[e][j][k] for polar j, azimuth k. The taps read the virtual
+// Hermitian-completed magnitude cube (lines 327-338): z <= N from the stored kz-major half volume [z <= N][x][y],
+// the x = 0 plane zero, z > N mirrored through (N, N, N) except on the y = 0 plane, which keeps the padded
+// real-space value (the corner value).
+// 2N is a power of two, so the wrap of the tap indices is a mask; the mirror offsets are hoisted per axis.
+template <int N>
+__global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs,
+                                                       int n_dirs, int bandL, int bandU, const float *__restrict__ padc,
+                                                       float *__restrict__ Pp) {
+  constexpr int N2 = 2 * N, H = N + 1, MSK = N2 - 1;
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= n_dirs) return;
-  const int e = blockIdx.y, N2 = 2 * N;
-  const float *M = Mh + (long)e * N2 * N2 * (N + 1);
-  float4 u = dirs[d];
-  float pc = padc[e];
+  const int e = blockIdx.y;
+  const float *M = Mh + (long)e * N2 * N2 * H;
+  const float4 u = dirs[d];
+  const float pc = padc[e];
   float acc = 0.f;
   for (int r = bandL; r <= bandU; ++r) {
-    float p[3] = {r * u.x + (float)N, r * u.y + (float)N, r * u.z + (float)N};
-    float f[3];
-    int ii[3];
-    for (int t = 0; t < 3; ++t) ii[t] = vtk_floor(p[t], f[t]);
+    const float p0 = r * u.x + (float)N, p1 = r * u.y + (float)N, p2 = r * u.z + (float)N;
+    float fx, fy, fz;
+    const int ix = vtk_floor(p0, fx), iy = vtk_floor(p1, fy), iz = vtk_floor(p2, fz);
     float wx[4], wy[4], wz[4];
-    cubic_weights(wx, f[0]);
-    cubic_weights(wy, f[1]);
-    cubic_weights(wz, f[2]);
-    int mY = f[1] != 0.f, mZ = f[2] != 0.f;
-    int j1 = 1 - mY, j2 = 1 + 2 * mY, k1 = 1 - mZ, k2 = 1 + 2 * mZ;
-    if (!mY) wy[1] = 1.f;
-    if (!mZ) wz[1] = 1.f;
-    int xs[4];
-    for (int t = 0; t < 4; ++t) xs[t] = ((ii[0] - 1 + t) % N2 + N2) % N2;
+    cubic_weights(wx, fx);
+    cubic_weights(wy, fy);
+    cubic_weights(wz, fz);
+    // the reference uses only the middle row/plane when fy/fz == 0 (the forced (0, 1, 0, 0) weights add zeros)
+    if (fy == 0.f) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
+    if (fz == 0.f) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
+    int xo[4], xm[4];
+    bool x0[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int x = (ix - 1 + t) & MSK;
+      x0[t] = x == 0;
+      xo[t] = x * N2;
+      xm[t] = ((N2 - x) & MSK) * N2;
+    }
     float v = 0.f;
-    for (int k = k1; k <= k2; ++k) {
-      int zz = ((ii[2] - 1 + k) % N2 + N2) % N2;
-      for (int j = j1; j <= j2; ++j) {
-        int yy = ((ii[1] - 1 + j) % N2 + N2) % N2;
-        v += (wz[k] * wy[j]) * (wx[0] * mag_at(M, N, xs[0], yy, zz, pc) + wx[1] * mag_at(M, N, xs[1], yy, zz, pc) +
-                                wx[2] * mag_at(M, N, xs[2], yy, zz, pc) + wx[3] * mag_at(M, N, xs[3], yy, zz, pc));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int z = (iz - 1 + k) & MSK;
+      const bool mir = z > N;
+      const int zo = (mir ? N2 - z : z) * N2 * N2;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int y = (iy - 1 + j) & MSK;
+        float g[4];
+        if (!mir) {
+          const int base = zo + y;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xo[t]);
+        } else if (y == 0) {
+#pragma unroll
+          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : pc;
+        } else {
+          const int base = zo + (N2 - y);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xm[t]);
+        }
+        v += (wz[k] * wy[j]) * (wx[0] * g[0] + wx[1] * g[1] + wx[2] * g[2] + wx[3] * g[3]);
       }
     }
     acc += v;
