@@ -535,7 +535,12 @@ struct ettk_ctx {
     constexpr size_t smem = fft2d_smem<NN>();
     constexpr long H2 = NN / 2 + 1;
     Scope sc(this, family, bytes_per_elem * items * H2 * NN * NN);
-    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_fft2d<NN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static bool attr_set = false;  // per instantiation, once per process
+    if (!attr_set) {
+      CK(cudaFuncSetAttribute(k_fft2d<NN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CK(cudaFuncSetAttribute(k_fft2d<NN, Op>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+      attr_set = true;
+    }
     k_fft2d<NN, Op><<<dim3((unsigned)H2, (unsigned)items), 256, smem, st>>>(op);
     post_launch();
   }

@@ -25,6 +25,8 @@ struct KXY {
 // FFT of one line of N complex values in shared memory (element n at line[n * stride]) by a group of
 // MaxAB<N> consecutive lanes of one warp (lane = index within the group; act = false for a group without a
 // line). Every lane of the warp must make the call (warp-synchronous exchange through the line itself).
+// The exchange stores y[k1][j2] at k1*B + ((j2 + k1) mod B), so that both the stage-1 stores (lanes = j2)
+// and the stage-2 loads (lanes = k1) touch distinct banks.
 template <int N>
 ETTK_DEV void group_fft(float2 *line, int stride, int lane, bool act, int sign, const float2 *tw) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
@@ -40,13 +42,13 @@ ETTK_DEV void group_fft(float2 *line, int stride, int lane, bool act, int sign, 
   __syncwarp();
   if (s1) {
 #pragma unroll
-    for (int k1 = 0; k1 < A; ++k1) line[(k1 * B + lane) * stride] = v[k1];
+    for (int k1 = 0; k1 < A; ++k1) line[(k1 * B + ((lane + k1) & (B - 1))) * stride] = v[k1];
   }
   __syncwarp();
   float2 o[B];
   if (s2) {
 #pragma unroll
-    for (int j2 = 0; j2 < B; ++j2) o[j2] = line[(lane * B + j2) * stride];
+    for (int j2 = 0; j2 < B; ++j2) o[j2] = line[(lane * B + ((j2 + lane) & (B - 1))) * stride];
     dft_reg<B>(o, sign);
   }
   __syncwarp();

@@ -219,13 +219,16 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
   __shared__ float2 ex[A * B * (LINES + 1)];
-  __shared__ float2 hs[H * RL];
+  // row pitch of the staged spectra: even (16-byte reads of the two packed lines) and 2 (mod 16) complex
+  // values, so that the 8 k rows read by the lanes of one line cover all banks once
+  constexpr int HP = RL + 2;
+  __shared__ __align__(16) float2 hs[H * HP];
   load_full_twiddles<N>(tw);
   const long l_base = (long)blockIdx.x * RL;
   for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
     const int k = idx / RL, rl = idx - k * RL;
     const long l = l_base + rl;
-    hs[idx] = (l < n_lines) ? in[(l / NN) * H * NN + (long)k * NN + (l % NN)] : make_float2(0.f, 0.f);
+    hs[k * HP + rl] = (l < n_lines) ? in[(l / NN) * H * NN + (long)k * NN + (l % NN)] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   int line, lane;
@@ -239,16 +242,16 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     for (int j1 = 0; j1 < A; ++j1) {
       int k = B * j1 + lane;
       float2 a, b;
-      if (k <= N / 2) {
-        a = hs[k * RL + 2 * line];
-        b = hs[k * RL + 2 * line + 1];
-        if (k == 0 || k == N / 2) {
-          a.y = 0.f;
-          b.y = 0.f;
-        }
-      } else {
-        a = cconj(hs[(N - k) * RL + 2 * line]);
-        b = cconj(hs[(N - k) * RL + 2 * line + 1]);
+      const int kk = k <= N / 2 ? k : N - k;
+      const float4 ab = *reinterpret_cast<const float4 *>(&hs[kk * HP + 2 * line]);
+      a = make_float2(ab.x, ab.y);
+      b = make_float2(ab.z, ab.w);
+      if (k == 0 || k == N / 2) {
+        a.y = 0.f;
+        b.y = 0.f;
+      } else if (k > N / 2) {
+        a = cconj(a);
+        b = cconj(b);
       }
       v[j1] = make_float2(a.x - b.y, a.y + b.x);
     }

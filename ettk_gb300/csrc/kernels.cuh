@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict_
   extern __shared__ float wsm[];
   float *Kp = wsm;            // k-smoothed plane
   float *ring = wsm + PL;     // 3 j/k-smoothed planes, plane p in slot p % 3
+  float *bits = wsm + 4 * PL; // binary wedge of the current plane
   __shared__ double sh[32];
   const int e = blockIdx.y, i0 = blockIdx.x * SLAB;
   const WedgeVecs w = wv[e];
@@ -274,10 +275,12 @@ __global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict_
   for (int p = pstart; p <= pend; ++p) {
     for (int r = threadIdx.x; r < PL; r += blockDim.x) {
       const int j = r / H, k = r - j * H;
-      const float b0 = wedge_bit(w, f1, f2, p, j, k, N, H);
-      const float bm = k > 0 ? wedge_bit(w, f1, f2, p, j, k - 1, N, H) : 0.f;
-      const float bp = k < H - 1 ? wedge_bit(w, f1, f2, p, j, k + 1, N, H) : 0.f;
-      Kp[r] = smooth3v(sw, bm, b0, bp, k, H);
+      bits[r] = wedge_bit(w, f1, f2, p, j, k, N, H);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < PL; r += blockDim.x) {
+      const int k = r % H;
+      Kp[r] = smooth3v(sw, k > 0 ? bits[r - 1] : 0.f, bits[r], k < H - 1 ? bits[r + 1] : 0.f, k, H);
     }
     __syncthreads();  // also orders the previous emit's ring reads before this plane's ring write
     float *dst = ring + (p % 3) * PL;
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict_
 template <int N>
 constexpr int wedge_slab() { return N >= 32 ? 16 : 8; }
 template <int N>
-constexpr size_t wedge_smem() { return 4 * (size_t)N * (N / 2 + 1) * sizeof(float); }
+constexpr size_t wedge_smem() { return 5 * (size_t)N * (N / 2 + 1) * sizeof(float); }
 
 // norm of normalizeFourierHalf with its float roundings: norm = float(2*s1);
 // norm = float(sqrt((norm + s2) / (N*N*2*(H-1)))). Writes 1/norm (and norm) per item.
