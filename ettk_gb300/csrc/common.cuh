@@ -75,6 +75,42 @@ ETTK_DEV int vtk_floor(float x, float &f) {
   return q >> 16;
 }
 
+// ---- mbarrier + bulk tensor copy (TMA) helpers ------------------------------------------------
+ETTK_DEV uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+ETTK_DEV void mbar_init(void *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+ETTK_DEV void mbar_expect_tx(void *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase with the given parity; false if it did not complete within max_iter polls.
+ETTK_DEV bool mbar_wait(void *bar, uint32_t parity, int max_iter) {
+  const uint32_t a = smem_addr(bar);
+  for (int i = 0; i < max_iter; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// 3-D tile load of a tensor map (global memory) into shared memory, completing on bar. The innermost
+// coordinate x must be a multiple of 16 bytes / element size; dst 128-byte aligned.
+ETTK_DEV void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, void *bar) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_addr(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // Tricubic weights of vtkImageInterpolator (Filtering/vtkImageInterpolator.cxx:313-325).
 ETTK_DEV void cubic_weights(float F[4], float f) {
   float fm1 = f - 1.0f, fd2 = f * 0.5f, ft3 = f * 3.0f;

@@ -10,6 +10,8 @@
 //      pair's queues are exhausted or have counted candidatePeaks peaks,
 //   5. final candidate selection (eliminateEquivalentAngles with tolerance 2.5).
 #include "../../include/ettk_gpu.h"
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include "geometry.hpp"
 #include "kernels.cuh"
 #include "fft_reg.cuh"
@@ -22,6 +24,7 @@
 #include <array>
 #include <chrono>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +42,42 @@ struct CudaError : std::runtime_error {
   int code;
   CudaError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
+
+// cuTensorMapEncodeTiled from the driver, resolved once (null if unavailable: the kernels then stage
+// through the threads).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Host-encoded tensor maps of `count` consecutive N^3 float volumes (x fastest) with the reslice box
+// RT_X x RT_Y x RT_Z. Returns false (and no maps) where the box does not fit or encoding fails.
+bool encode_volume_maps(const float *base, int count, int N, std::vector<CUtensorMap> &maps) {
+  maps.clear();
+  auto enc = tensor_map_encoder();
+  if (!enc || N < RT_X || (((unsigned long long)base) & 15)) return false;
+  maps.resize(count);
+  const long n3 = (long)N * N * N;
+  const cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N};
+  const cuuint64_t strides[2] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4};
+  const cuuint32_t box[3] = {RT_X, RT_Y, RT_Z}, es[3] = {1, 1, 1};
+  for (int v = 0; v < count; ++v)
+    if (enc(&maps[v], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)(base + v * n3), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+      maps.clear();
+      return false;
+    }
+  return true;
+}
 
 // Output-index -> input-index map of a reslice item, in FP32 (default kernels) and FP64 (exact variant).
 inline void set_map(ResliceItem &it, const double m12[12]) {
@@ -328,6 +367,30 @@ struct ettk_ctx {
   DevBuf<double> w_acc, w_w, sp_acc;
   DevBuf<unsigned long long> w_peak, w_mm;
   DevBuf<ResliceItem> w_items;
+  // tensor maps of the particle and reference volumes (empty: the reslice stages through the threads)
+  DevBuf<CUtensorMap> tm_part, tm_ref;
+  bool tm_part_ok = false, tm_ref_ok = false;
+  DevBuf<int> status;  // set by kernels whose bounded waits ran out
+  const void *part_map(long p) const { return tm_part_ok ? (const void *)(tm_part.p + p) : nullptr; }
+  const void *ref_map(long r) const { return tm_ref_ok ? (const void *)(tm_ref.p + r) : nullptr; }
+  void upload_maps(const float *base, int count, DevBuf<CUtensorMap> &dst, bool &ok) {
+    std::vector<CUtensorMap> h;
+    ok = encode_volume_maps(base, count, N, h);
+    if (ok) {
+      dst.ensure(count);
+      CK(cudaMemcpyAsync(dst.p, h.data(), count * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));  // h is pageable and goes out of scope
+    }
+  }
+  void check_status() {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h) {
+      CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+      throw CudaError(ETTK_ERR_TIMEOUT, "a bulk tensor copy did not complete in time");
+    }
+  }
   DevBuf<WedgeVecs> w_wv;
   DevBuf<int> w_idx, w_idx2, w_cnt, w_active, w_pair_ref, w_pair_pp2, w_pair_part;
   DevBuf<int2> w_lists;
@@ -607,6 +670,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
       double m12[12];
       reslice_index(g, N, &t, m12);
       items[e].vol = partptr + (long)parts[i] * n3;
+      items[e].tmap = part_map(parts[i]);
       items[e].dims[0] = items[e].dims[1] = items[e].dims[2] = N;
       set_map(items[e], m12);
       w[e] = weights[i];
@@ -621,7 +685,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
     CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
     {
       Scope sc(this, "reslice", 8.0 * E * n3);
-      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2);
+      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2, status.p);
       post_launch();
     }
     PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
@@ -646,9 +710,12 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
   post_launch();
   CK(cudaMemcpyAsync(avg, w_tmp.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
   sync();
+  check_status();
 }
 
 void ettk_ctx::init_tables() {
+  status.ensure(1);
+  CK(cudaMemset(status.p, 0, sizeof(int)));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
@@ -852,7 +919,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
     Scope sc(this, "reslice", 8.0 * P * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4, status.p);
   }
   post_launch();
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
@@ -916,6 +983,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     reslice_index(g, N, &r.t, m12);
     ResliceItem it;
     it.vol = partptr + (long)r.part * n3;
+    it.tmap = part_map(r.part);
     it.dims[0] = it.dims[1] = it.dims[2] = N;
     set_map(it, m12);
     items[e] = it;
@@ -972,7 +1040,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   // normalisation sums
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, acc2, ACC);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, acc2, ACC, status.p);
   }
   post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
@@ -1014,6 +1082,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   hs_launch.reset();
   std::vector<EvalOut> out(E);
   read_back(out.data(), w_out.p, E * sizeof(EvalOut));
+  check_status();
   for (long e = 0; e < E; ++e) {
     res[e].dist = out[e].dist;
     Mat4 tr = Mat4::eye();
@@ -1136,6 +1205,7 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         for (size_t c = c0; c < c1; ++c) {
           ResliceItem it;
           it.vol = partptr + (long)ids[c] * n3;
+          it.tmap = part_map(ids[c]);
           it.dims[0] = it.dims[1] = it.dims[2] = N;
           double m12[12];
           reslice_index(partg[ids[c]], N, nullptr, m12);
@@ -1684,6 +1754,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->useW1.resize(R);
     c->refvol.ensure(R * n3);
     CK(cudaMemcpy(c->refvol.p, vols, R * n3 * 4, cudaMemcpyHostToDevice));
+    c->upload_maps(c->refvol.p, R, c->tm_ref, c->tm_ref_ok);
     std::vector<ResliceItem> items(R);
     std::vector<float> w1h((size_t)R * h3), w1s((size_t)R * c->nn);
     for (int r = 0; r < R; ++r) {
@@ -1691,6 +1762,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
       double m12[12];
       reslice_index(c->refg[r], c->N, nullptr, m12);
       items[r].vol = c->refvol.p + (long)r * n3;
+      items[r].tmap = c->ref_map(r);
       items[r].dims[0] = items[r].dims[1] = items[r].dims[2] = c->N;
       set_map(items[r], m12);
       std::vector<float> w;
@@ -1713,7 +1785,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
     k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, RS_SMEM, c->st>>>(c->w_items.p, c->N, c->w_v.p,
-                                                                                          c->w_acc.p, 2);
+                                                                                          c->w_acc.p, 2, c->status.p);
     c->post_launch();
     c->FI1.ensure(R * h3);
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
@@ -1723,6 +1795,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->Pp1.ensure(R * c->nn);
     c->spherical_projection(items, c->Pp1.p);
     c->sync();
+    c->check_status();
   });
 }
 
@@ -1742,6 +1815,7 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
       CK(cudaMemcpyAsync(c->partvol.p, vols, V * n3 * 4, cudaMemcpyHostToDevice, c->st));
       c->partptr = c->partvol.p;
     }
+    c->upload_maps(c->partptr, V, c->tm_part, c->tm_part_ok);
     std::vector<float> w2s((size_t)V * c->nn);
     for (int v = 0; v < V; ++v) {
       c->partg[v] = to_geom(meta[v]);
@@ -1795,10 +1869,12 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
     if (p >= 0) {
       if (p >= c->V) throw CudaError(ETTK_ERR_STATE, "particle index out of range");
       it.vol = c->partptr + (long)p * c->n3;
+      it.tmap = c->part_map(p);
       reslice_index(c->partg[p], c->N, nullptr, m12);
     } else {
       if (r < 0 || r >= c->R) throw CudaError(ETTK_ERR_STATE, "reference index out of range");
       it.vol = c->refvol.p + (long)r * c->n3;
+      it.tmap = c->ref_map(r);
       reslice_index(c->refg[r], c->N, nullptr, m12);
     }
     it.dims[0] = it.dims[1] = it.dims[2] = c->N;
@@ -1807,6 +1883,7 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
     c->spherical_projection({it}, c->w_sig.p);
     CK(cudaMemcpyAsync(Pp, c->w_sig.p, c->nn * 4, cudaMemcpyDeviceToHost, c->st));
     c->sync();
+    c->check_status();
   });
 }
 

@@ -12,6 +12,7 @@ struct ResliceItem {
   int dims[3];
   float m[12];   // origin[3], x axis[3], y axis[3], z axis[3]
   double md[12]; // the same in FP64 (used by the exact-coordinate variant)
+  const void *tmap = nullptr;  // device tensor map of vol (RT_X x RT_Y x RT_Z float boxes), or null
 };
 
 // nbfWedgedSubImage3D::getImage (inc/em/nbfWedgedSubImage3D.h:602-828): tricubic reslice of the
@@ -20,14 +21,21 @@ struct ResliceItem {
 // of valid values and their count into acc[item*acc_stride + 0/1].
 //
 // One 8x8x8 output brick per CTA. The input footprint of the brick (its corner coordinates widened by
-// the cubic support and a rounding margin) is staged in shared memory with 16-byte loads: the x range
-// starts at a multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge value
-// (the clamp border of the reference, exact because the x extent is a multiple of 4). For a rotation the
-// footprint is at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices,
-// unaligned volumes) read the taps from global memory.
+// the cubic support and a rounding margin) is staged in shared memory. When the item has a tensor map and
+// the fixed RT_X x RT_Y x RT_Z box at (x0, o1, o2) lies inside the volume (no clamping needed), one bulk
+// tensor copy (TMA) stages it; otherwise the threads stage it with 16-byte loads: the x range starts at a
+// multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge value (the clamp
+// border of the reference, exact because the x extent is a multiple of 4). For a rotation the footprint is
+// at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned volumes)
+// read the taps from global memory. A copy that does not complete sets *status (the host reports a
+// timeout) instead of waiting forever.
 constexpr int RB = 8;             // brick edge
 constexpr int RS_MAX = 9600;      // staged floats (37.5 KiB of dynamic shared memory, five CTAs per SM)
 constexpr size_t RS_SMEM = RS_MAX * sizeof(float);
+// Fixed box of the bulk tensor copy: it holds the footprint of any rotated brick (x from a multiple of 4)
+constexpr int RT_X = 24, RT_Y = 20, RT_Z = 20;
+static_assert(RT_X * RT_Y * RT_Z <= RS_MAX, "tensor box exceeds the staging buffer");
+constexpr int RT_WAIT = 1 << 22;  // polls of the copy barrier before the kernel reports a timeout
 
 // Tricubic sum with clamped taps read from global memory (bricks whose footprint is not staged).
 static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz, int ix, int iy, int iz,
@@ -55,11 +63,13 @@ static __device__ __noinline__ float tricubic_global(const float *__restrict__ v
 // matters); otherwise the same sequence runs in FP32.
 template <bool PRECISE>
 __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
-                                                          float *__restrict__ out, double *acc, int acc_stride) {
-  extern __shared__ float4 box4[];
+                                                          float *__restrict__ out, double *acc, int acc_stride,
+                                                          int *status) {
+  extern __shared__ __align__(128) float4 box4[];
   const float *box = reinterpret_cast<const float *>(box4);
   __shared__ double sh[32];
   __shared__ int geo[6];  // o[3], ext[3]
+  __shared__ __align__(8) unsigned long long tma_bar;
   const ResliceItem &it = items[blockIdx.y];
   const int nb = N / RB;
   const int bx = blockIdx.x / (nb * nb), by = (blockIdx.x / nb) % nb, bz = blockIdx.x % nb;
@@ -94,10 +104,25 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
   const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5];
   const int x0 = o0 & ~3;                        // floor to a multiple of 4
   const int w4 = (o0 + e0 - x0 + 3) >> 2;        // 16-byte groups per staged row
-  const int P = w4 * 4;                          // staged row pitch (floats)
-  const bool staged = e0 >= 5 && e0 <= 64 && e1 >= 5 && e1 <= 64 && e2 >= 5 && e2 <= 64 && e1 * e2 * P <= RS_MAX &&
-                      (dx & 3) == 0 && (((unsigned long long)vol) & 15) == 0;
-  if (staged) {
+  const bool use_tma = it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && x0 >= 0 && x0 + RT_X <= dx && o1 >= 0 &&
+                       o1 + RT_Y <= dy && o2 >= 0 && o2 + RT_Z <= dz && o0 + e0 <= x0 + RT_X && e1 <= RT_Y &&
+                       e2 <= RT_Z;
+  const int P = use_tma ? RT_X : w4 * 4;         // staged row pitch (floats)
+  const int E1 = use_tma ? RT_Y : e1;            // staged rows per plane
+  const bool staged = use_tma || (e0 >= 5 && e0 <= 64 && e1 >= 5 && e1 <= 64 && e2 >= 5 && e2 <= 64 &&
+                                  e1 * e2 * P <= RS_MAX && (dx & 3) == 0 && (((unsigned long long)vol) & 15) == 0);
+  if (use_tma) {
+    if (threadIdx.x == 0) mbar_init(&tma_bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&tma_bar, RT_X * RT_Y * RT_Z * (uint32_t)sizeof(float));
+      tma_load_3d(box4, it.tmap, x0, o1, o2, &tma_bar);
+    }
+    if (!mbar_wait(&tma_bar, 0, RT_WAIT)) {
+      atomicExch(status, 1);
+      mbar_wait(&tma_bar, 0, RT_WAIT);  // the copy may still land: wait again (bounded) before the buffer is reused
+    }
+  } else if (staged) {
     // flat index -> (row, group) and row -> (y, z) by multiply-high (exact for divisors <= 64, index < 2^16)
     const unsigned mw = 0xFFFFFFFFu / (unsigned)w4 + 1u, me = 0xFFFFFFFFu / (unsigned)e1 + 1u;
     const int n4 = e1 * e2 * w4;
@@ -163,8 +188,8 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
       if (!((dz > 1) && (fz != 0.f))) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
       float acc2 = 0.f;
       if (staged) {
-        const float *b0 = box + ((iz - 1 - o2) * e1 + (iy - 1 - o1)) * P + (ix - 1 - x0);
-        const int rz = e1 * P;
+        const float *b0 = box + ((iz - 1 - o2) * E1 + (iy - 1 - o1)) * P + (ix - 1 - x0);
+        const int rz = E1 * P;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
 #pragma unroll
