@@ -8,6 +8,7 @@
 // stores of strided axes are coalesced across lines. Conventions as fft.cuh (FFTW: forward
 // exp(-i...), unnormalised; the c2r pass uses only the real parts of the k=0 and k=N/2 inputs).
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 #include "fft.cuh"
 
@@ -158,6 +159,13 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   }
 }
 
+// Input functors that can tell a line r[z] = c (-1)^(x+y+z) over the whole line (the constant padding of
+// the spherical projection) declare kPadLines and pad_line(line, c, sign(x+y)).
+template <class T, class = void>
+struct has_pad_lines : std::false_type {};
+template <class T>
+struct has_pad_lines<T, std::void_t<decltype(T::kPadLines)>> : std::true_type {};
+
 // Real-to-complex pass along the contiguous axis: two real lines (2c, 2c+1) packed into one complex
 // FFT; Pre(line, k) supplies the real inputs (line = item*N*N + x*N + y). The half spectra are written
 // kz-major, out[item][kz][x][y] (kz < N/2+1), through the exchange buffer so that consecutive threads
@@ -169,6 +177,26 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
   __shared__ float2 ex[A * B * (LINES + 1)];
+  const long l_base = (long)blockIdx.x * RL;
+  if constexpr (has_pad_lines<Pre>::value) {
+    // a CTA whose lines are all padding lines writes their spectra directly: the N-point transform of
+    // c (-1)^(x+y+z) is N c (-1)^(x+y) at k = N/2 and zero elsewhere
+    float c0, s0;
+    const long lt = l_base + (threadIdx.x % RL);
+    if (__syncthreads_and(lt >= n_lines || pre.pad_line(lt, c0, s0))) {
+      for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+        const int k = idx / RL, rl = idx - k * RL;
+        const long l = l_base + rl;
+        if (l < n_lines) {
+          float2 v = make_float2(0.f, 0.f);
+          float cc, sg;
+          if (k == N / 2 && pre.pad_line(l, cc, sg)) v = make_float2((float)N * cc * sg, 0.f);
+          out[(l / NN) * H * NN + (long)k * NN + (l % NN)] = v;
+        }
+      }
+      return;
+    }
+  }
   load_full_twiddles<N>(tw);
   int line, lane;
   thread_map<N, LINES, true>(line, lane);
@@ -196,7 +224,6 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
   }
   __syncthreads();
-  const long l_base = (long)blockIdx.x * RL;
   for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
     const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
     const long l = l_base + rl;

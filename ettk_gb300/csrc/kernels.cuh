@@ -30,10 +30,11 @@ struct ResliceItem {
 // read the taps from global memory. A copy that does not complete sets *status (the host reports a
 // timeout) instead of waiting forever.
 constexpr int RB = 8;             // brick edge
-constexpr int RS_MAX = 9600;      // staged floats (37.5 KiB of dynamic shared memory, five CTAs per SM)
+constexpr int RS_MAX = 10080;     // staged floats (39.4 KiB of dynamic shared memory, five CTAs per SM)
 constexpr size_t RS_SMEM = RS_MAX * sizeof(float);
-// Fixed box of the bulk tensor copy: it holds the footprint of any rotated brick (x from a multiple of 4)
-constexpr int RT_X = 24, RT_Y = 20, RT_Z = 20;
+// Fixed box of the bulk tensor copy: it holds the footprint of any rotated brick (x from a multiple of 4);
+// 21 rows per plane keep the plane pitch (24 * 21 floats) off a multiple of the 32 banks
+constexpr int RT_X = 24, RT_Y = 21, RT_Z = 20;
 static_assert(RT_X * RT_Y * RT_Z <= RS_MAX, "tensor box exceeds the staging buffer");
 constexpr int RT_WAIT = 1 << 22;  // polls of the copy barrier before the kernel reports a timeout
 
@@ -108,9 +109,11 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
                        o1 + RT_Y <= dy && o2 >= 0 && o2 + RT_Z <= dz && o0 + e0 <= x0 + RT_X && e1 <= RT_Y &&
                        e2 <= RT_Z;
   const int P = use_tma ? RT_X : w4 * 4;         // staged row pitch (floats)
-  const int E1 = use_tma ? RT_Y : e1;            // staged rows per plane
+  // staged rows per plane: odd, so that the plane pitch E1 * P is never a multiple of 32 floats (taps that
+  // differ only in z would otherwise share a bank)
+  const int E1 = use_tma ? RT_Y : (e1 | 1);
   const bool staged = use_tma || (e0 >= 5 && e0 <= 64 && e1 >= 5 && e1 <= 64 && e2 >= 5 && e2 <= 64 &&
-                                  e1 * e2 * P <= RS_MAX && (dx & 3) == 0 && (((unsigned long long)vol) & 15) == 0);
+                                  E1 * e2 * P <= RS_MAX && (dx & 3) == 0 && (((unsigned long long)vol) & 15) == 0);
   if (use_tma) {
     if (threadIdx.x == 0) mbar_init(&tma_bar, 1);
     __syncthreads();
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
       float4 f = __ldg(reinterpret_cast<const float4 *>(vol + ((long)z * dy + y) * dx + xl));
       if (xs < 0) f = make_float4(f.x, f.x, f.x, f.x);
       else if (xs > dx - 4) f = make_float4(f.w, f.w, f.w, f.w);
-      box4[i] = f;
+      box4[(uz * E1 + uy) * w4 + c4] = f;
     }
   }
   __syncthreads();
@@ -646,6 +649,18 @@ struct PrePadded {
     float x = v[e * (long)N * N * N + id];
     float img = (x > -FLT_MAX) ? x - mean : 0.f;
     return (img - meanAll) * mask[id] + meanAll;
+  }
+  static constexpr bool kPadLines = true;
+  // line (x, y) with x >= N or y >= N lies wholly in the padding: r[z] = c (-1)^(x+y+z)
+  ETTK_DEV bool pad_line(long line, float &c, float &sign_xy) {
+    const int N2 = 2 * N;
+    const long per = (long)N2 * N2;
+    const long e = line / per;
+    const int r = (int)(line - e * per), x = r / N2, y = r - x * N2;
+    if (x < N && y < N) return false;
+    c = windowed(e, 0);
+    sign_xy = ((x + y) & 1) ? -1.f : 1.f;
+    return true;
   }
   long cl[2] = {-1, -1}, ce[2] = {0, 0};  // two-slot line cache (slot = line & 1)
   int cx[2] = {0, 0}, cy[2] = {0, 0};
