@@ -42,7 +42,7 @@ class Params(ctypes.Structure):
         ("restrict_translation", ctypes.c_float), ("restrict_rotation", ctypes.c_float),
         ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
         ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
-        ("mutual_correlation", ctypes.c_int), ("max_batch", ctypes.c_int),
+        ("mutual_correlation", ctypes.c_int), ("max_batch", ctypes.c_int), ("wigner_precision", ctypes.c_int),
     ]
 
 
@@ -107,7 +107,8 @@ def make_params(p):
         restrict_translation=p["restrict_translation"], restrict_rotation=p["restrict_rotation"],
         candidate_peaks=int(p["candidate_peaks"]), number_of_candidates=int(p["number_of_candidates"]),
         wedge_compensation=int(bool(p["wedge_compensation"])), overlap_normalized=int(bool(p["overlap_normalized"])),
-        mutual_correlation=int(bool(p.get("mutual_correlation", False))), max_batch=int(p.get("max_batch", 0)))
+        mutual_correlation=int(bool(p.get("mutual_correlation", False))), max_batch=int(p.get("max_batch", 0)),
+        wigner_precision=int(p.get("wigner_precision", 0)))
 
 
 def make_meta(metas):

@@ -16,6 +16,7 @@
 #include "kernels.cuh"
 #include "fft_reg.cuh"
 #include "fft2d.cuh"
+#include "wigner_tc.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -343,6 +344,36 @@ struct ettk_ctx {
   // constant tables
   DevBuf<float> mask, maskfft, filter, lw, plm, dtab, sinth;
   DevBuf<int> doff;
+  DevBuf<double> dtab64;  // FP64 Wigner-d table (wigner_precision 4 only)
+  // Wigner-d synthesis of NJ correlation jobs into w_S (zeroed by the caller) in the configured precision
+  template <int BB, int MODE>
+  void synth_tc(long NJ) {
+    static bool attr_set = false;  // per instantiation, once per process
+    if (!attr_set) {
+      CK(cudaFuncSetAttribute(k_so3_synth_tc<BB, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)WigTC<BB, MODE>::SMEM));
+      attr_set = true;
+    }
+    k_so3_synth_tc<BB, MODE><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)((NJ + 63) / 64)), 128,
+                               WigTC<BB, MODE>::SMEM, st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab.p, doff.p, w_S.p,
+                                                            status.p);
+  }
+  template <int BB>
+  void synth(long NJ) {
+    switch (p.wigner_precision) {
+      case WIG_BF16: synth_tc<BB, WIG_BF16>(NJ); break;
+      case WIG_SPLIT: synth_tc<BB, WIG_SPLIT>(NJ); break;
+      case WIG_TF32: synth_tc<BB, WIG_TF32>(NJ); break;
+      case WIG_FP64:
+        k_so3_synth_f64<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(64, (NJ * 2 * BB + 255) / 256)),
+                              256, 0, st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab64.p, doff.p, w_S.p);
+        break;
+      default:
+        k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(64, (NJ + 7) / 8)), 256, 0,
+                          st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab.p, doff.p, w_S.p);
+    }
+    post_launch();
+  }
   DevBuf<float4> dirs;
   DevBuf<float2> Fm1;
   double sum_filter = 0;
@@ -852,18 +883,27 @@ void ettk_ctx::init_tables() {
     total += (long)(B - std::max(std::abs(m1), std::abs(m2))) * n;
   }
   std::vector<float> hd(total);
+  std::vector<double> hd64(p.wigner_precision == WIG_FP64 ? total : 0);
   std::vector<double> col(B);
   for (int cell = 0; cell < ncell; ++cell) {
     int m1 = cell / (2 * B - 1) - (B - 1), m2 = cell % (2 * B - 1) - (B - 1);
     int l0 = std::max(std::abs(m1), std::abs(m2));
     for (int j = 0; j < n; ++j) {
       small_d(B, m1, m2, th[j], col.data());
-      for (int l = l0; l < B; ++l) hd[off[cell] + (size_t)(l - l0) * n + j] = (float)(sqrt((2.0 * l + 1.0) / 2.0) * col[l]);
+      for (int l = l0; l < B; ++l) {
+        const double v = sqrt((2.0 * l + 1.0) / 2.0) * col[l];
+        hd[off[cell] + (size_t)(l - l0) * n + j] = (float)v;
+        if (!hd64.empty()) hd64[off[cell] + (size_t)(l - l0) * n + j] = v;
+      }
     }
   }
   dtab.ensure(total);
   doff.ensure(ncell);
   CK(cudaMemcpy(dtab.p, hd.data(), total * 4, cudaMemcpyHostToDevice));
+  if (!hd64.empty()) {
+    dtab64.ensure(total);
+    CK(cudaMemcpy(dtab64.p, hd64.data(), total * 8, cudaMemcpyHostToDevice));
+  }
   CK(cudaMemcpy(doff.p, off.data(), ncell * 4, cudaMemcpyHostToDevice));
   std::vector<float> hs(n);
   for (int j = 0; j < n; ++j) hs[j] = (float)sin(M_PI * (2 * j + 1) / 4 / (double)(float)B);
@@ -1302,9 +1342,7 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
     CK(cudaMemsetAsync(w_S.p, 0, NJ * nso3 * sizeof(float2), st));                                           \
     {                                                                                                         \
     Scope sc_s(this, "so3_synth", 8.0 * NJ * nso3 + 4.0 * dtab.n);                                           \
-    k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(64, (NJ + 7) / 8)), 256, 0,  \
-                      st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab.p, doff.p, w_S.p);                              \
-    post_launch();                                                                                            \
+    synth<BB>(NJ);                                                                                            \
     }                                                                                                         \
     fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, 1, (long)n, 0, 1}, -1);                                    \
     fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n, (long)n * n, 1, (long)n}, -1);                          \
@@ -1539,9 +1577,7 @@ void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C)
     k_sht<BB><<<2, 256, smem_sht, st>>>(w_sig.p, lw.p, w_coef.p);                                         \
     post_launch();                                                                                        \
     CK(cudaMemsetAsync(w_S.p, 0, nso3 * sizeof(float2), st));                                            \
-    k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), 1), 256, 0, st>>>(w_coef.p, w_jobs.p, 1, dtab.p,  \
-                                                                          doff.p, w_S.p);                 \
-    post_launch();                                                                                        \
+    synth<BB>(1);                                                                                         \
     fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, 1, (long)n, 0, 1}, -1);                               \
     fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, n, (long)n * n, 1, (long)n}, -1);                     \
     CK(cudaMemsetAsync(w_mm.p, 0, 2 * sizeof(unsigned long long), st));                                   \
@@ -1568,6 +1604,7 @@ void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C)
   CK(cudaMemcpyAsync(mm, w_mm.p, sizeof(mm), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(w, w_w.p, sizeof(w), cudaMemcpyDeviceToHost, st));
   sync();
+  check_status();
   if (scaled) {
     auto unpack = [](unsigned long long k, bool isMin) {
       uint32_t u = (uint32_t)(k >> 32);
@@ -1687,7 +1724,8 @@ int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **out) {
   *out = nullptr;
   const ettk_params &p = *params;
   if (!pow2(p.N) || p.N < 16 || p.N > 128 || !(p.B == 8 || p.B == 16 || p.B == 32 || p.B == 64) ||
-      p.mutual_correlation != 0 || p.candidate_peaks < 1 || p.number_of_candidates < 1)
+      p.mutual_correlation != 0 || p.candidate_peaks < 1 || p.number_of_candidates < 1 || p.wigner_precision < 0 ||
+      p.wigner_precision > WIG_FP64)
     return ETTK_ERR_ARG;
   ettk_ctx *c = new (std::nothrow) ettk_ctx;
   if (!c) return ETTK_ERR_OOM;
@@ -1723,6 +1761,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_peak.release();
   c->w_mm.release();
   c->doff.release();
+  c->dtab64.release();
   c->dirs.release();
   c->w_items.release();
   c->w_wv.release();

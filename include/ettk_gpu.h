@@ -53,6 +53,9 @@ typedef struct {
   int overlap_normalized;       /* nbfImageMetric::setToComputeOverlapNormalizedDistances */
   int mutual_correlation;       /* nbfImageMetric::setToUseMutualCorrelation (must be 0) */
   int max_batch;                /* pairs aligned per device batch (0 = automatic) */
+  int wigner_precision;         /* Wigner-d contraction of the SO(3) correlation (no reference setting; the
+                                   reference contracts in FP64): 0 FP32 (default, parity), 1 BF16 tensor cores,
+                                   2 split-BF16 tensor cores, 3 TF32 tensor cores, 4 FP64 (precision reference) */
 } ettk_params;
 
 /* Per-volume metadata: the columns of the reference's 33-column volume list

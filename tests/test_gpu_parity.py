@@ -57,6 +57,50 @@ def test_soft(metric32, scaled):
     assert np.unravel_index(g.argmax(), g.shape) == np.unravel_index(o.argmax(), o.shape)
 
 
+# Wigner-d contraction precision modes (wigner_precision): 1 BF16, 2 split-BF16, 3 TF32 tensor cores,
+# 4 FP64. Tolerances relative to the range of C: the 8 (BF16), 11 (TF32) and ~16 (split) mantissa bits of the
+# operands; split-BF16 and FP64 must also find the oracle's best cell.
+PRECISION_TOL = {1: 2e-2, 2: 1e-4, 3: 2e-3, 4: 1e-4}
+
+
+@pytest.mark.parametrize("B", [16, 64])
+@pytest.mark.parametrize("precision", [1, 2, 3, 4])
+def test_soft_precision(ds32, B, precision):
+    params = dict(ds32.params, B=B, wigner_precision=precision)
+    m = ProjectionRotationMetric3D(params)
+    try:
+        rng = np.random.default_rng(5 + B)
+        F1 = rng.random((2 * B, 2 * B)).astype(np.float32)
+        F2 = rng.random((2 * B, 2 * B)).astype(np.float32)
+        g = m.soft(F1, F2)
+    finally:
+        m.close()
+    o = pyoracle.soft(B, F1.astype(np.float64), F2.astype(np.float64))
+    rng_ = o.max() - o.min()
+    assert np.abs(g - o).max() <= PRECISION_TOL[precision] * rng_
+    gi = np.unravel_index(g.argmax(), g.shape)
+    if precision in (2, 4):
+        assert gi == np.unravel_index(o.argmax(), o.shape)
+    else:  # the cell found is a maximum of the oracle to within the tolerance
+        assert o.max() - o[gi] <= 2 * PRECISION_TOL[precision] * rng_
+
+
+def test_align_split_bf16_matches_fp32(ds32, metric32):
+    """Full alignments with the split-BF16 tensor-core contraction give the FP32 path's cells and shifts."""
+    n = len(ds32.meta)
+    idx = [(0, i) for i in range(n)]
+    D32 = metric32.getDistances(idx)
+    m = ProjectionRotationMetric3D(dict(ds32.params, wigner_precision=2))
+    try:
+        m.set_references([vol(ds32.references[0], ds32.ref_meta[0])])
+        m.set_particles([vol(ds32.particles[i], ds32.meta[i]) for i in range(n)])
+        Dtc = m.getDistances(idx)
+    finally:
+        m.close()
+    assert np.allclose(Dtc[:, 1:, :], D32[:, 1:, :], atol=1e-5)
+    assert np.allclose(Dtc[:, 0, :], D32[:, 0, :], rtol=1e-4, atol=0)
+
+
 def test_ccf(ds32, metric32):
     rng = np.random.default_rng(5)
     for p in range(3):
