@@ -6,6 +6,10 @@ soft_bw8.npz   SOFT 1.0's own bandwidth-8 test signals (external/soft-1.0/random
                computes it, and an S^2 rotation as ::harmonics does.
 align32_b16.npz  oracle alignments of the first particles of the 32^3 B=16 workload (a regression pin
                of the oracle itself), with a checksum of the generated particles.
+align128_b64.npz oracle alignments of the first two particles of the 128^3 B=64 workload (the large-size
+               path: (2N)^3 = 256^3 spherical projections, B=64 SO(3) correlations), with a checksum.
+
+Usage: python make_golden.py [soft|align32|align128 ...]   (no argument: all)
 """
 import hashlib
 import os
@@ -29,7 +33,24 @@ def read_s2(path):
     return v[0::2].reshape(16, 16)
 
 
-def main():
+def align_golden(name, n, out):
+    ds = synthetic.generate(name, n_particles=n)
+    dist, mats = [], []
+    for i in range(n):
+        o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
+        dist.append(o["distance"])
+        mats.append(o["matrix"])
+    np.savez_compressed(os.path.join(HERE, out), n=n, distance=np.array(dist), matrix=np.array(mats),
+                        particles_sha256=hashlib.sha256(ds.particles.tobytes()).hexdigest())
+
+
+def main(which):
+    if "align32" in which:
+        align_golden("align32_b16", 4, "align32_b16.npz")
+    if "align128" in which:
+        align_golden("align128_b64", 2, "align128_b64.npz")
+    if "soft" not in which:
+        return
     R = pyoracle.ref_lib()
     if R is None:
         raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
@@ -44,16 +65,6 @@ def main():
     R.ref_rotate(B, np.ascontiguousarray(sig), *angles, Rr)
     np.savez_compressed(os.path.join(HERE, "soft_bw8.npz"), sig=sig, pat=pat, C=C, R=Rr, angles=angles)
 
-    n = 4
-    ds = synthetic.generate("align32_b16", n_particles=n)
-    dist, mats = [], []
-    for i in range(n):
-        o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
-        dist.append(o["distance"])
-        mats.append(o["matrix"])
-    np.savez_compressed(os.path.join(HERE, "align32_b16.npz"), n=n, distance=np.array(dist), matrix=np.array(mats),
-                        particles_sha256=hashlib.sha256(ds.particles.tobytes()).hexdigest())
-
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or ["soft", "align32", "align128"])

@@ -144,6 +144,36 @@ def test_align_pairs_64(ds64):
     m.close()
 
 
+def test_align_pairs_128_golden():
+    """The large shape (128^3, B=64: 256^3 spherical projections, the strided (x, y) passes of 2N = 256, TMA
+    boxes inside 128^3 volumes) against the oracle's alignments frozen in tests/golden/align128_b64.npz
+    (computed afresh where this machine generates different particles)."""
+    import hashlib
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "align128_b64.npz"))
+    n = int(g["n"])
+    ds = synthetic.generate("align128_b64", n_particles=n)
+    if hashlib.sha256(ds.particles.tobytes()).hexdigest() == str(g["particles_sha256"]):
+        ref = [(g["distance"][i], g["matrix"][i]) for i in range(n)]
+    else:  # this machine's libm generated different particles (last-ulp exp): run the oracle here instead
+        ref = []
+        for i in range(n):
+            o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
+            ref.append((o["distance"], o["matrix"]))
+    m = ProjectionRotationMetric3D(ds.params)
+    try:
+        m.set_references([vol(ds.references[0], ds.ref_meta[0])])
+        m.set_particles([vol(ds.particles[i], ds.meta[i]) for i in range(n)])
+        D = m.getDistances([(0, i) for i in range(n)])
+    finally:
+        m.close()
+    for i, (dist, mat) in enumerate(ref):
+        T = D[i, 1:17, 0].reshape(4, 4)
+        assert abs(D[i, 0, 0] - dist) <= 1e-4 * abs(dist)
+        assert np.allclose(T[:3, :3], mat[:3, :3], atol=1e-5)
+        assert np.allclose(T[:3, 3], mat[:3, 3], atol=1e-4)
+
+
 def test_class_average(ds32, metric32):
     """Wedge-weighted class average (getImageMPI + getImage) against the oracle: 1e-5 relative RMS."""
     members = [0, 1, 2, 3, 4]
