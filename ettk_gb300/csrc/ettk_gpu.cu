@@ -17,6 +17,7 @@
 #include "fft_reg.cuh"
 #include "fft2d.cuh"
 #include "wigner_tc.cuh"
+#include "refine.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -672,6 +673,16 @@ struct ettk_ctx {
   }
   void align(int npairs, const int *pairs, float *D, int cols, int ncand);
   void soft_diag(const float *F1, const float *F2, int scaled, float *C);
+
+  // ---------------------------------------------------------------- continuous pose refinement
+  DevBuf<float> rf_fw, rf_y1, rf_a;  // per pair: wedge * filter (kz-major half), filtered reference; adjoint field
+  DevBuf<int> rf_pair;                // evaluation -> pair
+  DevBuf<double> rf_acc;              // [E][4] correlation sums, then [E][16] gradient sums
+  std::vector<int> rf_part;           // pair -> particle
+  void refine_setup(const std::vector<EvalReq> &req);
+  void refine_eval(const std::vector<std::array<double, 12>> &maps, const std::vector<int> &pair, bool grad,
+                   std::vector<double> &rho, std::vector<double> &g6);
+  void refine(const std::vector<EvalReq> &req, int iterations, std::vector<Mat4> &out, std::vector<double> &rho);
   void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
 };
 
@@ -744,12 +755,199 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
   check_status();
 }
 
+// ---------------------------------------------------------------- continuous pose refinement
+
+// Per pair at its starting pose T0: fw = W1 * W2(T0) * filter (as the CCF evaluation builds it) and the
+// reference filtered by fw, y1 = C2R(FI1 * fw) (scale irrelevant to the normalised correlation).
+void ettk_ctx::refine_setup(const std::vector<EvalReq> &req) {
+  const long P = (long)req.size();
+  const int ACC = 8;
+  w_wv.ensure(P);
+  w_idx.ensure(P);
+  w_fw.ensure(P * h3);
+  w_cA.ensure(P * h3);
+  w_acc.ensure(P * ACC);
+  rf_fw.ensure(P * h3);
+  rf_y1.ensure(P * n3);
+  std::vector<WedgeVecs> wv(P);
+  std::vector<int> refidx(P);
+  rf_part.resize(P);
+  for (long e = 0; e < P; ++e) {
+    const VolumeGeom &g = partg[req[e].part];
+    WedgeVecs w{};
+    w.full = g.full_wedge() ? 1 : 0;
+    if (!w.full) wedge_vectors(g, &req[e].t, w.v1, w.v2);
+    wv[e] = w;
+    refidx[e] = req[e].ref;
+    rf_part[e] = req[e].part;
+  }
+  CK(cudaMemcpyAsync(w_wv.p, wv.data(), P * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_idx.p, refidx.data(), P * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, P * ACC * sizeof(double), st));
+  if (p.wedge_compensation) {
+    with_n(N, [&](auto nn) { wedge_t<decltype(nn)::value>(P, w_acc.p, ACC); });
+  } else {
+    for (long e = 0; e < P; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  CK(cudaMemcpyAsync(rf_fw.p, w_fw.p, P * h3 * 4, cudaMemcpyDeviceToDevice, st));
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, rf_fw.p, w_cA.p, HalfSums<NN>{w_acc.p, ACC, 2}}, P, "refine", 20.0);
+  });
+  c2r_z(N, w_cA.p, PostStore{rf_y1.p, N}, P * N * N);
+}
+
+// rho (and with grad, its gradient w.r.t. the right perturbation (w, d) at each map) of E evaluations;
+// maps[e] = index map (origin, axes), pair[e] = the refine_setup pair it belongs to.
+void ettk_ctx::refine_eval(const std::vector<std::array<double, 12>> &maps, const std::vector<int> &pair, bool grad,
+                           std::vector<double> &rho, std::vector<double> &g6) {
+  const long E = (long)maps.size();
+  w_items.ensure(E);
+  w_v.ensure(E * n3);
+  w_r.ensure(E * n3);
+  w_cB.ensure(E * h3);
+  w_acc.ensure(E * 2);
+  rf_pair.ensure(E);
+  rf_acc.ensure(E * 20);
+  if (grad) rf_a.ensure(E * n3);
+  std::vector<ResliceItem> items(E);
+  for (long e = 0; e < E; ++e) {
+    const int part = rf_part[pair[e]];
+    ResliceItem it;
+    it.vol = partptr + (long)part * n3;
+    it.tmap = part_map(part);
+    it.dims[0] = it.dims[1] = it.dims[2] = N;
+    set_map(it, maps[e].data());
+    items[e] = it;
+  }
+  CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(rf_pair.p, pair.data(), E * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, E * 2 * sizeof(double), st));
+  CK(cudaMemsetAsync(rf_acc.p, 0, E * 20 * sizeof(double), st));
+  {
+    Scope sc(this, "reslice", 8.0 * E * n3);
+    // clamped values everywhere: rho stays smooth when a shift moves the window past the fixed image's edge
+    k_reslice_brick<false, true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(
+        w_items.p, N, w_v.p, w_acc.p, 2, status.p);
+    post_launch();
+  }
+  // g = K u, u = valid (r - mean) maskfft shift
+  auto filtered = [&](auto pre) {
+    r2c_z(N, pre, w_cB.p, E * N * N);
+    with_n(N, [&](auto nn) {
+      constexpr int NN = decltype(nn)::value;
+      fft2d_t<NN>(OpFwdFilterIdx<NN>{w_cB.p, rf_fw.p, rf_pair.p}, E, "refine", 20.0);
+    });
+    xy_kxy(N, w_cB.p, E, +1);
+    c2r_z(N, w_cB.p, PostStore{w_r.p, N}, E * N * N);
+  };
+  const dim3 gn(nblocks<int>(n3, 256, 64), E);
+  CK(cudaMemsetAsync(w_acc.p, 0, E * 2 * sizeof(double), st));
+  k_masked_mean<<<gn, 256, 0, st>>>(w_v.p, mask.p, (int)n3, w_acc.p);  // window: the spherical mask m1
+  post_launch();
+  filtered(PreMaskedParticle{w_v.p, mask.p, w_acc.p, N});
+  k_ncc_sums<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, mask.p, (int)n3, rf_acc.p);
+  post_launch();
+  if (grad) {
+    k_ncc_adjoint<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, mask.p, (int)n3, rf_acc.p, rf_a.p);
+    post_launch();
+    filtered(PreCopy{rf_a.p, N});  // K a into w_r
+    Scope sc(this, "refine_grad", 8.0 * E * n3);
+    k_reslice_grad<<<dim3(nblocks<int>(n3, 256, 64), E), 256, 0, st>>>(w_items.p, N, w_v.p, w_r.p, mask.p,
+                                                                        rf_acc.p + E * 4);
+    post_launch();
+  }
+  std::vector<double> h(E * 20);
+  read_back(h.data(), rf_acc.p, E * 20 * sizeof(double));
+  check_status();
+  rho.assign(E, 0.0);
+  if (grad) g6.assign(E * 6, 0.0);
+  for (long e = 0; e < E; ++e) {
+    const double syg = h[e * 4], sgg = h[e * 4 + 1], syy = h[e * 4 + 2];
+    rho[e] = (sgg > 0 && syy > 0) ? syg / sqrt(sgg * syy) : 0.0;
+    if (grad) {
+      const double *a = h.data() + E * 4 + e * 16;
+      const double dbar = a[13] > 0 ? a[12] / a[13] : 0.0;
+      for (int k = 0; k < 3; ++k) {
+        g6[e * 6 + k] = a[3 + k] - dbar * a[9 + k];      // d rho / d w (radians)
+        g6[e * 6 + 3 + k] = a[k] - dbar * a[6 + k];      // d rho / d d (voxels)
+      }
+    }
+  }
+}
+
+// Gradient ascent of rho from each request's pose: per iteration one gradient and a three-step line search
+// along the gradient in voxel units (rotation scaled by the mask radius), accepting only improvements.
+void ettk_ctx::refine(const std::vector<EvalReq> &req, int iterations, std::vector<Mat4> &out,
+                      std::vector<double> &rho_out) {
+  const long P = (long)req.size();
+  refine_setup(req);
+  std::vector<std::array<double, 12>> cur(P);
+  for (long i = 0; i < P; ++i) reslice_index(partg[req[i].part], N, &req[i].t, cur[i].data());
+  std::vector<int> self(P);
+  for (long i = 0; i < P; ++i) self[i] = (int)i;
+  const double Rg = 0.6 * (p.mask_radius > 0 ? p.mask_radius : 0.5 * N);
+  std::vector<double> alpha(P, 0.5), rho, g6, rt;
+  std::vector<char> done(P, 0);
+  for (int it = 0; it < iterations; ++it) {
+    refine_eval(cur, self, true, rho, g6);
+    std::vector<std::array<double, 12>> trial;
+    std::vector<int> tp, tpair;
+    const double fac[3] = {0.5, 1.0, 2.0};
+    for (long i = 0; i < P; ++i) {
+      if (done[i]) continue;
+      const double *g = &g6[i * 6];
+      const double gu[6] = {g[0] / Rg, g[1] / Rg, g[2] / Rg, g[3], g[4], g[5]};
+      double nrm = 0;
+      for (double v : gu) nrm += v * v;
+      nrm = sqrt(nrm);
+      if (!(nrm > 0)) {
+        done[i] = 1;
+        continue;
+      }
+      for (double f : fac) {
+        const double t = alpha[i] * f;
+        const double w[3] = {gu[0] / nrm * t / Rg, gu[1] / nrm * t / Rg, gu[2] / nrm * t / Rg};
+        const double d[3] = {gu[3] / nrm * t, gu[4] / nrm * t, gu[5] / nrm * t};
+        std::array<double, 12> m;
+        perturb_index(cur[i].data(), N, w, d, m.data());
+        trial.push_back(m);
+        tp.push_back((int)i);
+      }
+    }
+    if (trial.empty()) break;
+    refine_eval(trial, tp, false, rt, g6);
+    for (size_t k = 0; k < trial.size(); k += 3) {
+      const int i = tp[k];
+      int best = -1;
+      double bv = rho[i];
+      for (int q = 0; q < 3; ++q)
+        if (rt[k + q] > bv) {
+          bv = rt[k + q];
+          best = q;
+        }
+      if (best >= 0) {
+        cur[i] = trial[k + best];
+        alpha[i] = std::min(2.0, std::max(1e-3, alpha[i] * fac[best]));
+      } else {
+        alpha[i] *= 0.25;
+        if (alpha[i] < 1e-3) done[i] = 1;
+      }
+    }
+  }
+  refine_eval(cur, self, false, rho_out, g6);
+  out.resize(P);
+  for (long i = 0; i < P; ++i) out[i] = pose_from_index(partg[req[i].part], N, cur[i].data());
+}
+
 void ettk_ctx::init_tables() {
   status.ensure(1);
   CK(cudaMemset(status.p, 0, sizeof(int)));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  CK(cudaFuncSetAttribute(k_reslice_brick<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_reslice_brick<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   N = p.N;
   H = N / 2 + 1;
@@ -1762,6 +1960,11 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_mm.release();
   c->doff.release();
   c->dtab64.release();
+  c->rf_fw.release();
+  c->rf_y1.release();
+  c->rf_a.release();
+  c->rf_pair.release();
+  c->rf_acc.release();
   c->dirs.release();
   c->w_items.release();
   c->w_wv.release();
@@ -1897,6 +2100,61 @@ int ettk_gpu_ccf(ettk_ctx *c, int r, int p, double *t, float *dist) {
     c->eval_batch({q}, res);
     *dist = res[0].dist;
     memcpy(t, res[0].t.e, sizeof(res[0].t.e));
+  });
+}
+
+int ettk_gpu_refine_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, int cols, int ncand, int iterations) {
+  if (!c || npairs < 0 || (npairs && (!pairs || !D)) || cols < 17 || ncand < 1 || iterations < 0)
+    return fail(c, ETTK_ERR_ARG, "invalid refine arguments");
+  return guarded(c, [&] {
+    const int maxb = 256;
+    for (int b0 = 0; b0 < npairs; b0 += maxb) {
+      const int P = std::min(maxb, npairs - b0);
+      std::vector<EvalReq> req(P);
+      for (int i = 0; i < P; ++i) {
+        const int r = pairs[2 * (b0 + i)], q = pairs[2 * (b0 + i) + 1];
+        if (r < 0 || r >= c->R || q < 0 || q >= c->V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+        const float *row = D + (long)(b0 + i) * cols * ncand;
+        if (row[0] == -1.f) throw CudaError(ETTK_ERR_STATE, "refine needs aligned rows (distance -1 found)");
+        req[i].ref = r;
+        req[i].part = q;
+        for (int k = 0; k < 16; ++k) req[i].t.e[k] = row[(1 + k) * ncand];
+      }
+      std::vector<Mat4> out;
+      std::vector<double> rho;
+      c->refine(req, iterations, out, rho);
+      for (int i = 0; i < P; ++i) {
+        float *row = D + (long)(b0 + i) * cols * ncand;
+        row[0] = (float)(1.0 - rho[i]);
+        for (int k = 0; k < 16; ++k) row[(1 + k) * ncand] = (float)out[i].e[k];
+      }
+    }
+  });
+}
+
+int ettk_gpu_refine_objective(ettk_ctx *c, int npairs, const int *pairs, const double *poses, const double *theta,
+                              double *rho, double *grad) {
+  if (!c || npairs <= 0 || !pairs || !poses || !theta || !rho) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] {
+    std::vector<EvalReq> req(npairs);
+    std::vector<std::array<double, 12>> maps(npairs);
+    std::vector<int> self(npairs);
+    for (int i = 0; i < npairs; ++i) {
+      const int r = pairs[2 * i], q = pairs[2 * i + 1];
+      if (r < 0 || r >= c->R || q < 0 || q >= c->V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+      req[i].ref = r;
+      req[i].part = q;
+      memcpy(req[i].t.e, poses + 16 * (long)i, sizeof(req[i].t.e));
+      double m0[12];
+      reslice_index(c->partg[q], c->N, &req[i].t, m0);
+      perturb_index(m0, c->N, theta + 6 * (long)i, theta + 6 * (long)i + 3, maps[i].data());
+      self[i] = i;
+    }
+    c->refine_setup(req);
+    std::vector<double> r, g;
+    c->refine_eval(maps, self, grad != nullptr, r, g);
+    for (int i = 0; i < npairs; ++i) rho[i] = r[i];
+    if (grad) memcpy(grad, g.data(), 6 * (size_t)npairs * sizeof(double));
   });
 }
 

@@ -161,6 +161,52 @@ inline void reslice_index(const VolumeGeom &g, int N, const Mat4 *t, double out1
   }
 }
 
+// Inverse of reslice_index: the transform t whose index matrix is out12 (origin, x/y/z axis columns).
+inline Mat4 pose_from_index(const VolumeGeom &g, int N, const double out12[12]) {
+  Mat4 idx = Mat4::eye();
+  for (int i = 0; i < 3; ++i) {
+    idx.e[4 * i + 3] = out12[i];
+    idx.e[4 * i + 0] = out12[3 + i];
+    idx.e[4 * i + 1] = out12[6 + i];
+    idx.e[4 * i + 2] = out12[9 + i];
+  }
+  Mat4 inM = Mat4::eye(), outM = Mat4::eye();
+  double oo[3] = {-(double)(float)N / 2.0, -(double)(float)N / 2.0, -(double)(float)N / 2.0 - g.cut_offset};
+  for (int i = 0; i < 3; ++i) {
+    inM.e[4 * i + 3] = -(double)g.position[i];  // inverses of the two translations
+    outM.e[4 * i + 3] = -oo[i];
+  }
+  Mat4 fin = mul(mul(inM, idx), outM), li;
+  if (!invert(g.local(), li)) li = Mat4::eye();
+  return mul(li, fin);
+}
+
+// Index map perturbed on the right by a rotation exp([w]x) about the box centre c = (N/2, N/2, N/2) and a shift d
+// of the output grid: p'(x) = M (exp([w]x)(x - c) + c + d) + o, with M the axis columns of out12.
+inline void perturb_index(const double in12[12], int N, const double w[3], const double d[3], double out12[12]) {
+  const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (th > 0) {  // Rodrigues
+    const double k[3] = {w[0] / th, w[1] / th, w[2] / th}, s = sin(th), c1 = 1 - cos(th);
+    const double K[9] = {0, -k[2], k[1], k[2], 0, -k[0], -k[1], k[0], 0};
+    double K2[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) K2[3 * i + j] = K[3 * i] * K[j] + K[3 * i + 1] * K[3 + j] + K[3 * i + 2] * K[6 + j];
+    for (int i = 0; i < 9; ++i) R[i] += s * K[i] + c1 * K2[i];
+  }
+  const double c = 0.5 * N;
+  double M[9];  // M[3*i + col]
+  for (int col = 0; col < 3; ++col)
+    for (int i = 0; i < 3; ++i) M[3 * i + col] = in12[3 + 3 * col + i];
+  double t[3];  // c - R c + d
+  for (int i = 0; i < 3; ++i) t[i] = c - (R[3 * i] + R[3 * i + 1] + R[3 * i + 2]) * c + d[i];
+  for (int i = 0; i < 3; ++i) {
+    out12[i] = in12[i] + M[3 * i] * t[0] + M[3 * i + 1] * t[1] + M[3 * i + 2] * t[2];
+    for (int col = 0; col < 3; ++col)
+      out12[3 + 3 * col + i] = M[3 * i] * R[col] + M[3 * i + 1] * R[3 + col] + M[3 * i + 2] * R[6 + col];
+  }
+}
+
 // Plane normals of the wedge rotated by inv(Euler*matrix*t) (nbfWedgedSubImage3D::getWedgeImageHalf).
 inline void wedge_vectors(const VolumeGeom &g, const Mat4 *t, double v1[3], double v2[3]) {
   double n1[3], n2[3];

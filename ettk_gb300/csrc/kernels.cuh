@@ -62,7 +62,8 @@ static __device__ __noinline__ float tricubic_global(const float *__restrict__ v
 // PRECISE: the voxel coordinate follows the reference's FP64 sequence ((origin + c*z) + b*y) + a*x
 // without FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5 output parity
 // matters); otherwise the same sequence runs in FP32.
-template <bool PRECISE>
+// CLAMP_ALL: every voxel takes the clamped tricubic value (no -max background), for the continuous refinement.
+template <bool PRECISE, bool CLAMP_ALL = false>
 __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
                                                           float *__restrict__ out, double *acc, int acc_stride,
                                                           int *status) {
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
         w = __dadd_rn(w, __dmul_rn((double)b, it.md[6 + t]));
         q[t] = __dadd_rn(w, __dmul_rn((double)a, it.md[3 + t]));
       }
-      inside = !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 || q[2] > dz - 0.5);
+      inside = CLAMP_ALL || !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 || q[2] > dz - 0.5);
       const long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0),
                       r2 = __double2ll_rn(q[2] * 65536.0);
       ix = (int)(r0 >> 16);
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
       p0 = p0 + a * it.m[3];
       p1 = p1 + a * it.m[4];
       p2 = p2 + a * it.m[5];
-      inside = !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
+      inside = CLAMP_ALL || !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
       ix = vtk_floor(p0, fx);
       iy = vtk_floor(p1, fy);
       iz = vtk_floor(p2, fz);

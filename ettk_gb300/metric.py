@@ -136,6 +136,30 @@ class ProjectionRotationMetric3D:
                                             out.ctypes.data), "average")
         return out
 
+    # -- continuous pose refinement (no counterpart in the reference) ---------------------------
+    def refine(self, indexes, D, iterations=12):
+        """Refines candidate 0 of the rows of D (as getDistances returned them) in place by gradient ascent of
+        the wedge-constrained normalised correlation; distance becomes 1 - rho. Returns D."""
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        assert D.dtype == np.float32 and D.flags.c_contiguous and D.shape[0] == idx.shape[0]
+        self._check(self.L.ettk_gpu_refine_pairs(self._ctx, idx.shape[0], idx.ctypes.data, D.ctypes.data, D.shape[1],
+                                                 D.shape[2], int(iterations)), "refine_pairs")
+        return D
+
+    def refine_objective(self, indexes, poses, theta, grad=True):
+        """rho (and d rho / d(w, d)) at poses (n x 4 x 4) perturbed by theta (n x 6: rotation vector in
+        radians about the box centre, then shift in voxels)."""
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        n = idx.shape[0]
+        T = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(n, 16))
+        th = np.ascontiguousarray(np.asarray(theta, np.float64).reshape(n, 6))
+        rho = np.zeros(n)
+        g = np.zeros((n, 6)) if grad else None
+        self._check(self.L.ettk_gpu_refine_objective(self._ctx, n, idx.ctypes.data, T.ctypes.data, th.ctypes.data,
+                                                     rho.ctypes.data, g.ctypes.data if grad else None),
+                    "refine_objective")
+        return (rho, g) if grad else rho
+
     # -- diagnostics ---------------------------------------------------------------------------
     def ccf(self, r, p, T):
         t = np.ascontiguousarray(np.asarray(T, np.float64).reshape(16)).copy()

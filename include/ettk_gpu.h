@@ -98,6 +98,21 @@ int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, 
 int ettk_gpu_average(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
                      float *avg);
 
+/* Continuous 6-DOF refinement of aligned pairs (no counterpart in the reference, whose refine() runs a
+   Powell search over RotateX/Y/Z offsets with one CCF per step, inc/em/nbfFourierImageMetric.h:1701-1809):
+   from the pose of candidate 0 of each row of D (as ettk_gpu_align_pairs wrote it), gradient ascent of the
+   masked normalised correlation between the wedge*filter-constrained reference and particle, with the
+   gradient from the hand-written adjoint of reslice -> R2C -> filter -> C2R (rotation about the box centre
+   and shift, continuous). Writes the refined 4x4 pose and distance 1 - rho into the row. */
+int ettk_gpu_refine_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
+                          int iterations);
+
+/* The refinement objective and its gradient (for checks): for pair i at pose T = poses[16 i..] perturbed by
+   theta[6 i..] = (rotation vector w in radians about the box centre, shift d in voxels) of the output grid,
+   rho[i] and, when grad is non-null, grad[6 i..] = d rho / d(w, d) at that perturbed pose. */
+int ettk_gpu_refine_objective(ettk_ctx *ctx, int npairs, const int *pairs, const double *poses,
+                              const double *theta, double *rho, double *grad);
+
 /* Diagnostics (staged parity checks; no counterpart in the reference API):
  * one executeFourierNewHalf call (inc/em/nbfFourierImageMetric.h:1077-1323) of particle p against
  * reference r at transform t (updated in place with the found shift); returns the distance in *dist. */

@@ -925,6 +925,101 @@ float oracle_ccf(const OracleParams *P, const OracleVolume *ref, const OracleVol
   return d;
 }
 
+/* Objective of the continuous pose refinement (no counterpart in the reference; the GPU's refine.cuh states
+ * it), restated in FP64 for its gradient check: the particle resliced by the index map of t perturbed on the
+ * right by exp([w]x) about the box centre and the shift d (theta = w[3], d[3]), clamped tricubic everywhere;
+ * u = (r - mu) m1 shift with mu = sum(m1 r) / sum(m1); g = C2R(R2C(u) fw), y1 = C2R(R2C(I1 maskfft shift) fw)
+ * with fw = wedge1 * wedge2(t) * filter and the DC zeroed (executeFourierNewHalf's I1 branch); returns
+ * rho = sum(m1 y1 g) / sqrt(sum(m1 y1^2) sum(m1 g^2)). */
+double oracle_refine_objective(const OracleParams *P, const OracleVolume *ref, const OracleVolume *part,
+                               const double *t16, const double *theta) {
+  CCF ccf(*P, *ref, *part);
+  const int N = P->N, H = N / 2 + 1;
+  const long n3 = (long)N * N * N, h3 = (long)N * N * H;
+  M4 t;
+  memcpy(t.e, t16, sizeof(t.e));
+  std::vector<double> fw(h3);
+  {
+    std::vector<float> w2;
+    if (P->wedge_compensation) wedge_half(*part, N, &t, w2);
+    for (long i = 0; i < h3; ++i) fw[i] = P->wedge_compensation ? (double)(ccf.filter[i] * (w2[i] * ccf.wedge1[i]))
+                                                                 : (double)ccf.filter[i];
+    fw[((long)(N / 2) * N + N / 2) * H + (H - 1)] = 0;
+  }
+  auto shift = [&](long id) {
+    const int i = (int)(id / ((long)N * N)), j = (int)((id / N) % N), k = (int)(id % N);
+    return ((i + j + k) % 2) ? -1.0 : 1.0;
+  };
+  auto filt = [&](std::vector<double> &R) {
+    std::vector<cplx> F(h3);
+    rfft3d(R.data(), F.data(), N, N, N);
+    for (long i = 0; i < h3; ++i) F[i] *= fw[i];
+    irfft3d(F.data(), R.data(), N, N, N);
+  };
+  std::vector<double> y1(n3), g(n3);
+  for (long id = 0; id < n3; ++id) y1[id] = ccf.I1[id] * (double)ccf.maskfft[id] * shift(id);
+  filt(y1);
+  /* index map of t (reslice_index), perturbed */
+  M4 local = local_matrix(*part), fin;
+  m4_mul(local.e, t.e, fin.e);
+  if (m4_det(fin.e) == 0) fin = m4_identity();
+  double inM[16], outM[16], tmp[16], idx[16];
+  for (int i = 0; i < 16; ++i) inM[i] = outM[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  for (int i = 0; i < 3; ++i) {
+    inM[4 * i + 3] = (double)part->position[i];
+    outM[4 * i + 3] = -(double)(float)N / 2.0 - (i == 2 ? part->cut_offset : 0.0);
+  }
+  m4_mul(inM, fin.e, tmp);
+  m4_mul(tmp, outM, idx);
+  const double *w = theta, *d = theta + 3;
+  const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (th > 0) {
+    const double k[3] = {w[0] / th, w[1] / th, w[2] / th}, sn = sin(th), c1 = 1 - cos(th);
+    const double K[9] = {0, -k[2], k[1], k[2], 0, -k[0], -k[1], k[0], 0};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double k2 = 0;
+        for (int q = 0; q < 3; ++q) k2 += K[3 * i + q] * K[3 * q + j];
+        R[3 * i + j] += sn * K[3 * i + j] + c1 * k2;
+      }
+  }
+  const double c = 0.5 * N;
+  double M[9], o[3], Mp[9], op[3], tv[3];
+  for (int i = 0; i < 3; ++i) {
+    o[i] = idx[4 * i + 3];
+    for (int col = 0; col < 3; ++col) M[3 * i + col] = idx[4 * i + col];
+  }
+  for (int i = 0; i < 3; ++i) tv[i] = c - (R[3 * i] + R[3 * i + 1] + R[3 * i + 2]) * c + d[i];
+  for (int i = 0; i < 3; ++i) {
+    op[i] = o[i] + M[3 * i] * tv[0] + M[3 * i + 1] * tv[1] + M[3 * i + 2] * tv[2];
+    for (int col = 0; col < 3; ++col) Mp[3 * i + col] = M[3 * i] * R[col] + M[3 * i + 1] * R[3 + col] + M[3 * i + 2] * R[6 + col];
+  }
+  std::vector<double> r(n3);
+  double sw = 0, swr = 0;
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b)
+      for (int cz = 0; cz < N; ++cz) {
+        double p[3];
+        for (int i = 0; i < 3; ++i) p[i] = ((op[i] + cz * Mp[3 * i + 2]) + b * Mp[3 * i + 1]) + a * Mp[3 * i];
+        const long id = ((long)a * N + b) * N + cz;
+        r[id] = vtk_tricubic_float(part->data, part->dims, p, false);
+        sw += ccf.mask[id];
+        swr += ccf.mask[id] * r[id];
+      }
+  const double mu = sw > 0 ? swr / sw : 0.0;
+  for (long id = 0; id < n3; ++id) g[id] = (r[id] - mu) * (double)ccf.mask[id] * shift(id);
+  filt(g);
+  double syg = 0, sgg = 0, syy = 0;
+  for (long id = 0; id < n3; ++id) {
+    const double m = ccf.mask[id];
+    syg += m * y1[id] * g[id];
+    sgg += m * g[id] * g[id];
+    syy += m * y1[id] * y1[id];
+  }
+  return (sgg > 0 && syy > 0) ? syg / sqrt(sgg * syy) : 0.0;
+}
+
 /* Class average of M members (volumes + metadata, weights, 4x4 alignment matrices); out [x][y][z]. */
 int oracle_average(const OracleParams *P, int M, const OracleVolume *vols, const float *weights, const double *mats,
                    double *out) {

@@ -82,6 +82,8 @@ def lib():
         L.oracle_sht.argtypes = [ctypes.c_int, dp, dp]
         L.oracle_ccf.argtypes = [P, V, V, dp]
         L.oracle_ccf.restype = ctypes.c_float
+        L.oracle_refine_objective.argtypes = [P, V, V, dp, dp]
+        L.oracle_refine_objective.restype = ctypes.c_double
         L.oracle_average.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
@@ -140,6 +142,17 @@ def ccf(params, ref, ref_meta, part, part_meta, T):
     t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16)).copy()
     d = lib().oracle_ccf(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t)
     return float(d), t.reshape(4, 4)
+
+
+def refine_objective(params, ref, ref_meta, part, part_meta, T, theta):
+    """FP64 objective of the continuous refinement at pose T perturbed by theta (rotation vector in radians
+    about the box centre, then shift in voxels)."""
+    P = make_params(params)
+    r = make_volume(ref, ref_meta)
+    q = make_volume(part, part_meta)
+    t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16))
+    th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(6))
+    return float(lib().oracle_refine_objective(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t, th))
 
 
 def get_image(params, vol, meta, T=None):
