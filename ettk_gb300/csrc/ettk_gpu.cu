@@ -2132,6 +2132,70 @@ int ettk_gpu_refine_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, i
   });
 }
 
+int ettk_gpu_classify(ettk_ctx *c, int iterations, int *labels, float *refs_out, float *dist_out) {
+  if (!c || iterations < 1 || !labels) return fail(c, ETTK_ERR_ARG, "invalid classify arguments");
+  if (c->R < 1 || c->V < 1) return fail(c, ETTK_ERR_STATE, "set references and particles first");
+  const int R = c->R, V = c->V, N = c->N;
+  const long n3 = c->n3;
+  const int cols = 17;
+  std::vector<int> pairs(2L * R * V);
+  for (int v = 0; v < V; ++v)
+    for (int r = 0; r < R; ++r) {
+      pairs[2L * (v * R + r)] = r;
+      pairs[2L * (v * R + r) + 1] = v;
+    }
+  std::vector<float> D((size_t)R * V * cols), avg((size_t)R * n3);
+  std::vector<ettk_volume_meta> meta(R);
+  for (auto &m : meta) {  // class averages: no wedge, identity pose, centred
+    m = ettk_volume_meta{};
+    m.lwedge = -90.f;
+    m.uwedge = 90.f;
+    for (int i = 0; i < 16; ++i) m.matrix[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    for (int i = 0; i < 3; ++i) m.position[i] = 0.5f * (float)N;
+  }
+  for (int it = 0; it < iterations; ++it) {
+    // 1. every particle against every class reference (getDistances, src/MPI_Classification.cpp:1087)
+    std::fill(D.begin(), D.end(), -1.f);
+    int rc = ettk_gpu_align_pairs(c, R * V, pairs.data(), D.data(), cols, 1);
+    if (rc != ETTK_OK) return rc;
+    // 2. each particle to its closest class (ties: the lower class index)
+    for (int v = 0; v < V; ++v) {
+      int best = 0;
+      for (int r = 1; r < R; ++r)
+        if (D[(size_t)(v * R + r) * cols] < D[(size_t)(v * R + best) * cols]) best = r;
+      labels[v] = best;
+      if (dist_out) dist_out[v] = D[(size_t)(v * R + best) * cols];
+    }
+    // 3. wedge-weighted average of each class under its members' alignments (getImageMPI + getImage)
+    for (int r = 0; r < R; ++r) {
+      std::vector<int> mem;
+      std::vector<float> w;
+      std::vector<double> mats;
+      for (int v = 0; v < V; ++v)
+        if (labels[v] == r) {
+          mem.push_back(v);
+          w.push_back(1.f);
+          const float *row = &D[(size_t)(v * R + r) * cols];
+          for (int k = 0; k < 16; ++k) mats.push_back(row[1 + k]);
+        }
+      if (mem.empty()) {  // an empty class keeps its reference
+        rc = guarded(c, [&] {
+          CK(cudaMemcpy(avg.data() + (size_t)r * n3, c->refvol.p + (size_t)r * n3, n3 * 4, cudaMemcpyDeviceToHost));
+        });
+        if (rc != ETTK_OK) return rc;
+        continue;
+      }
+      rc = ettk_gpu_average(c, (int)mem.size(), mem.data(), w.data(), mats.data(), avg.data() + (size_t)r * n3);
+      if (rc != ETTK_OK) return rc;
+    }
+    // 4. the averages become the references of the next pass
+    rc = ettk_gpu_set_references(c, R, avg.data(), meta.data());
+    if (rc != ETTK_OK) return rc;
+  }
+  if (refs_out) memcpy(refs_out, avg.data(), (size_t)R * n3 * sizeof(float));
+  return ETTK_OK;
+}
+
 int ettk_gpu_refine_objective(ettk_ctx *c, int npairs, const int *pairs, const double *poses, const double *theta,
                               double *rho, double *grad) {
   if (!c || npairs <= 0 || !pairs || !poses || !theta || !rho) return fail(c, ETTK_ERR_ARG, "invalid arguments");

@@ -136,6 +136,21 @@ class ProjectionRotationMetric3D:
                                             out.ctypes.data), "average")
         return out
 
+    # -- multireference classification (src/MPI_Classification.cpp align -> assign -> re-average) -----
+    def classify(self, iterations):
+        """Runs `iterations` passes of align all particles x references -> assign to the closest class ->
+        wedge-weighted class averages as the new references. Returns (labels, references [R][z][y][x],
+        distances)."""
+        V = len(self._parts)
+        R = len(self._refs)
+        N = self.params["N"]
+        labels = np.zeros(V, np.int32)
+        refs = np.zeros((R, N, N, N), np.float32)
+        dist = np.zeros(V, np.float32)
+        self._check(self.L.ettk_gpu_classify(self._ctx, int(iterations), labels.ctypes.data, refs.ctypes.data,
+                                             dist.ctypes.data), "classify")
+        return labels, refs, dist
+
     # -- continuous pose refinement (no counterpart in the reference) ---------------------------
     def refine(self, indexes, D, iterations=12):
         """Refines candidate 0 of the rows of D (as getDistances returned them) in place by gradient ascent of

@@ -60,6 +60,9 @@ WORKLOADS = {
     # 64^3, 10 references with 30% shared blobs
     "mra64_b32": Workload("mra64_b32", 2, 64, 32, 8000, 40, (3.0, 6.0), 20.0, (0.5, 1.0), 8, 0.05,
                           (45.0, 70.0), True, 10.0, n_refs=10, shared_fraction=0.3),
+    # 32^3, 3 references with 30% shared blobs (small multireference classification case for tests)
+    "mra32_b16": Workload("mra32_b16", 5, 32, 16, 60, 20, (1.5, 3.0), 10.0, (0.5, 1.0), 4, 0.1,
+                          (60.0, 60.0), False, 6.0, n_refs=3, shared_fraction=0.3),
     # 128^3 precision stress, B=64
     "align128_b64": Workload("align128_b64", 4, 128, 64, 1000, 80, (3.0, 8.0), 40.0, (0.5, 1.0), 8, 0.05,
                              (45.0, 70.0), True, 10.0),

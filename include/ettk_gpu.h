@@ -98,6 +98,14 @@ int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, 
 int ettk_gpu_average(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
                      float *avg);
 
+/* Multireference classification (the align -> assign -> re-average loop of src/MPI_Classification.cpp:954-1170,
+   alignment_mode 3): each pass aligns every particle against every current reference (as
+   ettk_gpu_align_pairs), assigns each particle to the class of smallest distance (labels[V]; dist_out[V] its
+   distance, optional), rebuilds each class reference as the wedge-weighted average of its members under their
+   alignments (as ettk_gpu_average; an empty class keeps its reference) and makes the averages the references
+   of the next pass. refs_out (optional, R*N^3 floats, x fastest) receives the last averages. */
+int ettk_gpu_classify(ettk_ctx *ctx, int iterations, int *labels, float *refs_out, float *dist_out);
+
 /* Continuous 6-DOF refinement of aligned pairs (no counterpart in the reference, whose refine() runs a
    Powell search over RotateX/Y/Z offsets with one CCF per step, inc/em/nbfFourierImageMetric.h:1701-1809):
    from the pose of candidate 0 of each row of D (as ettk_gpu_align_pairs wrote it), gradient ascent of the
