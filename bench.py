@@ -302,6 +302,16 @@ def main():
     dom_name, dom = max(kernels.items(), key=lambda kv: kv[1]["ms"])
     achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
     total_prof_ms = sum(v["ms"] for v in kernels.values())
+    # DRAM bytes per launch of the dominant kernel: the ncu figure per volume (profiles/roofline_traffic.json,
+    # dram__bytes_read.sum + dram__bytes_write.sum of a capture) scaled to this run's volumes per launch
+    traffic, alg_per_launch = None, dom["bytes"] / max(1, dom["launches"])
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            rec = json.load(f).get(dom_name)
+        if rec and dom_name == "reslice":
+            traffic = rec["dram_bytes_per_volume"] * alg_per_launch / (8.0 * N ** 3)
+    except (OSError, ValueError, KeyError):
+        traffic = None
     value = world * P * a.steps / (ms * 1e-3)
     e2e = world * P * a.steps / (ms_e2e * 1e-3)
     out = {
@@ -316,7 +326,8 @@ def main():
                 "d2h_bytes_per_step": P * 17 * 4},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": alg_per_launch,
                      "kernel_share": dom["ms"] / total_prof_ms if total_prof_ms else None,
                      "families": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                                       "GBps": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None}
