@@ -399,6 +399,8 @@ struct ettk_ctx {
   DevBuf<double> w_acc, w_w, sp_acc;
   DevBuf<unsigned long long> w_peak, w_mm;
   DevBuf<ResliceItem> w_items;
+  DevBuf<int> w_ridx;     // items resliced directly
+  DevBuf<int2> w_mpairs;  // (mirror item, direct item) pairs of a chunk
   // tensor maps of the particle and reference volumes (empty: the reslice stages through the threads)
   DevBuf<CUtensorMap> tm_part, tm_ref;
   bool tm_part_ok = false, tm_ref_ok = false;
@@ -727,7 +729,7 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
     CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
     {
       Scope sc(this, "reslice", 8.0 * E * n3);
-      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2, status.p);
+      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2, status.p, nullptr);
       post_launch();
     }
     PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
@@ -828,7 +830,7 @@ void ettk_ctx::refine_eval(const std::vector<std::array<double, 12>> &maps, cons
     Scope sc(this, "reslice", 8.0 * E * n3);
     // clamped values everywhere: rho stays smooth when a shift moves the window past the fixed image's edge
     k_reslice_brick<false, true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(
-        w_items.p, N, w_v.p, w_acc.p, 2, status.p);
+        w_items.p, N, w_v.p, w_acc.p, 2, status.p, nullptr);
     post_launch();
   }
   // g = K u, u = valid (r - mean) maskfft shift
@@ -1157,7 +1159,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
     Scope sc(this, "reslice", 8.0 * P * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4, status.p);
+    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4, status.p, nullptr);
   }
   post_launch();
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
@@ -1278,7 +1280,39 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   // normalisation sums
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, acc2, ACC, status.p);
+    // mirror evaluations (the request right after its direct one, Scale(-1,-1,-1) * T with T a rotation, no cut
+    // offset) take the direct reslice reversed on every axis (k_reslice_mirror); only the others are resliced
+    std::vector<int> direct;
+    std::vector<int2> mirrors;
+    for (long e = 0; e < E; ++e) {
+      bool mirror = false;
+      if (e > 0 && (mirrors.empty() || mirrors.back().x != (int)(e - 1)) && req[e].part == req[e - 1].part &&
+          partg[req[e].part].cut_offset == 0.f) {
+        const Mat4 &t = req[e - 1].t;
+        if (t.e[3] == 0 && t.e[7] == 0 && t.e[11] == 0) {
+          Mat4 S = Mat4::eye();
+          S.e[0] = S.e[5] = S.e[10] = -1.0;
+          const Mat4 m = mul(S, t);
+          mirror = true;
+          for (int k = 0; k < 16; ++k) mirror = mirror && m.e[k] == req[e].t.e[k];
+        }
+      }
+      if (mirror) mirrors.push_back(make_int2((int)e, (int)(e - 1)));
+      else direct.push_back((int)e);
+    }
+    w_ridx.ensure(E);
+    w_mpairs.ensure(std::max<long>(1, (long)mirrors.size()));
+    CK(cudaMemcpyAsync(w_ridx.p, direct.data(), direct.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!mirrors.empty())
+      CK(cudaMemcpyAsync(w_mpairs.p, mirrors.data(), mirrors.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    if (!direct.empty())
+      k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), (unsigned)direct.size()), 256, RS_SMEM, st>>>(
+          w_items.p, N, w_v.p, acc2, ACC, status.p, w_ridx.p);
+    if (!mirrors.empty()) {
+      post_launch();
+      k_reslice_mirror<<<dim3(nblocks<int>(n3, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
+          w_items.p, w_mpairs.p, N, w_v.p, acc2, ACC);
+    }
   }
   post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
@@ -1960,6 +1994,8 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_mm.release();
   c->doff.release();
   c->dtab64.release();
+  c->w_ridx.release();
+  c->w_mpairs.release();
   c->rf_fw.release();
   c->rf_y1.release();
   c->rf_a.release();
@@ -2027,7 +2063,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
     k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, RS_SMEM, c->st>>>(c->w_items.p, c->N, c->w_v.p,
-                                                                                          c->w_acc.p, 2, c->status.p);
+                                                                                          c->w_acc.p, 2, c->status.p, nullptr);
     c->post_launch();
     c->FI1.ensure(R * h3);
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};

@@ -66,13 +66,14 @@ static __device__ __noinline__ float tricubic_global(const float *__restrict__ v
 template <bool PRECISE, bool CLAMP_ALL = false>
 __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
                                                           float *__restrict__ out, double *acc, int acc_stride,
-                                                          int *status) {
+                                                          int *status, const int *__restrict__ item_index) {
   extern __shared__ __align__(128) float4 box4[];
   const float *box = reinterpret_cast<const float *>(box4);
   __shared__ double sh[32];
   __shared__ int geo[6];  // o[3], ext[3]
   __shared__ __align__(8) unsigned long long tma_bar;
-  const ResliceItem &it = items[blockIdx.y];
+  const int eidx = item_index ? item_index[blockIdx.y] : (int)blockIdx.y;  // item resliced by this CTA row
+  const ResliceItem &it = items[eidx];
   const int nb = N / RB;
   const int bx = blockIdx.x / (nb * nb), by = (blockIdx.x / nb) % nb, bz = blockIdx.x % nb;
   const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
@@ -210,13 +211,13 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
       s += val;
       cnt += 1;
     }
-    out[(long)blockIdx.y * n3 + ((long)a * N + b) * N + cz] = val;
+    out[(long)eidx * n3 + ((long)a * N + b) * N + cz] = val;
   }
   if (acc) {
     double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
     if (threadIdx.x == 0) {
-      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 0], bs);
-      atomicAdd(&acc[(long)blockIdx.y * acc_stride + 1], bc);
+      atomicAdd(&acc[(long)eidx * acc_stride + 0], bs);
+      atomicAdd(&acc[(long)eidx * acc_stride + 1], bc);
     }
   }
 }
@@ -238,6 +239,63 @@ struct Smooth3 {
   float w_lo[2];    // at index 0: (0, +1)
   float w_hi[2];    // at last index: (-1, 0)
 };
+// Mirror evaluations of the candidate loop (the CCF at Scale(-1,-1,-1) * T, execute 678-776): for a pure
+// rotation T and no cut offset, the output index a of the mirror samples the fixed image where index N - a of
+// the direct reslice does (box coordinates a - N/2 are negated), so r'[a][b][c] = r[N-a][N-b][N-c] for indices
+// >= 1; the index-0 planes, whose partner N lies outside the box, are interpolated from the mirror's own map.
+// pairs[y] = (mirror item, direct item); sums of valid values and their count into acc as the reslice.
+static __global__ void __launch_bounds__(256) k_reslice_mirror(const ResliceItem *__restrict__ items,
+                                                               const int2 *__restrict__ pairs, int N,
+                                                               float *__restrict__ out, double *acc, int acc_stride) {
+  __shared__ double sh[32];
+  const int em = pairs[blockIdx.y].x, ed = pairs[blockIdx.y].y;
+  const ResliceItem &it = items[em];
+  const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
+  const long n3 = (long)N * N * N;
+  const float *src = out + (long)ed * n3;
+  float *dst = out + (long)em * n3;
+  float s = 0.f;
+  int cnt = 0;
+  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
+    const int a = id / (N * N), b = (id / N) % N, cz = id % N;
+    float val;
+    if (a > 0 && b > 0 && cz > 0) {
+      val = src[((long)(N - a) * N + (N - b)) * N + (N - cz)];
+    } else {
+      float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
+      p0 = p0 + b * it.m[6];
+      p1 = p1 + b * it.m[7];
+      p2 = p2 + b * it.m[8];
+      p0 = p0 + a * it.m[3];
+      p1 = p1 + a * it.m[4];
+      p2 = p2 + a * it.m[5];
+      val = -FLT_MAX;
+      if (!(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f)) {
+        float fx, fy, fz;
+        const int ix = vtk_floor(p0, fx), iy = vtk_floor(p1, fy), iz = vtk_floor(p2, fz);
+        float wx[4], wy[4], wz[4];
+        cubic_weights(wx, fx);
+        cubic_weights(wy, fy);
+        cubic_weights(wz, fz);
+        if (!((dy > 1) && (fy != 0.f))) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
+        if (!((dz > 1) && (fz != 0.f))) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
+        val = tricubic_global(it.vol, dx, dy, dz, ix, iy, iz, wx[0], wx[1], wx[2], wx[3], wy[0], wy[1], wy[2], wy[3],
+                              wz[0], wz[1], wz[2], wz[3]);
+      }
+    }
+    dst[id] = val;
+    if (val > -FLT_MAX) {
+      s += val;
+      cnt += 1;
+    }
+  }
+  const double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc[(long)em * acc_stride + 0], bs);
+    atomicAdd(&acc[(long)em * acc_stride + 1], bc);
+  }
+}
+
 // Binary wedge (nbfWedge3D::getImageHalf, inc/em/nbfWedge3D.h:312-356): ((v1.d)(v2.d) <= 0) with
 // d = (i-N/2, j-N/2, k-N/2) on the centred half grid. Near the planes the test is redone in FP64 with the
 // reference's operation order (no FMA) so exact-zero cases resolve as they do there.
