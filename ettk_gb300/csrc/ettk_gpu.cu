@@ -1343,9 +1343,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
                     PrunedLines{E * H * N, (long)H * N, (long)H * N * N, (long)N, (long)N * N, (long)N,
                                 (long)W * H * N, (long)H * N}, o0);
   pruned_fft<true>(w_p1.p, w_p2.p, PrunedLines{E * W * H, 1, (long)N, 1, 0, 1, (long)W, 1}, o0);
-  size_t smz = 2 * (size_t)W * H * sizeof(float2);
+  size_t smz = 2 * (size_t)H * (4 * ((W + 3) / 4)) * sizeof(float2);
   if (smz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_z_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
-  k_pruned_z_peak<<<dim3(W, E), 256, smz, st>>>(w_p2.p, N, W, lo, o2, rr2, w_peak.p);
+  k_pruned_z_peak<<<dim3(W, E), 128, smz, st>>>(w_p2.p, N, W, lo, o2, rr2, w_peak.p);
   post_launch();
   }
   k_score<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, w_peak.p, (int)E, W, sum_filter, p.overlap_normalized,

@@ -537,44 +537,70 @@ struct PostStoreScaled {
 // out[Y][Z] = sum_kz c_KZ Re(q2[X][Y][kz] exp(+2 pi i KZ (lo + Z) / 2N)), KZ = kz + o2 (c = 1 at KZ = 0 and
 // KZ = N, else 2: the hc2r of the reference's (2N)^3 C2R); T = out * (-1)^(X+Y+Z) / (2N)^3 inside the sphere
 // radius^2 < r^2 (else -max); packed argmax (first occurrence in [X][Y][Z] order) into peak[e].
-// q2 is [item][X][kz][Y]; dynamic shared memory: the q2 plane as [Y][kz] (W*H) and Ez W*H complex values.
-static __global__ void __launch_bounds__(256) k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo,
+// q2 is [item][X][kz][Y]. Dynamic shared memory: the q2 plane and Ez, both [kz][WP] complex (WP = W rounded up to
+// 4, zero-padded). Each thread accumulates a 4 x 4 tile of (Y, Z) outputs over kz (per output the same
+// sequential kz sum as a direct loop), so a kz step costs 8 shared loads for 16 outputs.
+static __global__ void __launch_bounds__(128) k_pruned_z_peak(const float2 *__restrict__ q2, int N, int W, int lo,
                                                               int o2, float rr2, unsigned long long *peak) {
-  extern __shared__ float2 sm[];
-  const int H = N / 2 + 1;
-  float2 *P2 = sm;           // [W][H]
-  float2 *Ez = P2 + W * H;   // [W][H] (with the hc2r coefficient folded in)
+  extern __shared__ float4 zsm[];
+  const int H = N / 2 + 1, TW = (W + 3) / 4, WP = 4 * TW;
+  float2 *P2 = reinterpret_cast<float2 *>(zsm);   // [H][WP]
+  float2 *Ez = P2 + H * WP;                       // [H][WP] (with the hc2r coefficient folded in)
   const int X = blockIdx.x, e = blockIdx.y;
   const float2 *src = q2 + ((long)e * W + X) * (long)W * H;
-  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
-    const int kz = i / W, Y = i - kz * W;
-    P2[Y * H + kz] = src[i];
+  for (int i = threadIdx.x; i < H * WP; i += blockDim.x) {
+    const int kz = i / WP, Y = i - kz * WP;
+    P2[i] = Y < W ? src[kz * W + Y] : make_float2(0.f, 0.f);
   }
-  for (int i = threadIdx.x; i < W * H; i += blockDim.x) {
-    int Z = i / H, kz = i - Z * H;
-    int KZ = kz + o2;
-    int ph = (KZ * (lo + Z)) & (2 * N - 1);
-    float sn, cs;
-    sincospif((float)ph / (float)N, &sn, &cs);
-    float c = (KZ == N || KZ == 0) ? 1.f : 2.f;
-    Ez[i] = make_float2(c * cs, c * sn);
+  for (int i = threadIdx.x; i < H * WP; i += blockDim.x) {
+    const int kz = i / WP, Z = i - kz * WP;
+    float2 v = make_float2(0.f, 0.f);
+    if (Z < W) {
+      const int KZ = kz + o2;
+      const int ph = (KZ * (lo + Z)) & (2 * N - 1);
+      float sn, cs;
+      sincospif((float)ph / (float)N, &sn, &cs);
+      const float c = (KZ == N || KZ == 0) ? 1.f : 2.f;
+      v = make_float2(c * cs, c * sn);
+    }
+    Ez[i] = v;
   }
   __syncthreads();
   const float inv = 1.0f / (float)(8L * N * N * N);
   const int half = (W - 1) / 2;
   unsigned long long best = 0;
-  for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
-    int Y = i / W, Z = i - Y * W;
-    float acc = 0.f;
+  const float4 *P4 = reinterpret_cast<const float4 *>(P2), *E4 = reinterpret_cast<const float4 *>(Ez);
+  for (int t = threadIdx.x; t < TW * TW; t += blockDim.x) {
+    const int Y0 = 4 * (t / TW), Z0 = 4 * (t % TW);
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
     for (int kz = 0; kz < H; ++kz) {
-      float2 v = P2[Y * H + kz], t = Ez[Z * H + kz];
-      acc += v.x * t.x - v.y * t.y;
+      const int rp = (kz * WP + Y0) >> 1, re = (kz * WP + Z0) >> 1;
+      const float4 pa = P4[rp], pb = P4[rp + 1], ea = E4[re], eb = E4[re + 1];
+      const float2 pv[4] = {make_float2(pa.x, pa.y), make_float2(pa.z, pa.w), make_float2(pb.x, pb.y),
+                            make_float2(pb.z, pb.w)};
+      const float2 ev[4] = {make_float2(ea.x, ea.y), make_float2(ea.z, ea.w), make_float2(eb.x, eb.y),
+                            make_float2(eb.z, eb.w)};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += pv[i].x * ev[j].x - pv[i].y * ev[j].y;
     }
-    float T = acc * parity_sign(lo + X, lo + Y, lo + Z) * inv;
-    float rad = (float)((half - X) * (half - X) + (half - Y) * (half - Y) + (half - Z) * (half - Z));
-    if (!(rad < rr2)) T = -FLT_MAX;
-    unsigned long long key = pack_max(T, (uint32_t)(((long)X * W + Y) * W + Z));
-    best = key > best ? key : best;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int Y = Y0 + i, Z = Z0 + j;
+        if (Y >= W || Z >= W) continue;
+        float T = acc[i][j] * parity_sign(lo + X, lo + Y, lo + Z) * inv;
+        const float rad = (float)((half - X) * (half - X) + (half - Y) * (half - Y) + (half - Z) * (half - Z));
+        if (!(rad < rr2)) T = -FLT_MAX;
+        const unsigned long long key = pack_max(T, (uint32_t)(((long)X * W + Y) * W + Z));
+        best = key > best ? key : best;
+      }
   }
   best = warp_max_u64(best);
   if ((threadIdx.x & 31) == 0) atomicMax(&peak[e], best);
