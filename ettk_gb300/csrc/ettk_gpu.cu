@@ -62,14 +62,15 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // Host-encoded tensor maps of `count` consecutive N^3 float volumes (x fastest) with the reslice box
 // RT_X x RT_Y x RT_Z. Returns false (and no maps) where the box does not fit or encoding fails.
-bool encode_volume_maps(const float *base, int count, int N, std::vector<CUtensorMap> &maps) {
+bool encode_volume_maps(const float *base, int count, int N, std::vector<CUtensorMap> &maps, const int *dims3 = nullptr) {
   maps.clear();
   auto enc = tensor_map_encoder();
-  if (!enc || N < RT_X || (((unsigned long long)base) & 15)) return false;
+  const int nx = dims3 ? dims3[0] : N, ny = dims3 ? dims3[1] : N, nz = dims3 ? dims3[2] : N;
+  if (!enc || nx < RT_X || ny < RT_Y || nz < RT_Z || (nx & 3) || (((unsigned long long)base) & 15)) return false;
   maps.resize(count);
-  const long n3 = (long)N * N * N;
-  const cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N};
-  const cuuint64_t strides[2] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4};
+  const long n3 = (long)nx * ny * nz;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
   const cuuint32_t box[3] = {RT_X, RT_Y, RT_Z}, es[3] = {1, 1, 1};
   for (int v = 0; v < count; ++v)
     if (enc(&maps[v], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)(base + v * n3), dims, strides, box, es,
@@ -405,11 +406,19 @@ struct ettk_ctx {
   DevBuf<CUtensorMap> tm_part, tm_ref;
   bool tm_part_ok = false, tm_ref_ok = false;
   DevBuf<int> status;  // set by kernels whose bounded waits ran out
-  const void *part_map(long p) const { return tm_part_ok ? (const void *)(tm_part.p + p) : nullptr; }
+  const void *part_map(long p) const { return tm_part_ok ? (const void *)(tm_part.p + (from_tomo ? 0 : p)) : nullptr; }
+  // particles are fixed N^3 images (partptr + p n3), or sub-volumes of one tomogram (tomo, dims tomo_dims)
+  DevBuf<float> tomo;
+  int tomo_dims[3] = {0, 0, 0};
+  bool from_tomo = false;
+  const float *part_vol(long p) const { return from_tomo ? tomo.p : partptr + p * n3; }
+  void part_dims(int d[3]) const {
+    for (int i = 0; i < 3; ++i) d[i] = from_tomo ? tomo_dims[i] : N;
+  }
   const void *ref_map(long r) const { return tm_ref_ok ? (const void *)(tm_ref.p + r) : nullptr; }
-  void upload_maps(const float *base, int count, DevBuf<CUtensorMap> &dst, bool &ok) {
+  void upload_maps(const float *base, int count, DevBuf<CUtensorMap> &dst, bool &ok, const int *dims3 = nullptr) {
     std::vector<CUtensorMap> h;
-    ok = encode_volume_maps(base, count, N, h);
+    ok = encode_volume_maps(base, count, N, h, dims3);
     if (ok) {
       dst.ensure(count);
       CK(cudaMemcpyAsync(dst.p, h.data(), count * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st));
@@ -713,9 +722,9 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
       memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
       double m12[12];
       reslice_index(g, N, &t, m12);
-      items[e].vol = partptr + (long)parts[i] * n3;
+      items[e].vol = part_vol(parts[i]);
       items[e].tmap = part_map(parts[i]);
-      items[e].dims[0] = items[e].dims[1] = items[e].dims[2] = N;
+      part_dims(items[e].dims);
       set_map(items[e], m12);
       w[e] = weights[i];
     }
@@ -816,9 +825,9 @@ void ettk_ctx::refine_eval(const std::vector<std::array<double, 12>> &maps, cons
   for (long e = 0; e < E; ++e) {
     const int part = rf_part[pair[e]];
     ResliceItem it;
-    it.vol = partptr + (long)part * n3;
+    it.vol = part_vol(part);
     it.tmap = part_map(part);
-    it.dims[0] = it.dims[1] = it.dims[2] = N;
+    part_dims(it.dims);
     set_map(it, maps[e].data());
     items[e] = it;
   }
@@ -1222,9 +1231,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     double m12[12];
     reslice_index(g, N, &r.t, m12);
     ResliceItem it;
-    it.vol = partptr + (long)r.part * n3;
+    it.vol = part_vol(r.part);
     it.tmap = part_map(r.part);
-    it.dims[0] = it.dims[1] = it.dims[2] = N;
+    part_dims(it.dims);
     set_map(it, m12);
     items[e] = it;
     WedgeVecs w{};
@@ -1476,9 +1485,9 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         size_t c1 = std::min(ids.size(), c0 + chunk);
         for (size_t c = c0; c < c1; ++c) {
           ResliceItem it;
-          it.vol = partptr + (long)ids[c] * n3;
+          it.vol = part_vol(ids[c]);
           it.tmap = part_map(ids[c]);
-          it.dims[0] = it.dims[1] = it.dims[2] = N;
+          part_dims(it.dims);
           double m12[12];
           reslice_index(partg[ids[c]], N, nullptr, m12);
           set_map(it, m12);
@@ -1994,6 +2003,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_mm.release();
   c->doff.release();
   c->dtab64.release();
+  c->tomo.release();
   c->w_ridx.release();
   c->w_mpairs.release();
   c->rf_fw.release();
@@ -2077,6 +2087,8 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
   });
 }
 
+static void particle_tables(ettk_ctx *c, const ettk_volume_meta *meta);
+
 static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_volume_meta *meta, bool device) {
   if (!c || V <= 0 || !vols || !meta) return fail(c, ETTK_ERR_ARG, "invalid particle arguments");
   if (!device && !finite_volume(vols, (long)V * c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite particle volume");
@@ -2086,6 +2098,7 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
     c->partg.resize(V);
     c->useW2.resize(V);
     c->pp2_ready.assign(V, 0);
+    c->from_tomo = false;
     if (device) {
       c->partptr = vols;
     } else {
@@ -2094,18 +2107,48 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
       c->partptr = c->partvol.p;
     }
     c->upload_maps(c->partptr, V, c->tm_part, c->tm_part_ok);
-    std::vector<float> w2s((size_t)V * c->nn);
-    for (int v = 0; v < V; ++v) {
-      c->partg[v] = to_geom(meta[v]);
-      std::vector<float> w;
-      int use = 0;
-      spherical_wedge_host(c->partg[v], c->B, w, use);
-      std::copy(w.begin(), w.end(), w2s.begin() + (size_t)v * c->nn);
-      c->useW2[v] = use;
-    }
-    c->W2sph.ensure(V * c->nn);
-    CK(cudaMemcpyAsync(c->W2sph.p, w2s.data(), V * c->nn * 4, cudaMemcpyHostToDevice, c->st));
-    c->Pp2.ensure(V * c->nn);
+    particle_tables(c, meta);
+    c->sync();
+  });
+}
+
+// Pose geometry, spherical wedges and projection slots of the particle set (both particle sources).
+static void particle_tables(ettk_ctx *c, const ettk_volume_meta *meta) {
+  const int V = c->V;
+  std::vector<float> w2s((size_t)V * c->nn);
+  for (int v = 0; v < V; ++v) {
+    c->partg[v] = to_geom(meta[v]);
+    std::vector<float> w;
+    int use = 0;
+    spherical_wedge_host(c->partg[v], c->B, w, use);
+    std::copy(w.begin(), w.end(), w2s.begin() + (size_t)v * c->nn);
+    c->useW2[v] = use;
+  }
+  c->W2sph.ensure(V * c->nn);
+  CK(cudaMemcpyAsync(c->W2sph.p, w2s.data(), V * c->nn * 4, cudaMemcpyHostToDevice, c->st));
+  c->Pp2.ensure(V * c->nn);
+}
+
+int ettk_gpu_set_particles_tomogram(ettk_ctx *c, int nx, int ny, int nz, const float *tomogram, int V,
+                                    const ettk_volume_meta *meta) {
+  if (!c || nx < 1 || ny < 1 || nz < 1 || !tomogram || V <= 0 || !meta)
+    return fail(c, ETTK_ERR_ARG, "invalid tomogram arguments");
+  const long nt = (long)nx * ny * nz;
+  if (!finite_volume(tomogram, nt)) return fail(c, ETTK_ERR_NAN, "non-finite tomogram");
+  return guarded(c, [&] {
+    c->V = V;
+    c->partg.resize(V);
+    c->useW2.resize(V);
+    c->pp2_ready.assign(V, 0);
+    c->tomo.ensure(nt);
+    CK(cudaMemcpyAsync(c->tomo.p, tomogram, nt * 4, cudaMemcpyHostToDevice, c->st));
+    c->tomo_dims[0] = nx;
+    c->tomo_dims[1] = ny;
+    c->tomo_dims[2] = nz;
+    c->from_tomo = true;
+    c->partptr = c->tomo.p;
+    c->upload_maps(c->tomo.p, 1, c->tm_part, c->tm_part_ok, c->tomo_dims);
+    particle_tables(c, meta);
     c->sync();
   });
 }
@@ -2265,7 +2308,7 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
     double m12[12];
     if (p >= 0) {
       if (p >= c->V) throw CudaError(ETTK_ERR_STATE, "particle index out of range");
-      it.vol = c->partptr + (long)p * c->n3;
+      it.vol = c->part_vol(p);
       it.tmap = c->part_map(p);
       reslice_index(c->partg[p], c->N, nullptr, m12);
     } else {
@@ -2275,6 +2318,7 @@ int ettk_gpu_spherical_projection(ettk_ctx *c, int r, int p, float *Pp) {
       reslice_index(c->refg[r], c->N, nullptr, m12);
     }
     it.dims[0] = it.dims[1] = it.dims[2] = c->N;
+    if (p >= 0) c->part_dims(it.dims);
     set_map(it, m12);
     c->w_sig.ensure(c->nn);
     c->spherical_projection({it}, c->w_sig.p);

@@ -86,6 +86,16 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_set_particles(self._ctx, len(volumes), vols.ctypes.data, meta), "set_particles")
         self._parts = volumes
 
+    def set_particles_tomogram(self, tomogram, metas):
+        """Particles cut from one tomogram ([z][y][x] float32) at metas[i]["position"] (voxel coordinates of
+        the tomogram), as nbfWedgedSubImage3D's tomogram path; metas are volume-list metadata dicts."""
+        t = np.ascontiguousarray(tomogram, np.float32)
+        nz, ny, nx = t.shape
+        meta = _lib.make_meta(metas)
+        self._check(self.L.ettk_gpu_set_particles_tomogram(self._ctx, nx, ny, nz, t.ctypes.data, len(metas), meta),
+                    "set_particles_tomogram")
+        self._parts = [None] * len(metas)
+
     def set_particles_device(self, dev_ptr, metas):
         meta = _lib.make_meta(metas)
         self._check(self.L.ettk_gpu_set_particles_device(self._ctx, len(metas), ctypes.c_void_p(dev_ptr), meta),

@@ -83,6 +83,13 @@ int ettk_gpu_set_particles(ettk_ctx *ctx, int V, const float *volumes, const ett
 /* Same as ettk_gpu_set_particles with `volumes` already in device memory of the context's GPU. */
 int ettk_gpu_set_particles_device(ettk_ctx *ctx, int V, const float *d_volumes, const ettk_volume_meta *meta);
 
+/* Particles cut from one tomogram (nbfWedgedSubImage3D::getImage's tomogram path,
+   inc/em/nbfWedgedSubImage3D.h:602-746): tomogram is nx*ny*nz floats, x fastest; meta[v].position is the
+   particle centre in tomogram voxel coordinates (and cut_offset the z offset of the box). Every reslice of a
+   particle (spherical projection, CCF evaluations, averages) reads the tomogram directly. */
+int ettk_gpu_set_particles_tomogram(ettk_ctx *ctx, int nx, int ny, int nz, const float *tomogram, int V,
+                                    const ettk_volume_meta *meta);
+
 /* Replaces nbfCorrelationImageMetric::getDistances(list1, list2, indexes, D, type=3)
  * (inc/em/nbfCorrelationImageMetric.h:1873-2009): pairs[2*i] = reference index, pairs[2*i+1] =
  * particle index. D is the reference's Array<float,3> D(npairs, cols, ncand) in C order:
