@@ -117,13 +117,24 @@ def make_params(p):
         wigner_precision=int(p.get("wigner_precision", 0)))
 
 
+_META_DTYPE = np.dtype({"names": [f[0] for f in VolumeMeta._fields_],
+                         "formats": [("<f4", (3,)) if f[0] in ("normal", "position") else
+                                     ("<f8", (16,)) if f[0] == "matrix" else "<f4" for f in VolumeMeta._fields_],
+                         "offsets": [getattr(VolumeMeta, f[0]).offset for f in VolumeMeta._fields_],
+                         "itemsize": ctypes.sizeof(VolumeMeta)})
+
+
 def make_meta(metas):
-    arr = (VolumeMeta * len(metas))()
-    for i, m in enumerate(metas):
-        v = arr[i]
-        v.lwedge, v.uwedge = m["lwedge"], m["uwedge"]
-        v.normal[:] = [float(x) for x in m.get("normal", (0.0, 0.0, 0.0))]
-        v.matrix[:] = [float(x) for x in np.asarray(m.get("matrix", np.eye(4)), np.float64).reshape(16)]
-        v.position[:] = [float(x) for x in m["position"]]
-        v.cut_offset = float(m.get("cut_offset", 0.0))
+    """ctypes array of ettk_volume_meta from volume-list metadata dicts (columns filled with numpy)."""
+    n = len(metas)
+    a = np.zeros(n, _META_DTYPE)
+    if n:
+        a["lwedge"] = [m["lwedge"] for m in metas]
+        a["uwedge"] = [m["uwedge"] for m in metas]
+        a["normal"] = [m.get("normal", (0.0, 0.0, 0.0)) for m in metas]
+        eye = np.eye(4)
+        a["matrix"] = np.asarray([np.asarray(m.get("matrix", eye), np.float64).reshape(16) for m in metas])
+        a["position"] = [m["position"] for m in metas]
+        a["cut_offset"] = [m.get("cut_offset", 0.0) for m in metas]
+    arr = (VolumeMeta * n).from_buffer_copy(a.tobytes()) if n else (VolumeMeta * 0)()
     return arr

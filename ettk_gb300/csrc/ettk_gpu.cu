@@ -1393,9 +1393,6 @@ bool transform_valid(const ettk_params &p, const Mat4 &t) {
   return ang <= p.restrict_rotation;
 }
 
-// eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
-// matrices can be closer than `tol` in L1 are compared (each entry must differ by < tol); visiting only
-// those pairs in increasing j order is equivalent to the reference's full double loop.
 // Runs f(0..n-1) on up to 16 host threads (independent items; f must not throw).
 template <class F>
 void parallel_for(int n, F f) {
@@ -1414,6 +1411,9 @@ void parallel_for(int n, F f) {
   for (auto &x : th) x.join();
 }
 
+// eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
+// matrices can be closer than `tol` in L1 are compared (each entry must differ by < tol); visiting only
+// those pairs in increasing j order is equivalent to the reference's full double loop.
 void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
   size_t K = pos.size();
   std::vector<Mat4> mats(K);
@@ -1889,11 +1889,17 @@ void spherical_wedge_host(const VolumeGeom &g, int B, std::vector<float> &W, int
     double v1[3], v2[3];
     wedge_vectors(g, nullptr, v1, v2);
     float phiK = (float)(M_PI / (n - 1)), thetaK = (float)(2.0 * M_PI / (n - 1));
+    std::vector<float> cj(n), sj(n), si(n), ci(n);
+    for (int k = 0; k < n; ++k) {
+      cj[k] = cosf(k * thetaK);
+      sj[k] = sinf(k * thetaK);
+      si[k] = sinf(k * phiK);
+      ci[k] = cosf(k * phiK);
+    }
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) {
-        float cj = cosf(j * thetaK), sj = sinf(j * thetaK), si = sinf(i * phiK), ci = cosf(i * phiK);
-        double a = v1[0] * cj * si + v1[1] * sj * si + v1[2] * ci;
-        double b = v2[0] * cj * si + v2[1] * sj * si + v2[2] * ci;
+        double a = v1[0] * cj[j] * si[i] + v1[1] * sj[j] * si[i] + v1[2] * ci[i];
+        double b = v2[0] * cj[j] * si[i] + v2[1] * sj[j] * si[i] + v2[2] * ci[i];
         W[(size_t)i * n + j] = (a * b <= 0.0) ? 1.0f : 0.0f;
       }
   }
@@ -1936,10 +1942,19 @@ void wedge_half_host(const VolumeGeom &g, int N, std::vector<float> &W) {
       for (int k = 0; k < H; ++k) W[((size_t)i * N + j) * H + k] = t[i + (size_t)N * (j + (size_t)N * k)];
 }
 
+// No NaN or infinity in v[0..n) (exponent field all ones), checked in 1 MiB slices on the host threads.
 bool finite_volume(const float *v, long n) {
-  for (long i = 0; i < n; ++i)
-    if (!std::isfinite(v[i])) return false;
-  return true;
+  const long slice = 1L << 18;
+  const int ns = (int)((n + slice - 1) / slice);
+  std::atomic<int> bad{0};
+  parallel_for(ns, [&](int t) {
+    const uint32_t *u = reinterpret_cast<const uint32_t *>(v) + (long)t * slice;
+    const long m = std::min(slice, n - (long)t * slice);
+    uint32_t any = 0;
+    for (long i = 0; i < m; ++i) any |= (uint32_t)((u[i] & 0x7f800000u) == 0x7f800000u);
+    if (any) bad.store(1);
+  });
+  return bad.load() == 0;
 }
 
 template <class F>
@@ -2106,8 +2121,8 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
       CK(cudaMemcpyAsync(c->partvol.p, vols, V * n3 * 4, cudaMemcpyHostToDevice, c->st));
       c->partptr = c->partvol.p;
     }
+    particle_tables(c, meta);  // host work overlaps the volume upload
     c->upload_maps(c->partptr, V, c->tm_part, c->tm_part_ok);
-    particle_tables(c, meta);
     c->sync();
   });
 }
@@ -2116,14 +2131,14 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
 static void particle_tables(ettk_ctx *c, const ettk_volume_meta *meta) {
   const int V = c->V;
   std::vector<float> w2s((size_t)V * c->nn);
-  for (int v = 0; v < V; ++v) {
+  parallel_for(V, [&](int v) {
     c->partg[v] = to_geom(meta[v]);
     std::vector<float> w;
     int use = 0;
     spherical_wedge_host(c->partg[v], c->B, w, use);
     std::copy(w.begin(), w.end(), w2s.begin() + (size_t)v * c->nn);
     c->useW2[v] = use;
-  }
+  });
   c->W2sph.ensure(V * c->nn);
   CK(cudaMemcpyAsync(c->W2sph.p, w2s.data(), V * c->nn * 4, cudaMemcpyHostToDevice, c->st));
   c->Pp2.ensure(V * c->nn);
