@@ -435,7 +435,7 @@ struct ettk_ctx {
     }
   }
   DevBuf<WedgeVecs> w_wv;
-  DevBuf<int> w_idx, w_idx2, w_cnt, w_active, w_pair_ref, w_pair_pp2, w_pair_part;
+  DevBuf<int> w_idx, w_idx2, w_cnt, w_active, w_pair_ref, w_pair_pp2, w_pair_part, w_i1;
   DevBuf<int2> w_lists;
   DevBuf<EvalOut> w_out;
   DevBuf<SigDesc> w_sd;
@@ -1220,33 +1220,66 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   w_out.ensure(E);
   w_p1.ensure(E * W * N * H);
   w_p2.ensure(E * W * W * H);
+  // Reference branch sharing: the wedge * filter, F1, y1 and FFT1re of an evaluation depend only on its
+  // reference and its wedge planes; the binary wedge tests the product of two plane distances, so planes
+  // negated together (the mirror Scale(-1,-1,-1) * T of the request before) give a bit-identical wedge.
+  // Device slots: the Dn evaluations that compute the branch first, then those that share one (i1src).
   std::vector<ResliceItem> items(E);
   std::vector<WedgeVecs> wv(E);
-  std::vector<int> refidx(E);
+  std::vector<int> refidx(E), ord(E), slot_of(E), i1src(E);
+  long Dn = 0;
   {
     HostScope hs_prep(this, "host_eval_prep");
-  for (long e = 0; e < E; ++e) {
-    const EvalReq &r = req[e];
-    const VolumeGeom &g = partg[r.part];
-    double m12[12];
-    reslice_index(g, N, &r.t, m12);
-    ResliceItem it;
-    it.vol = part_vol(r.part);
-    it.tmap = part_map(r.part);
-    part_dims(it.dims);
-    set_map(it, m12);
-    items[e] = it;
-    WedgeVecs w{};
-    w.full = g.full_wedge() ? 1 : 0;
-    if (!w.full) wedge_vectors(g, &r.t, w.v1, w.v2);
-    wv[e] = w;
-    refidx[e] = r.ref;
-  }
+    std::vector<WedgeVecs> wo(E);
+    std::vector<char> shares(E, 0);
+    for (long e = 0; e < E; ++e) {
+      const VolumeGeom &g = partg[req[e].part];
+      WedgeVecs w{};
+      w.full = g.full_wedge() ? 1 : 0;
+      if (!w.full) wedge_vectors(g, &req[e].t, w.v1, w.v2);
+      wo[e] = w;
+      if (e > 0 && !shares[e - 1] && req[e].ref == req[e - 1].ref && w.full == wo[e - 1].full) {
+        const WedgeVecs &q = wo[e - 1];
+        bool same = true, neg = true;
+        for (int k = 0; k < 3; ++k) {
+          same = same && w.v1[k] == q.v1[k] && w.v2[k] == q.v2[k];
+          neg = neg && w.v1[k] == -q.v1[k] && w.v2[k] == -q.v2[k];
+        }
+        shares[e] = w.full || same || neg;
+      }
+    }
+    for (long e = 0; e < E; ++e)
+      if (!shares[e]) slot_of[e] = (int)Dn++;
+    long m = Dn;
+    for (long e = 0; e < E; ++e)
+      if (shares[e]) slot_of[e] = (int)m++;
+    for (long e = 0; e < E; ++e) {
+      const int s = slot_of[e];
+      ord[s] = (int)e;
+      i1src[s] = shares[e] ? slot_of[e - 1] : s;
+      const EvalReq &r = req[e];
+      double m12[12];
+      reslice_index(partg[r.part], N, &r.t, m12);
+      ResliceItem it;
+      it.vol = part_vol(r.part);
+      it.tmap = part_map(r.part);
+      part_dims(it.dims);
+      set_map(it, m12);
+      items[s] = it;
+      wv[s] = wo[e];
+      refidx[s] = r.ref;
+    }
   }
   std::unique_ptr<HostScope> hs_launch(new HostScope(this, "host_eval_issue"));
   CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(w_wv.p, wv.data(), E * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(w_idx.p, refidx.data(), E * sizeof(int), cudaMemcpyHostToDevice, st));
+  const int *i1 = nullptr;  // slot -> slot holding its reference branch (null when every slot holds its own)
+  if (Dn < E) {
+    w_i1.ensure(E);
+    CK(cudaMemcpyAsync(w_i1.p, i1src.data(), E * sizeof(int), cudaMemcpyHostToDevice, st));
+    i1 = w_i1.p;
+  }
   CK(cudaMemsetAsync(w_acc.p, 0, E * ACC * 2 * sizeof(double), st));
   CK(cudaMemsetAsync(w_peak.p, 0, E * sizeof(unsigned long long), st));
   double *acc = w_acc.p;
@@ -1255,26 +1288,26 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   bool useWedge = p.wedge_compensation != 0;
   // wedge (W1 * W2(T)) * filter and its sum
   if (useWedge) {
-    Scope sc_w(this, "wedge", 4.0 * E * h3);
+    Scope sc_w(this, "wedge", 4.0 * Dn * h3);
     switch (N) {
-      case 16: wedge_t<16>(E, acc, ACC); break;
-      case 32: wedge_t<32>(E, acc, ACC); break;
-      case 64: wedge_t<64>(E, acc, ACC); break;
-      case 128: wedge_t<128>(E, acc, ACC); break;
+      case 16: wedge_t<16>(Dn, acc, ACC); break;
+      case 32: wedge_t<32>(Dn, acc, ACC); break;
+      case 64: wedge_t<64>(Dn, acc, ACC); break;
+      case 128: wedge_t<128>(Dn, acc, ACC); break;
       default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
     }
   } else {
-    for (long e = 0; e < E; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
+    for (long e = 0; e < Dn; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
   }
-  // I1 branch: F1 = FI1 * fw (DC zeroed) with its normalisation sums, inverse (x, y) passes, C2R scaled by
-  // 1/norm, then k1_m and R2C(I1' m1)
+  // I1 branch (slots 0..Dn-1): F1 = FI1 * fw (DC zeroed) with its normalisation sums, inverse (x, y) passes,
+  // C2R scaled by 1/norm, then k1_m and R2C(I1' m1)
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
-    fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, w_fw.p, w_cA.p, HalfSums<NN>{acc, ACC, 2}}, E, "fft_xy", 20.0);
+    fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, w_fw.p, w_cA.p, HalfSums<NN>{acc, ACC, 2}}, Dn, "fft_xy", 20.0);
   });
-  k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)E, w_norm.p, nullptr);
+  k_norms<<<nblocks<int>(Dn, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)Dn, w_norm.p, nullptr);
   post_launch();
-  c2r_z(N, w_cA.p, PostStoreScaled{w_r.p, N, w_norm.p, ilog2((long)N * N)}, E * N * N);
+  c2r_z(N, w_cA.p, PostStoreScaled{w_r.p, N, w_norm.p, ilog2((long)N * N)}, Dn * N * N);
   PreY1M1 py;
   py.y = w_r.p;
   py.m1 = mask.p;
@@ -1283,8 +1316,8 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   py.acc_stride = ACC;
   py.slot = 4;
   py.lines_per_block = lines_per_block(N);
-  r2c_z(N, py, w_cA.p, E * N * N);
-  xy_kxy(N, w_cA.p, E, -1);
+  r2c_z(N, py, w_cA.p, Dn * N * N);
+  xy_kxy(N, w_cA.p, Dn, -1);
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift), forward (x, y) passes then * fw with the
   // normalisation sums
   {
@@ -1293,10 +1326,10 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     // offset) take the direct reslice reversed on every axis (k_reslice_mirror); only the others are resliced
     std::vector<int> direct;
     std::vector<int2> mirrors;
+    std::vector<char> is_mirror(E, 0);
     for (long e = 0; e < E; ++e) {
       bool mirror = false;
-      if (e > 0 && (mirrors.empty() || mirrors.back().x != (int)(e - 1)) && req[e].part == req[e - 1].part &&
-          partg[req[e].part].cut_offset == 0.f) {
+      if (e > 0 && !is_mirror[e - 1] && req[e].part == req[e - 1].part && partg[req[e].part].cut_offset == 0.f) {
         const Mat4 &t = req[e - 1].t;
         if (t.e[3] == 0 && t.e[7] == 0 && t.e[11] == 0) {
           Mat4 S = Mat4::eye();
@@ -1306,8 +1339,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
           for (int k = 0; k < 16; ++k) mirror = mirror && m.e[k] == req[e].t.e[k];
         }
       }
-      if (mirror) mirrors.push_back(make_int2((int)e, (int)(e - 1)));
-      else direct.push_back((int)e);
+      is_mirror[e] = mirror;
+      if (mirror) mirrors.push_back(make_int2(slot_of[e], slot_of[e - 1]));
+      else direct.push_back(slot_of[e]);
     }
     w_ridx.ensure(E);
     w_mpairs.ensure(std::max<long>(1, (long)mirrors.size()));
@@ -1328,27 +1362,28 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   r2c_z(N, pp, w_cB.p, E * N * N);
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
-    fft2d_t<NN>(OpFwdFilter<NN>{w_cB.p, w_fw.p, HalfSums<NN>{acc2, ACC, 2}}, E, "fft_xy", 20.0);
+    fft2d_t<NN>(OpFwdFilter<NN>{w_cB.p, w_fw.p, HalfSums<NN>{acc2, ACC, 2}, i1}, E, "fft_xy", 20.0);
   });
   k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc2, ACC, 2, N, (int)E, w_norm2.p, nullptr);
   post_launch();
-  // FFT2re over FFT1re, inverse (x, y) passes of F2/norm2, C2R, R2C(I2'^2 shift), forward passes + cross term
+  // FFT2re (into cC), inverse (x, y) passes of F2/norm2, C2R, R2C(I2'^2 shift) into cB, forward passes + cross
+  // term
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
-    fft2d_t<NN>(OpFft2reInv<NN>{w_cA.p, w_cB.p, w_norm2.p}, E, "fft_xy", 32.0);
+    fft2d_t<NN>(OpFft2reInv<NN>{w_cA.p, i1, w_cC.p, w_cB.p, w_norm2.p}, E, "fft_xy", 32.0);
   });
   c2r_z(N, w_cB.p, PostStore{w_r.p, N}, E * N * N);
-  r2c_z(N, PreSquareShift{w_r.p, N}, w_cC.p, E * N * N);
+  r2c_z(N, PreSquareShift{w_r.p, N}, w_cB.p, E * N * N);
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
-    fft2d_t<NN>(OpFwdCross<NN>{w_cC.p, Fm1.p, w_cA.p, 8.0f}, E, "fft_xy", 24.0);
+    fft2d_t<NN>(OpFwdCross<NN>{w_cB.p, Fm1.p, w_cC.p, 8.0f}, E, "fft_xy", 24.0);
   });
   int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
   {
   Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
   // x: lines (item, kz, ky) of the kz-major spectrum, stride N, into q1[item][X][kz][ky];
   // y: lines (item, X, kz), contiguous, into q2[item][X][kz][Y]
-  pruned_fft<false>(w_cC.p, w_p1.p,
+  pruned_fft<false>(w_cB.p, w_p1.p,
                     PrunedLines{E * H * N, (long)H * N, (long)H * N * N, (long)N, (long)N * N, (long)N,
                                 (long)W * H * N, (long)H * N}, o0);
   pruned_fft<true>(w_p1.p, w_p2.p, PrunedLines{E * W * H, 1, (long)N, 1, 0, 1, (long)W, 1}, o0);
@@ -1358,19 +1393,20 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   post_launch();
   }
   k_score<<<nblocks<int>(E, 128), 128, 0, st>>>(acc, ACC, w_peak.p, (int)E, W, sum_filter, p.overlap_normalized,
-                                                useWedge ? 1 : 0, N, w_out.p);
+                                                useWedge ? 1 : 0, N, w_out.p, i1);
   post_launch();
   hs_launch.reset();
   std::vector<EvalOut> out(E);
   read_back(out.data(), w_out.p, E * sizeof(EvalOut));
   check_status();
-  for (long e = 0; e < E; ++e) {
-    res[e].dist = out[e].dist;
+  for (long s = 0; s < E; ++s) {
+    const int e = ord[s];
+    res[e].dist = out[s].dist;
     Mat4 tr = Mat4::eye();
-    if (!(out[e].shift[0] == 0 && out[e].shift[1] == 0 && out[e].shift[2] == 0)) {
-      tr.e[3] = -(double)out[e].shift[0];
-      tr.e[7] = -(double)out[e].shift[1];
-      tr.e[11] = -(double)out[e].shift[2];
+    if (!(out[s].shift[0] == 0 && out[s].shift[1] == 0 && out[s].shift[2] == 0)) {
+      tr.e[3] = -(double)out[s].shift[0];
+      tr.e[7] = -(double)out[s].shift[1];
+      tr.e[11] = -(double)out[s].shift[2];
     }
     res[e].t = mul(req[e].t, tr);
   }
@@ -2036,6 +2072,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_pair_ref.release();
   c->w_pair_pp2.release();
   c->w_pair_part.release();
+  c->w_i1.release();
   c->w_lists.release();
   c->w_out.release();
   c->w_sd.release();

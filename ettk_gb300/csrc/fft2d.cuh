@@ -155,12 +155,13 @@ struct OpFwdFilter {
   float2 *d;
   const float *fw;
   HalfSums<N> sums;
+  const int *fw_index = nullptr;  // item whose wedge * filter applies (null: the item itself)
   int sign = -1;
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N>::at(e, kz, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
     const long g = KXY<N>::at(e, kz, i);
-    v = cscale(v, fw[g]);
+    v = cscale(v, fw[fw_index ? KXY<N>::at(fw_index[e], kz, i) : g]);
     if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
     sums.add(v);
     d[g] = v;
@@ -168,11 +169,14 @@ struct OpFwdFilter {
   ETTK_DEV void end(int e, int kz) { sums.flush(e, kz); }
 };
 
-// FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3) stored over FFT1re (nbfFourierImageMetric.h:1174-1177), then
-// the inverse (x, y) passes of F2 / norm2.
+// FFT2re = 2 * FFT1re * conj(F2 / norm2 * N^3) (nbfFourierImageMetric.h:1174-1177) into its own buffer, then
+// the inverse (x, y) passes of F2 / norm2. FFT1re of item e is a[a_index[e]] (evaluations that share the
+// reference branch read one copy; it is never written here, so no item reads what another overwrites).
 template <int N>
 struct OpFft2reInv {
-  float2 *a;                 // FFT1re (updated in the prologue)
+  const float2 *a;           // FFT1re
+  const int *a_index;        // item whose FFT1re applies (null: the item itself)
+  float2 *fft2re;            // FFT2re out
   float2 *b;                 // F2 (transformed in place)
   const float *inv_norm2;
   int sign = +1;
@@ -182,7 +186,8 @@ struct OpFft2reInv {
     const float sc = inv_norm2[e];
     const float2 bb = b[g];
     const float2 bs = cscale(bb, sc * (float)((long)N * N * N));
-    a[g] = cscale(cmul(a[g], cconj(bs)), 2.0f);
+    const float2 f1 = a[a_index ? KXY<N>::at(a_index[e], kz, i) : g];
+    fft2re[g] = cscale(cmul(f1, cconj(bs)), 2.0f);
     return cscale(bb, sc);
   }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { b[KXY<N>::at(e, kz, i)] = v; }

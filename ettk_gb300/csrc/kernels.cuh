@@ -611,14 +611,15 @@ struct EvalOut {
   float dist;
   float shift[3];
 };
+// acc of item e holds k1_m (slot 4) and sum(w*f) (slot 6) at item i1_index[e] (null: e itself).
 static __global__ void k_score(const double *acc, int acc_stride, const unsigned long long *peak, int n_items, int W,
-                        double sum_filter, int overlap, int use_wedge, int N, EvalOut *out) {
+                        double sum_filter, int overlap, int use_wedge, int N, EvalOut *out, const int *i1_index) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_items) return;
   unsigned long long key = peak[e];
   float T = ordered_to_float((uint32_t)(key >> 32));
   uint32_t idx = 0xffffffffu - (uint32_t)(key & 0xffffffffu);
-  const double *a = acc + (long)e * acc_stride;
+  const double *a = acc + (long)(i1_index ? i1_index[e] : e) * acc_stride;
   float k1_m = (float)a[4];
   double big = 8.0 * N * N * N;
   double pk;
