@@ -5,6 +5,7 @@
 #include <cfloat>
 
 #define ETTK_DEV __device__ __forceinline__
+#define ETTK_HD __host__ __device__ __forceinline__
 
 namespace ettk {
 
@@ -77,6 +78,15 @@ ETTK_DEV int vtk_floor(float x, float &f) {
 
 // ---- mbarrier + bulk tensor copy (TMA) helpers ------------------------------------------------
 ETTK_DEV uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// 16-byte asynchronous global -> shared copies (both addresses 16-byte aligned), committed and waited in groups
+ETTK_DEV void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+ETTK_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+ETTK_DEV void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
 ETTK_DEV void mbar_init(void *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");

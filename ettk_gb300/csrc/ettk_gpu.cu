@@ -590,10 +590,37 @@ struct ettk_ctx {
   template <int NN, class Pre>
   void r2c_z_t(Pre pre, float2 *out, long lines) {
     constexpr int L = reg_lines<NN>();
-    int blocks = (int)((lines + 2 * L - 1) / (2 * L));
+    long tiles = (lines + 2 * L - 1) / (2 * L);
     Scope sc(this, "fft_r2c_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
-    k_r2c_reg<NN, L, Pre><<<blocks, 256, 0, st>>>(pre, out, lines);
+    bool streamed = false;
+    if constexpr (has_stream<Pre>::value) {
+      if ((((unsigned long long)pre.stream_src()) & 15) == 0) {
+        constexpr size_t smem = r2c_stream_smem<NN>();
+        const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre>, smem));
+        k_r2c_stream<NN, L, Pre><<<grid, 256, smem, st>>>(pre, out, lines);
+        streamed = true;
+      }
+    }
+    if (!streamed) k_r2c_reg<NN, L, Pre><<<(unsigned)tiles, 256, 0, st>>>(pre, out, lines);
     post_launch();
+  }
+  // CTAs of a persistent kernel: resident CTAs per SM (with `smem` dynamic shared memory) x SMs, computed
+  // once per kernel and device (the dynamic size is opted in first: static + dynamic may exceed 48 KB)
+  template <class K>
+  long resident_grid(K *kernel, size_t smem) {
+    static std::map<std::pair<const void *, int>, long> cache;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    const std::pair<const void *, int> key((const void *)kernel, device);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0, sms = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, smem));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const long g = (long)std::max(1, per_sm) * std::max(1, sms);
+    cache[key] = g;
+    return g;
   }
   template <class Pre>
   void r2c_z(int len, Pre pre, float2 *out, long lines) {
@@ -619,9 +646,15 @@ struct ettk_ctx {
   template <int NN, class Post>
   void c2r_z_t(const float2 *in, Post post, long lines) {
     constexpr int L = reg_lines<NN>();
-    int blocks = (int)((lines + 2 * L - 1) / (2 * L));
+    long tiles = (lines + 2 * L - 1) / (2 * L);
     Scope sc(this, "fft_c2r_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
-    k_c2r_reg<NN, L, Post><<<blocks, 256, 0, st>>>(in, post, lines);
+    if (lines % (2 * L) == 0 && (((unsigned long long)in) & 15) == 0) {
+      constexpr size_t smem = c2r_stream_smem<NN>();
+      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_stream<NN, L, Post>, smem));
+      k_c2r_stream<NN, L, Post><<<grid, 256, smem, st>>>(in, post, lines);
+    } else {
+      k_c2r_reg<NN, L, Post><<<(unsigned)tiles, 256, 0, st>>>(in, post, lines);
+    }
     post_launch();
   }
   template <class Post>

@@ -237,6 +237,95 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   }
 }
 
+// Input functors whose values come from one real N^3 array per item declare kStream, expose the array as
+// stream_src() and compute the input from its element with apply(line, k, raw); end_tile(first line) closes a
+// tile of lines (one item).
+template <class T, class = void>
+struct has_stream : std::false_type {};
+template <class T>
+struct has_stream<T, std::void_t<decltype(T::kStream)>> : std::true_type {};
+
+template <int N>
+__host__ __device__ constexpr int stream_pitch() { return N + 4; }  // staged line pitch (floats): 16-byte rows, 8 banks apart per 2 lines
+
+// Persistent form of k_r2c_reg for streamed inputs: each CTA walks tiles of 2*LINES contiguous real lines
+// (t = blockIdx.x, + gridDim.x, ...); the next tile is copied into the other half of a double buffer
+// (cp.async, 16-byte chunks) while the current one is transformed, so loads stay in flight through the
+// transform and the stores. Tiles never straddle two items (2*LINES divides N*N).
+template <int N, int LINES, class Pre>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_r2c_stream(Pre pre, float2 *__restrict__ out, long n_lines) {
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES, NP = stream_pitch<N>();
+  constexpr long NN = (long)N * N;
+  static_assert(NN % RL == 0, "a tile must not straddle two items");
+  __shared__ float2 tw[N];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  extern __shared__ __align__(16) float stg[];  // 2 x [RL][NP]
+  load_full_twiddles<N>(tw);
+  int line, lane;
+  thread_map<N, LINES, true>(line, lane);
+  const long n_tiles = (n_lines + RL - 1) / RL;
+  const float *src = pre.stream_src();
+  auto stage = [&](long t, float *buf) {
+    const long lt = t * RL;
+    const int nl = (int)min((long)RL, n_lines - lt);
+    for (int c = threadIdx.x; c < nl * (N / 4); c += blockDim.x) {
+      const int r = c / (N / 4), q = c - r * (N / 4);
+      cp_async16(buf + r * NP + 4 * q, src + (lt + r) * N + 4 * q);
+    }
+    cp_async_commit();
+  };
+  long t = blockIdx.x;
+  if (t < n_tiles) stage(t, stg);
+  for (int it = 0; t < n_tiles; ++it, t += gridDim.x) {
+    const float *cur = stg + (it & 1) * (RL * NP);
+    if (t + gridDim.x < n_tiles) {
+      stage(t + gridDim.x, stg + ((it + 1) & 1) * (RL * NP));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const long l_base = t * RL;
+    const long l0 = l_base + 2 * line;
+    const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
+    float2 v[A], o[B];
+    pre.begin();
+    if (lane < B) {
+#pragma unroll
+      for (int j1 = 0; j1 < A; ++j1) {
+        const int k = B * j1 + lane;
+        const float a = ok0 ? pre.apply(l0, k, cur[(2 * line) * NP + k]) : 0.f;
+        const float b = ok1 ? pre.apply(l0 + 1, k, cur[(2 * line + 1) * NP + k]) : 0.f;
+        v[j1] = make_float2(a, b);
+      }
+    }
+    pre.end_tile(l_base);
+    __syncthreads();
+    four_step<N, LINES>(v, o, line, lane, -1, tw, ex);
+    __syncthreads();
+    if (lane < A) {
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+      const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
+      const long l = l_base + rl;
+      if (l < n_lines) {
+        const float2 zk = ex[k * (LINES + 1) + cl];
+        const float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + cl];
+        const float2 xv = (rl & 1) ? make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x))
+                                   : make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+        out[(l / NN) * H * NN + (long)k * NN + (l % NN)] = xv;
+      }
+    }
+    __syncthreads();  // ex and this half of the buffer are reused by the next tiles
+  }
+}
+template <int N>
+constexpr size_t r2c_stream_smem() { return 2 * (size_t)(2 * (256 / MaxAB<N>::v)) * stream_pitch<N>() * sizeof(float); }
+
 // Complex-to-real pass along the contiguous axis (two half spectra -> one packed complex inverse). The
 // kz-major input is staged in shared memory [kz][line] with consecutive threads loading consecutive lines.
 template <int N, int LINES, class Post>
@@ -296,6 +385,82 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   }
   post.end();
 }
+
+// Persistent form of k_c2r_reg: tiles of 2*LINES lines, the next tile's H kz rows (each one contiguous run of
+// 2*LINES complex values of the kz-major input) copied by cp.async into the other half of a double buffer.
+template <int N, int LINES, class Post>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_c2r_stream(const float2 *__restrict__ in, Post post, long n_lines) {
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES, HP = RL + 2;
+  constexpr long NN = (long)N * N;
+  static_assert(NN % RL == 0, "a tile must not straddle two items");
+  __shared__ float2 tw[N];
+  __shared__ float2 ex[A * B * (LINES + 1)];
+  extern __shared__ __align__(16) float2 hsb[];  // 2 x [H][HP]
+  load_full_twiddles<N>(tw);
+  const long n_tiles = (n_lines + RL - 1) / RL;
+  auto stage = [&](long t, float2 *buf) {
+    const long lt = t * RL;
+    const int nl = (int)min((long)RL, n_lines - lt);  // even: lines come in item planes of N*N
+    const float2 *base = in + (lt / NN) * H * NN + (lt % NN);
+    for (int c = threadIdx.x; c < H * (nl / 2); c += blockDim.x) {
+      const int k = c / (nl / 2), q = c - k * (nl / 2);
+      cp_async16(buf + k * HP + 2 * q, base + (long)k * NN + 2 * q);
+    }
+    cp_async_commit();
+  };
+  int line, lane;
+  thread_map<N, LINES, true>(line, lane);
+  long t = blockIdx.x;
+  if (t < n_tiles) stage(t, hsb);
+  for (int it = 0; t < n_tiles; ++it, t += gridDim.x) {
+    const float2 *hs = hsb + (it & 1) * (H * HP);
+    if (t + gridDim.x < n_tiles) {
+      stage(t + gridDim.x, hsb + ((it + 1) & 1) * (H * HP));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const long l0 = t * RL + 2 * line;
+    const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
+    float2 v[A], o[B];
+    if (lane < B) {
+#pragma unroll
+      for (int j1 = 0; j1 < A; ++j1) {
+        int k = B * j1 + lane;
+        float2 a, b;
+        const int kk = k <= N / 2 ? k : N - k;
+        const float4 ab = *reinterpret_cast<const float4 *>(&hs[kk * HP + 2 * line]);
+        a = make_float2(ab.x, ab.y);
+        b = make_float2(ab.z, ab.w);
+        if (k == 0 || k == N / 2) {
+          a.y = 0.f;
+          b.y = 0.f;
+        } else if (k > N / 2) {
+          a = cconj(a);
+          b = cconj(b);
+        }
+        v[j1] = make_float2(a.x - b.y, a.y + b.x);
+      }
+    }
+    __syncthreads();
+    four_step<N, LINES>(v, o, line, lane, +1, tw, ex);
+    post.begin();
+    if (lane < A) {
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) {
+        int k = lane + A * k2;
+        if (ok0) post(l0, k, o[k2].x);
+        if (ok1) post(l0 + 1, k, o[k2].y);
+      }
+    }
+    post.end();
+    __syncthreads();  // ex and this half of the buffer are reused by the next tiles
+  }
+}
+template <int N>
+constexpr size_t c2r_stream_smem() { return 2 * (size_t)(N / 2 + 1) * (2 * (256 / MaxAB<N>::v) + 2) * sizeof(float2); }
 
 // Lines of a pruned, zero-padded inverse transform: line l = outer * inner_n + inner reads n_in complex
 // inputs at in + outer * in_outer + (inner / in_div) * in_mid + inner % in_div + n * in_stride and writes

@@ -414,24 +414,27 @@ struct PreY1M1 {
   long lines_per_block = 0;  // real lines handled by one CTA (never straddles two items)
   // per-thread cache of the in-item row of the two real lines a thread alternates between (slot = line & 1)
   long cl[2] = {-1, -1}, cr[2] = {0, 0};
+  static constexpr bool kStream = true;
+  ETTK_HD const float *stream_src() const { return y; }
   ETTK_DEV void begin() { s = 0.f; }
-  ETTK_DEV float operator()(long line, int k) {
+  ETTK_DEV float apply(long line, int k, float v) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       cl[sl] = line;
       cr[sl] = line % ((long)N * N);
     }
-    float v = y[line * N + k];
     float m = m1[cr[sl] * N + k];
     s += v * v * m;
     return v * m;
   }
-  ETTK_DEV void end() {
+  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k]); }
+  ETTK_DEV void end() { flush(((long)blockIdx.x * lines_per_block) / ((long)N * N)); }
+  ETTK_DEV void end_tile(long first_line) { flush(first_line / ((long)N * N)); }
+  ETTK_DEV void flush(long item) {
     __shared__ double shm[32];
     double b = block_sum((double)s, shm);
-    if (threadIdx.x == 0) atomicAdd(&acc[item_of_block() * acc_stride + slot], b);
+    if (threadIdx.x == 0) atomicAdd(&acc[item * acc_stride + slot], b);
   }
-  ETTK_DEV long item_of_block() const { return ((long)blockIdx.x * lines_per_block) / ((long)N * N); }
 };
 
 // Resliced particle: (valid ? v - meanInside : 0) * maskfft * shift
@@ -447,9 +450,13 @@ struct PreParticle {
   long cl[2] = {-1, -1};
   int cr[2] = {0, 0}, cij[2] = {0, 0};
   float cmean[2] = {0.f, 0.f};
+  static constexpr bool kStream = true;
+  ETTK_HD const float *stream_src() const { return v; }
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
-  ETTK_DEV float operator()(long line, int k) {
+  ETTK_DEV void end_tile(long) {}
+  ETTK_DEV float operator()(long line, int k) { return apply(line, k, v[line * N + k]); }
+  ETTK_DEV float apply(long line, int k, float val) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       long n2 = (long)N * N;
@@ -464,7 +471,6 @@ struct PreParticle {
       }
       cmean[sl] = mean;
     }
-    float val = v[line * N + k];
     float out = (val > -FLT_MAX) ? val - cmean[sl] : 0.f;
     float m = maskfft ? maskfft[(long)cr[sl] * N + k] : 1.f;
     return out * m * (((cij[sl] + k) & 1) ? -1.f : 1.f);
@@ -477,16 +483,19 @@ struct PreSquareShift {
   int N;
   long cl[2] = {-1, -1};  // two-slot line cache (slot = line & 1)
   int cij[2] = {0, 0};
+  static constexpr bool kStream = true;
+  ETTK_HD const float *stream_src() const { return y; }
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
-  ETTK_DEV float operator()(long line, int k) {
+  ETTK_DEV void end_tile(long) {}
+  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k]); }
+  ETTK_DEV float apply(long line, int k, float v) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       cl[sl] = line;
       int r = (int)(line % ((long)N * N));
       cij[sl] = r / N + r % N;
     }
-    float v = y[line * N + k];
     return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
