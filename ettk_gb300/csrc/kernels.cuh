@@ -28,13 +28,16 @@ struct ResliceItem {
 // border of the reference, exact because the x extent is a multiple of 4). For a rotation the footprint is
 // at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned volumes)
 // read the taps from global memory. A copy that does not complete sets *status (the host reports a
-// timeout) instead of waiting forever.
+// timeout) instead of waiting forever. The 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block, whose
+// rotated taps spread over more banks than a 1 x 4 x 8 row; the brick's outputs go through a small shared
+// buffer so that the stores are whole 32-byte rows.
 constexpr int RB = 8;             // brick edge
-constexpr int RS_MAX = 10080;     // staged floats (39.4 KiB of dynamic shared memory, five CTAs per SM)
+constexpr int RS_MAX = 11760;     // staged floats (45.9 KiB of dynamic shared memory, four CTAs per SM)
 constexpr size_t RS_SMEM = RS_MAX * sizeof(float);
-// Fixed box of the bulk tensor copy: it holds the footprint of any rotated brick (x from a multiple of 4);
-// 21 rows per plane keep the plane pitch (24 * 21 floats) off a multiple of the 32 banks
-constexpr int RT_X = 24, RT_Y = 21, RT_Z = 20;
+// Fixed box of the bulk tensor copy: it holds the footprint of any rotated brick (x from a multiple of 4).
+// The row pitch of 28 floats (-4 mod 32 banks) and plane pitch of 28 * 21 (12 mod 32) spread the taps of a
+// warp's voxels over the banks (about a third fewer shared-memory wavefronts than 24-float rows)
+constexpr int RT_X = 28, RT_Y = 21, RT_Z = 20;
 static_assert(RT_X * RT_Y * RT_Z <= RS_MAX, "tensor box exceeds the staging buffer");
 constexpr int RT_WAIT = 1 << 22;  // polls of the copy barrier before the kernel reports a timeout
 
@@ -64,7 +67,7 @@ static __device__ __noinline__ float tricubic_global(const float *__restrict__ v
 // matters); otherwise the same sequence runs in FP32.
 // CLAMP_ALL: every voxel takes the clamped tricubic value (no -max background), for the continuous refinement.
 template <bool PRECISE, bool CLAMP_ALL = false>
-__global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
+__global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
                                                           float *__restrict__ out, double *acc, int acc_stride,
                                                           int *status, const int *__restrict__ item_index) {
   extern __shared__ __align__(128) float4 box4[];
@@ -72,6 +75,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
   __shared__ double sh[32];
   __shared__ int geo[6];  // o[3], ext[3]
   __shared__ __align__(8) unsigned long long tma_bar;
+  __shared__ float obuf[RB * 66];  // brick outputs at a*66 + b*8 + c (conflict-free for both voxel maps)
   const int eidx = item_index ? item_index[blockIdx.y] : (int)blockIdx.y;  // item resliced by this CTA row
   const ResliceItem &it = items[eidx];
   const int nb = N / RB;
@@ -148,7 +152,9 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
   int cnt = 0;
 #pragma unroll 1
   for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
-    const int a = bx * RB + v / (RB * RB), b = by * RB + (v / RB) % RB, cz = bz * RB + v % RB;
+    const int w = v >> 5, ln = v & 31;
+    const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
+    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
     bool inside;
     int ix, iy, iz;
     float fx, fy, fz;
@@ -211,7 +217,12 @@ __global__ void __launch_bounds__(256, PRECISE ? 4 : 5) k_reslice_brick(const Re
       s += val;
       cnt += 1;
     }
-    out[(long)eidx * n3 + ((long)a * N + b) * N + cz] = val;
+    obuf[la * 66 + lb * 8 + lc] = val;
+  }
+  __syncthreads();
+  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
+    const int la = v >> 6, lb = (v >> 3) & 7, lc = v & 7;
+    out[(long)eidx * n3 + ((long)(bx * RB + la) * N + (by * RB + lb)) * N + bz * RB + lc] = obuf[la * 66 + lb * 8 + lc];
   }
   if (acc) {
     double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
