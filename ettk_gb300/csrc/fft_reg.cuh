@@ -89,8 +89,11 @@ ETTK_DEV void load_full_twiddles(float2 *tw) {
 }
 
 // Core: thread (line, lane) with lane < B holds x[B*j1 + lane] (j1 < A) in `v`; after the call the
-// thread with lane < A holds X[lane + A*k2] (k2 < B) in `o`. ex is the CTA exchange buffer
-// [A*B][LINES+1] (index (k1*B + j2)*(LINES+1) + line; the pad keeps lane-strided accesses off one bank).
+// thread with lane < A holds X[lane + A*k2] (k2 < B) in `o`. ex is the CTA exchange buffer: row
+// r = k1*B + j2 of line `line` at r*P + (r/B)*Q + line. Adjacent lines in a warp (the line-major thread map)
+// take P = LINES+1, Q = 0; adjacent lanes (CONTIG) take P = 17*LINES/16, Q = LINES/16, which keeps both the
+// lane-strided writes (rows k1*B + lane) and reads (rows lane*B + j2) of a half-warp on distinct 8-byte bank
+// pairs (a search over P, Q of the 64-bit half-warp conflict count gives these as minimal).
 template <int N>
 struct MaxAB {
   static const int v = (Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B;
@@ -107,23 +110,35 @@ ETTK_DEV void thread_map(int &line, int &lane) {
     lane = threadIdx.x / LINES;
   }
 }
-template <int N, int LINES>
+template <int LINES, bool CONTIG>
+struct ExPitch {
+  static constexpr int P = CONTIG ? LINES + LINES / 16 : LINES + 1, Q = CONTIG ? LINES / 16 : 0;
+};
+// float2 elements of the exchange buffer: the four-step layout, and the [A*B][LINES+1] spectra the r2c
+// passes stage in the same buffer afterwards
+template <int N, int LINES, bool CONTIG>
+__host__ __device__ constexpr int ex_size() {
+  constexpr int A = Split<N>::A, B = Split<N>::B;
+  constexpr int fs = A * B * ExPitch<LINES, CONTIG>::P + A * ExPitch<LINES, CONTIG>::Q;
+  return fs > A * B * (LINES + 1) ? fs : A * B * (LINES + 1);
+}
+template <int N, int LINES, bool CONTIG>
 ETTK_DEV void four_step(float2 (&v)[Split<N>::A], float2 (&o)[Split<N>::B], int line, int lane, int sign,
                         const float2 *tw, float2 *ex) {
-  constexpr int A = Split<N>::A, B = Split<N>::B;
+  constexpr int A = Split<N>::A, B = Split<N>::B, P = ExPitch<LINES, CONTIG>::P, Q = ExPitch<LINES, CONTIG>::Q;
   if (lane < B) {
     dft_reg<A>(v, sign);
 #pragma unroll
     for (int k1 = 0; k1 < A; ++k1) {
       float2 w = twid<N>(tw, lane * k1, sign);
       float2 t = v[k1];
-      ex[(k1 * B + lane) * (LINES + 1) + line] = make_float2(t.x * w.x - t.y * w.y, t.x * w.y + t.y * w.x);
+      ex[(k1 * B + lane) * P + k1 * Q + line] = make_float2(t.x * w.x - t.y * w.y, t.x * w.y + t.y * w.x);
     }
   }
   __syncthreads();
   if (lane < A) {
 #pragma unroll
-    for (int j2 = 0; j2 < B; ++j2) o[j2] = ex[(lane * B + j2) * (LINES + 1) + line];
+    for (int j2 = 0; j2 < B; ++j2) o[j2] = ex[(lane * B + j2) * P + lane * Q + line];
     dft_reg<B>(o, sign);
   }
 }
@@ -134,7 +149,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     k_fft_reg(float2 *__restrict__ data, LineMap map, int sign, const float *__restrict__ line_scale, long scale_div) {
   constexpr int A = Split<N>::A, B = Split<N>::B;
   __shared__ float2 tw[N];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<N, LINES, CONTIG>()];
   load_full_twiddles<N>(tw);
   int line, lane;
   thread_map<N, LINES, CONTIG>(line, lane);
@@ -152,7 +167,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     }
   }
   __syncthreads();
-  four_step<N, LINES>(v, o, line, lane, sign, tw, ex);
+  four_step<N, LINES, CONTIG>(v, o, line, lane, sign, tw, ex);
   if (lane < A && ok) {
 #pragma unroll
     for (int k2 = 0; k2 < B; ++k2) data[base + (long)(lane + A * k2) * map.elem_stride] = o[k2];
@@ -174,9 +189,10 @@ template <int N, int LINES, class Pre>
 __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
     k_r2c_reg(Pre pre, float2 *__restrict__ out, long n_lines) {
   constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES;
+  constexpr int SP = ExPitch<LINES, true>::P;  // pitch of the staged spectra [k][line] (conflict-free rows)
   constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<N, LINES, true>()];
   const long l_base = (long)blockIdx.x * RL;
   if constexpr (has_pad_lines<Pre>::value) {
     // a CTA whose lines are all padding lines writes their spectra directly: the N-point transform of
@@ -216,20 +232,20 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   }
   pre.end();
   __syncthreads();
-  four_step<N, LINES>(v, o, line, lane, -1, tw, ex);
+  four_step<N, LINES, true>(v, o, line, lane, -1, tw, ex);
   __syncthreads();
   // full spectrum of the packed line back into the exchange buffer, [k][LINES]
   if (lane < A) {
 #pragma unroll
-    for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
+    for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * SP + line] = o[k2];
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
     const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
     const long l = l_base + rl;
     if (l < n_lines) {
-      const float2 zk = ex[k * (LINES + 1) + cl];
-      const float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + cl];
+      const float2 zk = ex[k * SP + cl];
+      const float2 zn = ex[((N - k) & (N - 1)) * SP + cl];
       const float2 xv = (rl & 1) ? make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x))
                                  : make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
       out[(l / NN) * H * NN + (long)k * NN + (l % NN)] = xv;
@@ -256,10 +272,11 @@ template <int N, int LINES, class Pre>
 __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
     k_r2c_stream(Pre pre, float2 *__restrict__ out, long n_lines) {
   constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES, NP = stream_pitch<N>();
+  constexpr int SP = ExPitch<LINES, true>::P;  // pitch of the staged spectra [k][line] (conflict-free rows)
   constexpr long NN = (long)N * N;
   static_assert(NN % RL == 0, "a tile must not straddle two items");
   __shared__ float2 tw[N];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<N, LINES, true>()];
   extern __shared__ __align__(16) float stg[];  // 2 x [RL][NP]
   load_full_twiddles<N>(tw);
   int line, lane;
@@ -302,19 +319,19 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     }
     pre.end_tile(l_base);
     __syncthreads();
-    four_step<N, LINES>(v, o, line, lane, -1, tw, ex);
+    four_step<N, LINES, true>(v, o, line, lane, -1, tw, ex);
     __syncthreads();
     if (lane < A) {
 #pragma unroll
-      for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * (LINES + 1) + line] = o[k2];
+      for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * SP + line] = o[k2];
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
       const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
       const long l = l_base + rl;
       if (l < n_lines) {
-        const float2 zk = ex[k * (LINES + 1) + cl];
-        const float2 zn = ex[((N - k) & (N - 1)) * (LINES + 1) + cl];
+        const float2 zk = ex[k * SP + cl];
+        const float2 zn = ex[((N - k) & (N - 1)) * SP + cl];
         const float2 xv = (rl & 1) ? make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x))
                                    : make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
         out[(l / NN) * H * NN + (long)k * NN + (l % NN)] = xv;
@@ -334,7 +351,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES;
   constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<N, LINES, true>()];
   // row pitch of the staged spectra: even (16-byte reads of the two packed lines) and 2 (mod 16) complex
   // values, so that the 8 k rows read by the lanes of one line cover all banks once
   constexpr int HP = RL + 2;
@@ -373,7 +390,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     }
   }
   __syncthreads();
-  four_step<N, LINES>(v, o, line, lane, +1, tw, ex);
+  four_step<N, LINES, true>(v, o, line, lane, +1, tw, ex);
   post.begin();
   if (lane < A) {
 #pragma unroll
@@ -395,7 +412,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   constexpr long NN = (long)N * N;
   static_assert(NN % RL == 0, "a tile must not straddle two items");
   __shared__ float2 tw[N];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<N, LINES, true>()];
   extern __shared__ __align__(16) float2 hsb[];  // 2 x [H][HP]
   load_full_twiddles<N>(tw);
   const long n_tiles = (n_lines + RL - 1) / RL;
@@ -445,7 +462,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
       }
     }
     __syncthreads();
-    four_step<N, LINES>(v, o, line, lane, +1, tw, ex);
+    four_step<N, LINES, true>(v, o, line, lane, +1, tw, ex);
     post.begin();
     if (lane < A) {
 #pragma unroll
@@ -479,7 +496,7 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
                  int off) {
   constexpr int A = Split<NN>::A, B = Split<NN>::B;
   __shared__ float2 tw[NN];
-  __shared__ float2 ex[A * B * (LINES + 1)];
+  __shared__ float2 ex[ex_size<NN, LINES, CONTIG>()];
   load_full_twiddles<NN>(tw);
   int line, lane;
   thread_map<NN, LINES, CONTIG>(line, lane);
@@ -498,7 +515,7 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
     }
   }
   __syncthreads();
-  four_step<NN, LINES>(v, o, line, lane, +1, tw, ex);
+  four_step<NN, LINES, CONTIG>(v, o, line, lane, +1, tw, ex);
   if (lane < A && ok) {
 #pragma unroll
     for (int k2 = 0; k2 < B; ++k2) {
