@@ -110,6 +110,9 @@ ETTK_DEV bool mbar_wait(void *bar, uint32_t parity, int max_iter) {
   }
   return false;
 }
+// Orders this thread's earlier generic-proxy accesses of shared memory before later async-proxy (bulk copy)
+// writes to it.
+ETTK_DEV void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // 3-D tile load of a tensor map (global memory) into shared memory, completing on bar. The innermost
 // coordinate x must be a multiple of 16 bytes / element size; dst 128-byte aligned.
 ETTK_DEV void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, void *bar) {

@@ -531,6 +531,18 @@ struct ettk_ctx {
     ++launches;
     CK(cudaGetLastError());
   }
+  // Tricubic reslice of n_items items (device array `items_dev`, optionally through item_index) into
+  // out[item][a][b][c], with the valid-value sums into acc (k_reslice_brick, one 8^3 brick per CTA)
+  void reslice(const ResliceItem *items_dev, float *out, double *acc_, int acc_stride, const int *item_index,
+               long n_items, bool clamp_all = false) {
+    if (n_items <= 0) return;
+    const dim3 grid((N / RB) * (N / RB) * (N / RB), (unsigned)n_items);
+    if (clamp_all)
+      k_reslice_brick<false, true><<<grid, 256, RS_SMEM, st>>>(items_dev, N, out, acc_, acc_stride, status.p, item_index);
+    else
+      k_reslice_brick<false><<<grid, 256, RS_SMEM, st>>>(items_dev, N, out, acc_, acc_stride, status.p, item_index);
+    post_launch();
+  }
 
   // wedge * filter of E evaluations (missing-wedge compensation), rolling-window kernel
   template <int NN>
@@ -871,9 +883,7 @@ void ettk_ctx::refine_eval(const std::vector<std::array<double, 12>> &maps, cons
   {
     Scope sc(this, "reslice", 8.0 * E * n3);
     // clamped values everywhere: rho stays smooth when a shift moves the window past the fixed image's edge
-    k_reslice_brick<false, true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(
-        w_items.p, N, w_v.p, w_acc.p, 2, status.p, nullptr);
-    post_launch();
+    reslice(w_items.p, w_v.p, w_acc.p, 2, nullptr, E, true);
   }
   // g = K u, u = valid (r - mean) maskfft shift
   auto filtered = [&](auto pre) {
@@ -1201,9 +1211,8 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
     Scope sc(this, "reslice", 8.0 * P * n3);
-    k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), P), 256, RS_SMEM, st>>>(w_items.p, N, sp_v.p, sp_acc.p, 4, status.p, nullptr);
+    reslice(w_items.p, sp_v.p, sp_acc.p, 4, nullptr, P);
   }
-  post_launch();
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
   post_launch();
   PrePadded pre{sp_v.p, mask.p, sp_acc.p, 4, N};
@@ -1381,16 +1390,13 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     CK(cudaMemcpyAsync(w_ridx.p, direct.data(), direct.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!mirrors.empty())
       CK(cudaMemcpyAsync(w_mpairs.p, mirrors.data(), mirrors.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    if (!direct.empty())
-      k_reslice_brick<false><<<dim3((N / RB) * (N / RB) * (N / RB), (unsigned)direct.size()), 256, RS_SMEM, st>>>(
-          w_items.p, N, w_v.p, acc2, ACC, status.p, w_ridx.p);
+    reslice(w_items.p, w_v.p, acc2, ACC, w_ridx.p, (long)direct.size());
     if (!mirrors.empty()) {
-      post_launch();
       k_reslice_mirror<<<dim3(nblocks<int>(n3, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
           w_items.p, w_mpairs.p, N, w_v.p, acc2, ACC);
+      post_launch();
     }
   }
-  post_launch();
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
   r2c_z(N, pp, w_cB.p, E * N * N);
   with_n(N, [&](auto nn) {
@@ -2157,9 +2163,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->w_items.ensure(R);
     CK(cudaMemcpyAsync(c->w_items.p, items.data(), R * sizeof(ResliceItem), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(c->w_acc.p, 0, R * 2 * sizeof(double), c->st));
-    k_reslice_brick<false><<<dim3((c->N / RB) * (c->N / RB) * (c->N / RB), R), 256, RS_SMEM, c->st>>>(c->w_items.p, c->N, c->w_v.p,
-                                                                                          c->w_acc.p, 2, c->status.p, nullptr);
-    c->post_launch();
+    c->reslice(c->w_items.p, c->w_v.p, c->w_acc.p, 2, nullptr, R);
     c->FI1.ensure(R * h3);
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
     c->r2c_z(c->N, pre, c->FI1.p, (long)R * c->N * c->N);

@@ -21,9 +21,12 @@ struct ResliceItem {
 // of valid values and their count into acc[item*acc_stride + 0/1].
 //
 // One 8x8x8 output brick per CTA. The input footprint of the brick (its corner coordinates widened by
-// the cubic support and a rounding margin) is staged in shared memory. When the item has a tensor map and
-// the fixed RT_X x RT_Y x RT_Z box at (x0, o1, o2) lies inside the volume (no clamping needed), one bulk
-// tensor copy (TMA) stages it; otherwise the threads stage it with 16-byte loads: the x range starts at a
+// the cubic support and a rounding margin) is staged in shared memory. A brick whose footprint misses the
+// volume on some axis, or whose corners all lie more than a voxel beyond the valid range on one axis, is
+// background throughout and stages nothing. When the item has a tensor map and the fixed
+// RT_X x RT_Y x RT_Z box at (x0, o1, o2) lies inside the volume and holds the footprint, one bulk tensor copy
+// (TMA) stages it (bricks at the edge of the volume are faster with the tight 16-byte staging below than with
+// a zero-filled box copy and a clamping pass). Otherwise the threads stage it with 16-byte loads: the x range starts at a
 // multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge value (the clamp
 // border of the reference, exact because the x extent is a multiple of 4). For a rotation the footprint is
 // at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned volumes)
@@ -73,7 +76,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   extern __shared__ __align__(128) float4 box4[];
   const float *box = reinterpret_cast<const float *>(box4);
   __shared__ double sh[32];
-  __shared__ int geo[6];  // o[3], ext[3]
+  __shared__ int geo[7];  // o[3], ext[3], mode
   __shared__ __align__(8) unsigned long long tma_bar;
   __shared__ float obuf[RB * 66];  // brick outputs at a*66 + b*8 + c (conflict-free for both voxel maps)
   const int eidx = item_index ? item_index[blockIdx.y] : (int)blockIdx.y;  // item resliced by this CTA row
@@ -100,20 +103,40 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
         lo[t] = fminf(lo[t], __shfl_xor_sync(0xffffffffu, lo[t], off));
         hi[t] = fmaxf(hi[t], __shfl_xor_sync(0xffffffffu, hi[t], off));
       }
-    if (lane == 0)
+    if (lane == 0) {
+      const int d[3] = {dx, dy, dz};
+      int o[3], e[3];
+      bool outside = false;
       for (int t = 0; t < 3; ++t) {
-        int o = (int)floorf(lo[t]) - 2;
-        geo[t] = o;
-        geo[3 + t] = (int)floorf(hi[t]) + 4 - o + 1;  // taps reach floor(p)+1+2; p may exceed hi by rounding
+        o[t] = (int)floorf(lo[t]) - 2;
+        e[t] = (int)floorf(hi[t]) + 4 - o[t] + 1;  // taps reach floor(p)+1+2; p may exceed hi by rounding
+        if (!CLAMP_ALL)
+          outside = outside || o[t] + e[t] <= 0 || o[t] >= d[t] || hi[t] < -1.5f || lo[t] > (float)d[t] + 0.5f;
+        geo[t] = o[t];
+        geo[3 + t] = e[t];
       }
+      const int x0 = o[0] & ~3;
+      int mode = 0;
+      if (outside) mode = 2;
+      else if (it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && x0 >= 0 && x0 + RT_X <= dx && o[1] >= 0 &&
+               o[1] + RT_Y <= dy && o[2] >= 0 && o[2] + RT_Z <= dz && o[0] + e[0] <= x0 + RT_X && e[1] <= RT_Y &&
+               e[2] <= RT_Z)
+        mode = 1;  // the box lies inside the volume: one bulk copy, no clamping
+      geo[6] = mode;
+    }
   }
   __syncthreads();
-  const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5];
+  const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5], mode = geo[6];
+  const long n3 = (long)N * N * N;
+  if (mode == 2) {  // every voxel lies outside the volume: background, nothing staged, nothing summed
+    for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x)
+      out[(long)eidx * n3 + ((long)(bx * RB + (v >> 6)) * N + (by * RB + ((v >> 3) & 7))) * N + bz * RB + (v & 7)] =
+          -FLT_MAX;
+    return;
+  }
   const int x0 = o0 & ~3;                        // floor to a multiple of 4
   const int w4 = (o0 + e0 - x0 + 3) >> 2;        // 16-byte groups per staged row
-  const bool use_tma = it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && x0 >= 0 && x0 + RT_X <= dx && o1 >= 0 &&
-                       o1 + RT_Y <= dy && o2 >= 0 && o2 + RT_Z <= dz && o0 + e0 <= x0 + RT_X && e1 <= RT_Y &&
-                       e2 <= RT_Z;
+  const bool use_tma = mode == 1;
   const int P = use_tma ? RT_X : w4 * 4;         // staged row pitch (floats)
   // staged rows per plane: odd, so that the plane pitch E1 * P is never a multiple of 32 floats (taps that
   // differ only in z would otherwise share a bank)
@@ -147,7 +170,6 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
     }
   }
   __syncthreads();
-  const long n3 = (long)N * N * N;
   float s = 0.f;
   int cnt = 0;
 #pragma unroll 1
