@@ -401,6 +401,7 @@ struct ettk_ctx {
   DevBuf<unsigned long long> w_peak, w_mm;
   DevBuf<ResliceItem> w_items;
   DevBuf<int> w_ridx;     // items resliced directly
+  DevBuf<float> w_faces;  // per slot: faces one step past the reslice box (direct evaluations with a mirror)
   DevBuf<int2> w_mpairs;  // (mirror item, direct item) pairs of a chunk
   // tensor maps of the particle and reference volumes (empty: the reslice stages through the threads)
   DevBuf<CUtensorMap> tm_part, tm_ref;
@@ -1269,6 +1270,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   std::vector<ResliceItem> items(E);
   std::vector<WedgeVecs> wv(E);
   std::vector<int> refidx(E), ord(E), slot_of(E), i1src(E);
+  std::vector<int> direct;
+  std::vector<int2> mirrors;
+  w_faces.ensure(E * 3 * (long)(N + 1) * (N + 1));
   long Dn = 0;
   {
     HostScope hs_prep(this, "host_eval_prep");
@@ -1310,6 +1314,30 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
       items[s] = it;
       wv[s] = wo[e];
       refidx[s] = r.ref;
+    }
+    // mirror evaluations (the request right after its direct one, Scale(-1,-1,-1) * T with T a rotation, no
+    // cut offset) take the direct reslice reversed on every axis plus its faces one step past the box
+    // (k_reslice_mirror); only the others are resliced
+    std::vector<char> is_mirror(E, 0);
+    for (long e = 0; e < E; ++e) {
+      bool mirror = false;
+      if (e > 0 && !is_mirror[e - 1] && req[e].part == req[e - 1].part && partg[req[e].part].cut_offset == 0.f) {
+        const Mat4 &t = req[e - 1].t;
+        if (t.e[3] == 0 && t.e[7] == 0 && t.e[11] == 0) {
+          Mat4 S = Mat4::eye();
+          S.e[0] = S.e[5] = S.e[10] = -1.0;
+          const Mat4 m = mul(S, t);
+          mirror = true;
+          for (int k = 0; k < 16; ++k) mirror = mirror && m.e[k] == req[e].t.e[k];
+        }
+      }
+      is_mirror[e] = mirror;
+      if (mirror) {
+        mirrors.push_back(make_int2(slot_of[e], slot_of[e - 1]));
+        items[slot_of[e - 1]].faces = w_faces.p + (long)slot_of[e - 1] * 3 * (N + 1) * (N + 1);
+      } else {
+        direct.push_back(slot_of[e]);
+      }
     }
   }
   std::unique_ptr<HostScope> hs_launch(new HostScope(this, "host_eval_issue"));
@@ -1363,39 +1391,21 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift), forward (x, y) passes then * fw with the
   // normalisation sums
   {
-    Scope sc(this, "reslice", 8.0 * E * n3);
-    // mirror evaluations (the request right after its direct one, Scale(-1,-1,-1) * T with T a rotation, no cut
-    // offset) take the direct reslice reversed on every axis (k_reslice_mirror); only the others are resliced
-    std::vector<int> direct;
-    std::vector<int2> mirrors;
-    std::vector<char> is_mirror(E, 0);
-    for (long e = 0; e < E; ++e) {
-      bool mirror = false;
-      if (e > 0 && !is_mirror[e - 1] && req[e].part == req[e - 1].part && partg[req[e].part].cut_offset == 0.f) {
-        const Mat4 &t = req[e - 1].t;
-        if (t.e[3] == 0 && t.e[7] == 0 && t.e[11] == 0) {
-          Mat4 S = Mat4::eye();
-          S.e[0] = S.e[5] = S.e[10] = -1.0;
-          const Mat4 m = mul(S, t);
-          mirror = true;
-          for (int k = 0; k < 16; ++k) mirror = mirror && m.e[k] == req[e].t.e[k];
-        }
-      }
-      is_mirror[e] = mirror;
-      if (mirror) mirrors.push_back(make_int2(slot_of[e], slot_of[e - 1]));
-      else direct.push_back(slot_of[e]);
-    }
     w_ridx.ensure(E);
     w_mpairs.ensure(std::max<long>(1, (long)mirrors.size()));
     CK(cudaMemcpyAsync(w_ridx.p, direct.data(), direct.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!mirrors.empty())
       CK(cudaMemcpyAsync(w_mpairs.p, mirrors.data(), mirrors.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+  }
+  {
+    Scope sc(this, "reslice", 8.0 * direct.size() * n3);
     reslice(w_items.p, w_v.p, acc2, ACC, w_ridx.p, (long)direct.size());
-    if (!mirrors.empty()) {
-      k_reslice_mirror<<<dim3(nblocks<int>(n3, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
-          w_items.p, w_mpairs.p, N, w_v.p, acc2, ACC);
-      post_launch();
-    }
+  }
+  if (!mirrors.empty()) {
+    Scope sc(this, "reslice_mirror", 8.0 * mirrors.size() * n3);
+    k_reslice_mirror<<<dim3(nblocks<int>(n3, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
+        w_items.p, w_mpairs.p, N, w_v.p, acc2, ACC);
+    post_launch();
   }
   PreParticle pp{w_v.p, maskfft.p, acc2, ACC, N};
   r2c_z(N, pp, w_cB.p, E * N * N);
@@ -2095,6 +2105,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->dtab64.release();
   c->tomo.release();
   c->w_ridx.release();
+  c->w_faces.release();
   c->w_mpairs.release();
   c->rf_fw.release();
   c->rf_y1.release();

@@ -13,7 +13,15 @@ struct ResliceItem {
   float m[12];   // origin[3], x axis[3], y axis[3], z axis[3]
   double md[12]; // the same in FP64 (used by the exact-coordinate variant)
   const void *tmap = nullptr;  // device tensor map of vol (RT_X x RT_Y x RT_Z float boxes), or null
+  // Optional: the reslice also writes the values one step past the box on each axis (index N), as three
+  // faces [3][(N+1)^2]: face 0 holds a = N at (b, c), face 1 b = N at (a, c), face 2 c = N at (a, b) (a voxel
+  // on several faces is in the first). The mirror evaluation reads them (k_reslice_mirror).
+  float *faces = nullptr;
 };
+__host__ __device__ inline long face_index(int a, int b, int c, int N) {
+  const long F = (long)(N + 1) * (N + 1);
+  return a == N ? (long)b * (N + 1) + c : b == N ? F + (long)a * (N + 1) + c : 2 * F + (long)a * (N + 1) + b;
+}
 
 // nbfWedgedSubImage3D::getImage (inc/em/nbfWedgedSubImage3D.h:602-828): tricubic reslice of the
 // fixed image under Euler*matrix*t into an N^3 box (output [x][y][z], z fastest), background
@@ -86,11 +94,14 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
   const float *vol = it.vol;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // bricks on the last layer of an axis also produce the face one step past the box on that axis
+  const int ea = (it.faces && bx == nb - 1) ? 1 : 0, eb = (it.faces && by == nb - 1) ? 1 : 0,
+            ec = (it.faces && bz == nb - 1) ? 1 : 0;
   if (warp == 0) {
     // footprint of the 8 corners (same affine map as the per-voxel coordinates), lanes 0..7
     const int c8 = lane & 7;
-    const int a = bx * RB + ((c8 & 1) ? RB - 1 : 0), b = by * RB + ((c8 & 2) ? RB - 1 : 0),
-              cz = bz * RB + ((c8 & 4) ? RB - 1 : 0);
+    const int a = bx * RB + ((c8 & 1) ? RB - 1 + ea : 0), b = by * RB + ((c8 & 2) ? RB - 1 + eb : 0),
+              cz = bz * RB + ((c8 & 4) ? RB - 1 + ec : 0);
     float lo[3], hi[3];
     for (int t = 0; t < 3; ++t) {
       float q = it.m[t] + cz * it.m[9 + t];
@@ -128,10 +139,16 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   __syncthreads();
   const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5], mode = geo[6];
   const long n3 = (long)N * N * N;
+  const int nxa = RB + ea, nxb = RB + eb, nxc = RB + ec, n_ext = (ea | eb | ec) ? nxa * nxb * nxc : 0;
   if (mode == 2) {  // every voxel lies outside the volume: background, nothing staged, nothing summed
     for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x)
       out[(long)eidx * n3 + ((long)(bx * RB + (v >> 6)) * N + (by * RB + ((v >> 3) & 7))) * N + bz * RB + (v & 7)] =
           -FLT_MAX;
+    for (int i = threadIdx.x; i < n_ext; i += blockDim.x) {
+      const int la = i / (nxb * nxc), lb = (i / nxc) % nxb, lc = i % nxc;
+      if (la < RB && lb < RB && lc < RB) continue;
+      it.faces[face_index(bx * RB + la, by * RB + lb, bz * RB + lc, N)] = -FLT_MAX;
+    }
     return;
   }
   const int x0 = o0 & ~3;                        // floor to a multiple of 4
@@ -172,12 +189,8 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   __syncthreads();
   float s = 0.f;
   int cnt = 0;
-#pragma unroll 1
-  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
-    const int w = v >> 5, ln = v & 31;
-    const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
-    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
-    bool inside;
+  // tricubic value of output voxel (a, b, cz) from the staged footprint (or global memory); inside: valid
+  auto voxel = [&](int a, int b, int cz, bool &inside) -> float {
     int ix, iy, iz;
     float fx, fy, fz;
     if (PRECISE) {
@@ -236,6 +249,17 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
                                wz[1], wz[2], wz[3]);
       }
       val = acc2;
+    }
+    return val;
+  };
+#pragma unroll 1
+  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
+    const int w = v >> 5, ln = v & 31;
+    const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
+    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
+    bool inside;
+    const float val = voxel(a, b, cz, inside);
+    if (inside) {
       s += val;
       cnt += 1;
     }
@@ -245,6 +269,14 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
     const int la = v >> 6, lb = (v >> 3) & 7, lc = v & 7;
     out[(long)eidx * n3 + ((long)(bx * RB + la) * N + (by * RB + lb)) * N + bz * RB + lc] = obuf[la * 66 + lb * 8 + lc];
+  }
+  // faces one step past the box (not part of this item's output or sums)
+  for (int i = threadIdx.x; i < n_ext; i += blockDim.x) {
+    const int la = i / (nxb * nxc), lb = (i / nxc) % nxb, lc = i % nxc;
+    if (la < RB && lb < RB && lc < RB) continue;
+    bool inside;
+    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
+    it.faces[face_index(a, b, cz, N)] = voxel(a, b, cz, inside);
   }
   if (acc) {
     double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
@@ -273,49 +305,25 @@ struct Smooth3 {
   float w_hi[2];    // at last index: (-1, 0)
 };
 // Mirror evaluations of the candidate loop (the CCF at Scale(-1,-1,-1) * T, execute 678-776): for a pure
-// rotation T and no cut offset, the output index a of the mirror samples the fixed image where index N - a of
-// the direct reslice does (box coordinates a - N/2 are negated), so r'[a][b][c] = r[N-a][N-b][N-c] for indices
-// >= 1; the index-0 planes, whose partner N lies outside the box, are interpolated from the mirror's own map.
-// pairs[y] = (mirror item, direct item); sums of valid values and their count into acc as the reslice.
+// rotation T and no cut offset, output index a of the mirror samples the fixed image where index N - a of
+// the direct reslice does (box coordinates a - N/2 are negated), so r'[a][b][c] = r[N-a][N-b][N-c], with the
+// direct reslice's faces one step past its box (ResliceItem::faces) for the indices N. The positions agree
+// with the mirror's own map to float rounding. pairs[y] = (mirror item, direct item); sums of valid values
+// and their count into acc as the reslice.
 static __global__ void __launch_bounds__(256) k_reslice_mirror(const ResliceItem *__restrict__ items,
                                                                const int2 *__restrict__ pairs, int N,
                                                                float *__restrict__ out, double *acc, int acc_stride) {
   __shared__ double sh[32];
   const int em = pairs[blockIdx.y].x, ed = pairs[blockIdx.y].y;
-  const ResliceItem &it = items[em];
-  const int dx = it.dims[0], dy = it.dims[1], dz = it.dims[2];
   const long n3 = (long)N * N * N;
   const float *src = out + (long)ed * n3;
+  const float *faces = items[ed].faces;
   float *dst = out + (long)em * n3;
   float s = 0.f;
   int cnt = 0;
   for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
-    const int a = id / (N * N), b = (id / N) % N, cz = id % N;
-    float val;
-    if (a > 0 && b > 0 && cz > 0) {
-      val = src[((long)(N - a) * N + (N - b)) * N + (N - cz)];
-    } else {
-      float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
-      p0 = p0 + b * it.m[6];
-      p1 = p1 + b * it.m[7];
-      p2 = p2 + b * it.m[8];
-      p0 = p0 + a * it.m[3];
-      p1 = p1 + a * it.m[4];
-      p2 = p2 + a * it.m[5];
-      val = -FLT_MAX;
-      if (!(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f)) {
-        float fx, fy, fz;
-        const int ix = vtk_floor(p0, fx), iy = vtk_floor(p1, fy), iz = vtk_floor(p2, fz);
-        float wx[4], wy[4], wz[4];
-        cubic_weights(wx, fx);
-        cubic_weights(wy, fy);
-        cubic_weights(wz, fz);
-        if (!((dy > 1) && (fy != 0.f))) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
-        if (!((dz > 1) && (fz != 0.f))) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
-        val = tricubic_global(it.vol, dx, dy, dz, ix, iy, iz, wx[0], wx[1], wx[2], wx[3], wy[0], wy[1], wy[2], wy[3],
-                              wz[0], wz[1], wz[2], wz[3]);
-      }
-    }
+    const int x = N - id / (N * N), y = N - (id / N) % N, z = N - id % N;
+    const float val = (x < N && y < N && z < N) ? src[((long)x * N + y) * N + z] : faces[face_index(x, y, z, N)];
     dst[id] = val;
     if (val > -FLT_MAX) {
       s += val;
