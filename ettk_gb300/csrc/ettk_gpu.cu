@@ -607,10 +607,17 @@ struct ettk_ctx {
     Scope sc(this, "fft_r2c_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
     bool streamed = false;
     if constexpr (has_stream<Pre>::value) {
-      if ((((unsigned long long)pre.stream_src()) & 15) == 0) {
-        constexpr size_t smem = r2c_stream_smem<NN>();
-        const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre>, smem));
-        k_r2c_stream<NN, L, Pre><<<grid, 256, smem, st>>>(pre, out, lines);
+      const unsigned long long sa = (unsigned long long)pre.stream_src(), aa = (unsigned long long)pre.stream_aux();
+      if ((sa & 15) == 0 && (aa & 15) == 0) {
+        if (aa) {
+          constexpr size_t smem = r2c_stream_smem<NN, true>();
+          const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre, true>, smem));
+          k_r2c_stream<NN, L, Pre, true><<<grid, 256, smem, st>>>(pre, out, lines);
+        } else {
+          constexpr size_t smem = r2c_stream_smem<NN, false>();
+          const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre, false>, smem));
+          k_r2c_stream<NN, L, Pre, false><<<grid, 256, smem, st>>>(pre, out, lines);
+        }
         streamed = true;
       }
     }

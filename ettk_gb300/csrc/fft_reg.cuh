@@ -254,8 +254,9 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
 }
 
 // Input functors whose values come from one real N^3 array per item declare kStream, expose the array as
-// stream_src() and compute the input from its element with apply(line, k, raw); end_tile(first line) closes a
-// tile of lines (one item).
+// stream_src() and an optional second operand shared by all items (N^3, same line layout) as stream_aux(),
+// and compute the input from the two elements with apply(line, k, raw, aux) (aux = 1 without an operand);
+// end_tile(first line) closes a tile of lines (one item).
 template <class T, class = void>
 struct has_stream : std::false_type {};
 template <class T>
@@ -268,7 +269,7 @@ __host__ __device__ constexpr int stream_pitch() { return N + 4; }  // staged li
 // (t = blockIdx.x, + gridDim.x, ...); the next tile is copied into the other half of a double buffer
 // (cp.async, 16-byte chunks) while the current one is transformed, so loads stay in flight through the
 // transform and the stores. Tiles never straddle two items (2*LINES divides N*N).
-template <int N, int LINES, class Pre>
+template <int N, int LINES, class Pre, bool AUX>
 __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
     k_r2c_stream(Pre pre, float2 *__restrict__ out, long n_lines) {
   constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES, NP = stream_pitch<N>();
@@ -277,27 +278,38 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   static_assert(NN % RL == 0, "a tile must not straddle two items");
   __shared__ float2 tw[N];
   __shared__ float2 ex[ex_size<N, LINES, true>()];
-  extern __shared__ __align__(16) float stg[];  // 2 x [RL][NP]
+  extern __shared__ __align__(16) float stg[];  // 2 x [RL][NP] (inputs), then with AUX 2 x [RL][NP] (operand)
   load_full_twiddles<N>(tw);
   int line, lane;
   thread_map<N, LINES, true>(line, lane);
   const long n_tiles = (n_lines + RL - 1) / RL;
   const float *src = pre.stream_src();
-  auto stage = [&](long t, float *buf) {
+  const float *aux = pre.stream_aux();
+  auto stage = [&](long t, int half) {
     const long lt = t * RL;
     const int nl = (int)min((long)RL, n_lines - lt);
+    float *buf = stg + half * (RL * NP);
     for (int c = threadIdx.x; c < nl * (N / 4); c += blockDim.x) {
       const int r = c / (N / 4), q = c - r * (N / 4);
       cp_async16(buf + r * NP + 4 * q, src + (lt + r) * N + 4 * q);
     }
+    if (AUX) {
+      float *abuf = stg + (2 + half) * (RL * NP);
+      const float *a0 = aux + (lt % NN) * N;  // the operand's rows of these lines (one item)
+      for (int c = threadIdx.x; c < nl * (N / 4); c += blockDim.x) {
+        const int r = c / (N / 4), q = c - r * (N / 4);
+        cp_async16(abuf + r * NP + 4 * q, a0 + (long)r * N + 4 * q);
+      }
+    }
     cp_async_commit();
   };
   long t = blockIdx.x;
-  if (t < n_tiles) stage(t, stg);
+  if (t < n_tiles) stage(t, 0);
   for (int it = 0; t < n_tiles; ++it, t += gridDim.x) {
     const float *cur = stg + (it & 1) * (RL * NP);
+    const float *acur = stg + (2 + (it & 1)) * (RL * NP);
     if (t + gridDim.x < n_tiles) {
-      stage(t + gridDim.x, stg + ((it + 1) & 1) * (RL * NP));
+      stage(t + gridDim.x, (it + 1) & 1);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
@@ -312,8 +324,9 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
 #pragma unroll
       for (int j1 = 0; j1 < A; ++j1) {
         const int k = B * j1 + lane;
-        const float a = ok0 ? pre.apply(l0, k, cur[(2 * line) * NP + k]) : 0.f;
-        const float b = ok1 ? pre.apply(l0 + 1, k, cur[(2 * line + 1) * NP + k]) : 0.f;
+        const float a = ok0 ? pre.apply(l0, k, cur[(2 * line) * NP + k], AUX ? acur[(2 * line) * NP + k] : 1.f) : 0.f;
+        const float b =
+            ok1 ? pre.apply(l0 + 1, k, cur[(2 * line + 1) * NP + k], AUX ? acur[(2 * line + 1) * NP + k] : 1.f) : 0.f;
         v[j1] = make_float2(a, b);
       }
     }
@@ -340,8 +353,10 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     __syncthreads();  // ex and this half of the buffer are reused by the next tiles
   }
 }
-template <int N>
-constexpr size_t r2c_stream_smem() { return 2 * (size_t)(2 * (256 / MaxAB<N>::v)) * stream_pitch<N>() * sizeof(float); }
+template <int N, bool AUX>
+constexpr size_t r2c_stream_smem() {
+  return (AUX ? 4 : 2) * (size_t)(2 * (256 / MaxAB<N>::v)) * stream_pitch<N>() * sizeof(float);
+}
 
 // Complex-to-real pass along the contiguous axis (two half spectra -> one packed complex inverse). The
 // kz-major input is staged in shared memory [kz][line] with consecutive threads loading consecutive lines.

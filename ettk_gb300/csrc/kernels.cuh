@@ -457,18 +457,20 @@ struct PreY1M1 {
   long cl[2] = {-1, -1}, cr[2] = {0, 0};
   static constexpr bool kStream = true;
   ETTK_HD const float *stream_src() const { return y; }
+  ETTK_HD const float *stream_aux() const { return m1; }
   ETTK_DEV void begin() { s = 0.f; }
-  ETTK_DEV float apply(long line, int k, float v) {
+  ETTK_DEV float apply(long, int, float v, float m) {
+    s += v * v * m;
+    return v * m;
+  }
+  ETTK_DEV float operator()(long line, int k) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       cl[sl] = line;
       cr[sl] = line % ((long)N * N);
     }
-    float m = m1[cr[sl] * N + k];
-    s += v * v * m;
-    return v * m;
+    return apply(line, k, y[line * N + k], m1[cr[sl] * N + k]);
   }
-  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k]); }
   ETTK_DEV void end() { flush(((long)blockIdx.x * lines_per_block) / ((long)N * N)); }
   ETTK_DEV void end_tile(long first_line) { flush(first_line / ((long)N * N)); }
   ETTK_DEV void flush(long item) {
@@ -493,11 +495,15 @@ struct PreParticle {
   float cmean[2] = {0.f, 0.f};
   static constexpr bool kStream = true;
   ETTK_HD const float *stream_src() const { return v; }
+  ETTK_HD const float *stream_aux() const { return maskfft; }
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV void end_tile(long) {}
-  ETTK_DEV float operator()(long line, int k) { return apply(line, k, v[line * N + k]); }
-  ETTK_DEV float apply(long line, int k, float val) {
+  ETTK_DEV float operator()(long line, int k) {
+    const long r = line % ((long)N * N);
+    return apply(line, k, v[line * N + k], maskfft ? maskfft[r * N + k] : 1.f);
+  }
+  ETTK_DEV float apply(long line, int k, float val, float m) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       long n2 = (long)N * N;
@@ -513,7 +519,6 @@ struct PreParticle {
       cmean[sl] = mean;
     }
     float out = (val > -FLT_MAX) ? val - cmean[sl] : 0.f;
-    float m = maskfft ? maskfft[(long)cr[sl] * N + k] : 1.f;
     return out * m * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
@@ -526,11 +531,12 @@ struct PreSquareShift {
   int cij[2] = {0, 0};
   static constexpr bool kStream = true;
   ETTK_HD const float *stream_src() const { return y; }
+  ETTK_HD const float *stream_aux() const { return nullptr; }
   ETTK_DEV void begin() {}
   ETTK_DEV void end() {}
   ETTK_DEV void end_tile(long) {}
-  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k]); }
-  ETTK_DEV float apply(long line, int k, float v) {
+  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k], 1.f); }
+  ETTK_DEV float apply(long line, int k, float v, float) {
     const int sl = (int)(line & 1);
     if (line != cl[sl]) {
       cl[sl] = line;
