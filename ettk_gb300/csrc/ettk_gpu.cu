@@ -687,6 +687,35 @@ struct ettk_ctx {
       default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
     }
   }
+  // C2R, elementwise Mid, R2C of the same z lines in one persistent pass, in place on kz-major spectra
+  template <int NN, class Mid>
+  void c2r_r2c_z_t(float2 *data, Mid mid, long lines) {
+    constexpr int L = reg_lines<NN>();
+    const long tiles = (lines + 2 * L - 1) / (2 * L);
+    Scope sc(this, "fft_c2r_r2c_z", 16.0 * lines * (NN / 2 + 1));
+    if (lines % (2 * L) != 0 || (((unsigned long long)data) & 15) || (((unsigned long long)mid.aux) & 15))
+      throw CudaError(ETTK_ERR_ARG, "fused z pass: lines must fill whole tiles of 16-byte aligned data");
+    if (mid.aux) {
+      constexpr size_t smem = c2r_r2c_stream_smem<NN, true>();
+      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_r2c_stream<NN, L, Mid, true>, smem));
+      k_c2r_r2c_stream<NN, L, Mid, true><<<grid, 256, smem, st>>>(data, mid, lines);
+    } else {
+      constexpr size_t smem = c2r_r2c_stream_smem<NN, false>();
+      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_r2c_stream<NN, L, Mid, false>, smem));
+      k_c2r_r2c_stream<NN, L, Mid, false><<<grid, 256, smem, st>>>(data, mid, lines);
+    }
+    post_launch();
+  }
+  template <class Mid>
+  void c2r_r2c_z(int len, float2 *data, Mid mid, long lines) {
+    switch (len) {
+      case 16: c2r_r2c_z_t<16>(data, mid, lines); break;
+      case 32: c2r_r2c_z_t<32>(data, mid, lines); break;
+      case 64: c2r_r2c_z_t<64>(data, mid, lines); break;
+      case 128: c2r_r2c_z_t<128>(data, mid, lines); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
+    }
+  }
   // (x, y) passes of a 3-D transform of `items` kz-major spectra [len/2+1][len][len]: one CTA per kz plane
   // (k_fft2d) up to len = 128, two strided register passes beyond.
   template <int NN, class Op>
@@ -723,10 +752,12 @@ struct ettk_ctx {
   void init_tables();
   void spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out /*device, items*nn*/);
   void eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> &res);
-  // executeFourierNewHalf for any number of requests, in device chunks of at most 1024 evaluations
+  // executeFourierNewHalf for any number of requests, in device chunks of at most 4096 evaluations at 64^3
+  // (scaled by 64^3 / N^3, 256 to 8192; about 6.4 MB of scratch per 64^3 evaluation): fewer chunks mean
+  // fewer host round trips and larger grids
   void eval_batch(const std::vector<EvalReq> &req, std::vector<EvalRes> &res) {
     res.resize(req.size());
-    const size_t chunk = 1024;
+    const size_t chunk = (size_t)std::min(8192L, std::max(256L, 4096L * 64 * 64 * 64 / n3));
     for (size_t c0 = 0; c0 < req.size(); c0 += chunk) {
       size_t c1 = std::min(req.size(), c0 + chunk);
       std::vector<EvalReq> sub(req.begin() + c0, req.begin() + c1);
@@ -1257,11 +1288,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   w_wv.ensure(E);
   w_idx.ensure(E);
   w_fw.ensure(E * h3);
-  w_tmp.ensure(E * h3);
   w_cA.ensure(E * h3);
   w_cB.ensure(E * h3);
   w_cC.ensure(E * h3);
-  w_r.ensure(E * n3);
   w_v.ensure(E * n3);
   w_acc.ensure(E * ACC * 2);
   w_norm.ensure(E);
@@ -1384,16 +1413,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   });
   k_norms<<<nblocks<int>(Dn, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)Dn, w_norm.p, nullptr);
   post_launch();
-  c2r_z(N, w_cA.p, PostStoreScaled{w_r.p, N, w_norm.p, ilog2((long)N * N)}, Dn * N * N);
-  PreY1M1 py;
-  py.y = w_r.p;
-  py.m1 = mask.p;
-  py.N = N;
-  py.acc = acc;
-  py.acc_stride = ACC;
-  py.slot = 4;
-  py.lines_per_block = lines_per_block(N);
-  r2c_z(N, py, w_cA.p, Dn * N * N);
+  c2r_r2c_z(N, w_cA.p, MidScaleY1M1{w_norm.p, ilog2((long)N * N), mask.p, acc, ACC, 4, N}, Dn * N * N);
   xy_kxy(N, w_cA.p, Dn, -1);
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift), forward (x, y) passes then * fw with the
   // normalisation sums
@@ -1428,8 +1448,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
     constexpr int NN = decltype(nn)::value;
     fft2d_t<NN>(OpFft2reInv<NN>{w_cA.p, i1, w_cC.p, w_cB.p, w_norm2.p}, E, "fft_xy", 32.0);
   });
-  c2r_z(N, w_cB.p, PostStore{w_r.p, N}, E * N * N);
-  r2c_z(N, PreSquareShift{w_r.p, N}, w_cB.p, E * N * N);
+  c2r_r2c_z(N, w_cB.p, MidSquareShift{N}, E * N * N);
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
     fft2d_t<NN>(OpFwdCross<NN>{w_cB.p, Fm1.p, w_cC.p, 8.0f}, E, "fft_xy", 24.0);

@@ -494,6 +494,141 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
 template <int N>
 constexpr size_t c2r_stream_smem() { return 2 * (size_t)(N / 2 + 1) * (2 * (256 / MaxAB<N>::v) + 2) * sizeof(float2); }
 
+// C2R and R2C of the same z lines in one pass: each tile of 2*LINES lines (kz-major half spectra, staged by
+// cp.async into a double buffer as in k_c2r_stream) is transformed back to real lines, Mid maps every real
+// value (and, with AUX, the element of the shared operand Mid::aux, staged beside the input), and the results
+// are transformed forward and stored kz-major over the input (each tile reads all its input before it writes).
+// The real lines pass through the exchange buffer between the two transforms: the intermediate real volume
+// of the unfused passes never reaches HBM. The arithmetic is that of k_c2r_stream + k_r2c_stream.
+template <int N, int LINES>
+__host__ __device__ constexpr int zz_ex_size() {
+  return ex_size<N, LINES, true>() > (2 * LINES * stream_pitch<N>() + 1) / 2 ? ex_size<N, LINES, true>()
+                                                                            : (2 * LINES * stream_pitch<N>() + 1) / 2;
+}
+template <int N, int LINES, class Mid, bool AUX>
+__global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N>::A : Split<N>::B))
+    k_c2r_r2c_stream(float2 *__restrict__ data, Mid mid, long n_lines) {
+  constexpr int A = Split<N>::A, B = Split<N>::B, H = N / 2 + 1, RL = 2 * LINES, HP = RL + 2, NP = stream_pitch<N>();
+  constexpr int SP = ExPitch<LINES, true>::P;
+  constexpr long NN = (long)N * N;
+  static_assert(NN % RL == 0, "a tile must not straddle two items");
+  __shared__ float2 tw[N];
+  __shared__ __align__(16) float2 ex[zz_ex_size<N, LINES>()];
+  extern __shared__ __align__(16) float2 zbuf[];  // 2 x [H][HP] spectra, then with AUX 2 x [RL][NP] floats
+  float *abuf = reinterpret_cast<float *>(zbuf + 2 * H * HP);
+  float *rt = reinterpret_cast<float *>(ex);  // real lines [RL][NP] between the two transforms
+  load_full_twiddles<N>(tw);
+  const long n_tiles = (n_lines + RL - 1) / RL;
+  const float *aux = mid.aux;
+  auto stage = [&](long t, int half) {
+    const long lt = t * RL;
+    const int nl = (int)min((long)RL, n_lines - lt);  // even: lines come in item planes of N*N
+    const float2 *base = data + (lt / NN) * H * NN + (lt % NN);
+    float2 *buf = zbuf + half * (H * HP);
+    for (int c = threadIdx.x; c < H * (nl / 2); c += blockDim.x) {
+      const int k = c / (nl / 2), q = c - k * (nl / 2);
+      cp_async16(buf + k * HP + 2 * q, base + (long)k * NN + 2 * q);
+    }
+    if (AUX) {
+      float *ab = abuf + half * (RL * NP);
+      const float *a0 = aux + (lt % NN) * N;
+      for (int c = threadIdx.x; c < nl * (N / 4); c += blockDim.x) {
+        const int r = c / (N / 4), q = c - r * (N / 4);
+        cp_async16(ab + r * NP + 4 * q, a0 + (long)r * N + 4 * q);
+      }
+    }
+    cp_async_commit();
+  };
+  int line, lane;
+  thread_map<N, LINES, true>(line, lane);
+  long t = blockIdx.x;
+  if (t < n_tiles) stage(t, 0);
+  for (int it = 0; t < n_tiles; ++it, t += gridDim.x) {
+    const float2 *hs = zbuf + (it & 1) * (H * HP);
+    const float *acur = abuf + (it & 1) * (RL * NP);
+    if (t + gridDim.x < n_tiles) {
+      stage(t + gridDim.x, (it + 1) & 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const long l_base = t * RL;
+    const long l0 = l_base + 2 * line;
+    const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
+    // inverse (as k_c2r_stream)
+    float2 v[A], o[B];
+    if (lane < B) {
+#pragma unroll
+      for (int j1 = 0; j1 < A; ++j1) {
+        int k = B * j1 + lane;
+        float2 a, b;
+        const int kk = k <= N / 2 ? k : N - k;
+        const float4 ab = *reinterpret_cast<const float4 *>(&hs[kk * HP + 2 * line]);
+        a = make_float2(ab.x, ab.y);
+        b = make_float2(ab.z, ab.w);
+        if (k == 0 || k == N / 2) {
+          a.y = 0.f;
+          b.y = 0.f;
+        } else if (k > N / 2) {
+          a = cconj(a);
+          b = cconj(b);
+        }
+        v[j1] = make_float2(a.x - b.y, a.y + b.x);
+      }
+    }
+    __syncthreads();
+    four_step<N, LINES, true>(v, o, line, lane, +1, tw, ex);
+    __syncthreads();  // ex is reused for the real lines
+    if (lane < A) {
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) {
+        const int k = lane + A * k2;
+        rt[(2 * line) * NP + k] = o[k2].x;
+        rt[(2 * line + 1) * NP + k] = o[k2].y;
+      }
+    }
+    __syncthreads();
+    // forward (as k_r2c_stream), inputs Mid(real value)
+    mid.begin();
+    if (lane < B) {
+#pragma unroll
+      for (int j1 = 0; j1 < A; ++j1) {
+        const int k = B * j1 + lane;
+        const float a = ok0 ? mid(l0, k, rt[(2 * line) * NP + k], AUX ? acur[(2 * line) * NP + k] : 1.f) : 0.f;
+        const float b = ok1 ? mid(l0 + 1, k, rt[(2 * line + 1) * NP + k], AUX ? acur[(2 * line + 1) * NP + k] : 1.f) : 0.f;
+        v[j1] = make_float2(a, b);
+      }
+    }
+    mid.end_tile(l_base);
+    __syncthreads();
+    four_step<N, LINES, true>(v, o, line, lane, -1, tw, ex);
+    __syncthreads();
+    if (lane < A) {
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) ex[(lane + A * k2) * SP + line] = o[k2];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+      const int k = idx / RL, rl = idx - k * RL, cl = rl >> 1;
+      const long l = l_base + rl;
+      if (l < n_lines) {
+        const float2 zk = ex[k * SP + cl];
+        const float2 zn = ex[((N - k) & (N - 1)) * SP + cl];
+        const float2 xv = (rl & 1) ? make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x))
+                                   : make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+        data[(l / NN) * H * NN + (long)k * NN + (l % NN)] = xv;
+      }
+    }
+    __syncthreads();  // ex and this half of the buffer are reused by the next tiles
+  }
+}
+template <int N, bool AUX>
+constexpr size_t c2r_r2c_stream_smem() {
+  return 2 * (size_t)(N / 2 + 1) * (2 * (256 / MaxAB<N>::v) + 2) * sizeof(float2) +
+         (AUX ? 2 * (size_t)(2 * (256 / MaxAB<N>::v)) * stream_pitch<N>() * sizeof(float) : 0);
+}
+
 // Lines of a pruned, zero-padded inverse transform: line l = outer * inner_n + inner reads n_in complex
 // inputs at in + outer * in_outer + (inner / in_div) * in_mid + inner % in_div + n * in_stride and writes
 // W outputs at out + outer * out_outer + inner + X * out_stride.

@@ -564,6 +564,49 @@ struct PreProductShift {
   }
 };
 
+// Elementwise steps between a C2R and an R2C of the same z lines (k_c2r_r2c_stream). Each maps the real value
+// of the inverse (and the element of `aux`, 1 without one) to the forward input and closes a tile with
+// end_tile(first line).
+// y2^2 * shift (nbfFourierImageMetric.h:1188-1190), as PostStore then PreSquareShift.
+struct MidSquareShift {
+  int N;
+  const float *aux = nullptr;
+  long cl[2] = {-1, -1};  // two-slot line cache (slot = line & 1)
+  int cij[2] = {0, 0};
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end_tile(long) {}
+  ETTK_DEV float operator()(long line, int k, float v, float) {
+    const int sl = (int)(line & 1);
+    if (line != cl[sl]) {
+      cl[sl] = line;
+      int r = (int)(line % ((long)N * N));
+      cij[sl] = r / N + r % N;
+    }
+    return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
+  }
+};
+// (y1 / norm) * m1 with k1_m = sum((y1 / norm)^2 m1) into acc[item][slot] (nbfFourierImageMetric.h:1143-1153), as
+// PostStoreScaled then PreY1M1; aux = m1.
+struct MidScaleY1M1 {
+  const float *scale;
+  int lg_nn;
+  const float *aux;
+  double *acc;
+  int acc_stride, slot, N;
+  float s = 0.f;
+  ETTK_DEV void begin() { s = 0.f; }
+  ETTK_DEV float operator()(long line, int, float v, float m) {
+    const float y = v * scale[line >> lg_nn];
+    s += y * y * m;
+    return y * m;
+  }
+  ETTK_DEV void end_tile(long first_line) {
+    __shared__ double shm[32];
+    double b = block_sum((double)s, shm);
+    if (threadIdx.x == 0) atomicAdd(&acc[(first_line / ((long)N * N)) * acc_stride + slot], b);
+  }
+};
+
 // Store real output of a C2R z-pass.
 struct PostStore {
   float *y;
