@@ -66,7 +66,7 @@ constexpr size_t fft2d_smem() { return (size_t)N * (N + 1) * sizeof(float2); }
 // One CTA per (kz plane, item) = (blockIdx.x, blockIdx.y). Op supplies sign, begin(), load(e, kz, i),
 // store(e, kz, i, x, y, v) and end(e, kz) (all threads call begin/end).
 template <int N, class Op>
-__global__ void __launch_bounds__(256, N <= 64 ? 5 : 1) k_fft2d(Op op) {
+__global__ void __launch_bounds__(256, N <= 64 ? 6 : 1) k_fft2d(Op op) {
   constexpr int G = MaxAB<N>::v;      // lanes per line
   constexpr int GROUPS = 256 / G;     // lines in flight
   constexpr int WG = 32 / G;          // groups per warp

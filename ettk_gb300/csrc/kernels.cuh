@@ -367,7 +367,7 @@ ETTK_DEV float smooth3v(const Smooth3 &sw, float vm, float v0, float vp, int pos
 // along i, multiplied by the reference wedge and the filter, stored, and summed into acc[item][acc_slot]
 // (sum(wedge*filter) of the overlap normalisation). Filter, reference wedges and output are kz-major.
 template <int N, int SLAB>
-__global__ void __launch_bounds__(256) k_wedge_roll(const WedgeVecs *__restrict__ wv, Smooth3 sw,
+__global__ void __launch_bounds__(256, 3) k_wedge_roll(const WedgeVecs *__restrict__ wv, Smooth3 sw,
                                                     const float *__restrict__ w1, const int *__restrict__ w1_index,
                                                     const float *__restrict__ filter, float *__restrict__ out,
                                                     double *acc, int acc_stride, int acc_slot) {
