@@ -1258,9 +1258,17 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
   post_launch();
   r2c_z(N2, pre, sp_F.p, P * N2 * N2);
-  xy_kxy(N2, sp_F.p, P, -1);
-  k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
-  post_launch();
+  // (x, y) passes storing |F| directly (the complex spectrum is not used again)
+  switch (N2) {
+    case 32: fft2d_t<32>(OpPaddedMagnitude<32>{sp_F.p, sp_M.p}, P); break;
+    case 64: fft2d_t<64>(OpPaddedMagnitude<64>{sp_F.p, sp_M.p}, P); break;
+    case 128: fft2d_t<128>(OpPaddedMagnitude<128>{sp_F.p, sp_M.p}, P); break;
+    default: {
+      xy_kxy(N2, sp_F.p, P, -1);
+      k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
+      post_launch();
+    }
+  }
   Scope sc_ss(this, "sphere_sample", 4.0 * P * big_h + 4.0 * P * nn);
   switch (N) {
 #define SS_CASE(NN)                                                                                              \

@@ -59,6 +59,14 @@ ETTK_DEV void group_fft(float2 *line, int stride, int lane, bool act, int sign, 
   __syncwarp();
 }
 
+// Operators whose planes are zero outside a band of rows declare rows(kz, r0, r1): rows x < r0 or x >= r1 of
+// plane kz are zero (not loaded, not transformed along y).
+template <class T, class = void>
+struct has_rows : std::false_type {};
+template <class T>
+struct has_rows<T, std::void_t<decltype(std::declval<const T &>().rows(0, std::declval<int &>(), std::declval<int &>()))>>
+    : std::true_type {};
+
 // Shared memory of k_fft2d: the plane with a row pitch of N+1 complex values.
 template <int N>
 constexpr size_t fft2d_smem() { return (size_t)N * (N + 1) * sizeof(float2); }
@@ -75,10 +83,12 @@ __global__ void __launch_bounds__(256, N <= 64 ? 6 : 1) k_fft2d(Op op) {
   __shared__ float2 tw[N];
   load_full_twiddles<N>(tw);
   const int kz = blockIdx.x, e = blockIdx.y;
+  int rlo = 0, rhi = N;
+  if constexpr (has_rows<Op>::value) op.rows(kz, rlo, rhi);
   op.begin();
   for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
     const int x = i / N, y = i - x * N;
-    pl[x * P + y] = op.load(e, kz, i);
+    pl[x * P + y] = (x >= rlo && x < rhi) ? op.load(e, kz, i) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   // the groups of one warp take lines 8 apart, which puts their rows / columns 16 words apart in the banks
@@ -86,7 +96,7 @@ __global__ void __launch_bounds__(256, N <= 64 ? 6 : 1) k_fft2d(Op op) {
   const int sub = (grp % WG) * (GROUPS / WG) + grp / WG;
   for (int r0 = 0; r0 < N; r0 += GROUPS) {
     const int r = r0 + sub;
-    group_fft<N>(pl + (r < N ? r : 0) * P, 1, lane, r < N, op.sign, tw);
+    group_fft<N>(pl + (r < N ? r : 0) * P, 1, lane, r >= rlo && r < rhi, op.sign, tw);
   }
   __syncthreads();
   for (int c0 = 0; c0 < N; c0 += GROUPS) {
@@ -109,6 +119,30 @@ struct OpPlain {
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N>::at(e, kz, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { d[KXY<N>::at(e, kz, i)] = v; }
+  ETTK_DEV void end(int, int) {}
+};
+
+// Forward (x, y) passes of the (2N)^3 spectrum of the padded spherical-projection volume (z pass done), storing
+// |F| (as the magnitude step of cartesianToSpherical) into a real kz-major array. The padded real volume is
+// the windowed N^3 image at x, y, z < N and the constant c (-1)^(x+y+z) elsewhere (PrePadded); the z transform
+// of a line with x >= N or y >= N is zero except at kz = N, so every plane but the last is zero in rows
+// x >= N.
+template <int N2>
+struct OpPaddedMagnitude {
+  const float2 *d;
+  float *mag;
+  int sign = -1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void rows(int kz, int &r0, int &r1) const {
+    if (kz < KXY<N2>::H - 1) {
+      r0 = 0;
+      r1 = N2 / 2;
+    }
+  }
+  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N2>::at(e, kz, i)]; }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
+    mag[KXY<N2>::at(e, kz, i)] = sqrtf(v.x * v.x + v.y * v.y);
+  }
   ETTK_DEV void end(int, int) {}
 };
 
