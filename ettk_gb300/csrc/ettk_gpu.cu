@@ -395,7 +395,7 @@ struct ettk_ctx {
   std::vector<VolumeGeom> partg;
   std::vector<int> useW2, pp2_ready;
   // work buffers
-  DevBuf<float> w_r, w_v, w_fw, w_tmp, w_tmp2, w_C, w_q1, w_q2, w_sig, w_norm, w_norm2, sp_v, sp_M, sp_padc, sp_Pp;
+  DevBuf<float> w_r, w_v, w_fw, w_tmp, w_C, w_q1, w_q2, w_sig, w_norm, w_norm2, sp_v, sp_M, sp_padc;
   DevBuf<float2> w_cA, w_cB, w_cC, w_p1, w_p2, w_coef, w_S, sp_F;
   DevBuf<double> w_acc, w_w, sp_acc;
   DevBuf<unsigned long long> w_peak, w_mm;
@@ -651,16 +651,6 @@ struct ettk_ctx {
       case 128: r2c_z_t<128>(pre, out, lines); break;
       case 256: r2c_z_t<256>(pre, out, lines); break;
       default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
-    }
-  }
-  // real lines handled by one CTA of the r2c/c2r passes
-  static int lines_per_block(int len) {
-    switch (len) {
-      case 16: return 2 * reg_lines<16>();
-      case 32: return 2 * reg_lines<32>();
-      case 64: return 2 * reg_lines<64>();
-      case 128: return 2 * reg_lines<128>();
-      default: return 2 * reg_lines<256>();
     }
   }
   template <int NN, class Post>
@@ -2125,8 +2115,8 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
                          &c->W1half, &c->Pp1, &c->W1sph, &c->partvol, &c->W2sph, &c->Pp2, &c->w_r, &c->w_v,
-                         &c->w_fw, &c->w_tmp, &c->w_tmp2, &c->w_C, &c->w_q1, &c->w_q2, &c->w_sig, &c->w_norm,
-                         &c->w_norm2, &c->sp_v, &c->sp_M, &c->sp_padc, &c->sp_Pp};
+                         &c->w_fw, &c->w_tmp, &c->w_C, &c->w_q1, &c->w_q2, &c->w_sig, &c->w_norm,
+                         &c->w_norm2, &c->sp_v, &c->sp_M, &c->sp_padc};
   for (auto b : fb) b->release();
   DevBuf<float2> *cb[] = {&c->Fm1, &c->FI1, &c->w_cA, &c->w_cB, &c->w_cC, &c->w_p1, &c->w_p2, &c->w_coef, &c->w_S, &c->sp_F};
   for (auto b : cb) b->release();

@@ -499,7 +499,7 @@ constexpr size_t c2r_stream_smem() { return 2 * (size_t)(N / 2 + 1) * (2 * (256 
 // value (and, with AUX, the element of the shared operand Mid::aux, staged beside the input), and the results
 // are transformed forward and stored kz-major over the input (each tile reads all its input before it writes).
 // The real lines pass through the exchange buffer between the two transforms: the intermediate real volume
-// of the unfused passes never reaches HBM. The arithmetic is that of k_c2r_stream + k_r2c_stream.
+// of two separate passes never reaches HBM. The arithmetic is that of k_c2r_stream followed by k_r2c_stream.
 template <int N, int LINES>
 __host__ __device__ constexpr int zz_ex_size() {
   return ex_size<N, LINES, true>() > (2 * LINES * stream_pitch<N>() + 1) / 2 ? ex_size<N, LINES, true>()

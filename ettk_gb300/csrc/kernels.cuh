@@ -444,42 +444,6 @@ static __global__ void k_norms(const double *acc, int acc_stride, int slot, int 
 
 // ---- R2C z-pass input functors ------------------------------------------------------------
 
-// y1 * m1 with the accumulation k1_m = sum(y1^2 m1) (inc/em/nbfFourierImageMetric.h:1143-1153).
-struct PreY1M1 {
-  const float *y;
-  const float *m1;
-  int N;
-  double *acc;
-  int acc_stride, slot;
-  float s = 0.f;  // per-thread partial (a thread sees at most a few dozen elements); FP64 across threads
-  long lines_per_block = 0;  // real lines handled by one CTA (never straddles two items)
-  // per-thread cache of the in-item row of the two real lines a thread alternates between (slot = line & 1)
-  long cl[2] = {-1, -1}, cr[2] = {0, 0};
-  static constexpr bool kStream = true;
-  ETTK_HD const float *stream_src() const { return y; }
-  ETTK_HD const float *stream_aux() const { return m1; }
-  ETTK_DEV void begin() { s = 0.f; }
-  ETTK_DEV float apply(long, int, float v, float m) {
-    s += v * v * m;
-    return v * m;
-  }
-  ETTK_DEV float operator()(long line, int k) {
-    const int sl = (int)(line & 1);
-    if (line != cl[sl]) {
-      cl[sl] = line;
-      cr[sl] = line % ((long)N * N);
-    }
-    return apply(line, k, y[line * N + k], m1[cr[sl] * N + k]);
-  }
-  ETTK_DEV void end() { flush(((long)blockIdx.x * lines_per_block) / ((long)N * N)); }
-  ETTK_DEV void end_tile(long first_line) { flush(first_line / ((long)N * N)); }
-  ETTK_DEV void flush(long item) {
-    __shared__ double shm[32];
-    double b = block_sum((double)s, shm);
-    if (threadIdx.x == 0) atomicAdd(&acc[item * acc_stride + slot], b);
-  }
-};
-
 // Resliced particle: (valid ? v - meanInside : 0) * maskfft * shift
 // (nbfWedgedSubImage3D.h:794-802 then nbfFourierImageMetric.h:1165-1166).
 struct PreParticle {
@@ -523,30 +487,6 @@ struct PreParticle {
   }
 };
 
-// y2^2 * shift (nbfFourierImageMetric.h:1188-1190)
-struct PreSquareShift {
-  const float *y;
-  int N;
-  long cl[2] = {-1, -1};  // two-slot line cache (slot = line & 1)
-  int cij[2] = {0, 0};
-  static constexpr bool kStream = true;
-  ETTK_HD const float *stream_src() const { return y; }
-  ETTK_HD const float *stream_aux() const { return nullptr; }
-  ETTK_DEV void begin() {}
-  ETTK_DEV void end() {}
-  ETTK_DEV void end_tile(long) {}
-  ETTK_DEV float operator()(long line, int k) { return apply(line, k, y[line * N + k], 1.f); }
-  ETTK_DEV float apply(long line, int k, float v, float) {
-    const int sl = (int)(line & 1);
-    if (line != cl[sl]) {
-      cl[sl] = line;
-      int r = (int)(line % ((long)N * N));
-      cij[sl] = r / N + r % N;
-    }
-    return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
-  }
-};
-
 // Generic: src * aux * shift over one N^3 volume per item (the constant transforms of the
 // reference and of the mask: R2C(I1*maskfft*shift), R2C(m1*shift)).
 struct PreProductShift {
@@ -567,7 +507,7 @@ struct PreProductShift {
 // Elementwise steps between a C2R and an R2C of the same z lines (k_c2r_r2c_stream). Each maps the real value
 // of the inverse (and the element of `aux`, 1 without one) to the forward input and closes a tile with
 // end_tile(first line).
-// y2^2 * shift (nbfFourierImageMetric.h:1188-1190), as PostStore then PreSquareShift.
+// y2^2 * shift (nbfFourierImageMetric.h:1188-1190) of the C2R output y2.
 struct MidSquareShift {
   int N;
   const float *aux = nullptr;
@@ -585,8 +525,8 @@ struct MidSquareShift {
     return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
-// (y1 / norm) * m1 with k1_m = sum((y1 / norm)^2 m1) into acc[item][slot] (nbfFourierImageMetric.h:1143-1153), as
-// PostStoreScaled then PreY1M1; aux = m1.
+// (y1 / norm) * m1 with k1_m = sum((y1 / norm)^2 m1) into acc[item][slot] (nbfFourierImageMetric.h:1143-1153):
+// the C2R output scaled by the item's 1/norm (normalizeFourierHalf, linear through the inverse passes); aux = m1.
 struct MidScaleY1M1 {
   const float *scale;
   int lg_nn;
@@ -615,18 +555,6 @@ struct PostStore {
   ETTK_DEV void end() {}
   ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v; }
 };
-// Same with a per-item scale (the 1/norm of normalizeFourierHalf, linear through the inverse passes);
-// item = line >> lg_nn (N*N lines per item).
-struct PostStoreScaled {
-  float *y;
-  int N;
-  const float *scale;
-  int lg_nn;
-  ETTK_DEV void begin() {}
-  ETTK_DEV void end() {}
-  ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v * scale[line >> lg_nn]; }
-};
-
 // Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
 // [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
 // and reads only this window). Same FFTW order: complex inverse along x, then y (k_pruned_fft, 2N-point
