@@ -1428,7 +1428,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   }
   if (!mirrors.empty()) {
     Scope sc(this, "reslice_mirror", 8.0 * mirrors.size() * n3);
-    k_reslice_mirror<<<dim3(nblocks<int>(n3, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
+    k_reslice_mirror<<<dim3(nblocks<int>(n3 / 4, 256, 64), (unsigned)mirrors.size()), 256, 0, st>>>(
         w_items.p, w_mpairs.p, N, w_v.p, acc2, ACC);
     post_launch();
   }

@@ -321,14 +321,22 @@ static __global__ void __launch_bounds__(256) k_reslice_mirror(const ResliceItem
   float *dst = out + (long)em * n3;
   float s = 0.f;
   int cnt = 0;
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
-    const int x = N - id / (N * N), y = N - (id / N) % N, z = N - id % N;
-    const float val = (x < N && y < N && z < N) ? src[((long)x * N + y) * N + z] : faces[face_index(x, y, z, N)];
-    dst[id] = val;
-    if (val > -FLT_MAX) {
-      s += val;
-      cnt += 1;
+  // one aligned quad of outputs (c = 4j .. 4j+3 of row (a, b)) per thread and step
+  const int nq = (int)(n3 / 4), qrow = N / 4;
+  for (int qd = blockIdx.x * blockDim.x + threadIdx.x; qd < nq; qd += gridDim.x * blockDim.x) {
+    const int row = qd / qrow, c0 = 4 * (qd - row * qrow);
+    const int x = N - row / N, y = N - row % N;
+    float v[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int z = N - (c0 + t);
+      v[t] = (x < N && y < N && z < N) ? src[((long)x * N + y) * N + z] : faces[face_index(x, y, z, N)];
+      if (v[t] > -FLT_MAX) {
+        s += v[t];
+        cnt += 1;
+      }
     }
+    reinterpret_cast<float4 *>(dst)[qd] = make_float4(v[0], v[1], v[2], v[3]);
   }
   const double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
   if (threadIdx.x == 0) {
