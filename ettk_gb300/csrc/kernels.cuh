@@ -976,13 +976,20 @@ static __global__ void k_so3_real(const float2 *__restrict__ S, float *__restric
   const int job = blockIdx.y;
   const float scale = (1.0f / n) * ((float)B / 3.14159265358979f);
   unsigned long long bmax = 0, bmin = 0;
-  for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
-    int a = id / (n * n), b = (id / n) & (n - 1), g = id & (n - 1);
-    float v = S[(((long)job * n + b) * n + a) * n + g].x * scale;
-    C[(long)job * n3 + id] = v;
-    unsigned long long kx = pack_max(v, (uint32_t)id), kn = pack_min(v, (uint32_t)id);
-    bmax = kx > bmax ? kx : bmax;
-    bmin = kn > bmin ? kn : bmin;
+  // four consecutive gamma per thread and step: two 16-byte reads of S, one 16-byte store of C
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)(n3 / 4); q += gridDim.x * blockDim.x) {
+    const int id = 4 * q;
+    const int a = id / (n * n), b = (id / n) & (n - 1), g = id & (n - 1);
+    const float4 *s4 = reinterpret_cast<const float4 *>(S + (((long)job * n + b) * n + a) * n + g);
+    const float4 p0 = s4[0], p1 = s4[1];
+    const float v[4] = {p0.x * scale, p0.z * scale, p1.x * scale, p1.z * scale};
+    reinterpret_cast<float4 *>(C + (long)job * n3)[q] = make_float4(v[0], v[1], v[2], v[3]);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      unsigned long long kx = pack_max(v[t], (uint32_t)(id + t)), kn = pack_min(v[t], (uint32_t)(id + t));
+      bmax = kx > bmax ? kx : bmax;
+      bmin = kn > bmin ? kn : bmin;
+    }
   }
   if (mm) {
     bmax = warp_max_u64(bmax);
