@@ -1523,21 +1523,31 @@ void parallel_for(int n, F f) {
 // eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
 // matrices can be closer than `tol` in L1 are compared (each entry must differ by < tol); visiting only
 // those pairs in increasing j order is equivalent to the reference's full double loop.
-void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
+// mats_in, when given, holds euler_candidate of every entry of pos (as computed by the caller).
+void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol, const std::vector<Mat4> *mats_in = nullptr) {
   size_t K = pos.size();
-  std::vector<Mat4> mats(K);
-  for (size_t i = 0; i < K; ++i) mats[i] = euler_candidate(pos[i].v[0], pos[i].v[1], pos[i].v[2]);
-  // bucket on the third column of the rotation (entries 2, 6, 10)
+  std::vector<Mat4> own;
+  if (!mats_in) {
+    own.resize(K);
+    for (size_t i = 0; i < K; ++i) own[i] = euler_candidate(pos[i].v[0], pos[i].v[1], pos[i].v[2]);
+  }
+  const std::vector<Mat4> &mats = mats_in ? *mats_in : own;
+  // bucket on the third column of the rotation (entries 2, 6, 10): cells in one flat counting-sort table
   double cell = std::max((double)tol, 1e-3);
   int nc = (int)ceil(2.0 / cell) + 3;
   auto key = [&](double v) { return std::min(nc - 1, std::max(0, (int)floor((v + 1.0) / cell) + 1)); };
-  std::vector<std::vector<int>> grid((size_t)nc * nc * nc);
-  std::vector<int> kx(K), ky(K), kz(K);
+  const size_t ncell = (size_t)nc * nc * nc;
+  std::vector<int> kx(K), ky(K), kz(K), start(ncell + 1, 0), members(K);
   for (size_t i = 0; i < K; ++i) {
     kx[i] = key(mats[i].e[2]);
     ky[i] = key(mats[i].e[6]);
     kz[i] = key(mats[i].e[10]);
-    grid[((size_t)kx[i] * nc + ky[i]) * nc + kz[i]].push_back((int)i);
+    ++start[((size_t)kx[i] * nc + ky[i]) * nc + kz[i] + 1];
+  }
+  for (size_t c = 0; c < ncell; ++c) start[c + 1] += start[c];
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (size_t i = 0; i < K; ++i) members[fill[((size_t)kx[i] * nc + ky[i]) * nc + kz[i]]++] = (int)i;
   }
   const float dead = -FLT_MAX;
   std::vector<int> nb;
@@ -1547,7 +1557,8 @@ void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol) {
       for (int b = ky[i] - 1; b <= ky[i] + 1; ++b)
         for (int c = kz[i] - 1; c <= kz[i] + 1; ++c) {
           if (a < 0 || b < 0 || c < 0 || a >= nc || b >= nc || c >= nc) continue;
-          for (int j : grid[((size_t)a * nc + b) * nc + c]) nb.push_back(j);
+          const size_t cc = ((size_t)a * nc + b) * nc + c;
+          for (int m = start[cc]; m < start[cc + 1]; ++m) nb.push_back(members[m]);
         }
     std::sort(nb.begin(), nb.end());
     for (int j : nb) {
@@ -1764,6 +1775,7 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
       std::vector<int2> L(lists.begin() + (long)q * cap, lists.begin() + (long)q * cap + c);
       std::sort(L.begin(), L.end(), [](const int2 &a, const int2 &b) { return a.x < b.x; });
       std::vector<Cand> pos;
+      std::vector<Mat4> mats;
       for (auto &e : L) {
         int a = e.x / (n * n), bb = (e.x / n) % n, g = e.x % n;
         float val = __builtin_bit_cast(float, e.y);
@@ -1771,9 +1783,13 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
         if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
         float gamma = (float)(g / (double)B * 180.0);
-        if (transform_valid(p, euler_candidate(alpha, beta, gamma))) pos.push_back({{alpha, beta, gamma, -val}, -1});
+        const Mat4 m = euler_candidate(alpha, beta, gamma);
+        if (transform_valid(p, m)) {
+          pos.push_back({{alpha, beta, gamma, -val}, -1});
+          mats.push_back(m);
+        }
       }
-      eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f);
+      eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f, &mats);
     };
     parallel_for(2 * P, build_queue);
     }
