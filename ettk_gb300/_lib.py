@@ -58,7 +58,8 @@ SYMBOLS = [
     "ettk_gpu_set_particles_device", "ettk_gpu_align_pairs", "ettk_gpu_ccf", "ettk_gpu_spherical_projection",
     "ettk_gpu_soft", "ettk_gpu_kernel_launches", "ettk_gpu_last_error", "ettk_gpu_stream", "ettk_gpu_profile",
     "ettk_gpu_profile_read", "ettk_gpu_soft_noalloc", "ettk_gpu_average", "ettk_gpu_refine_pairs",
-    "ettk_gpu_refine_objective", "ettk_gpu_classify", "ettk_gpu_set_particles_tomogram",
+    "ettk_gpu_refine_objective", "ettk_gpu_classify", "ettk_gpu_set_particles_tomogram", "ettk_gpu_variance",
+    "ettk_gpu_symmetrize",
 ]
 
 _lib = None
@@ -95,6 +96,8 @@ def load(path=None):
     L.ettk_gpu_refine_pairs.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.ettk_gpu_refine_objective.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_classify.argtypes = [vp, ctypes.c_int, vp, vp, vp]
+    L.ettk_gpu_variance.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
+    L.ettk_gpu_symmetrize.argtypes = [vp, vp, ctypes.c_int, vp]
     L.ettk_gpu_set_particles_tomogram.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                   P(VolumeMeta)]
     L.ettk_gpu_profile_read.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_longlong),

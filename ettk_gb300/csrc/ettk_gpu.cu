@@ -769,6 +769,11 @@ struct ettk_ctx {
                    std::vector<double> &rho, std::vector<double> &g6);
   void refine(const std::vector<EvalReq> &req, int iterations, std::vector<Mat4> &out, std::vector<double> &rho);
   void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
+  void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
+  void symmetrize(const float *vol, int fold, float *out);
+  // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
+  // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
+  void reslice_members(const int *idx, int E, const int *parts, const double *mats);
 };
 
 // Class average (getImageMPI + getImage): members resliced under Euler(normal) * alignment with their
@@ -836,6 +841,110 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
   k_avg_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3, w_tmp.p);
   post_launch();
   CK(cudaMemcpyAsync(avg, w_tmp.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+  check_status();
+}
+
+void ettk_ctx::reslice_members(const int *idx, int E, const int *parts, const double *mats) {
+  std::vector<ResliceItem> items(E);
+  for (int e = 0; e < E; ++e) {
+    const int i = idx[e];
+    VolumeGeom g = partg[parts[i]];
+    for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    Mat4 t;
+    memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
+    double m12[12];
+    reslice_index(g, N, &t, m12);
+    items[e].vol = part_vol(parts[i]);
+    items[e].tmap = part_map(parts[i]);
+    part_dims(items[e].dims);
+    set_map(items[e], m12);
+  }
+  w_items.ensure(E);
+  w_v.ensure((long)E * n3);
+  w_acc.ensure(2L * E);
+  CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
+  Scope sc(this, "reslice", 8.0 * E * n3);
+  k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), E), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p, 2,
+                                                                                      status.p, nullptr);
+  post_launch();
+}
+
+// Variance of the class members about an average (getImageVarianceMPI with setAverageImage): members in
+// chunks, reslices as the average makes them, |w| (T - avg)^2 / sum|w| accumulated per voxel in FP64.
+void ettk_ctx::variance(int M, const int *parts, const float *weights, const double *mats, const float *avg,
+                        float *var) {
+  std::vector<int> idx;
+  double sw = 0;
+  for (int i = 0; i < M; ++i) {
+    if (parts[i] < 0 || parts[i] >= V) throw CudaError(ETTK_ERR_ARG, "member index out of range");
+    sw += fabs((double)weights[i]);
+    if (fabs(weights[i]) > 0) idx.push_back(i);
+  }
+  DevBuf<double> &vacc = w_w;  // reused accumulator
+  vacc.ensure(n3);
+  CK(cudaMemsetAsync(vacc.p, 0, n3 * sizeof(double), st));
+  w_tmp.ensure(n3);
+  CK(cudaMemcpyAsync(w_tmp.p, avg, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
+  const int chunk = 256;
+  for (size_t c0 = 0; c0 < idx.size(); c0 += chunk) {
+    const int E = (int)std::min<size_t>(chunk, idx.size() - c0);
+    reslice_members(idx.data() + c0, E, parts, mats);
+    std::vector<float> w(E);
+    for (int e = 0; e < E; ++e) w[e] = weights[idx[c0 + e]];
+    w_norm.ensure(E);
+    CK(cudaMemcpyAsync(w_norm.p, w.data(), E * sizeof(float), cudaMemcpyHostToDevice, st));
+    k_var_accum<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_v.p, w_acc.p, w_norm.p, E, sw, w_tmp.p, N, vacc.p);
+    post_launch();
+  }
+  w_r.ensure(n3);
+  k_var_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(vacc.p, N, w_r.p);
+  post_launch();
+  CK(cudaMemcpyAsync(var, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+  check_status();
+}
+
+// n-fold symmetrisation about z of a volume taken as a fixed image (position N/2, identity matrix).
+void ettk_ctx::symmetrize(const float *vol, int fold, float *out) {
+  if (fold <= 1) {
+    memcpy(out, vol, n3 * sizeof(float));
+    return;
+  }
+  w_tmp.ensure(n3);
+  CK(cudaMemcpyAsync(w_tmp.p, vol, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
+  VolumeGeom g{};  // fixed image: position N/2, no normal, identity matrix, no cut offset, full wedge
+  g.lwedge = -90.f;
+  g.uwedge = 90.f;
+  for (int k = 0; k < 3; ++k) g.position[k] = (float)(N / 2.0);
+  for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+  std::vector<ResliceItem> items(fold);
+  for (int i = 0; i < fold; ++i) {
+    Mat4 t = Mat4::eye();
+    rotate(t, i * 360.0 / fold, 0, 0, 1);
+    double m12[12];
+    reslice_index(g, N, &t, m12);
+    items[i].vol = w_tmp.p;
+    items[i].tmap = nullptr;
+    items[i].dims[0] = items[i].dims[1] = items[i].dims[2] = N;
+    set_map(items[i], m12);
+  }
+  w_items.ensure(fold);
+  w_v.ensure((long)fold * n3);
+  w_acc.ensure(2L * fold);
+  CK(cudaMemcpyAsync(w_items.p, items.data(), fold * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, 2L * fold * sizeof(double), st));
+  {
+    Scope sc(this, "reslice", 8.0 * fold * n3);
+    k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), fold), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p,
+                                                                                           2, status.p, nullptr);
+    post_launch();
+  }
+  w_r.ensure(n3);
+  k_sym_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_v.p, w_acc.p, fold, N, w_r.p);
+  post_launch();
+  CK(cudaMemcpyAsync(out, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
   sync();
   check_status();
 }
@@ -2478,6 +2587,20 @@ int ettk_gpu_average(ettk_ctx *c, int M, const int *particles, const float *weig
   if (!c || M < 0 || (M && (!particles || !weights || !matrices)) || !avg) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (c->V == 0) return fail(c, ETTK_ERR_STATE, "particles must be set first");
   return guarded(c, [&] { c->average(M, particles, weights, matrices, avg); });
+}
+
+int ettk_gpu_variance(ettk_ctx *c, int M, const int *parts, const float *weights, const double *mats,
+                      const float *avg, float *var) {
+  if (!c || M <= 0 || !parts || !weights || !mats || !avg || !var) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (c->V <= 0) return fail(c, ETTK_ERR_STATE, "no particles");
+  if (!finite_volume(avg, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite average");
+  return guarded(c, [&] { c->variance(M, parts, weights, mats, avg, var); });
+}
+
+int ettk_gpu_symmetrize(ettk_ctx *c, const float *vol, int fold, float *out) {
+  if (!c || !vol || !out || fold < 1 || fold > 360) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
+  return guarded(c, [&] { c->symmetrize(vol, fold, out); });
 }
 
 long long ettk_gpu_kernel_launches(ettk_ctx *c) { return c ? c->launches : 0; }

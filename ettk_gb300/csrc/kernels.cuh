@@ -729,6 +729,51 @@ static __global__ void k_avg_finish(const float *__restrict__ y, int N, const do
   }
 }
 
+// getImage's output of a resliced volume (valid: value - meanInside with meanInside rounded to float as the
+// reference's Pixel; invalid: 0), inc/em/nbfWedgedSubImage3D.h:794-802, in FP64.
+ETTK_DEV double get_image_value(float v, const double *acc) {
+  const float cnt = (float)acc[1];
+  const float mean = (float)(acc[0] / (double)cnt);
+  return (v > -FLT_MAX) ? (double)v - (double)mean : 0.0;
+}
+
+// nbfImageFilter::symmetrize (inc/em/nbfImageFilter.h:527-554): the mean of the fold reslices ([i][x][y][z],
+// sums in acc[i][0..1]) as getImage values, summed in order in FP64, written [z][y][x].
+static __global__ void k_sym_finish(const float *__restrict__ v, const double *__restrict__ acc, int fold, int N,
+                                    float *__restrict__ out) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < fold; ++i) s += get_image_value(v[(long)i * n3 + id], acc + 2 * i);
+    const int x = (int)(id / ((long)N * N)), y = (int)((id / N) % N), z = (int)(id % N);
+    out[x + (long)N * (y + (long)N * z)] = (float)(s / fold);
+  }
+}
+
+// getImageVarianceMPI (inc/em/nbfWedgedAverageImage3D.h:440-493): var[x][y][z] += |w_e| (T_e - avg)^2 / sum|w| over
+// the chunk's members in order (FP64); avg is [z][y][x], the member reslices [e][x][y][z] with sums acc[e][0..1].
+static __global__ void k_var_accum(const float *__restrict__ v, const double *__restrict__ acc, const float *__restrict__ w,
+                                   int n_members, double sw, const float *__restrict__ avg, int N, double *__restrict__ var) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(id / ((long)N * N)), y = (int)((id / N) % N), z = (int)(id % N);
+    const double a = (double)avg[x + (long)N * (y + (long)N * z)];
+    double s = var[id];
+    for (int e = 0; e < n_members; ++e) {
+      const double d = get_image_value(v[(long)e * n3 + id], acc + 2 * e) - a;
+      s += fabs((double)w[e]) * (d * d) / sw;
+    }
+    var[id] = s;
+  }
+}
+static __global__ void k_var_finish(const double *__restrict__ var, int N, float *__restrict__ out) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(id / ((long)N * N)), y = (int)((id / N) % N), z = (int)(id % N);
+    out[x + (long)N * (y + (long)N * z)] = (float)var[id];
+  }
+}
+
 // ---- spherical projection ------------------------------------------------------------------
 
 // mean over all voxels of the mean-subtracted particle (nbfImageFilter::execute meanValue,

@@ -146,6 +146,28 @@ class ProjectionRotationMetric3D:
                                             out.ctypes.data), "average")
         return out
 
+    # -- nbfWedgedAverageImage3D::getImageVarianceMPI / nbfImageFilter::symmetrize -------------------------
+    def variance(self, particles, weights, matrices, avg):
+        """Variance of the members about `avg` ([z][y][x], as average() returns it); returns [z][y][x]."""
+        n = len(particles)
+        N = self.params["N"]
+        idx = np.ascontiguousarray(particles, np.int32)
+        w = np.ascontiguousarray(weights, np.float32)
+        M = np.ascontiguousarray(np.asarray(matrices, np.float64).reshape(n, 16))
+        a = np.ascontiguousarray(avg, np.float32)
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_variance(self._ctx, n, idx.ctypes.data, w.ctypes.data, M.ctypes.data,
+                                             a.ctypes.data, out.ctypes.data), "variance")
+        return out
+
+    def symmetrize(self, vol, fold):
+        """n-fold symmetrisation about z of a [z][y][x] volume; returns [z][y][x]."""
+        N = self.params["N"]
+        v = np.ascontiguousarray(vol, np.float32)
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
+        return out
+
     # -- multireference classification (src/MPI_Classification.cpp align -> assign -> re-average) -----
     def classify(self, iterations):
         """Runs `iterations` passes of align all particles x references -> assign to the closest class ->

@@ -105,6 +105,18 @@ int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, 
 int ettk_gpu_average(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
                      float *avg);
 
+/* Variance of class members about an average (nbfWedgedAverageImage3D::getImageVarianceMPI after
+   setAverageImage, inc/em/nbfWedgedAverageImage3D.h:440-493): var = sum over members with weight != 0 of
+   |w| (T - avg)^2 / sum |w|, T the member resampled as ettk_gpu_average resamples it (getImage, mean of valid
+   voxels removed). avg and var are N^3 floats, x fastest (avg as ettk_gpu_average returns it). */
+int ettk_gpu_variance(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
+                      const float *avg, float *var);
+
+/* n-fold symmetrisation about the z axis (nbfImageFilter::symmetrize, inc/em/nbfImageFilter.h:527-554): the
+   mean over i < fold of the volume, as a fixed image centred at N/2, resampled under RotateZ(i * 360 / fold)
+   with the mean of its valid voxels removed. fold = 1 returns the volume unchanged. N^3 floats, x fastest. */
+int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
+
 /* Multireference classification (the align -> assign -> re-average loop of src/MPI_Classification.cpp:954-1170,
    alignment_mode 3): each pass aligns every particle against every current reference (as
    ettk_gpu_align_pairs), assigns each particle to the class of smallest distance (labels[V]; dist_out[V] its

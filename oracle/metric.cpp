@@ -1020,6 +1020,57 @@ double oracle_refine_objective(const OracleParams *P, const OracleVolume *ref, c
   return (sgg > 0 && syy > 0) ? syg / sqrt(sgg * syy) : 0.0;
 }
 
+/* nbfImageFilter::symmetrize (inc/em/nbfImageFilter.h:527-554): the mean over i < fold of getImage of the
+ * volume as a fixed image (position dims/2, identity matrix, no normal) under RotateZ(i * 360 / fold), each a
+ * tricubic reslice with the mean of its valid voxels removed and invalid voxels zero (inc/em/nbfWedgedAverageImage3D.h
+ * 252-257 then inc/em/nbfWedgedSubImage3D.h:602-828). fold <= 1 returns the volume unchanged. out [x][y][z]. */
+int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, double *out) {
+  const int N = P->N;
+  const long n3 = (long)N * N * N;
+  if (fold <= 1) {
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) out[((long)x * N + y) * N + z] = (double)v->data[x + (long)N * (y + (long)N * z)];
+    return 0;
+  }
+  std::vector<double> acc(n3, 0.0), img;
+  for (int i = 0; i < fold; ++i) {
+    M4 t = m4_identity();
+    m4_rotate_pre(t, i * 360.0 / fold, 0, 0, 1);
+    get_image(*v, N, &t, img);
+    for (long k = 0; k < n3; ++k) acc[k] += img[k];
+  }
+  for (long k = 0; k < n3; ++k) out[k] = acc[k] / fold;
+  return 0;
+}
+
+/* nbfWedgedAverageImage3D::getImageVarianceMPI (inc/em/nbfWedgedAverageImage3D.h:440-493): sum over members with
+ * w != 0 of |w| (T - average)^2 / sum |w|, T = getImage of the member under its alignment with its own matrix
+ * reset (as the average). average and out [x][y][z]. */
+int oracle_variance(const OracleParams *P, int M, const OracleVolume *vols, const float *weights, const double *mats,
+                    const double *avg, double *out) {
+  const int N = P->N;
+  const long n3 = (long)N * N * N;
+  double sw = 0;
+  for (int i = 0; i < M; ++i) sw += fabs((double)weights[i]);
+  for (long k = 0; k < n3; ++k) out[k] = 0;
+  std::vector<double> img;
+  for (int i = 0; i < M; ++i) {
+    if (!(fabs(weights[i]) > 0)) continue;
+    OracleVolume v = vols[i];
+    for (int k = 0; k < 16; ++k) v.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    M4 t;
+    memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
+    get_image(v, N, &t, img);
+    const double aw = fabs((double)weights[i]);
+    for (long k = 0; k < n3; ++k) {
+      const double d = img[k] - avg[k];
+      out[k] += aw * (d * d) / sw;
+    }
+  }
+  return 0;
+}
+
 /* Class average of M members (volumes + metadata, weights, 4x4 alignment matrices); out [x][y][z]. */
 int oracle_average(const OracleParams *P, int M, const OracleVolume *vols, const float *weights, const double *mats,
                    double *out) {

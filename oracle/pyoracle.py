@@ -85,6 +85,8 @@ def lib():
         L.oracle_refine_objective.argtypes = [P, V, V, dp, dp]
         L.oracle_refine_objective.restype = ctypes.c_double
         L.oracle_average.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp]
+        L.oracle_symmetrize.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_variance.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -240,6 +242,37 @@ def average(params, vols, metas, weights, mats):
     N = params["N"]
     out = np.zeros(N ** 3, np.float64)
     lib().oracle_average(ctypes.byref(P), n, ctypes.addressof(arr), w.ctypes.data, m.ctypes.data, out)
+    return out.reshape(N, N, N)
+
+
+def symmetrize(params, vol, fold):
+    """nbfImageFilter::symmetrize of a fixed-image volume ([z][y][x]); returned as [x][y][z]."""
+    P = make_params(params)
+    N = params["N"]
+    meta = {"lwedge": -90.0, "uwedge": 90.0}
+    v = make_volume(vol, meta)
+    out = np.zeros(N ** 3, np.float64)
+    lib().oracle_symmetrize(ctypes.byref(P), ctypes.byref(v), int(fold), out.ctypes.data)
+    return out.reshape(N, N, N)
+
+
+def variance(params, vols, metas, weights, mats, avg_xyz):
+    """getImageVarianceMPI of the members against an average given as [x][y][z]; returned as [x][y][z]."""
+    P = make_params(params)
+    n = len(vols)
+    arr = (OracleVolume * n)()
+    keep = []
+    for i in range(n):
+        v = make_volume(vols[i], metas[i])
+        keep.append(v)
+        arr[i] = v
+    w = np.ascontiguousarray(weights, np.float32)
+    m = np.ascontiguousarray(np.asarray(mats, np.float64).reshape(n, 16))
+    a = np.ascontiguousarray(avg_xyz, np.float64)
+    N = params["N"]
+    out = np.zeros(N ** 3, np.float64)
+    lib().oracle_variance(ctypes.byref(P), n, ctypes.addressof(arr), w.ctypes.data, m.ctypes.data, a.ctypes.data,
+                          out.ctypes.data)
     return out.reshape(N, N, N)
 
 
