@@ -59,7 +59,7 @@ SYMBOLS = [
     "ettk_gpu_soft", "ettk_gpu_kernel_launches", "ettk_gpu_last_error", "ettk_gpu_stream", "ettk_gpu_profile",
     "ettk_gpu_profile_read", "ettk_gpu_soft_noalloc", "ettk_gpu_average", "ettk_gpu_refine_pairs",
     "ettk_gpu_refine_objective", "ettk_gpu_classify", "ettk_gpu_set_particles_tomogram", "ettk_gpu_variance",
-    "ettk_gpu_symmetrize",
+    "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
 ]
 
 _lib = None
@@ -98,6 +98,10 @@ def load(path=None):
     L.ettk_gpu_classify.argtypes = [vp, ctypes.c_int, vp, vp, vp]
     L.ettk_gpu_variance.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_symmetrize.argtypes = [vp, vp, ctypes.c_int, vp]
+    L.ettk_gpu_symmetrize_rotational.argtypes = [vp, vp, vp]
+    L.ettk_gpu_outlier_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float,
+                                          ctypes.c_int, vp, vp, vp, P(ctypes.c_float)]
+    L.ettk_gpu_soft_weights.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp]
     L.ettk_gpu_set_particles_tomogram.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                   P(VolumeMeta)]
     L.ettk_gpu_profile_read.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_longlong),

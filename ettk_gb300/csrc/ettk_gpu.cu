@@ -35,6 +35,8 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <cmath>
+#include <limits>
 
 using namespace ettk;
 
@@ -771,6 +773,7 @@ struct ettk_ctx {
   void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
   void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
   void symmetrize(const float *vol, int fold, float *out);
+  void symmetrize_rotational(const float *vol, float *out);
   // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
   // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
   void reslice_members(const int *idx, int E, const int *parts, const double *mats);
@@ -943,6 +946,32 @@ void ettk_ctx::symmetrize(const float *vol, int fold, float *out) {
   }
   w_r.ensure(n3);
   k_sym_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_v.p, w_acc.p, fold, N, w_r.p);
+  post_launch();
+  CK(cudaMemcpyAsync(out, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+  check_status();
+}
+
+// Rotational symmetrisation of the classification loop (src/MPI_Classification.cpp:1005-1024): the
+// (radius, z) profile summed over 180 angles on the cylinder about z, then interpolated back at every voxel.
+void ettk_ctx::symmetrize_rotational(const float *vol, float *out) {
+  CylGeom g;
+  g.N = N;
+  g.R = N / 2;
+  g.T = 180;
+  g.c = (double)(N / 2);
+  g.max_rho = (double)(N / 2);
+  g.max_theta = (double)(2 * 3.14159265358979f);  // float arithmetic, as vtkMath::Pi returns float
+  g.two_pi = 2.0 * (double)3.14159265358979f;
+  g.rstep = (g.max_rho - 0) / (g.R - 1);
+  g.tstep = (g.max_theta - 0) / (g.T - 1);
+  w_tmp.ensure(n3);
+  w_w.ensure((long)g.R * N);
+  w_r.ensure(n3);
+  CK(cudaMemcpyAsync(w_tmp.p, vol, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
+  k_cyl_profile<<<(g.R * N + 127) / 128, 128, 0, st>>>(w_tmp.p, g, w_w.p);
+  post_launch();
+  k_cyl_expand<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_w.p, g, w_r.p);
   post_launch();
   CK(cudaMemcpyAsync(out, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
   sync();
@@ -2601,6 +2630,67 @@ int ettk_gpu_symmetrize(ettk_ctx *c, const float *vol, int fold, float *out) {
   if (!c || !vol || !out || fold < 1 || fold > 360) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
   return guarded(c, [&] { c->symmetrize(vol, fold, out); });
+}
+
+int ettk_gpu_symmetrize_rotational(ettk_ctx *c, const float *vol, float *out) {
+  if (!c || !vol || !out) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (c->N < 4) return fail(c, ETTK_ERR_ARG, "volume too small for the cylindrical grid");
+  if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
+  return guarded(c, [&] { c->symmetrize_rotational(vol, out); });
+}
+
+int ettk_gpu_outlier_cutoff(int R, int V, const float *D, int ld, float top_fraction, int rule, int *best,
+                            float *dist, int *keep, float *cutoff) {
+  if (R < 1 || V < 1 || !D || ld < 1 || rule < 0 || rule > 2 || !best || !dist || !keep) return ETTK_ERR_ARG;
+  if (!(top_fraction == top_fraction)) return ETTK_ERR_NAN;
+  for (long i = 0; i < (long)V * R; ++i)
+    if (!std::isfinite(D[(size_t)i * ld])) return ETTK_ERR_NAN;
+  // each volume's class of smallest distance, the first on ties (minIndex over the classes)
+  for (int v = 0; v < V; ++v) {
+    int b = 0;
+    for (int r = 1; r < R; ++r)
+      if (D[(size_t)(v * (long)R + r) * ld] < D[(size_t)(v * (long)R + b) * ld]) b = r;
+    const float d = D[(size_t)(v * (long)R + b) * ld];
+    best[v] = b;
+    dist[v] = rule == 0 ? std::fabs(d) : d;
+    keep[v] = 1;
+  }
+  if (!(top_fraction < 1)) {
+    if (cutoff) *cutoff = std::numeric_limits<float>::infinity();
+    return ETTK_OK;
+  }
+  std::vector<float> sorted(dist, dist + V);
+  std::sort(sorted.begin(), sorted.end());
+  // index = fraction * (n - 1) in float arithmetic, truncated, as the reference indexes its sorted vector
+  long at = (long)(top_fraction * (float)(V - 1));
+  at = std::max(0L, std::min<long>(at, V - 1));
+  const float cut = sorted[at];
+  for (int v = 0; v < V; ++v) keep[v] = rule == 1 ? (dist[v] <= cut) : (dist[v] < cut);
+  if (cutoff) *cutoff = cut;
+  return ETTK_OK;
+}
+
+int ettk_gpu_soft_weights(int R, int V, const float *D, int ld, float *W, float *radii) {
+  if (R < 1 || V < 1 || !D || ld < 1 || !W) return ETTK_ERR_ARG;
+  const float decay = .025f;
+  for (int r = 0; r < R; ++r) {
+    float mx = -std::numeric_limits<float>::max();
+    for (int v = 0; v < V; ++v) {
+      const float d = D[(size_t)(v * (long)R + r) * ld];
+      if (!std::isfinite(d)) return ETTK_ERR_NAN;
+      mx = std::max(mx, d);
+    }
+    // radius: largest distance to the class plus decay * ln(0.01), in double, stored as float
+    const float rad = (float)((double)mx + (double)decay * std::log(.01));
+    if (radii) radii[r] = rad;
+    for (int v = 0; v < V; ++v) {
+      const float d = D[(size_t)(v * (long)R + r) * ld];
+      const float e = std::exp((-(d - rad)) / decay);  // float exponent, as on the float distance array
+      const float w = (float)((1 + 2.0 * e) / (1 + 1.0 * e) - 1.0);
+      W[(size_t)r * V + v] = w > .01 ? w : 0.f;
+    }
+  }
+  return ETTK_OK;
 }
 
 long long ettk_gpu_kernel_launches(ettk_ctx *c) { return c ? c->launches : 0; }

@@ -774,6 +774,95 @@ static __global__ void k_var_finish(const double *__restrict__ var, int N, float
   }
 }
 
+// ---- rotational symmetrisation ---------------------------------------------------------------
+// src/MPI_Classification.cpp:1005-1024 with nbfCylindricalDomain3 (inc/nbfCylindricalDomain3.h:126-233) and the
+// clamped trilinear rule of nbfLinearInterpolator::interpolateSingle (inc/nbfLinearInterpolator.h:186-262), in
+// FP64 with every product and sum rounded on its own (no contraction), so that the only departures from the
+// CPU arithmetic are the last bits of cos / sin / atan2.
+
+struct CylGeom {
+  int N, R, T;                // volume edge, radii N/2, angles 180
+  double c, max_rho;          // axis at (N/2, N/2); largest radius N/2
+  double rstep, tstep;        // (N/2)/(R-1) and max_theta/(T-1)
+  double max_theta, two_pi;   // 2 * float pi of VTK 5.10, both as doubles
+};
+
+// Clamped axis rule: at or below 0 -> cell 0, weight 0; at or above n-1 -> cell n-2, weight 1.
+ETTK_DEV double cyl_axis(double x, int n, int &f) {
+  if (x <= 0.0) {
+    f = 0;
+    return 0.0;
+  }
+  if (x >= (double)(n - 1)) {
+    f = n - 2;
+    return 1.0;
+  }
+  f = (int)floor(x);
+  return __dsub_rn(x, (double)f);
+}
+
+// The eight-term blend of interpolateSingle in its order: v000, v100, v010, v001, v101, v011, v110, v111.
+ETTK_DEV double cyl_blend(double a, double b, double c, double v000, double v100, double v010, double v001,
+                          double v101, double v011, double v110, double v111) {
+  const double ia = __dsub_rn(1.0, a), ib = __dsub_rn(1.0, b), ic = __dsub_rn(1.0, c);
+  double s = __dmul_rn(__dmul_rn(__dmul_rn(ia, ib), ic), v000);
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(a, ib), ic), v100));
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(ia, b), ic), v010));
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(ia, ib), c), v001));
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(a, ib), c), v101));
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(ia, b), c), v011));
+  s = __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(a, b), ic), v110));
+  return __dadd_rn(s, __dmul_rn(__dmul_rn(__dmul_rn(a, b), c), v111));
+}
+
+// cartesian2cylindrical + the angular sum: prof[i][k] = sum over the T angles, in order, of the volume (x
+// fastest) interpolated at (c + rho_i cos theta_j, c + rho_i sin theta_j, k). One thread per (radius, plane).
+static __global__ void __launch_bounds__(128) k_cyl_profile(const float *__restrict__ vol, CylGeom g,
+                                                            double *__restrict__ prof) {
+  __shared__ double cs[180], sn[180];
+  for (int j = threadIdx.x; j < g.T; j += blockDim.x) {
+    const double th = __dadd_rn(__dmul_rn(g.tstep, (double)j), 0.0);
+    sincos(th, &sn[j], &cs[j]);
+  }
+  __syncthreads();
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= g.R * g.N) return;
+  const int i = id / g.N, k = id % g.N, N = g.N;
+  const double rho = __dadd_rn(__dmul_rn(g.rstep, (double)i), 0.0);
+  int zf;
+  const double cz = cyl_axis((double)k, N, zf);
+  const long NN = (long)N * N;
+  double s = 0.0;
+  for (int j = 0; j < g.T; ++j) {
+    int xf, yf;
+    const double a = cyl_axis(__dadd_rn(g.c, __dmul_rn(rho, cs[j])), N, xf);
+    const double b = cyl_axis(__dadd_rn(g.c, __dmul_rn(rho, sn[j])), N, yf);
+    const float *p = vol + xf + (long)N * yf + NN * zf;
+    s = __dadd_rn(s, cyl_blend(a, b, cz, p[0], p[1], p[N], p[NN], p[NN + 1], p[NN + N], p[N + 1], p[NN + N + 1]));
+  }
+  prof[(long)i * N + k] = s;
+}
+
+// cylindrical2cartesian of the angle-independent profile: out (x fastest) at each voxel's radius
+// (N/2-1) r / (N/2) and angle atan2(y - c, x - c) (wrapped to [0, 2 pi)) scaled to the T-1 cells.
+static __global__ void k_cyl_expand(const double *__restrict__ prof, CylGeom g, float *__restrict__ out) {
+  const int N = g.N;
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(id % N), y = (int)((id / N) % N), z = (int)(id / ((long)N * N));
+    const double dx = __dsub_rn(g.c, (double)x), dy = __dsub_rn(g.c, (double)y);
+    double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    r = __dmul_rn(__ddiv_rn(r, g.max_rho), (double)(g.R - 1));
+    double t = atan2(__dsub_rn((double)y, g.c), __dsub_rn((double)x, g.c));
+    if (t < 0.0) t = __dadd_rn(t, g.two_pi);
+    t = __dmul_rn(__ddiv_rn(t, g.max_theta), (double)(g.T - 1));
+    int rf, tf, zf;
+    const double a = cyl_axis(r, g.R, rf), b = cyl_axis(t, g.T, tf), c = cyl_axis((double)z, N, zf);
+    const double *p = prof + (long)rf * N + zf;  // the profile at (rf, zf); the angle index selects nothing
+    out[id] = (float)cyl_blend(a, b, c, p[0], p[N], p[0], p[1], p[N + 1], p[1], p[N], p[N + 1]);
+  }
+}
+
 // ---- spherical projection ------------------------------------------------------------------
 
 // mean over all voxels of the mean-subtracted particle (nbfImageFilter::execute meanValue,

@@ -168,6 +168,16 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
         return out
 
+    def symmetrize_rotational(self, vol):
+        """Rotational (cylindrical) symmetrisation about z of a [z][y][x] volume, as the classification loop's
+        apply_rotational_symmetry; returns [z][y][x] (the angular sum, about 180 times the mean)."""
+        N = self.params["N"]
+        v = np.ascontiguousarray(vol, np.float32)
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_symmetrize_rotational(self._ctx, v.ctypes.data, out.ctypes.data),
+                    "symmetrize_rotational")
+        return out
+
     # -- multireference classification (src/MPI_Classification.cpp align -> assign -> re-average) -----
     def classify(self, iterations):
         """Runs `iterations` passes of align all particles x references -> assign to the closest class ->

@@ -117,6 +117,35 @@ int ettk_gpu_variance(ettk_ctx *ctx, int M, const int *particles, const float *w
    with the mean of its valid voxels removed. fold = 1 returns the volume unchanged. N^3 floats, x fastest. */
 int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
 
+/* Rotational symmetrisation of the classification loop (apply_rotational_symmetry,
+   src/MPI_Classification.cpp:1005-1024, with nbfCylindricalDomain3, inc/nbfCylindricalDomain3.h:126-233): the
+   volume sampled on a cylinder about the z axis through (N/2, N/2) (N/2 radii from 0 to N/2, 180 angles over
+   [0, 2 pi] with both ends, every z plane; clamped trilinear interpolation), summed over the angles (a sum,
+   so the result carries a factor of about 180, as in the reference) and interpolated back at each voxel's
+   radius. FP64 on the device, N^3 floats in and out, x fastest. */
+int ettk_gpu_symmetrize_rotational(ettk_ctx *ctx, const float *vol, float *out);
+
+/* Host-only helpers of the classification iteration (no context, no device work). D holds one row of ld
+   floats per (volume, class) pair, row v * R + r, the distance in column 0: the layout ettk_gpu_align_pairs
+   writes for pairs ordered volume-major. */
+
+/* Best class and outlier cutoff. best[v] = the class of smallest distance (the first on ties), dist[v] its
+   distance; with top_fraction < 1 the cutoff is the sorted dist at index (int)(top_fraction * (V - 1)) (float
+   product) and keep[v] says whether volume v survives it; otherwise every keep[v] = 1 and *cutoff = inf.
+   rule 0: nbfLoopClustering::asignBestAlignmentAndClean (inc/em/nbfLoopClustering.h:2590-2637), |distance|
+           and keep = dist < cutoff;
+   rule 1: the weights of the next global average (src/MPI_Classification.cpp:922-934), keep = dist <= cutoff;
+   rule 2: the cleaned volume list (src/MPI_Classification.cpp:1137-1150), keep = dist < cutoff.
+   cutoff is optional. */
+int ettk_gpu_outlier_cutoff(int R, int V, const float *D, int ld, float top_fraction, int rule, int *best,
+                            float *dist, int *keep, float *cutoff);
+
+/* Soft class weights of nbfLoopClustering::computeNewReferences (inc/em/nbfLoopClustering.h:2406-2502; the
+   reference defines it but none of its drivers calls it): per class r, radius = max_v D(v, r) + 0.025 ln 0.01,
+   W[r * V + v] = (1 + 2e) / (1 + e) - 1 with e = exp(-(D(v, r) - radius) / 0.025) (float exponent), weights
+   of 0.01 or less set to 0. radii (optional, R floats) receives the radii. */
+int ettk_gpu_soft_weights(int R, int V, const float *D, int ld, float *W, float *radii);
+
 /* Multireference classification (the align -> assign -> re-average loop of src/MPI_Classification.cpp:954-1170,
    alignment_mode 3): each pass aligns every particle against every current reference (as
    ettk_gpu_align_pairs), assigns each particle to the class of smallest distance (labels[V]; dist_out[V] its

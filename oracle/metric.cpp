@@ -1044,6 +1044,82 @@ int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, do
   return 0;
 }
 
+/* Clamped trilinear interpolation of nbfLinearInterpolator::interpolateSingle (inc/nbfLinearInterpolator.h:186-262)
+ * along one axis of extent n: a coordinate at or below 0 takes cell 0 with weight 0, one at or above n-1 takes
+ * cell n-2 with weight 1, others floor and fraction. */
+static double cyl_axis(double x, int n, int *f) {
+  if (x <= 0) {
+    *f = 0;
+    return 0.0;
+  }
+  if (x >= n - 1) {
+    *f = n - 2;
+    return 1.0;
+  }
+  *f = (int)floor(x);
+  return x - *f;
+}
+
+/* The eight-term blend of interpolateSingle in its order; v[dx][dy][dz]. */
+static double cyl_blend(double a, double b, double c, const double v[2][2][2]) {
+  return (1 - a) * (1 - b) * (1 - c) * v[0][0][0] + a * (1 - b) * (1 - c) * v[1][0][0] +
+         (1 - a) * b * (1 - c) * v[0][1][0] + (1 - a) * (1 - b) * c * v[0][0][1] + a * (1 - b) * c * v[1][0][1] +
+         (1 - a) * b * c * v[0][1][1] + a * b * (1 - c) * v[1][1][0] + a * b * c * v[1][1][1];
+}
+
+/* Rotational symmetrisation of the classification loop (src/MPI_Classification.cpp:1005-1024) with
+ * nbfCylindricalDomain3 (inc/nbfCylindricalDomain3.h:126-233): the volume (x fastest) sampled on a cylinder
+ * about the z axis through (N/2, N/2): N/2 radii rho_i = (N/2)/(N/2-1) i, 180 angles theta_j = 2 pi_f / 179 j
+ * (pi_f = the float pi of VTK 5.10's vtkMath::Pi, both ends included) and every z plane, by the clamped
+ * trilinear interpolation above; the samples summed over the angles in order (a sum, not a mean); the
+ * (radius, z) profile interpolated back at each voxel's radius (N/2-1) r / (N/2) and angle (the angle weight
+ * multiplies equal values). FP64; out [x][y][z]. */
+int oracle_symmetrize_rotational(int N, const float *vol, double *out) {
+  if (N < 4 || (N & 1)) return 1;
+  const int R = N / 2, T = 180;
+  const double c = (double)(N / 2), max_rho = (double)(N / 2), two_pi = 2.0 * (double)3.14159265358979f;
+  const double max_theta = (double)(2 * 3.14159265358979f);
+  const double rstep = (max_rho - 0) / (R - 1), tstep = (max_theta - 0) / (T - 1);
+  std::vector<double> prof((size_t)R * N);
+  auto A = [&](int x, int y, int z) { return (double)vol[x + (long)N * (y + (long)N * z)]; };
+  for (int i = 0; i < R; ++i)
+    for (int k = 0; k < N; ++k) {
+      double s = 0;
+      for (int j = 0; j < T; ++j) {
+        const double rho = rstep * i + 0.0, theta = tstep * j + 0.0;
+        const double X = c + rho * cos(theta), Y = c + rho * sin(theta), Z = (double)k;
+        int xf, yf, zf;
+        const double a = cyl_axis(X, N, &xf), b = cyl_axis(Y, N, &yf), cc = cyl_axis(Z, N, &zf);
+        double v[2][2][2];
+        for (int dx = 0; dx < 2; ++dx)
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dz = 0; dz < 2; ++dz) v[dx][dy][dz] = A(xf + dx, yf + dy, zf + dz);
+        s += cyl_blend(a, b, cc, v);
+      }
+      prof[(size_t)i * N + k] = s;
+    }
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y) {
+      double r = sqrt((c - x) * (c - x) + (c - y) * (c - y));
+      r = (r - 0) / (max_rho - 0) * (R - 1);
+      double t = atan2(y - c, x - c);
+      if (t < 0) t = t + two_pi;
+      t = t / max_theta * (T - 1);
+      int rf, tf;
+      const double a = cyl_axis(r, R, &rf), b = cyl_axis(t, T, &tf);
+      for (int z = 0; z < N; ++z) {
+        int zf;
+        const double cc = cyl_axis((double)z, N, &zf);
+        double v[2][2][2];
+        for (int dx = 0; dx < 2; ++dx)
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dz = 0; dz < 2; ++dz) v[dx][dy][dz] = prof[(size_t)(rf + dx) * N + zf + dz];
+        out[((long)x * N + y) * N + z] = cyl_blend(a, b, cc, v);
+      }
+    }
+  return 0;
+}
+
 /* nbfWedgedAverageImage3D::getImageVarianceMPI (inc/em/nbfWedgedAverageImage3D.h:440-493): sum over members with
  * w != 0 of |w| (T - average)^2 / sum |w|, T = getImage of the member under its alignment with its own matrix
  * reset (as the average). average and out [x][y][z]. */

@@ -13,6 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libsoft_ref.so")
+CYL_REF_PATH = os.path.join(HERE, "_ref", "libcyl_ref.so")
 
 
 class OracleParams(ctypes.Structure):
@@ -87,6 +88,7 @@ def lib():
         L.oracle_average.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp]
         L.oracle_symmetrize.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p]
         L.oracle_variance.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
+        L.oracle_symmetrize_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -256,6 +258,16 @@ def symmetrize(params, vol, fold):
     return out.reshape(N, N, N)
 
 
+def symmetrize_rotational(vol):
+    """Rotational (cylindrical) symmetrisation of an N^3 volume ([z][y][x]); returned as [x][y][z]."""
+    v = np.ascontiguousarray(vol, np.float32)
+    N = v.shape[0]
+    out = np.zeros(N ** 3, np.float64)
+    if lib().oracle_symmetrize_rotational(N, v.ctypes.data, out.ctypes.data) != 0:
+        raise ValueError("N must be even and at least 4")
+    return out.reshape(N, N, N)
+
+
 def variance(params, vols, metas, weights, mats, avg_xyz):
     """getImageVarianceMPI of the members against an average given as [x][y][z]; returned as [x][y][z]."""
     P = make_params(params)
@@ -310,3 +322,24 @@ def ref_lib():
         L.ref_rotate.argtypes = [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
         _ref = L
     return _ref
+
+
+_cyl_ref = None
+
+
+def ref_symmetrize_rotational(vol):
+    """The reference's own cylindrical-domain classes run through the rotational-symmetry step
+    (oracle/_ref/libcyl_ref.so); [x][y][z], or None when that library is absent."""
+    global _cyl_ref
+    if _cyl_ref is None:
+        if not os.path.exists(CYL_REF_PATH):
+            return None
+        L = ctypes.CDLL(CYL_REF_PATH)
+        L.cyl_ref_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        _cyl_ref = L
+    v = np.ascontiguousarray(vol, np.float32)
+    N = v.shape[0]
+    out = np.zeros(N ** 3, np.float64)
+    if _cyl_ref.cyl_ref_rotational(N, v.ctypes.data, out.ctypes.data) != 0:
+        raise ValueError("N must be even and at least 4")
+    return out.reshape(N, N, N)

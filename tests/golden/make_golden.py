@@ -8,8 +8,11 @@ align32_b16.npz  oracle alignments of the first particles of the 32^3 B=16 workl
                of the oracle itself), with a checksum of the generated particles.
 align128_b64.npz oracle alignments of the first two particles of the 128^3 B=64 workload (the large-size
                path: (2N)^3 = 256^3 spherical projections, B=64 SO(3) correlations), with a checksum.
+rotsym_n16.npz the rotational-symmetry step of the classification loop run by the reference's own
+               cylindrical-domain classes (oracle/_ref/libcyl_ref.so) on a seeded 16^3 volume and on a
+               volume with an off-axis blob.
 
-Usage: python make_golden.py [soft|align32|align128 ...]   (no argument: all)
+Usage: python make_golden.py [soft|align32|align128|rotsym ...]   (no argument: all)
 """
 import hashlib
 import os
@@ -44,7 +47,21 @@ def align_golden(name, n, out):
                         particles_sha256=hashlib.sha256(ds.particles.tobytes()).hexdigest())
 
 
+def rotsym_inputs():
+    rng = np.random.default_rng(2024)
+    noise = rng.standard_normal((16, 16, 16)).astype(np.float32)
+    z, y, x = np.mgrid[0:16, 0:16, 0:16]
+    blob = np.exp(-((x - 11.3) ** 2 + (y - 6.0) ** 2 + (z - 8.5) ** 2) / 6.0).astype(np.float32)
+    return np.stack([noise, blob])
+
+
 def main(which):
+    if "rotsym" in which:
+        vols = rotsym_inputs()
+        outs = [pyoracle.ref_symmetrize_rotational(v) for v in vols]
+        if outs[0] is None:
+            raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+        np.savez_compressed(os.path.join(HERE, "rotsym_n16.npz"), vol=vols, out=np.stack(outs))
     if "align32" in which:
         align_golden("align32_b16", 4, "align32_b16.npz")
     if "align128" in which:
@@ -67,4 +84,4 @@ def main(which):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["soft", "align32", "align128"])
+    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym"])

@@ -1,6 +1,13 @@
 """Average variance (nbfWedgedAverageImage3D::getImageVarianceMPI, inc/em/nbfWedgedAverageImage3D.h:440-493) and
 n-fold symmetrisation (nbfImageFilter::symmetrize, inc/em/nbfImageFilter.h:527-554) against the oracle's FP64
-restatements; 1e-5 relative RMS, as the class average."""
+restatements; 1e-5 relative RMS, as the class average.
+
+Rotational symmetrisation (src/MPI_Classification.cpp:1005-1024): the oracle's restatement is pinned bit for
+bit to the reference's own nbfCylindricalDomain3 / nbfLinearInterpolator (tests/golden/rotsym_n16.npz, and the
+harness library itself when it is built); the GPU (FP64, no contraction; only cos / sin / atan2 may differ in
+their last bits) is held to 1e-6 of the maximum per voxel, i.e. float output rounding."""
+import os
+
 import numpy as np
 import pytest
 
@@ -35,6 +42,49 @@ def test_symmetrize(ds32, fold):
         m.close()
     o = pyoracle.symmetrize(ds32.params, ds32.references[0], fold).transpose(2, 1, 0)
     assert rel_rms(g, o) <= 1e-5, (fold, rel_rms(g, o))
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rotsym_n16.npz")
+
+
+def test_oracle_rotational_matches_reference_golden():
+    g = np.load(GOLDEN)
+    for v, out in zip(g["vol"], g["out"]):
+        assert np.array_equal(pyoracle.symmetrize_rotational(v), out)
+
+
+def test_oracle_rotational_matches_reference_library():
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((32, 32, 32)).astype(np.float32)
+    r = pyoracle.ref_symmetrize_rotational(v)
+    if r is None:
+        pytest.skip("reference harness not built here (oracle/build_ref.sh needs the reference tree)")
+    assert np.array_equal(pyoracle.symmetrize_rotational(v), r)
+
+
+def test_oracle_rotational_is_symmetric():
+    # voxels at the same distance from the axis in one plane carry the same value up to the angle weight's
+    # rounding; (x, y) -> (y, x) and the quarter turns about (N/2, N/2) keep the distance
+    g = np.load(GOLDEN)
+    o = pyoracle.symmetrize_rotational(g["vol"][1])  # [x][y][z]
+    N = o.shape[0]
+    inner = o[1:, 1:, :]  # indices 1..N-1: the quarter turns about N/2 map them onto themselves
+    for t in (inner.transpose(1, 0, 2), np.rot90(inner, 1, (0, 1)), np.rot90(inner, 2, (0, 1))):
+        assert np.abs(t - inner).max() <= 1e-12 * np.abs(inner).max()
+    assert N == 16
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["reference", "particle"])
+def test_symmetrize_rotational(ds32, which):
+    vol = ds32.references[0] if which == "reference" else ds32.particles[1]
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        g = m.symmetrize_rotational(vol)
+    finally:
+        m.close()
+    o = pyoracle.symmetrize_rotational(vol).transpose(2, 1, 0)
+    assert np.abs(g - o).max() <= 1e-6 * np.abs(o).max(), np.abs(g - o).max() / np.abs(o).max()
 
 
 @pytest.mark.gpu
