@@ -774,6 +774,8 @@ struct ettk_ctx {
   void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
   void symmetrize(const float *vol, int fold, float *out);
   void symmetrize_rotational(const float *vol, float *out);
+  void average_spherical_wedge(int M, const int *parts, const float *weights, const double *mats, float *count,
+                               float *wedge);
   // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
   // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
   void reslice_members(const int *idx, int E, const int *parts, const double *mats);
@@ -976,6 +978,54 @@ void ettk_ctx::symmetrize_rotational(const float *vol, float *out) {
   CK(cudaMemcpyAsync(out, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
   sync();
   check_status();
+}
+
+// Spherical wedge of a class average (updateAccumulatedSphericalWedgeImageMPI + updateSphericalWedgeImage,
+// inc/em/nbfWedgedAverageImage3D.h:612-665): members with |w| > 0, own matrix reset as the average resamples
+// them, binary wedges under their alignments counted per sample on the device; the average's wedge is
+// count > max(count) / 2.
+void ettk_ctx::average_spherical_wedge(int M, const int *parts, const float *weights, const double *mats,
+                                       float *count, float *wedge) {
+  const int n = 2 * B;
+  std::vector<WedgeVecs> wv;
+  for (int i = 0; i < M; ++i) {
+    if (parts[i] < 0 || parts[i] >= V) throw CudaError(ETTK_ERR_ARG, "member index out of range");
+    if (!(fabs(weights[i]) > 0)) continue;
+    VolumeGeom g = partg[parts[i]];
+    for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    Mat4 t;
+    memcpy(t.e, mats + 16 * (long)i, sizeof(t.e));
+    WedgeVecs w{};
+    w.full = g.full_wedge() ? 1 : 0;
+    if (!w.full) wedge_vectors(g, &t, w.v1, w.v2);
+    wv.push_back(w);
+  }
+  const int E = (int)wv.size();
+  // cos / sin tables in float as the reference evaluates them: phiK = pi_f / (n - 1), thetaK = 2 pi_f / (n - 1)
+  const float phiK = (float)(M_PI / (n - 1)), thetaK = (float)(2.0 * M_PI / (n - 1));
+  std::vector<float> trig(4 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    trig[k] = cosf(k * thetaK);
+    trig[n + k] = sinf(k * thetaK);
+    trig[2 * n + k] = sinf(k * phiK);
+    trig[3 * n + k] = cosf(k * phiK);
+  }
+  w_wv.ensure(std::max(E, 1));
+  w_tmp.ensure(4L * n + (long)n * n);
+  if (E) CK(cudaMemcpyAsync(w_wv.p, wv.data(), E * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_tmp.p, trig.data(), trig.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  float *dcount = w_tmp.p + 4L * n;
+  k_sph_wedge_count<<<(n * n + 255) / 256, 256, 0, st>>>(w_wv.p, E, w_tmp.p, n, dcount);
+  post_launch();
+  std::vector<float> c((size_t)n * n);
+  CK(cudaMemcpyAsync(c.data(), dcount, c.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+  check_status();
+  const float mx = *std::max_element(c.begin(), c.end());
+  for (size_t k = 0; k < c.size(); ++k) {
+    if (count) count[k] = c[k];
+    wedge[k] = (c[k] > mx / 2.0) ? 1.f : 0.f;
+  }
 }
 
 // ---------------------------------------------------------------- continuous pose refinement
@@ -2144,6 +2194,24 @@ VolumeGeom to_geom(const ettk_volume_meta &m) {
   return g;
 }
 
+// conditionSphericalWindow (inc/em/nbfProjectionRotationMetric3D.h:1322-1345: Gaussian std 2, radius factor 1
+// on VTK dims (2B, 2B, 1), x = polar index) and the 0.95 gate of the window's use (487-490).
+void condition_spherical_host(std::vector<float> &W, int B, int &use) {
+  const int n = 2 * B;
+  std::vector<float> t((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) t[i + (size_t)n * j] = W[(size_t)i * n + j];
+  int dims[3] = {n, n, 1};
+  gaussian_smooth(t, dims, 2.0, 1.0);
+  double s = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      W[(size_t)i * n + j] = t[i + (size_t)n * j];
+      s += W[(size_t)i * n + j];
+    }
+  use = s <= (double)(.95f * (float)(n * n));
+}
+
 // nbfWedge3D::getSphericalImage + conditionSphericalWindow on the host (double arithmetic as the reference)
 void spherical_wedge_host(const VolumeGeom &g, int B, std::vector<float> &W, int &use) {
   int n = 2 * B;
@@ -2166,18 +2234,7 @@ void spherical_wedge_host(const VolumeGeom &g, int B, std::vector<float> &W, int
         W[(size_t)i * n + j] = (a * b <= 0.0) ? 1.0f : 0.0f;
       }
   }
-  std::vector<float> t((size_t)n * n);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) t[i + (size_t)n * j] = W[(size_t)i * n + j];
-  int dims[3] = {n, n, 1};
-  gaussian_smooth(t, dims, 2.0, 1.0);
-  double s = 0;
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) {
-      W[(size_t)i * n + j] = t[i + (size_t)n * j];
-      s += W[(size_t)i * n + j];
-    }
-  use = s <= (double)(.95f * (float)(n * n));
+  condition_spherical_host(W, B, use);
 }
 
 // nbfWedge3D::getImageHalf for the reference (no transform), host side
@@ -2524,6 +2581,7 @@ int ettk_gpu_classify(ettk_ctx *c, int iterations, int *labels, float *refs_out,
       if (dist_out) dist_out[v] = D[(size_t)(v * R + best) * cols];
     }
     // 3. wedge-weighted average of each class under its members' alignments (getImageMPI + getImage)
+    std::vector<std::vector<float>> sph(R);
     for (int r = 0; r < R; ++r) {
       std::vector<int> mem;
       std::vector<float> w;
@@ -2544,10 +2602,21 @@ int ettk_gpu_classify(ettk_ctx *c, int iterations, int *labels, float *refs_out,
       }
       rc = ettk_gpu_average(c, (int)mem.size(), mem.data(), w.data(), mats.data(), avg.data() + (size_t)r * n3);
       if (rc != ETTK_OK) return rc;
+      if (c->p.wedge_compensation) {  // the class's accumulated spherical wedge (doMra, nbfLoopClustering.h:1270-1278)
+        sph[r].resize((size_t)4 * c->B * c->B);
+        rc = ettk_gpu_average_spherical_wedge(c, (int)mem.size(), mem.data(), w.data(), mats.data(), nullptr,
+                                              sph[r].data());
+        if (rc != ETTK_OK) return rc;
+      }
     }
-    // 4. the averages become the references of the next pass
+    // 4. the averages become the references of the next pass, carrying their classes' spherical wedges
     rc = ettk_gpu_set_references(c, R, avg.data(), meta.data());
     if (rc != ETTK_OK) return rc;
+    for (int r = 0; r < R; ++r)
+      if (!sph[r].empty()) {
+        rc = ettk_gpu_set_reference_spherical_wedge(c, r, sph[r].data());
+        if (rc != ETTK_OK) return rc;
+      }
   }
   if (refs_out) memcpy(refs_out, avg.data(), (size_t)R * n3 * sizeof(float));
   return ETTK_OK;
@@ -2630,6 +2699,29 @@ int ettk_gpu_symmetrize(ettk_ctx *c, const float *vol, int fold, float *out) {
   if (!c || !vol || !out || fold < 1 || fold > 360) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
   return guarded(c, [&] { c->symmetrize(vol, fold, out); });
+}
+
+int ettk_gpu_average_spherical_wedge(ettk_ctx *c, int M, const int *particles, const float *weights,
+                                     const double *matrices, float *count, float *wedge) {
+  if (!c || M < 1 || !particles || !weights || !matrices || !wedge) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (c->V < 1) return fail(c, ETTK_ERR_STATE, "set particles first");
+  return guarded(c, [&] { c->average_spherical_wedge(M, particles, weights, matrices, count, wedge); });
+}
+
+int ettk_gpu_set_reference_spherical_wedge(ettk_ctx *c, int r, const float *wedge) {
+  if (!c || !wedge) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (r < 0 || r >= c->R) return fail(c, ETTK_ERR_ARG, "reference index out of range");
+  const int n = 2 * c->B;
+  for (long k = 0; k < (long)n * n; ++k)
+    if (!std::isfinite(wedge[k])) return fail(c, ETTK_ERR_NAN, "non-finite wedge");
+  return guarded(c, [&] {
+    std::vector<float> w(wedge, wedge + (size_t)n * n);
+    int use = 0;
+    condition_spherical_host(w, c->B, use);
+    c->sync();
+    CK(cudaMemcpy(c->W1sph.p + (long)r * c->nn, w.data(), (size_t)n * n * sizeof(float), cudaMemcpyHostToDevice));
+    c->useW1[r] = use;
+  });
 }
 
 int ettk_gpu_symmetrize_rotational(ettk_ctx *c, const float *vol, float *out) {

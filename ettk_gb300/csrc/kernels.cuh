@@ -774,6 +774,35 @@ static __global__ void k_var_finish(const double *__restrict__ var, int N, float
   }
 }
 
+// ---- spherical wedge of a class average --------------------------------------------------------
+// updateAccumulatedSphericalWedgeImageMPI (inc/em/nbfWedgedAverageImage3D.h:612-648): per sample (i, j) of the
+// (2B)^2 grid, the number of members whose binary spherical wedge covers it. Each member's wedge is the analytic
+// one of nbfWedge3D::getSphericalImage (inc/em/nbfWedge3D.h:363-429) with its plane normals rotated by the
+// inverse of Euler(normal) * alignment: ((v1.d)(v2.d) <= 0) with d = (cos th_j sin ph_i, sin th_j sin ph_i,
+// cos ph_i) from the float cos / sin tables trig = [cos th_j | sin th_j | sin ph_i | cos ph_i] (n each), the
+// products and sums in FP64 in the reference's order (no contraction). Counts are exact in float.
+static __global__ void k_sph_wedge_count(const WedgeVecs *__restrict__ wv, int E, const float *__restrict__ trig, int n,
+                                         float *__restrict__ count) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n * n) return;
+  const int i = id / n, j = id - (id / n) * n;
+  const double cj = trig[j], sj = trig[n + j], si = trig[2 * n + i], ci = trig[3 * n + i];
+  float c = 0.f;
+  for (int e = 0; e < E; ++e) {
+    const WedgeVecs &w = wv[e];
+    if (w.full) {
+      c += 1.f;
+      continue;
+    }
+    const double a = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(w.v1[0], cj), si), __dmul_rn(__dmul_rn(w.v1[1], sj), si)),
+                               __dmul_rn(w.v1[2], ci));
+    const double b = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(w.v2[0], cj), si), __dmul_rn(__dmul_rn(w.v2[1], sj), si)),
+                               __dmul_rn(w.v2[2], ci));
+    if (__dmul_rn(a, b) <= 0.0) c += 1.f;
+  }
+  count[id] = c;
+}
+
 // ---- rotational symmetrisation ---------------------------------------------------------------
 // src/MPI_Classification.cpp:1005-1024 with nbfCylindricalDomain3 (inc/nbfCylindricalDomain3.h:126-233) and the
 // clamped trilinear rule of nbfLinearInterpolator::interpolateSingle (inc/nbfLinearInterpolator.h:186-262), in

@@ -168,6 +168,28 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
         return out
 
+    def average_spherical_wedge(self, particles, weights, matrices):
+        """Spherical wedge of the class average of `particles` under `matrices` (updateSphericalWedgeImage).
+        Returns (binary wedge [2B][2B], member count per sample [2B][2B])."""
+        n = len(particles)
+        n2 = 2 * self.params["B"]
+        p = np.ascontiguousarray(np.asarray(particles, np.int32))
+        w = np.ascontiguousarray(np.asarray(weights, np.float32))
+        M = np.ascontiguousarray(np.asarray(matrices, np.float64).reshape(n, 16))
+        wedge = np.zeros((n2, n2), np.float32)
+        count = np.zeros((n2, n2), np.float32)
+        self._check(self.L.ettk_gpu_average_spherical_wedge(self._ctx, n, p.ctypes.data, w.ctypes.data, M.ctypes.data,
+                                                            count.ctypes.data, wedge.ctypes.data),
+                    "average_spherical_wedge")
+        return wedge, count
+
+    def set_reference_spherical_wedge(self, r, wedge):
+        """Explicit binary spherical wedge [2B][2B] for reference r (nbfWedge3D::setSphericalImage)."""
+        w = np.ascontiguousarray(wedge, np.float32)
+        assert w.size == (2 * self.params["B"]) ** 2
+        self._check(self.L.ettk_gpu_set_reference_spherical_wedge(self._ctx, int(r), w.ctypes.data),
+                    "set_reference_spherical_wedge")
+
     def symmetrize_rotational(self, vol):
         """Rotational (cylindrical) symmetrisation about z of a [z][y][x] volume, as the classification loop's
         apply_rotational_symmetry; returns [z][y][x] (the angular sum, about 180 times the mean)."""

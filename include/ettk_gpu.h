@@ -117,6 +117,22 @@ int ettk_gpu_variance(ettk_ctx *ctx, int M, const int *particles, const float *w
    with the mean of its valid voxels removed. fold = 1 returns the volume unchanged. N^3 floats, x fastest. */
 int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
 
+/* Spherical missing wedge of a class average (nbfWedgedAverageImage3D::updateAccumulatedSphericalWedgeImageMPI and
+   updateSphericalWedgeImage, inc/em/nbfWedgedAverageImage3D.h:612-665): for the members with weight != 0 (own
+   matrix reset, as ettk_gpu_average resamples them), the binary spherical wedge under the alignment
+   matrices[16*i] (nbfWedge3D::getSphericalImage, inc/em/nbfWedge3D.h:363-429) counted per sample of the
+   (2B)^2 grid ([polar][azimuth], count optional), and wedge = 1 where count > max(count) / 2, else 0. */
+int ettk_gpu_average_spherical_wedge(ettk_ctx *ctx, int M, const int *particles, const float *weights,
+                                     const double *matrices, float *count, float *wedge);
+
+/* Explicit spherical wedge for reference r (nbfWedge3D::setSphericalImage, as the MRA loop hands an average's
+   wedge to its precomputed reference, inc/em/nbfLoopClustering.h:1270-1278): the binary (2B)^2 map replaces the
+   one derived from the reference's wedge angles in the SO(3) stage, conditioned as every spherical window is
+   (Gaussian std 2, radius factor 1; used when its sum is at most 0.95 of the grid). Lasts until the next
+   ettk_gpu_set_references. The half-spectrum wedge of the translational stage stays the analytic one, as
+   nbfWedge3D::getImageHalf ignores explicit images (inc/em/nbfWedge3D.h:312-360). */
+int ettk_gpu_set_reference_spherical_wedge(ettk_ctx *ctx, int r, const float *wedge);
+
 /* Rotational symmetrisation of the classification loop (apply_rotational_symmetry,
    src/MPI_Classification.cpp:1005-1024, with nbfCylindricalDomain3, inc/nbfCylindricalDomain3.h:126-233): the
    volume sampled on a cylinder about the z axis through (N/2, N/2) (N/2 radii from 0 to N/2, 180 angles over
@@ -151,7 +167,9 @@ int ettk_gpu_soft_weights(int R, int V, const float *D, int ld, float *W, float 
    ettk_gpu_align_pairs), assigns each particle to the class of smallest distance (labels[V]; dist_out[V] its
    distance, optional), rebuilds each class reference as the wedge-weighted average of its members under their
    alignments (as ettk_gpu_average; an empty class keeps its reference) and makes the averages the references
-   of the next pass. refs_out (optional, R*N^3 floats, x fastest) receives the last averages. */
+   of the next pass; with wedge compensation each new reference carries its class's spherical wedge
+   (ettk_gpu_average_spherical_wedge + ettk_gpu_set_reference_spherical_wedge). refs_out (optional, R*N^3
+   floats, x fastest) receives the last averages. */
 int ettk_gpu_classify(ettk_ctx *ctx, int iterations, int *labels, float *refs_out, float *dist_out);
 
 /* Continuous 6-DOF refinement of aligned pairs (no counterpart in the reference, whose refine() runs a

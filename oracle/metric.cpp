@@ -54,6 +54,7 @@ typedef struct {
   double matrix[16];          /* nbfWedgedSubImage3D::matrix (row major) */
   float position[3];
   float cut_offset;
+  const float *spherical_wedge; /* explicit binary spherical wedge [2B][2B] (nbfWedge3D::setSphericalImage) or NULL */
 } OracleVolume;
 
 typedef struct {
@@ -268,7 +269,9 @@ void spherical_wedge(const OracleVolume &v, int B, std::vector<float> &W) {
   int n = 2 * B;
   Wedge w = make_wedge(v.lwedge, v.uwedge);
   W.assign((long)n * n, 1.0f);
-  if (!w.full()) {
+  if (v.spherical_wedge) {  /* an explicit image is returned as is (no transform: 363-375) */
+    W.assign(v.spherical_wedge, v.spherical_wedge + (long)n * n);
+  } else if (!w.full()) {
     M4 local = local_matrix(v), inv;
     if (!m4_invert(local.e, inv.e)) inv = local;
     double v1[3], v2[3];
@@ -1041,6 +1044,51 @@ int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, do
     for (long k = 0; k < n3; ++k) acc[k] += img[k];
   }
   for (long k = 0; k < n3; ++k) out[k] = acc[k] / fold;
+  return 0;
+}
+
+/* Spherical wedge of a class average: nbfWedgedAverageImage3D::updateAccumulatedSphericalWedgeImageMPI
+ * (inc/em/nbfWedgedAverageImage3D.h:612-648) sums, over members with |w| > 0 (matrix reset by setTransform(NULL)),
+ * the binary analytic wedge of nbfWedge3D::getSphericalImage (inc/em/nbfWedge3D.h:363-429) under
+ * inv(Euler(normal) * alignment) (nbfWedgedSubImage3D::getSphericalWedgeImage, inc/em/nbfWedgedSubImage3D.h:1007-1041),
+ * in float; updateSphericalWedgeImage (650-665) keeps accum > max(accum) / 2. count and wedge [2B][2B]. */
+int oracle_average_spherical_wedge(const OracleParams *P, int M, const OracleVolume *vols, const float *weights,
+                                   const double *mats, float *count, float *wedge) {
+  const int B = P->B, n = 2 * B;
+  const long nn = (long)n * n;
+  std::vector<float> acc(nn, 0.0f);
+  for (int m = 0; m < M; ++m) {
+    if (!(fabsf(weights[m]) > 0)) continue;
+    OracleVolume v = vols[m];
+    for (int k = 0; k < 16; ++k) v.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    Wedge w = make_wedge(v.lwedge, v.uwedge);
+    if (w.full()) {
+      for (long k = 0; k < nn; ++k) acc[k] += 1.0f;
+      continue;
+    }
+    M4 t, fin, inv;
+    memcpy(t.e, mats + 16 * (long)m, sizeof(t.e));
+    M4 local = local_matrix(v);
+    m4_mul(local.e, t.e, fin.e);
+    if (!m4_invert(fin.e, inv.e)) inv = fin;
+    double v1[3], v2[3];
+    m4_transform_vector(inv.e, w.n1, v1);
+    m4_transform_vector(inv.e, w.n2, v2);
+    float phiK = (float)(M_PI / (n - 1));
+    float thetaK = (float)(2.0 * M_PI / (n - 1));
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        float cj = cosf(j * thetaK), sj = sinf(j * thetaK), si = sinf(i * phiK), ci = cosf(i * phiK);
+        double a = v1[0] * cj * si + v1[1] * sj * si + v1[2] * ci;
+        double b = v2[0] * cj * si + v2[1] * sj * si + v2[2] * ci;
+        acc[(long)i * n + j] += (a * b <= 0.0) ? 1.0f : 0.0f;
+      }
+  }
+  float mx = *std::max_element(acc.begin(), acc.end());
+  for (long k = 0; k < nn; ++k) {
+    if (count) count[k] = acc[k];
+    wedge[k] = (acc[k] > mx / 2.0) ? 1.0f : 0.0f;
+  }
   return 0;
 }
 

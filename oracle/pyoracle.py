@@ -36,6 +36,7 @@ class OracleVolume(ctypes.Structure):
         ("lwedge", ctypes.c_float), ("uwedge", ctypes.c_float),
         ("normal", ctypes.c_float * 3), ("matrix", ctypes.c_double * 16),
         ("position", ctypes.c_float * 3), ("cut_offset", ctypes.c_float),
+        ("spherical_wedge", ctypes.POINTER(ctypes.c_float)),
     ]
 
 
@@ -89,6 +90,7 @@ def lib():
         L.oracle_symmetrize.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p]
         L.oracle_variance.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oracle_symmetrize_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_average_spherical_wedge.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -120,6 +122,10 @@ def make_volume(data, meta):
     v.matrix[:] = list(np.asarray(meta.get("matrix", np.eye(4)), dtype=np.float64).reshape(16))
     v.position[:] = list(meta.get("position", (nx / 2.0, ny / 2.0, nz / 2.0)))
     v.cut_offset = meta.get("cut_offset", 0.0)
+    if meta.get("spherical_wedge") is not None:
+        w = np.ascontiguousarray(meta["spherical_wedge"], np.float32)
+        v.spherical_wedge = w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        v._keep_w = w
     return v
 
 
@@ -256,6 +262,26 @@ def symmetrize(params, vol, fold):
     out = np.zeros(N ** 3, np.float64)
     lib().oracle_symmetrize(ctypes.byref(P), ctypes.byref(v), int(fold), out.ctypes.data)
     return out.reshape(N, N, N)
+
+
+def average_spherical_wedge(params, vols, metas, weights, mats):
+    """Spherical wedge of the class average of the volumes under `mats`: (binary wedge, count), [2B][2B]."""
+    P = make_params(params)
+    n = len(vols)
+    arr = (OracleVolume * n)()
+    keep = []
+    for i in range(n):
+        v = make_volume(vols[i], metas[i])
+        keep.append(v)
+        arr[i] = v
+    w = np.ascontiguousarray(np.asarray(weights, np.float32))
+    m = np.ascontiguousarray(np.asarray(mats, np.float64).reshape(n, 16))
+    n2 = 2 * params["B"]
+    count = np.zeros((n2, n2), np.float32)
+    wedge = np.zeros((n2, n2), np.float32)
+    lib().oracle_average_spherical_wedge(ctypes.byref(P), n, ctypes.addressof(arr), w.ctypes.data, m.ctypes.data,
+                                         count.ctypes.data, wedge.ctypes.data)
+    return wedge, count
 
 
 def symmetrize_rotational(vol):
