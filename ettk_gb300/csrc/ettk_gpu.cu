@@ -2701,6 +2701,46 @@ int ettk_gpu_symmetrize(ettk_ctx *c, const float *vol, int fold, float *out) {
   return guarded(c, [&] { c->symmetrize(vol, fold, out); });
 }
 
+int ettk_gpu_representation_distances(ettk_ctx *c, int V, int K, int depth, const float *R, int overlap_normalized,
+                                      float *D) {
+  if (!c || V < 1 || K < 1 || (depth != 1 && depth != 3) || !R || !D) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  const long n = (long)V * K * depth;
+  bool binary = depth == 3;
+  for (long k = 0; k < n; ++k) {
+    if (!std::isfinite(R[k])) return fail(c, ETTK_ERR_NAN, "non-finite representation");
+    if (depth == 3 && k % 3 == 2 && R[k] != 0.f && R[k] != 1.f) binary = false;
+  }
+  return guarded(c, [&] {
+    DevBuf<float> dR, dD;
+    struct Release {  // the buffers are freed however the call ends
+      DevBuf<float> &a, &b;
+      ~Release() {
+        a.release();
+        b.release();
+      }
+    } release{dR, dD};
+    dR.ensure(n);
+    dD.ensure((long)V * V);
+    CK(cudaMemcpyAsync(dR.p, R, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemsetAsync(dD.p, 0, (size_t)V * V * sizeof(float), c->st));
+    const int nb = (V + RD_T - 1) / RD_T;
+    const unsigned tiles = (unsigned)((long)nb * (nb + 1) / 2);
+    {
+      ettk_ctx::Scope sc(c, "repr_dist", (double)n * 4 * nb);
+      if (depth == 3 && binary)
+        k_repr_dist<3, true><<<tiles, 256, 0, c->st>>>(dR.p, V, K, overlap_normalized, dD.p);
+      else if (depth == 3)
+        k_repr_dist<3, false><<<tiles, 256, 0, c->st>>>(dR.p, V, K, overlap_normalized, dD.p);
+      else
+        k_repr_dist<1, false><<<tiles, 256, 0, c->st>>>(dR.p, V, K, overlap_normalized, dD.p);
+      c->post_launch();
+    }
+    CK(cudaMemcpyAsync(D, dD.p, (size_t)V * V * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    c->sync();
+    c->check_status();
+  });
+}
+
 int ettk_gpu_average_spherical_wedge(ettk_ctx *c, int M, const int *particles, const float *weights,
                                      const double *matrices, float *count, float *wedge) {
   if (!c || M < 1 || !particles || !weights || !matrices || !wedge) return fail(c, ETTK_ERR_ARG, "invalid arguments");

@@ -774,6 +774,103 @@ static __global__ void k_var_finish(const double *__restrict__ var, int N, float
   }
 }
 
+// ---- distances between low-dimensional representations ------------------------------------------
+// nbfCorrelationImageMetric::getDistances(representationFile, D) (inc/em/nbfCorrelationImageMetric.h:1726-1871):
+// R is the reference's representation array R(V, K, depth) in C order. depth 3 (getLowDimensionRepresentationHalf:
+// re, im, wedge bit per kept coefficient): c1 = c_i w_i w_j, c2 = c_j w_i w_j, d = c1 - c2 in complex<float>,
+// |d|^2 = d.re d.re + d.im d.im in float; overlap-normalised: sum_k |d|^2 in double (blitz sums float arrays in
+// double) / (float) sum_k w_i w_j; otherwise mean: a float running sum / K. depth 1 (the real representation):
+// sqrt of sum_{k >= 1} (r_i - r_j)^2 (float squares, double sum). Every pair accumulates sequentially in k with
+// each operation rounded on its own, so D matches the CPU bit for bit. One CTA per 32 x 32 tile of the upper
+// triangle (tiles with tj >= ti), 256 threads, 4 pairs a thread (one i, four consecutive j); the i and j rows of
+// each 32-coefficient chunk staged in shared memory as float4 (re, im, w, 0), k-major. BINARY (every weight 0 or
+// 1, as getLowDimensionRepresentationHalf writes them): the weighted values are the values themselves or zeros,
+// and the overlap is an integer count, so one FP64 add per pair and coefficient suffices for the same result.
+constexpr int RD_T = 32, RD_KC = 32;
+
+template <int DEPTH, bool BINARY>
+__global__ void __launch_bounds__(256) k_repr_dist(const float *__restrict__ R, int V, int K, int normalized,
+                                                   float *__restrict__ D) {
+  __shared__ float4 sI[RD_KC][RD_T], sJ[RD_KC][RD_T];
+  // tile (ti, tj) with tj >= ti from the linear block index (row-major over the upper triangle)
+  const int nb = (V + RD_T - 1) / RD_T;
+  int b = blockIdx.x, ti = 0;
+  while (b >= nb - ti) {
+    b -= nb - ti;
+    ++ti;
+  }
+  const int tj = ti + b;
+  const int i0 = ti * RD_T, j0 = tj * RD_T;
+  const int li = threadIdx.x >> 3, lj = (threadIdx.x & 7) * 4;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0}, ov[4] = {0.0, 0.0, 0.0, 0.0};
+  float accf[4] = {0.f, 0.f, 0.f, 0.f};
+  int cnt[4] = {0, 0, 0, 0};
+  const int kstart = DEPTH == 1 ? 1 : 0;
+  for (int k0 = 0; k0 < K; k0 += RD_KC) {
+    for (int t = threadIdx.x; t < 2 * RD_KC * RD_T; t += blockDim.x) {
+      const int side = t / (RD_KC * RD_T), r = (t / RD_KC) % RD_T, kk = t % RD_KC;
+      const int row = (side ? j0 : i0) + r, k = k0 + kk;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row < V && k < K) {
+        const float *p = R + ((long)row * K + k) * DEPTH;
+        v.x = p[0];
+        if (DEPTH == 3) {
+          v.y = p[1];
+          v.z = p[2];
+        }
+      }
+      (side ? sJ : sI)[kk][r] = v;
+    }
+    __syncthreads();
+    const int kn = min(RD_KC, K - k0);
+    for (int kk = 0; kk < kn; ++kk) {
+      if (k0 + kk < kstart) continue;
+      const float4 a = sI[kk][li];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 c = sJ[kk][lj + q];
+        if (DEPTH == 3 && BINARY) {
+          // w = 1: c1 - c2 is the plain difference; w = 0: both weighted values are zeros and |d|^2 = +0
+          const bool on = a.z != 0.f && c.z != 0.f;
+          const float dr = __fsub_rn(a.x, c.x), di = __fsub_rn(a.y, c.y);
+          const float t2 = on ? __fadd_rn(__fmul_rn(dr, dr), __fmul_rn(di, di)) : 0.f;
+          acc[q] = __dadd_rn(acc[q], (double)t2);
+          accf[q] = __fadd_rn(accf[q], t2);
+          cnt[q] += on;
+        } else if (DEPTH == 3) {
+          const float w = __fmul_rn(a.z, c.z);
+          const float r1 = __fmul_rn(__fmul_rn(a.x, a.z), c.z), i1 = __fmul_rn(__fmul_rn(a.y, a.z), c.z);
+          const float r2 = __fmul_rn(__fmul_rn(c.x, a.z), c.z), i2 = __fmul_rn(__fmul_rn(c.y, a.z), c.z);
+          const float dr = __fsub_rn(r1, r2), di = __fsub_rn(i1, i2);
+          const float t2 = __fadd_rn(__fmul_rn(dr, dr), __fmul_rn(di, di));
+          acc[q] = __dadd_rn(acc[q], (double)t2);
+          accf[q] = __fadd_rn(accf[q], t2);
+          ov[q] = __dadd_rn(ov[q], (double)w);
+        } else {
+          const float d = __fsub_rn(a.x, c.x);
+          acc[q] = __dadd_rn(acc[q], (double)__fmul_rn(d, d));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const int i = i0 + li;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = j0 + lj + q;
+    if (i >= V || j >= V || j <= i) continue;
+    float d;
+    if (DEPTH == 1) {
+      d = (float)sqrt(acc[q]);
+    } else {
+      const float overlap = BINARY ? (float)cnt[q] : (float)ov[q];
+      d = (normalized && overlap > 0) ? (float)(acc[q] / (double)overlap) : __fdiv_rn(accf[q], (float)K);
+    }
+    D[(long)i * V + j] = d;
+    D[(long)j * V + i] = d;
+  }
+}
+
 // ---- spherical wedge of a class average --------------------------------------------------------
 // updateAccumulatedSphericalWedgeImageMPI (inc/em/nbfWedgedAverageImage3D.h:612-648): per sample (i, j) of the
 // (2B)^2 grid, the number of members whose binary spherical wedge covers it. Each member's wedge is the analytic

@@ -168,6 +168,21 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
         return out
 
+    def representation_distances(self, R, overlap_normalized=None):
+        """nbfCorrelationImageMetric::getDistances(representations, D): R is (V, K, 3) (re, im, wedge bit) or
+        (V, K, 1) float32; returns the symmetric (V, V) distance matrix."""
+        R = np.ascontiguousarray(R, np.float32)
+        if R.ndim == 2:
+            R = R[:, :, None]
+        V, K, depth = R.shape
+        if overlap_normalized is None:
+            overlap_normalized = self.params["overlap_normalized"]
+        D = np.zeros((V, V), np.float32)
+        self._check(self.L.ettk_gpu_representation_distances(self._ctx, V, K, depth, R.ctypes.data,
+                                                             int(bool(overlap_normalized)), D.ctypes.data),
+                    "representation_distances")
+        return D
+
     def average_spherical_wedge(self, particles, weights, matrices):
         """Spherical wedge of the class average of `particles` under `matrices` (updateSphericalWedgeImage).
         Returns (binary wedge [2B][2B], member count per sample [2B][2B])."""

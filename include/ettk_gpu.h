@@ -117,6 +117,17 @@ int ettk_gpu_variance(ettk_ctx *ctx, int M, const int *particles, const float *w
    with the mean of its valid voxels removed. fold = 1 returns the volume unchanged. N^3 floats, x fastest. */
 int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
 
+/* Distance matrix between low-dimensional representations (nbfCorrelationImageMetric::getDistances(file, D),
+   inc/em/nbfCorrelationImageMetric.h:1726-1871, the pairwise step of the unsupervised classification). R is
+   the reference's representation array R(V, K, depth) in C order: depth 3 = (re, im, wedge bit) of the K kept
+   Fourier coefficients (getLowDimensionRepresentationHalf), depth 1 = a real vector
+   (getLowDimensionRepresentationReal). D (V*V floats, symmetric, zero diagonal) receives for depth 3 the squared
+   difference of the two spectra on their common wedge, sum |c_i w_i w_j - c_j w_i w_j|^2 divided by the
+   overlap sum w_i w_j (overlap_normalized != 0 and overlap > 0) or averaged over K; for depth 1 the Euclidean
+   distance of entries 1..K-1. Same float / double roundings as the reference (bit-identical results). */
+int ettk_gpu_representation_distances(ettk_ctx *ctx, int V, int K, int depth, const float *R, int overlap_normalized,
+                                      float *D);
+
 /* Spherical missing wedge of a class average (nbfWedgedAverageImage3D::updateAccumulatedSphericalWedgeImageMPI and
    updateSphericalWedgeImage, inc/em/nbfWedgedAverageImage3D.h:612-665): for the members with weight != 0 (own
    matrix reset, as ettk_gpu_average resamples them), the binary spherical wedge under the alignment

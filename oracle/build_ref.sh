@@ -1,9 +1,9 @@
 #!/bin/sh
 # Builds oracle/_ref/libsoft_ref.so from the reference's own SOFT 1.0 C sources
 # (read in place under the reference tree, never copied) plus the project's
-# fftw3.h shim and harness, and oracle/_ref/libcyl_ref.so from the reference's
-# cylindrical-domain headers on its vendored Blitz. Test infrastructure only;
-# needs the reference tree.
+# fftw3.h shim and harness, and oracle/_ref/libblitz_ref.so from the reference's
+# cylindrical-domain headers and representation-distance loop on its vendored
+# Blitz. Test infrastructure only; needs the reference tree.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${ETTK_REFERENCE_ROOT:-/root/reference}"
@@ -24,10 +24,11 @@ g++ -O2 -fPIC -std=c++17 -c "$HERE/fft64.cpp" -o "$OUT/obj/fft64.o" &
 wait
 g++ -shared -o "$OUT/libsoft_ref.so" "$OUT"/obj/*.o -lm
 echo "built $OUT/libsoft_ref.so"
-# The reference's cylindrical-domain classes (header-only, on its vendored Blitz 0.9) behind a C harness.
+# The reference's cylindrical-domain classes (header-only) and the representation-distance loop, on its
+# vendored Blitz 0.9, behind C harnesses.
 BLITZ="$REF/external/blitz-0.9"
 if [ -d "$BLITZ/blitz" ]; then
   g++ -O2 -fPIC -std=c++11 -w -ffp-contract=off -shared -I"$BLITZ" -I"$REF/inc" \
-    "$HERE/shim/cyl_ref_wrap.cpp" -o "$OUT/libcyl_ref.so"
-  echo "built $OUT/libcyl_ref.so"
+    "$HERE/shim/cyl_ref_wrap.cpp" "$HERE/shim/repr_blitz_wrap.cpp" -o "$OUT/libblitz_ref.so"
+  echo "built $OUT/libblitz_ref.so"
 fi

@@ -1047,6 +1047,44 @@ int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, do
   return 0;
 }
 
+/* nbfCorrelationImageMetric::getDistances(representationFile, D) (inc/em/nbfCorrelationImageMetric.h:1726-1871),
+ * single-process branch, with Blitz 0.9's types: complex<float> products and differences, sum() of a float
+ * expression accumulated in double, mean() in float, Pixel overlap stored as float. R(V, K, depth) C order;
+ * D (V*V) zero diagonal, symmetric. */
+int oracle_representation_distances(int V, int K, int depth, const float *R, int normalized, float *D) {
+  for (long k = 0; k < (long)V * V; ++k) D[k] = 0;
+  for (int i = 0; i < V; ++i)
+    for (int j = i + 1; j < V; ++j) {
+      float d;
+      if (depth == 1) {
+        double s = 0;
+        for (int k = 1; k < K; ++k) {
+          float e = R[(long)i * K + k] - R[(long)j * K + k];
+          s += (double)(e * e);
+        }
+        d = (float)sqrt(s);
+      } else {
+        double s = 0, ov = 0;
+        float sf = 0;
+        for (int k = 0; k < K; ++k) {
+          const float *a = R + ((long)i * K + k) * 3, *b = R + ((long)j * K + k) * 3;
+          float w1 = a[2], w2 = b[2];
+          float r1 = a[0] * w1 * w2, i1 = a[1] * w1 * w2, r2 = b[0] * w1 * w2, i2 = b[1] * w1 * w2;
+          float dr = r1 - r2, di = i1 - i2;
+          float t = dr * dr + di * di;
+          s += t;
+          sf += t;
+          ov += (double)(w1 * w2);
+        }
+        float overlap = (float)ov;
+        d = (normalized && overlap > 0) ? (float)(s / overlap) : sf / K;
+      }
+      D[(long)i * V + j] = d;
+      D[(long)j * V + i] = d;
+    }
+  return 0;
+}
+
 /* Spherical wedge of a class average: nbfWedgedAverageImage3D::updateAccumulatedSphericalWedgeImageMPI
  * (inc/em/nbfWedgedAverageImage3D.h:612-648) sums, over members with |w| > 0 (matrix reset by setTransform(NULL)),
  * the binary analytic wedge of nbfWedge3D::getSphericalImage (inc/em/nbfWedge3D.h:363-429) under

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libsoft_ref.so")
-CYL_REF_PATH = os.path.join(HERE, "_ref", "libcyl_ref.so")
+BLITZ_REF_PATH = os.path.join(HERE, "_ref", "libblitz_ref.so")
 
 
 class OracleParams(ctypes.Structure):
@@ -91,6 +91,8 @@ def lib():
         L.oracle_variance.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oracle_symmetrize_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_average_spherical_wedge.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
+        L.oracle_representation_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int,
+                                                                            ctypes.c_void_p]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -264,6 +266,17 @@ def symmetrize(params, vol, fold):
     return out.reshape(N, N, N)
 
 
+def representation_distances(R, normalized=True):
+    """getDistances over a representation array R (V, K, depth); returns (V, V) float32."""
+    R = np.ascontiguousarray(R, np.float32)
+    if R.ndim == 2:
+        R = R[:, :, None]
+    V, K, depth = R.shape
+    D = np.zeros((V, V), np.float32)
+    lib().oracle_representation_distances(V, K, depth, R.ctypes.data, int(bool(normalized)), D.ctypes.data)
+    return D
+
+
 def average_spherical_wedge(params, vols, metas, weights, mats):
     """Spherical wedge of the class average of the volumes under `mats`: (binary wedge, count), [2B][2B]."""
     P = make_params(params)
@@ -350,22 +363,45 @@ def ref_lib():
     return _ref
 
 
-_cyl_ref = None
+_blitz_ref = None
+
+
+def blitz_ref_lib():
+    """Harnesses on the reference's Blitz (oracle/_ref/libblitz_ref.so), or None when absent."""
+    global _blitz_ref
+    if _blitz_ref is None:
+        if not os.path.exists(BLITZ_REF_PATH):
+            return None
+        L = ctypes.CDLL(BLITZ_REF_PATH)
+        L.cyl_ref_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.repr_ref_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        _blitz_ref = L
+    return _blitz_ref
 
 
 def ref_symmetrize_rotational(vol):
-    """The reference's own cylindrical-domain classes run through the rotational-symmetry step
-    (oracle/_ref/libcyl_ref.so); [x][y][z], or None when that library is absent."""
-    global _cyl_ref
-    if _cyl_ref is None:
-        if not os.path.exists(CYL_REF_PATH):
-            return None
-        L = ctypes.CDLL(CYL_REF_PATH)
-        L.cyl_ref_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
-        _cyl_ref = L
+    """The reference's own cylindrical-domain classes run through the rotational-symmetry step;
+    [x][y][z], or None when the harness library is absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
     v = np.ascontiguousarray(vol, np.float32)
     N = v.shape[0]
     out = np.zeros(N ** 3, np.float64)
-    if _cyl_ref.cyl_ref_rotational(N, v.ctypes.data, out.ctypes.data) != 0:
+    if L.cyl_ref_rotational(N, v.ctypes.data, out.ctypes.data) != 0:
         raise ValueError("N must be even and at least 4")
     return out.reshape(N, N, N)
+
+
+def ref_representation_distances(R, normalized=True):
+    """The representation-distance loop in the reference's Blitz expressions; None when absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    R = np.ascontiguousarray(R, np.float32)
+    if R.ndim == 2:
+        R = R[:, :, None]
+    V, K, depth = R.shape
+    D = np.zeros((V, V), np.float32)
+    L.repr_ref_distances(V, K, depth, R.ctypes.data, int(bool(normalized)), D.ctypes.data)
+    return D

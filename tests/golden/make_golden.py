@@ -9,10 +9,13 @@ align32_b16.npz  oracle alignments of the first particles of the 32^3 B=16 workl
 align128_b64.npz oracle alignments of the first two particles of the 128^3 B=64 workload (the large-size
                path: (2N)^3 = 256^3 spherical projections, B=64 SO(3) correlations), with a checksum.
 rotsym_n16.npz the rotational-symmetry step of the classification loop run by the reference's own
-               cylindrical-domain classes (oracle/_ref/libcyl_ref.so) on a seeded 16^3 volume and on a
+               cylindrical-domain classes (oracle/_ref/libblitz_ref.so) on a seeded 16^3 volume and on a
                volume with an off-axis blob.
+repr_dist.npz  distance matrices between seeded low-dimensional representations (depth 3 with wedge bits,
+               and depth 1) from the representation-distance loop in the reference's Blitz expressions
+               (oracle/_ref/libblitz_ref.so), overlap-normalised and averaged.
 
-Usage: python make_golden.py [soft|align32|align128|rotsym ...]   (no argument: all)
+Usage: python make_golden.py [soft|align32|align128|rotsym|repr ...]   (no argument: all)
 """
 import hashlib
 import os
@@ -55,7 +58,29 @@ def rotsym_inputs():
     return np.stack([noise, blob])
 
 
+def repr_inputs():
+    rng = np.random.default_rng(77)
+    V, K = 13, 240
+    R3 = np.zeros((V, K, 3), np.float32)
+    R3[:, :, 0] = rng.standard_normal((V, K)) * (1 + np.arange(K) % 5)
+    R3[:, :, 1] = rng.standard_normal((V, K))
+    R3[:, :, 2] = (rng.random((V, K)) > 0.3).astype(np.float32)
+    R3[4, :, 2] = 0  # a volume sharing no coefficient with any other: overlap 0 falls back to the mean
+    R1 = rng.standard_normal((V, K, 1)).astype(np.float32)
+    return R3, R1
+
+
 def main(which):
+    if "repr" in which:
+        R3, R1 = repr_inputs()
+        out = {"R3": R3, "R1": R1}
+        for norm in (0, 1):
+            d3 = pyoracle.ref_representation_distances(R3, norm)
+            if d3 is None:
+                raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+            out["D3_%d" % norm] = d3
+            out["D1_%d" % norm] = pyoracle.ref_representation_distances(R1, norm)
+        np.savez_compressed(os.path.join(HERE, "repr_dist.npz"), **out)
     if "rotsym" in which:
         vols = rotsym_inputs()
         outs = [pyoracle.ref_symmetrize_rotational(v) for v in vols]
@@ -84,4 +109,4 @@ def main(which):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym"])
+    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym", "repr"])

@@ -1,0 +1,87 @@
+"""Distances between low-dimensional representations (nbfCorrelationImageMetric::getDistances(file, D),
+inc/em/nbfCorrelationImageMetric.h:1726-1871), the pairwise step of the unsupervised classification.
+
+The oracle restates the loop with the roundings Blitz gives it (complex<float> element arithmetic, sum() in
+double, mean() in float); tests/golden/repr_dist.npz holds the outputs of that loop written in the reference's
+own Blitz expressions on its vendored Blitz (oracle/_ref/libblitz_ref.so). Everything here is bit-exact: the
+GPU kernel accumulates every pair sequentially in k with each operation rounded as on the CPU."""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+from ettk_gb300 import synthetic
+from ettk_gb300.metric import ProjectionRotationMetric3D
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "repr_dist.npz")
+
+
+def rand_repr(V, K, depth, seed, binary=True):
+    rng = np.random.default_rng(seed)
+    R = rng.standard_normal((V, K, depth)).astype(np.float32)
+    if depth == 3:
+        R[:, :, 2] = (rng.random((V, K)) > 0.25) if binary else rng.uniform(0, 1.5, (V, K))
+    return np.ascontiguousarray(R, np.float32)
+
+
+def test_oracle_matches_reference_golden():
+    g = np.load(GOLDEN)
+    for norm in (0, 1):
+        assert np.array_equal(pyoracle.representation_distances(g["R3"], norm), g["D3_%d" % norm])
+        assert np.array_equal(pyoracle.representation_distances(g["R1"], norm), g["D1_%d" % norm])
+
+
+@pytest.mark.parametrize("binary", [True, False])
+def test_oracle_matches_reference_library(binary):
+    R = rand_repr(21, 517, 3, 5, binary)
+    r = pyoracle.ref_representation_distances(R, True)
+    if r is None:
+        pytest.skip("reference harness not built here (oracle/build_ref.sh needs the reference tree)")
+    assert np.array_equal(pyoracle.representation_distances(R, True), r)
+    assert np.array_equal(pyoracle.representation_distances(R, False), pyoracle.ref_representation_distances(R, False))
+
+
+def test_oracle_properties():
+    R = rand_repr(6, 64, 3, 9)
+    D = pyoracle.representation_distances(R, True)
+    assert np.array_equal(D, D.T) and (np.diag(D) == 0).all() and (D >= 0).all()
+    R[3] = R[1]
+    D = pyoracle.representation_distances(R, True)
+    assert D[1, 3] == 0
+
+
+@pytest.fixture(scope="module")
+def metric():
+    m = ProjectionRotationMetric3D(synthetic.default_params(synthetic.WORKLOADS["align32_b16"]))
+    yield m
+    m.close()
+
+
+@pytest.mark.gpu
+def test_gpu_golden(metric):
+    g = np.load(GOLDEN)
+    for norm in (0, 1):
+        assert np.array_equal(metric.representation_distances(g["R3"], norm), g["D3_%d" % norm])
+        assert np.array_equal(metric.representation_distances(g["R1"], norm), g["D1_%d" % norm])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("V,K", [(1, 5), (2, 3), (70, 1007), (97, 64)])
+@pytest.mark.parametrize("depth", [3, 1])
+@pytest.mark.parametrize("norm", [1, 0])
+def test_gpu_matches_oracle(metric, V, K, depth, norm):
+    R = rand_repr(V, K, depth, V * K + depth, binary=(V % 2 == 0))
+    g = metric.representation_distances(R, norm)
+    o = pyoracle.representation_distances(R, norm)
+    assert np.array_equal(g, o), np.abs(g - o).max()
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_bad_input(metric):
+    R = rand_repr(4, 10, 3, 1)
+    R[2, 3, 0] = np.inf
+    with pytest.raises(Exception):
+        metric.representation_distances(R)
+    with pytest.raises(Exception):
+        metric.representation_distances(np.zeros((3, 4, 2), np.float32))
