@@ -61,7 +61,7 @@ SYMBOLS = [
     "ettk_gpu_refine_objective", "ettk_gpu_classify", "ettk_gpu_set_particles_tomogram", "ettk_gpu_variance",
     "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
-    "ettk_gpu_representation_distances",
+    "ettk_gpu_representation_distances", "ettk_gpu_representations",
 ]
 
 _lib = None
@@ -103,6 +103,7 @@ def load(path=None):
     L.ettk_gpu_symmetrize_rotational.argtypes = [vp, vp, vp]
     L.ettk_gpu_average_spherical_wedge.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_set_reference_spherical_wedge.argtypes = [vp, ctypes.c_int, vp]
+    L.ettk_gpu_representations.argtypes = [vp, ctypes.c_int, vp, P(ctypes.c_int), vp]
     L.ettk_gpu_representation_distances.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                     vp]
     L.ettk_gpu_outlier_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float,

@@ -337,6 +337,12 @@ struct EvalRes {
 
 }  // namespace
 
+namespace {  // host helpers defined further down
+template <class F>
+void parallel_for(int n, F f);
+void wedge_half_host(const VolumeGeom &g, int N, std::vector<float> &W);
+}  // namespace
+
 struct ettk_ctx {
   int device = 0;
   ettk_params p{};
@@ -776,6 +782,11 @@ struct ettk_ctx {
   void symmetrize_rotational(const float *vol, float *out);
   void average_spherical_wedge(int M, const int *parts, const float *weights, const double *mats, float *count,
                                float *wedge);
+  // kept-coefficient offsets of the representation band (kz-major) in the reference's order, cached
+  std::vector<int> repr_idx;
+  DevBuf<int> repr_idx_dev;
+  const std::vector<int> &representation_band();
+  void representations(int M, const int *parts, float *R);
   // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
   // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
   void reslice_members(const int *idx, int E, const int *parts, const double *mats);
@@ -1025,6 +1036,87 @@ void ettk_ctx::average_spherical_wedge(int M, const int *parts, const float *wei
   for (size_t k = 0; k < c.size(); ++k) {
     if (count) count[k] = c[k];
     wedge[k] = (c[k] > mx / 2.0) ? 1.f : 0.f;
+  }
+}
+
+// The band of getLowDimensionRepresentationHalf: coefficients with |filter| > 0.5, listed as the reference
+// iterates its [x][y][kz] half spectrum (kz fastest), as offsets into the kz-major layout.
+const std::vector<int> &ettk_ctx::representation_band() {
+  if (!repr_idx.empty()) return repr_idx;
+  const int H = N / 2 + 1;
+  std::vector<float> fk(h3);
+  CK(cudaMemcpy(fk.data(), filter.p, h3 * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int k = 0; k < H; ++k) {
+        const int g = (k * N + x) * N + y;
+        if (std::fabs(fk[g]) > 0.5f) repr_idx.push_back(g);
+      }
+  repr_idx_dev.ensure(std::max<size_t>(repr_idx.size(), 1));
+  CK(cudaMemcpy(repr_idx_dev.p, repr_idx.data(), repr_idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return repr_idx;
+}
+
+// nbfFourierImageMetric::getLowDimensionRepresentationHalf (inc/em/nbfFourierImageMetric.h:1967-2034), fold 1,
+// padding 1, for M particles: A = getImage (own geometry, mean of valid voxels removed); F = R2C(A shift) *
+// filter; a = C2R(F) * mask (the image filter's mask); F2 = R2C(a), all unnormalised as FFTW; R[m][q] = (re, im)
+// of F2 at the band's q-th coefficient and the wedge bit getWedgeImageHalf > 0.5 there.
+void ettk_ctx::representations(int M, const int *parts, float *R) {
+  const std::vector<int> &band = representation_band();
+  const int K = (int)band.size(), H = N / 2 + 1;
+  const int chunk = (int)std::max(16L, std::min(256L, 256L * 64 * 64 * 64 / n3));
+  std::vector<float2> vals;
+  for (int c0 = 0; c0 < M; c0 += chunk) {
+    const int E = std::min(chunk, M - c0);
+    std::vector<ResliceItem> items(E);
+    for (int e = 0; e < E; ++e) {
+      const int p = parts[c0 + e];
+      double m12[12];
+      reslice_index(partg[p], N, nullptr, m12);
+      items[e].vol = part_vol(p);
+      items[e].tmap = part_map(p);
+      part_dims(items[e].dims);
+      set_map(items[e], m12);
+    }
+    w_items.ensure(E);
+    w_v.ensure((long)E * n3);
+    w_cA.ensure((long)E * h3);
+    w_acc.ensure(2L * E);
+    w_p1.ensure((long)E * K);
+    CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
+    reslice(w_items.p, w_v.p, w_acc.p, 2, nullptr, E);
+    PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
+    r2c_z(N, pre, w_cA.p, (long)E * N * N);
+    xy_kxy(N, w_cA.p, E, -1);
+    switch (N) {
+      case 16: fft2d_t<16>(OpFilterShared<16>{w_cA.p, filter.p}, E); break;
+      case 32: fft2d_t<32>(OpFilterShared<32>{w_cA.p, filter.p}, E); break;
+      case 64: fft2d_t<64>(OpFilterShared<64>{w_cA.p, filter.p}, E); break;
+      case 128: fft2d_t<128>(OpFilterShared<128>{w_cA.p, filter.p}, E); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported box size for representations");
+    }
+    c2r_r2c_z(N, w_cA.p, MidMask{mask.p}, (long)E * N * N);
+    xy_kxy(N, w_cA.p, E, -1);
+    if (K) {
+      k_repr_gather<<<nblocks<int>((long)E * K, 256, 4096), 256, 0, st>>>(w_cA.p, E, h3, repr_idx_dev.p, K, w_p1.p);
+      post_launch();
+    }
+    vals.resize((size_t)E * K);
+    CK(cudaMemcpyAsync(vals.data(), w_p1.p, vals.size() * sizeof(float2), cudaMemcpyDeviceToHost, st));
+    sync();
+    check_status();
+    parallel_for(E, [&](int e) {
+      std::vector<float> w;
+      wedge_half_host(partg[parts[c0 + e]], N, w);
+      float *r = R + (size_t)(c0 + e) * K * 3;
+      for (int q = 0; q < K; ++q) {
+        const int g = band[q], kz = g / (N * N), x = (g / N) % N, y = g % N;
+        r[3 * q] = vals[(size_t)e * K + q].x;
+        r[3 * q + 1] = vals[(size_t)e * K + q].y;
+        r[3 * q + 2] = w[((size_t)x * N + y) * H + kz] > .5f ? 1.f : 0.f;
+      }
+    });
   }
 }
 
@@ -2738,6 +2830,19 @@ int ettk_gpu_representation_distances(ettk_ctx *c, int V, int K, int depth, cons
     CK(cudaMemcpyAsync(D, dD.p, (size_t)V * V * sizeof(float), cudaMemcpyDeviceToHost, c->st));
     c->sync();
     c->check_status();
+  });
+}
+
+int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int *K, float *R) {
+  if (!c || !K) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (R && (M < 1 || !particles)) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] {
+    *K = (int)c->representation_band().size();
+    if (!R) return;
+    if (c->V < 1) throw CudaError(ETTK_ERR_STATE, "set particles first");
+    for (int i = 0; i < M; ++i)
+      if (particles[i] < 0 || particles[i] >= c->V) throw CudaError(ETTK_ERR_ARG, "particle index out of range");
+    c->representations(M, particles, R);
   });
 }
 

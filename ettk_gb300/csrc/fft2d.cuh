@@ -122,6 +122,21 @@ struct OpPlain {
   ETTK_DEV void end(int, int) {}
 };
 
+// Inverse (x, y) passes of spectra multiplied by one half-grid filter shared by all items (kz-major
+// [H][N][N]): nbfFourierFilter::executeHalf without a wedge (inc/em/nbfFourierFilter.h:587-603). In place.
+template <int N>
+struct OpFilterShared {
+  float2 *d;
+  const float *filter;
+  int sign = +1;
+  ETTK_DEV void begin() {}
+  ETTK_DEV float2 load(int e, int kz, int i) const {
+    return cscale(d[KXY<N>::at(e, kz, i)], filter[KXY<N>::at(0, kz, i)]);
+  }
+  ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { d[KXY<N>::at(e, kz, i)] = v; }
+  ETTK_DEV void end(int, int) {}
+};
+
 // Forward (x, y) passes of the (2N)^3 spectrum of the padded spherical-projection volume (z pass done), storing
 // |F| (as the magnitude step of cartesianToSpherical) into a real kz-major array. The padded real volume is
 // the windowed N^3 image at x, y, z < N and the constant c (-1)^(x+y+z) elsewhere (PrePadded); the z transform

@@ -533,6 +533,14 @@ struct MidSquareShift {
     return v * v * (((cij[sl] + k) & 1) ? -1.f : 1.f);
   }
 };
+// C2R output times the real-space mask of getLowDimensionRepresentationHalf (blitzFFTreal *= mask,
+// inc/em/nbfFourierImageMetric.h:2001-2003); aux = the mask [x][y][z], shared by all items.
+struct MidMask {
+  const float *aux;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end_tile(long) {}
+  ETTK_DEV float operator()(long, int, float v, float m) { return v * m; }
+};
 // (y1 / norm) * m1 with k1_m = sum((y1 / norm)^2 m1) into acc[item][slot] (nbfFourierImageMetric.h:1143-1153):
 // the C2R output scaled by the item's 1/norm (normalizeFourierHalf, linear through the inverse passes); aux = m1.
 struct MidScaleY1M1 {
@@ -868,6 +876,17 @@ __global__ void __launch_bounds__(256) k_repr_dist(const float *__restrict__ R, 
     }
     D[(long)i * V + j] = d;
     D[(long)j * V + i] = d;
+  }
+}
+
+// Kept coefficients of getLowDimensionRepresentationHalf: out[e][q] = F[e][idx[q]] (kz-major half spectra of
+// h3 entries; idx in the reference's [x][y][kz] order of the band |filter| > 0.5).
+static __global__ void k_repr_gather(const float2 *__restrict__ F, int E, long h3, const int *__restrict__ idx, int K,
+                                     float2 *__restrict__ out) {
+  const long n = (long)E * K;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const long e = t / K;
+    out[t] = F[e * h3 + idx[t - e * K]];
   }
 }
 

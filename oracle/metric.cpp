@@ -1047,6 +1047,44 @@ int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, do
   return 0;
 }
 
+/* nbfFourierImageMetric::getLowDimensionRepresentationHalf (inc/em/nbfFourierImageMetric.h:1967-2034) with
+ * fold 1 and padding 1 (imageFilter->execute(input1, true) then bypasses the mask): A = getImage of the volume,
+ * F = R2C(A * shift) * filter (executeHalf without a wedge), a = C2R(F) * mask, F2 = R2C(a), unnormalised; the
+ * kept coefficients are those with |filter| > 0.5 in the [x][y][kz] order of the half spectrum, stored as
+ * complex<float> beside the wedge bit getWedgeImageHalf > 0.5. R (optional): K x 3 floats; *K their number. */
+int oracle_representation(const OracleParams *P, const OracleVolume *v, float *R, int *K) {
+  const int N = P->N, H = N / 2 + 1;
+  const long n3 = (long)N * N * N, h3 = (long)N * N * H;
+  std::vector<double> a;
+  get_image(*v, N, nullptr, a);
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int z = 0; z < N; ++z)
+        if ((x + y + z) & 1) a[((long)x * N + y) * N + z] *= -1.0;
+  std::vector<float> f, mask, w;
+  build_filter(*P, f);
+  build_mask(*P, mask);
+  wedge_half(*v, N, nullptr, w);
+  std::vector<cplx> F(h3);
+  rfft3d(a.data(), F.data(), N, N, N);
+  for (long i = 0; i < h3; ++i) F[i] *= (double)f[i];
+  irfft3d(F.data(), a.data(), N, N, N);
+  for (long i = 0; i < n3; ++i) a[i] *= (double)mask[i];
+  rfft3d(a.data(), F.data(), N, N, N);
+  int k = 0;
+  for (long g = 0; g < h3; ++g)
+    if (fabs(f[g]) > 0.5) {
+      if (R) {
+        R[3L * k] = (float)F[g].real();
+        R[3L * k + 1] = (float)F[g].imag();
+        R[3L * k + 2] = w[g] > .5 ? 1.0f : 0.0f;
+      }
+      ++k;
+    }
+  *K = k;
+  return 0;
+}
+
 /* nbfCorrelationImageMetric::getDistances(representationFile, D) (inc/em/nbfCorrelationImageMetric.h:1726-1871),
  * single-process branch, with Blitz 0.9's types: complex<float> products and differences, sum() of a float
  * expression accumulated in double, mean() in float, Pixel overlap stored as float. R(V, K, depth) C order;

@@ -1,9 +1,13 @@
-"""Distances between low-dimensional representations (nbfCorrelationImageMetric::getDistances(file, D),
-inc/em/nbfCorrelationImageMetric.h:1726-1871), the pairwise step of the unsupervised classification.
+"""Low-dimensional representations (nbfFourierImageMetric::getLowDimensionRepresentationHalf,
+inc/em/nbfFourierImageMetric.h:1967-2034) and the distances between them (nbfCorrelationImageMetric::getDistances
+(file, D), inc/em/nbfCorrelationImageMetric.h:1726-1871), the pairwise step of the unsupervised classification.
+
+Representations: three unnormalised FP32 3-D transforms on the GPU against the oracle's FP64 ones, held to 2e-5
+of the largest coefficient magnitude; the band (which coefficients, in which order) and the wedge bits exactly.
 
 The oracle restates the loop with the roundings Blitz gives it (complex<float> element arithmetic, sum() in
 double, mean() in float); tests/golden/repr_dist.npz holds the outputs of that loop written in the reference's
-own Blitz expressions on its vendored Blitz (oracle/_ref/libblitz_ref.so). Everything here is bit-exact: the
+own Blitz expressions on its vendored Blitz (oracle/_ref/libblitz_ref.so). The distances are bit-exact: the
 GPU kernel accumulates every pair sequentially in k with each operation rounded as on the CPU."""
 import os
 
@@ -12,7 +16,9 @@ import pytest
 
 import pyoracle
 from ettk_gb300 import synthetic
-from ettk_gb300.metric import ProjectionRotationMetric3D
+from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+
+KW = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "repr_dist.npz")
 
@@ -85,3 +91,33 @@ def test_gpu_rejects_bad_input(metric):
         metric.representation_distances(R)
     with pytest.raises(Exception):
         metric.representation_distances(np.zeros((3, 4, 2), np.float32))
+
+
+@pytest.fixture(scope="module")
+def ds32():
+    return synthetic.generate("align32_b16", n_particles=4)
+
+
+def test_oracle_representation_band_and_linearity(ds32):
+    R = pyoracle.representation(ds32.params, ds32.particles[0], ds32.meta[0])
+    assert R.shape[1] == 3 and set(np.unique(R[:, 2])) <= {0.0, 1.0}
+    R2 = pyoracle.representation(ds32.params, 2 * ds32.particles[0], ds32.meta[0])
+    assert np.allclose(R2[:, :2], 2 * R[:, :2], rtol=1e-6, atol=1e-6 * np.abs(R[:, :2]).max())
+
+
+@pytest.mark.gpu
+def test_gpu_representations(ds32):
+    n = len(ds32.meta)
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        m.set_particles([WedgedSubImage3D(ds32.particles[i], **{k: ds32.meta[i][k] for k in KW}) for i in range(n)])
+        g = m.representations([3, 0, 1, 2])
+        D = m.representation_distances(g)
+    finally:
+        m.close()
+    o = np.stack([pyoracle.representation(ds32.params, ds32.particles[i], ds32.meta[i]) for i in (3, 0, 1, 2)])
+    assert g.shape == o.shape
+    assert np.array_equal(g[:, :, 2], o[:, :, 2])
+    assert np.abs(g[:, :, :2] - o[:, :, :2]).max() <= 2e-5 * np.abs(o[:, :, :2]).max()
+    Do = pyoracle.representation_distances(o, True)
+    assert np.allclose(D, Do, rtol=1e-4, atol=1e-6 * Do.max())
