@@ -44,6 +44,9 @@ def parse():
                     help="plain grid search vs grid search + adjoint refinement on the 64^3 B=32 workload: "
                          "alignments/s and error against the generating poses (one JSON line)")
     ap.add_argument("--refine-iterations", type=int, default=15)
+    ap.add_argument("--repr-study", action="store_true",
+                    help="unsupervised-classification step on the 64^3 workload: low-dimensional representations "
+                         "of --study-pairs particles and the distance matrix between them (one JSON line)")
     return ap.parse_args()
 
 
@@ -255,8 +258,52 @@ def adjoint_study(a):
     print(json.dumps(line), flush=True)
 
 
+def repr_study(a):
+    """getLowDimensionRepresentationHalf of V 64^3 particles and the V x V distance matrix of
+    nbfCorrelationImageMetric::getDistances between them, each timed once after one small warm-up call
+    (CUDA-synchronised wall time of the library call; the distance kernel's own time from the library's event
+    profile). Rates: representations/s, and pair-coefficients/s of the distance kernel (V (V - 1) / 2 pairs
+    times K coefficients, each one FP64 accumulation)."""
+    import numpy as np
+    from ettk_gb300 import synthetic
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+
+    V = a.study_pairs
+    ds = synthetic.generate(WORKLOAD, n_particles=8)  # parameters and per-particle wedge geometries
+    N = ds.params["N"]
+    rng = np.random.default_rng(5)  # seeded noise volumes: the timings do not depend on the content
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    m = ProjectionRotationMetric3D(ds.params)
+    m.set_particles([WedgedSubImage3D(rng.standard_normal((N, N, N), dtype=np.float32),
+                                      **{k: ds.meta[i % 8][k] for k in kw}) for i in range(V)])
+    m.representation_distances(m.representations([0, 1]))  # warm-up: one launch of each kernel
+    m.profile(True)
+    t0 = time.perf_counter()
+    R = m.representations(list(range(V)))
+    t1 = time.perf_counter()
+    D = m.representation_distances(R)
+    t2 = time.perf_counter()
+    prof = m.profile_read()
+    m.profile(False)
+    m.close()
+    K = R.shape[1]
+    kd = prof.get("repr_dist", {}).get("ms", float("nan"))
+    pk = V * (V - 1) / 2 * K
+    line = {"repr_study": {"V": V, "K": K, "representations_per_s": V / (t1 - t0),
+                           "distance_matrix_s": t2 - t1, "distance_kernel_ms": kd,
+                           "pair_coefficients_per_s": pk / (kd / 1e3),
+                           "binary_weights": bool(np.isin(R[:, :, 2], (0.0, 1.0)).all()),
+                           "finite": bool(np.isfinite(D).all())},
+            "config": {"workload": WORKLOAD, "fold": 1, "overlap_normalized": bool(ds.params["overlap_normalized"]),
+                       "data": "seeded noise volumes with the workload's wedge geometries"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.repr_study:
+        repr_study(a)
+        return
     if a.adjoint_study:
         adjoint_study(a)
         return
