@@ -103,7 +103,7 @@ def load(path=None):
     L.ettk_gpu_symmetrize_rotational.argtypes = [vp, vp, vp]
     L.ettk_gpu_average_spherical_wedge.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_set_reference_spherical_wedge.argtypes = [vp, ctypes.c_int, vp]
-    L.ettk_gpu_representations.argtypes = [vp, ctypes.c_int, vp, P(ctypes.c_int), vp]
+    L.ettk_gpu_representations.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, P(ctypes.c_int), vp]
     L.ettk_gpu_representation_distances.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                     vp]
     L.ettk_gpu_outlier_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float,

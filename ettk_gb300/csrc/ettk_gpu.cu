@@ -786,7 +786,7 @@ struct ettk_ctx {
   std::vector<int> repr_idx;
   DevBuf<int> repr_idx_dev;
   const std::vector<int> &representation_band();
-  void representations(int M, const int *parts, float *R);
+  void representations(int M, const int *parts, int fold, float *R);
   // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
   // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
   void reslice_members(const int *idx, int E, const int *parts, const double *mats);
@@ -1057,14 +1057,17 @@ const std::vector<int> &ettk_ctx::representation_band() {
   return repr_idx;
 }
 
-// nbfFourierImageMetric::getLowDimensionRepresentationHalf (inc/em/nbfFourierImageMetric.h:1967-2034), fold 1,
-// padding 1, for M particles: A = getImage (own geometry, mean of valid voxels removed); F = R2C(A shift) *
-// filter; a = C2R(F) * mask (the image filter's mask); F2 = R2C(a), all unnormalised as FFTW; R[m][q] = (re, im)
-// of F2 at the band's q-th coefficient and the wedge bit getWedgeImageHalf > 0.5 there.
-void ettk_ctx::representations(int M, const int *parts, float *R) {
+// nbfFourierImageMetric::getLowDimensionRepresentationHalf (inc/em/nbfFourierImageMetric.h:1967-2034), padding 1,
+// for M particles: A = getImage (own geometry, mean of valid voxels removed); with fold > 1, A = the mean of
+// A's getImage as an average image under RotateZ(i * 360 / fold) (nbfImageFilter::symmetrize); F = R2C(A shift)
+// * filter; a = C2R(F) * mask (the image filter's mask); F2 = R2C(a), all unnormalised as FFTW; R[m][q] = (re,
+// im) of F2 at the band's q-th coefficient and the wedge bit (getWedgeImageHalf > 0.5; 1 when fold > 1).
+void ettk_ctx::representations(int M, const int *parts, int fold, float *R) {
   const std::vector<int> &band = representation_band();
   const int K = (int)band.size(), H = N / 2 + 1;
-  const int chunk = (int)std::max(16L, std::min(256L, 256L * 64 * 64 * 64 / n3));
+  const int chunk = (int)std::max(1L, std::max(16L, std::min(256L, 256L * 64 * 64 * 64 / n3)) / std::max(1, fold));
+  std::vector<ResliceItem> sym_items;
+  std::vector<double> sym_acc0;
   std::vector<float2> vals;
   for (int c0 = 0; c0 < M; c0 += chunk) {
     const int E = std::min(chunk, M - c0);
@@ -1078,15 +1081,63 @@ void ettk_ctx::representations(int M, const int *parts, float *R) {
       part_dims(items[e].dims);
       set_map(items[e], m12);
     }
-    w_items.ensure(E);
-    w_v.ensure((long)E * n3);
+    const int F = fold > 1 ? fold : 1;
+    w_items.ensure((long)E * F);
+    w_v.ensure((long)E * F * n3);
     w_cA.ensure((long)E * h3);
-    w_acc.ensure(2L * E);
+    w_acc.ensure(2L * E * F);
     w_p1.ensure((long)E * K);
     CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
     reslice(w_items.p, w_v.p, w_acc.p, 2, nullptr, E);
-    PreParticle pre{w_v.p, nullptr, w_acc.p, 2, N};
+    const float *pre_src = w_v.p;
+    const double *pre_acc = w_acc.p;
+    if (F > 1) {
+      // the images as fixed images, each resliced under the F rotations about z (as ettk_gpu_symmetrize), the
+      // mean of each item's F getImage values as its symmetrised image
+      w_tmp.ensure((long)E * n3);
+      w_r.ensure((long)E * n3);
+      k_getimage_fixed<<<nblocks<int>((long)E * n3, 256, 8192), 256, 0, st>>>(w_v.p, w_acc.p, E, N, w_tmp.p);
+      post_launch();
+      VolumeGeom g{};
+      g.lwedge = -90.f;
+      g.uwedge = 90.f;
+      for (int k = 0; k < 3; ++k) g.position[k] = (float)(N / 2.0);
+      for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+      sym_items.assign((size_t)E * F, ResliceItem{});
+      for (int i = 0; i < F; ++i) {
+        Mat4 t = Mat4::eye();
+        rotate(t, i * 360.0 / F, 0, 0, 1);
+        double m12[12];
+        reslice_index(g, N, &t, m12);
+        for (int e = 0; e < E; ++e) {
+          ResliceItem &it = sym_items[(size_t)e * F + i];
+          it.vol = w_tmp.p + (long)e * n3;
+          it.tmap = nullptr;
+          it.dims[0] = it.dims[1] = it.dims[2] = N;
+          set_map(it, m12);
+        }
+      }
+      CK(cudaMemcpyAsync(w_items.p, sym_items.data(), sym_items.size() * sizeof(ResliceItem), cudaMemcpyHostToDevice,
+                         st));
+      CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * F * sizeof(double), st));
+      {
+        Scope sc(this, "reslice", 8.0 * E * F * n3);
+        k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), (unsigned)(E * F)), 256, RS_SMEM, st>>>(
+            w_items.p, N, w_v.p, w_acc.p, 2, status.p, nullptr);
+        post_launch();
+      }
+      k_sym_mean<<<nblocks<int>((long)E * n3, 256, 8192), 256, 0, st>>>(w_v.p, w_acc.p, F, E, N, w_r.p);
+      post_launch();
+      // every value valid and the mean already removed: sums (0, 1) per item
+      sym_acc0.assign(2 * (size_t)E, 0.0);
+      for (int e = 0; e < E; ++e) sym_acc0[2 * e + 1] = 1.0;
+      w_w.ensure(2L * E);
+      CK(cudaMemcpyAsync(w_w.p, sym_acc0.data(), sym_acc0.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+      pre_src = w_r.p;
+      pre_acc = w_w.p;
+    }
+    PreParticle pre{pre_src, nullptr, pre_acc, 2, N};
     r2c_z(N, pre, w_cA.p, (long)E * N * N);
     xy_kxy(N, w_cA.p, E, -1);
     switch (N) {
@@ -1108,13 +1159,13 @@ void ettk_ctx::representations(int M, const int *parts, float *R) {
     check_status();
     parallel_for(E, [&](int e) {
       std::vector<float> w;
-      wedge_half_host(partg[parts[c0 + e]], N, w);
+      if (F == 1) wedge_half_host(partg[parts[c0 + e]], N, w);
       float *r = R + (size_t)(c0 + e) * K * 3;
       for (int q = 0; q < K; ++q) {
         const int g = band[q], kz = g / (N * N), x = (g / N) % N, y = g % N;
         r[3 * q] = vals[(size_t)e * K + q].x;
         r[3 * q + 1] = vals[(size_t)e * K + q].y;
-        r[3 * q + 2] = w[((size_t)x * N + y) * H + kz] > .5f ? 1.f : 0.f;
+        r[3 * q + 2] = (F > 1 || w[((size_t)x * N + y) * H + kz] > .5f) ? 1.f : 0.f;
       }
     });
   }
@@ -2833,8 +2884,8 @@ int ettk_gpu_representation_distances(ettk_ctx *c, int V, int K, int depth, cons
   });
 }
 
-int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int *K, float *R) {
-  if (!c || !K) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int fold, int *K, float *R) {
+  if (!c || !K || fold < 1 || fold > 360) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (R && (M < 1 || !particles)) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   return guarded(c, [&] {
     *K = (int)c->representation_band().size();
@@ -2842,7 +2893,7 @@ int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int *K, f
     if (c->V < 1) throw CudaError(ETTK_ERR_STATE, "set particles first");
     for (int i = 0; i < M; ++i)
       if (particles[i] < 0 || particles[i] >= c->V) throw CudaError(ETTK_ERR_ARG, "particle index out of range");
-    c->representations(M, particles, R);
+    c->representations(M, particles, fold, R);
   });
 }
 

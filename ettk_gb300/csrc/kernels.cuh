@@ -758,6 +758,31 @@ static __global__ void k_sym_finish(const float *__restrict__ v, const double *_
   }
 }
 
+// getImage values of E reslices ([e][x][y][z], sums in acc[e][0..1]) as fixed images [e][z][y][x] (x fastest),
+// the input of nbfImageFilter::symmetrize in getLowDimensionRepresentationHalf.
+static __global__ void k_getimage_fixed(const float *__restrict__ v, const double *__restrict__ acc, int E, int N,
+                                        float *__restrict__ out) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < (long)E * n3; id += (long)gridDim.x * blockDim.x) {
+    const long e = id / n3, r = id - e * n3;
+    const int x = (int)(r % N), y = (int)((r / N) % N), z = (int)(r / ((long)N * N));
+    out[id] = (float)get_image_value(v[e * n3 + ((long)x * N + y) * N + z], acc + 2 * e);
+  }
+}
+
+// nbfImageFilter::symmetrize per item: the mean of the item's fold reslices (getImage values, [e*fold+i][x][y][z],
+// sums in acc[e*fold+i][0..1]) summed in order in FP64, written [e][x][y][z].
+static __global__ void k_sym_mean(const float *__restrict__ v, const double *__restrict__ acc, int fold, int E, int N,
+                                  float *__restrict__ out) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < (long)E * n3; id += (long)gridDim.x * blockDim.x) {
+    const long e = id / n3, r = id - e * n3;
+    double s = 0.0;
+    for (int i = 0; i < fold; ++i) s += get_image_value(v[(e * fold + i) * n3 + r], acc + 2 * (e * fold + i));
+    out[id] = (float)(s / fold);
+  }
+}
+
 // getImageVarianceMPI (inc/em/nbfWedgedAverageImage3D.h:440-493): var[x][y][z] += |w_e| (T_e - avg)^2 / sum|w| over
 // the chunk's members in order (FP64); avg is [z][y][x], the member reslices [e][x][y][z] with sums acc[e][0..1].
 static __global__ void k_var_accum(const float *__restrict__ v, const double *__restrict__ acc, const float *__restrict__ w,

@@ -168,14 +168,16 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
         return out
 
-    def representations(self, particles):
-        """getLowDimensionRepresentationHalf of the given particles: (M, K, 3) float32 (re, im, wedge bit)."""
+    def representations(self, particles, fold=1):
+        """getLowDimensionRepresentationHalf of the given particles (n-fold symmetrised about z when fold > 1):
+        (M, K, 3) float32 (re, im, wedge bit)."""
         p = np.ascontiguousarray(np.asarray(particles, np.int32))
         K = ctypes.c_int()
-        self._check(self.L.ettk_gpu_representations(self._ctx, 0, None, ctypes.byref(K), None), "representations")
-        R = np.zeros((len(p), K.value, 3), np.float32)
-        self._check(self.L.ettk_gpu_representations(self._ctx, len(p), p.ctypes.data, ctypes.byref(K), R.ctypes.data),
+        self._check(self.L.ettk_gpu_representations(self._ctx, 0, None, int(fold), ctypes.byref(K), None),
                     "representations")
+        R = np.zeros((len(p), K.value, 3), np.float32)
+        self._check(self.L.ettk_gpu_representations(self._ctx, len(p), p.ctypes.data, int(fold), ctypes.byref(K),
+                                                    R.ctypes.data), "representations")
         return R
 
     def representation_distances(self, R, overlap_normalized=None):

@@ -119,13 +119,14 @@ int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
 
 /* Low-dimensional representations of particles (nbfFourierImageMetric::getLowDimensionRepresentationHalf,
    inc/em/nbfFourierImageMetric.h:1967-2034, as nbfCorrelationImageMetric::getRepresentations collects them,
-   inc/em/nbfCorrelationImageMetric.h:1323-1372; fold 1, padding 1): per particle its image (own geometry,
-   mean of valid voxels removed) shifted, transformed, band-pass filtered, transformed back, masked with the
-   real-space mask and transformed again (unnormalised, as FFTW); the K coefficients where |filter| > 0.5 are
-   kept in the [x][y][kz] order of the half spectrum as (re, im, wedge bit) with the bit getWedgeImageHalf > 0.5.
-   *K receives K (the call with R = NULL only does that); R receives M * K * 3 floats, the representation array
-   R(M, K, 3) of ettk_gpu_representation_distances. */
-int ettk_gpu_representations(ettk_ctx *ctx, int M, const int *particles, int *K, float *R);
+   inc/em/nbfCorrelationImageMetric.h:1323-1372; padding 1): per particle its image (own geometry, mean of
+   valid voxels removed), with fold > 1 symmetrised n-fold about z (nbfImageFilter::symmetrize, as
+   ettk_gpu_symmetrize), shifted, transformed, band-pass filtered, transformed back, masked with the real-space
+   mask and transformed again (unnormalised, as FFTW); the K coefficients where |filter| > 0.5 are kept in the
+   [x][y][kz] order of the half spectrum as (re, im, wedge bit) with the bit getWedgeImageHalf > 0.5 (1 for
+   fold > 1). fold 1..360. *K receives K (the call with R = NULL only does that); R receives M * K * 3
+   floats, the representation array R(M, K, 3) of ettk_gpu_representation_distances. */
+int ettk_gpu_representations(ettk_ctx *ctx, int M, const int *particles, int fold, int *K, float *R);
 
 /* Distance matrix between low-dimensional representations (nbfCorrelationImageMetric::getDistances(file, D),
    inc/em/nbfCorrelationImageMetric.h:1726-1871, the pairwise step of the unsupervised classification). R is

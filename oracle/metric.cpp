@@ -1048,15 +1048,32 @@ int oracle_symmetrize(const OracleParams *P, const OracleVolume *v, int fold, do
 }
 
 /* nbfFourierImageMetric::getLowDimensionRepresentationHalf (inc/em/nbfFourierImageMetric.h:1967-2034) with
- * fold 1 and padding 1 (imageFilter->execute(input1, true) then bypasses the mask): A = getImage of the volume,
- * F = R2C(A * shift) * filter (executeHalf without a wedge), a = C2R(F) * mask, F2 = R2C(a), unnormalised; the
- * kept coefficients are those with |filter| > 0.5 in the [x][y][kz] order of the half spectrum, stored as
- * complex<float> beside the wedge bit getWedgeImageHalf > 0.5. R (optional): K x 3 floats; *K their number. */
-int oracle_representation(const OracleParams *P, const OracleVolume *v, float *R, int *K) {
+ * padding 1 (imageFilter->execute(input1, true) then bypasses the mask): A = getImage of the volume; with
+ * fold > 1 nbfImageFilter::symmetrize(A, fold) (oracle_symmetrize of A as a fixed image, A stored as float) and
+ * wedge bits 1; F = R2C(A * shift) * filter (executeHalf without a wedge), a = C2R(F) * mask, F2 = R2C(a),
+ * unnormalised; the kept coefficients are those with |filter| > 0.5 in the [x][y][kz] order of the half
+ * spectrum, stored as complex<float> beside the wedge bit getWedgeImageHalf > 0.5. R (optional): K x 3 floats;
+ * *K their number. */
+int oracle_representation(const OracleParams *P, const OracleVolume *v, int fold, float *R, int *K) {
   const int N = P->N, H = N / 2 + 1;
   const long n3 = (long)N * N * N, h3 = (long)N * N * H;
   std::vector<double> a;
   get_image(*v, N, nullptr, a);
+  if (fold > 1) {
+    std::vector<float> fx(n3);
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) fx[x + (long)N * (y + (long)N * z)] = (float)a[((long)x * N + y) * N + z];
+    OracleVolume fv;
+    memset(&fv, 0, sizeof(fv));
+    fv.data = fx.data();
+    fv.dims[0] = fv.dims[1] = fv.dims[2] = N;
+    fv.lwedge = -90.f;
+    fv.uwedge = 90.f;
+    for (int k = 0; k < 16; ++k) fv.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    for (int k = 0; k < 3; ++k) fv.position[k] = (float)(N / 2.0);
+    oracle_symmetrize(P, &fv, fold, a.data());
+  }
   for (int x = 0; x < N; ++x)
     for (int y = 0; y < N; ++y)
       for (int z = 0; z < N; ++z)
@@ -1077,7 +1094,7 @@ int oracle_representation(const OracleParams *P, const OracleVolume *v, float *R
       if (R) {
         R[3L * k] = (float)F[g].real();
         R[3L * k + 1] = (float)F[g].imag();
-        R[3L * k + 2] = w[g] > .5 ? 1.0f : 0.0f;
+        R[3L * k + 2] = (fold > 1 || w[g] > .5) ? 1.0f : 0.0f;
       }
       ++k;
     }

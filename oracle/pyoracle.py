@@ -93,7 +93,7 @@ def lib():
         L.oracle_average_spherical_wedge.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oracle_representation_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int,
                                                                             ctypes.c_void_p]
-        L.oracle_representation.argtypes = [P, V, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.oracle_representation.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -267,14 +267,14 @@ def symmetrize(params, vol, fold):
     return out.reshape(N, N, N)
 
 
-def representation(params, vol, meta):
+def representation(params, vol, meta, fold=1):
     """getLowDimensionRepresentationHalf of one volume: (K, 3) float32 (re, im, wedge bit)."""
     P = make_params(params)
     v = make_volume(vol, meta)
     K = ctypes.c_int()
-    lib().oracle_representation(ctypes.byref(P), ctypes.byref(v), None, ctypes.byref(K))
+    lib().oracle_representation(ctypes.byref(P), ctypes.byref(v), int(fold), None, ctypes.byref(K))
     R = np.zeros((K.value, 3), np.float32)
-    lib().oracle_representation(ctypes.byref(P), ctypes.byref(v), R.ctypes.data, ctypes.byref(K))
+    lib().oracle_representation(ctypes.byref(P), ctypes.byref(v), int(fold), R.ctypes.data, ctypes.byref(K))
     return R
 
 

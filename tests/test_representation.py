@@ -3,7 +3,8 @@ inc/em/nbfFourierImageMetric.h:1967-2034) and the distances between them (nbfCor
 (file, D), inc/em/nbfCorrelationImageMetric.h:1726-1871), the pairwise step of the unsupervised classification.
 
 Representations: three unnormalised FP32 3-D transforms on the GPU against the oracle's FP64 ones, held to 2e-5
-of the largest coefficient magnitude; the band (which coefficients, in which order) and the wedge bits exactly.
+of the largest coefficient magnitude (5e-5 with the n-fold symmetrisation's extra reslices); the band (which
+coefficients, in which order) and the wedge bits exactly.
 
 The oracle restates the loop with the roundings Blitz gives it (complex<float> element arithmetic, sum() in
 double, mean() in float); tests/golden/repr_dist.npz holds the outputs of that loop written in the reference's
@@ -101,8 +102,26 @@ def ds32():
 def test_oracle_representation_band_and_linearity(ds32):
     R = pyoracle.representation(ds32.params, ds32.particles[0], ds32.meta[0])
     assert R.shape[1] == 3 and set(np.unique(R[:, 2])) <= {0.0, 1.0}
+    R3 = pyoracle.representation(ds32.params, ds32.particles[0], ds32.meta[0], fold=3)
+    assert R3.shape == R.shape and (R3[:, 2] == 1).all()  # n-fold: wedge image 1 (fold > 1 branch)
+    assert np.array_equal(pyoracle.representation(ds32.params, ds32.particles[0], ds32.meta[0], fold=1), R)
     R2 = pyoracle.representation(ds32.params, 2 * ds32.particles[0], ds32.meta[0])
     assert np.allclose(R2[:, :2], 2 * R[:, :2], rtol=1e-6, atol=1e-6 * np.abs(R[:, :2]).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fold", [2, 3])
+def test_gpu_representations_nfold(ds32, fold):
+    n = len(ds32.meta)
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        m.set_particles([WedgedSubImage3D(ds32.particles[i], **{k: ds32.meta[i][k] for k in KW}) for i in range(n)])
+        g = m.representations([1, 2], fold=fold)
+    finally:
+        m.close()
+    o = np.stack([pyoracle.representation(ds32.params, ds32.particles[i], ds32.meta[i], fold=fold) for i in (1, 2)])
+    assert g.shape == o.shape and (g[:, :, 2] == 1).all()
+    assert np.abs(g[:, :, :2] - o[:, :, :2]).max() <= 5e-5 * np.abs(o[:, :, :2]).max()
 
 
 @pytest.mark.gpu
