@@ -387,6 +387,9 @@ def blitz_ref_lib():
         L = ctypes.CDLL(BLITZ_REF_PATH)
         L.cyl_ref_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.repr_ref_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.clustering_ref_soft_weights.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+        L.clustering_ref_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _blitz_ref = L
     return _blitz_ref
 
@@ -417,3 +420,33 @@ def ref_representation_distances(R, normalized=True):
     D = np.zeros((V, V), np.float32)
     L.repr_ref_distances(V, K, depth, R.ctypes.data, int(bool(normalized)), D.ctypes.data)
     return D
+
+
+def ref_soft_weights(d):
+    """computeNewReferences' radii and weights in the reference's Blitz expressions for distances d[V][R];
+    (W [R][V], radii [R]) or None when the harness library is absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    d = np.ascontiguousarray(d, np.float32)
+    V, R = d.shape
+    W = np.zeros((R, V), np.float32)
+    radii = np.zeros(R, np.float32)
+    L.clustering_ref_soft_weights(R, V, d.ctypes.data, W.ctypes.data, radii.ctypes.data)
+    return W, radii
+
+
+def ref_cutoff(d, fraction, rule):
+    """Best class and outlier cutoff in the reference's expressions for distances d[V][R]; (best, dist, keep) or
+    None when the harness library is absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    d = np.ascontiguousarray(d, np.float32)
+    V, R = d.shape
+    best = np.zeros(V, np.int32)
+    dist = np.zeros(V, np.float32)
+    keep = np.zeros(V, np.int32)
+    L.clustering_ref_cutoff(R, V, d.ctypes.data, float(fraction), int(rule), best.ctypes.data, dist.ctypes.data,
+                            keep.ctypes.data)
+    return best, dist, keep.astype(bool)

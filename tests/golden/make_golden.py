@@ -11,11 +11,14 @@ align128_b64.npz oracle alignments of the first two particles of the 128^3 B=64 
 rotsym_n16.npz the rotational-symmetry step of the classification loop run by the reference's own
                cylindrical-domain classes (oracle/_ref/libblitz_ref.so) on a seeded 16^3 volume and on a
                volume with an off-axis blob.
+clustering.npz soft class weights and outlier cutoffs (three rules, several fractions) of seeded distance
+               tables with ties, from the class-selection rules in the reference's expressions
+               (oracle/_ref/libblitz_ref.so).
 repr_dist.npz  distance matrices between seeded low-dimensional representations (depth 3 with wedge bits,
                and depth 1) from the representation-distance loop in the reference's Blitz expressions
                (oracle/_ref/libblitz_ref.so), overlap-normalised and averaged.
 
-Usage: python make_golden.py [soft|align32|align128|rotsym|repr ...]   (no argument: all)
+Usage: python make_golden.py [soft|align32|align128|rotsym|repr|clustering ...]   (no argument: all)
 """
 import hashlib
 import os
@@ -70,7 +73,29 @@ def repr_inputs():
     return R3, R1
 
 
+CLUSTER_FRACTIONS = (0.0, 0.29, 0.5, 0.9, 1.0)
+
+
+def clustering_inputs():
+    rng = np.random.default_rng(31)
+    d = rng.uniform(0.2, 0.9, (101, 4)).astype(np.float32)
+    d[::7] = np.round(d[::7] * 8) / 8  # ties within and across volumes
+    d[5, :] = -d[5, :]                  # negative distances: |.| only for rule 0
+    return d
+
+
 def main(which):
+    if "clustering" in which:
+        d = clustering_inputs()
+        sw = pyoracle.ref_soft_weights(d)
+        if sw is None:
+            raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+        out = {"d": d, "W": sw[0], "radii": sw[1]}
+        for rule in (0, 1, 2):
+            for f in CLUSTER_FRACTIONS:
+                b, dist, keep = pyoracle.ref_cutoff(d, f, rule)
+                out["best_%d_%g" % (rule, f)], out["dist_%d_%g" % (rule, f)], out["keep_%d_%g" % (rule, f)] = b, dist, keep
+        np.savez_compressed(os.path.join(HERE, "clustering.npz"), **out)
     if "repr" in which:
         R3, R1 = repr_inputs()
         out = {"R3": R3, "R1": R1}
@@ -109,4 +134,4 @@ def main(which):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym", "repr"])
+    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym", "repr", "clustering"])

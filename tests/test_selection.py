@@ -10,11 +10,58 @@ device work) against plain numpy restatements of the reference's code:
   sigmoid (1 + 2e) / (1 + e) - 1 with a float exponent, truncation at 0.01.
 
 Index and comparison rules are integer work and must agree exactly; soft weights go through expf, so they are
-held to 2 float ulps of the restatement."""
+held to 2 float ulps of the numpy restatement. Against the same rules written in the reference's own Blitz / C++
+expressions (tests/golden/clustering.npz, and oracle/_ref/libblitz_ref.so itself when built) everything,
+soft weights included, is bit-exact."""
+import os
+
 import numpy as np
 import pytest
 
+import pyoracle
 from ettk_gb300 import clustering
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "clustering.npz")
+FRACTIONS = (0.0, 0.29, 0.5, 0.9, 1.0)
+
+
+def as_table(d):
+    V, R = d.shape
+    D = -np.ones((V * R, 17, 1), np.float32)
+    D[:, 0, 0] = d.reshape(-1)
+    return D
+
+
+def test_matches_reference_golden():
+    g = np.load(GOLDEN)
+    d = g["d"]
+    R = d.shape[1]
+    W, radii = clustering.soft_weights(as_table(d), R)
+    assert np.array_equal(W, g["W"]) and np.array_equal(radii, g["radii"])
+    for rule in (0, 1, 2):
+        for f in FRACTIONS:
+            best, dist, keep, _ = clustering.best_alignment_and_clean(as_table(d), R, f, rule)
+            k = "%d_%g" % (rule, f)
+            assert np.array_equal(best, g["best_" + k]) and np.array_equal(dist, g["dist_" + k]), k
+            assert np.array_equal(keep, g["keep_" + k]), k
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_matches_reference_library(seed):
+    rng = np.random.default_rng(seed)
+    V, R = 37 * seed, seed + 1
+    d = rng.uniform(0.1, 1.0, (V, R)).astype(np.float32)
+    d[::3] = np.round(d[::3] * 4) / 4
+    ref = pyoracle.ref_soft_weights(d)
+    if ref is None:
+        pytest.skip("reference harness not built here (oracle/build_ref.sh needs the reference tree)")
+    W, radii = clustering.soft_weights(as_table(d), R)
+    assert np.array_equal(W, ref[0]) and np.array_equal(radii, ref[1])
+    for rule in (0, 1, 2):
+        for f in (0.0, 0.37, 0.8, 1.0):
+            best, dist, keep, _ = clustering.best_alignment_and_clean(as_table(d), R, f, rule)
+            rb, rd, rk = pyoracle.ref_cutoff(d, f, rule)
+            assert np.array_equal(best, rb) and np.array_equal(dist, rd) and np.array_equal(keep, rk)
 
 
 def table(V, R, cols=17, seed=0, ties=False):
