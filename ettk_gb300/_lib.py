@@ -61,7 +61,7 @@ SYMBOLS = [
     "ettk_gpu_refine_objective", "ettk_gpu_classify", "ettk_gpu_set_particles_tomogram", "ettk_gpu_variance",
     "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
-    "ettk_gpu_representation_distances", "ettk_gpu_representations",
+    "ettk_gpu_representation_distances", "ettk_gpu_representations", "ettk_gpu_mra_assign",
 ]
 
 _lib = None
@@ -109,6 +109,7 @@ def load(path=None):
     L.ettk_gpu_outlier_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float,
                                           ctypes.c_int, vp, vp, vp, P(ctypes.c_float)]
     L.ettk_gpu_soft_weights.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp]
+    L.ettk_gpu_mra_assign.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
     L.ettk_gpu_set_particles_tomogram.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                   P(VolumeMeta)]
     L.ettk_gpu_profile_read.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, P(ctypes.c_longlong),

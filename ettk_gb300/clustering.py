@@ -55,3 +55,17 @@ def soft_weights(D, R):
     if rc != _lib.ETTK_OK:
         raise EttkError(rc, "soft_weights: invalid table")
     return W, radii
+
+
+def mra_assign(S):
+    """Class choice of the MRA loop (nbfLoopClustering::doMra): S[v][r][j] is the distance of volume v, under the
+    alignment it received from reference r, against reference j. Returns labels [V] int32."""
+    S = np.ascontiguousarray(S, np.float32)
+    V, R, R2 = S.shape
+    if R != R2:
+        raise ValueError("S must be V x R x R")
+    labels = np.zeros(V, np.int32)
+    rc = _lib.load().ettk_gpu_mra_assign(R, V, S.ctypes.data, labels.ctypes.data)
+    if rc != _lib.ETTK_OK:
+        raise EttkError(rc, "mra_assign: invalid table")
+    return labels

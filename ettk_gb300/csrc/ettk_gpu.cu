@@ -2958,6 +2958,28 @@ int ettk_gpu_outlier_cutoff(int R, int V, const float *D, int ld, float top_frac
   return ETTK_OK;
 }
 
+int ettk_gpu_mra_assign(int R, int V, const float *S, int *labels) {
+  if (R < 1 || V < 1 || !S || !labels) return ETTK_ERR_ARG;
+  for (long k = 0; k < (long)V * R * R; ++k)
+    if (!std::isfinite(S[k])) return ETTK_ERR_NAN;
+  for (int v = 0; v < V; ++v) {
+    int best = 0;
+    float best_sum = 0.f;
+    for (int r = 0; r < R; ++r) {
+      // the partial sum over the references accumulates in double and is stored as float, as Blitz reduces
+      double s = 0.0;
+      for (int j = 0; j < R; ++j) s += (double)S[((size_t)v * R + r) * R + j];
+      const float fs = (float)s;
+      if (r == 0 || fs < best_sum) {
+        best = r;
+        best_sum = fs;
+      }
+    }
+    labels[v] = best;
+  }
+  return ETTK_OK;
+}
+
 int ettk_gpu_soft_weights(int R, int V, const float *D, int ld, float *W, float *radii) {
   if (R < 1 || V < 1 || !D || ld < 1 || !W) return ETTK_ERR_ARG;
   const float decay = .025f;

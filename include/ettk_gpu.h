@@ -178,6 +178,13 @@ int ettk_gpu_symmetrize_rotational(ettk_ctx *ctx, const float *vol, float *out);
 int ettk_gpu_outlier_cutoff(int R, int V, const float *D, int ld, float top_fraction, int rule, int *best,
                             float *dist, int *keep, float *cutoff);
 
+/* Class choice of the MRA loop (nbfLoopClustering::doMra, inc/em/nbfLoopClustering.h:1523-1592): each volume v
+   was scored, under the alignment it received from each reference r, against every reference j (getDistances
+   type 2 at translation restriction 0); S[(v * R + r) * R + j] holds that distance (the reference's
+   alignments(j, v * R + r, 0, 0)). labels[v] = the r whose sum over j is smallest (the first on ties; the sum
+   in double, compared as float). */
+int ettk_gpu_mra_assign(int R, int V, const float *S, int *labels);
+
 /* Soft class weights of nbfLoopClustering::computeNewReferences (inc/em/nbfLoopClustering.h:2406-2502; the
    reference defines it but none of its drivers calls it): per class r, radius = max_v D(v, r) + 0.025 ln 0.01,
    W[r * V + v] = (1 + 2e) / (1 + e) - 1 with e = exp(-(D(v, r) - radius) / 0.025) (float exponent), weights

@@ -388,6 +388,7 @@ def blitz_ref_lib():
         L.cyl_ref_rotational.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.repr_ref_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.clustering_ref_soft_weights.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+        L.clustering_ref_mra_assign.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.clustering_ref_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _blitz_ref = L
@@ -450,3 +451,15 @@ def ref_cutoff(d, fraction, rule):
     L.clustering_ref_cutoff(R, V, d.ctypes.data, float(fraction), int(rule), best.ctypes.data, dist.ctypes.data,
                             keep.ctypes.data)
     return best, dist, keep.astype(bool)
+
+
+def ref_mra_assign(S):
+    """doMra's class choice in the reference's Blitz expressions for S[v][r][j]; labels or None when absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    S = np.ascontiguousarray(S, np.float32)
+    V, R, _ = S.shape
+    labels = np.zeros(V, np.int32)
+    L.clustering_ref_mra_assign(R, V, S.ctypes.data, labels.ctypes.data)
+    return labels

@@ -65,3 +65,24 @@ extern "C" int clustering_ref_cutoff(int R, int V, const float *D, float fractio
   }
   return 0;
 }
+
+// nbfLoopClustering::doMra's class choice (inc/em/nbfLoopClustering.h:1572-1586): alignments(j, d, 0, 0) holds
+// the distance of duplicate d = i * R + r (volume i under reference r's alignment) against reference j;
+// partialSums(d) = sum over j (a Blitz partial reduction stored as Pixel); the class of volume i is the first
+// minimum over r of the reshaped sums. S: [i][r][j] = alignments(j, i * R + r); best: V labels.
+extern "C" int clustering_ref_mra_assign(int R, int V, const float *S, int *best) {
+  Array<float, 2> extractedDistances(R, V * R);
+  for (int i = 0; i < V; ++i)
+    for (int r = 0; r < R; ++r)
+      for (int j = 0; j < R; ++j) extractedDistances(j, i * R + r) = S[((long)i * R + r) * R + j];
+  Array<float, 1> partialSums(V * R);
+  firstIndex ii;
+  secondIndex jj;
+  partialSums = sum(extractedDistances(jj, ii), jj);
+  Array<float, 2> reshapedPartialSums(partialSums.data(), shape(V, R), neverDeleteData);
+  for (int i = 0; i < V; i++) {
+    TinyVector<int, 1> b = minIndex(reshapedPartialSums(i, Range::all()));
+    best[i] = b[0];
+  }
+  return 0;
+}

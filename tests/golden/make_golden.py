@@ -11,8 +11,8 @@ align128_b64.npz oracle alignments of the first two particles of the 128^3 B=64 
 rotsym_n16.npz the rotational-symmetry step of the classification loop run by the reference's own
                cylindrical-domain classes (oracle/_ref/libblitz_ref.so) on a seeded 16^3 volume and on a
                volume with an off-axis blob.
-clustering.npz soft class weights and outlier cutoffs (three rules, several fractions) of seeded distance
-               tables with ties, from the class-selection rules in the reference's expressions
+clustering.npz soft class weights, outlier cutoffs (three rules, several fractions) and the MRA class
+               choice of seeded distance tables with ties, from the class-selection rules in the reference's expressions
                (oracle/_ref/libblitz_ref.so).
 repr_dist.npz  distance matrices between seeded low-dimensional representations (depth 3 with wedge bits,
                and depth 1) from the representation-distance loop in the reference's Blitz expressions
@@ -84,6 +84,13 @@ def clustering_inputs():
     return d
 
 
+def mra_inputs():
+    rng = np.random.default_rng(41)
+    S = rng.uniform(0.3, 0.8, (60, 3, 3)).astype(np.float32)
+    S[::5] = np.round(S[::5] * 4) / 4  # ties between the alignments of a volume
+    return S
+
+
 def main(which):
     if "clustering" in which:
         d = clustering_inputs()
@@ -95,6 +102,8 @@ def main(which):
             for f in CLUSTER_FRACTIONS:
                 b, dist, keep = pyoracle.ref_cutoff(d, f, rule)
                 out["best_%d_%g" % (rule, f)], out["dist_%d_%g" % (rule, f)], out["keep_%d_%g" % (rule, f)] = b, dist, keep
+        S = mra_inputs()
+        out["S"], out["mra_labels"] = S, pyoracle.ref_mra_assign(S)
         np.savez_compressed(os.path.join(HERE, "clustering.npz"), **out)
     if "repr" in which:
         R3, R1 = repr_inputs()

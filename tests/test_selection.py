@@ -7,7 +7,9 @@ device work) against plain numpy restatements of the reference's code:
 - the refinement loop of src/MPI_Classification.cpp: next-average weights distance <= cutoff (922-934) and
   the cleaned list distance < cutoff (1137-1150);
 - nbfLoopClustering::computeNewReferences (2406-2502): radius max + 0.025 ln 0.01 (double, stored float),
-  sigmoid (1 + 2e) / (1 + e) - 1 with a float exponent, truncation at 0.01.
+  sigmoid (1 + 2e) / (1 + e) - 1 with a float exponent, truncation at 0.01;
+- nbfLoopClustering::doMra's class choice (1523-1592): per volume the alignment whose distances against all
+  references sum lowest (double sum stored as float, first minimum).
 
 Index and comparison rules are integer work and must agree exactly; soft weights go through expf, so they are
 held to 2 float ulps of the numpy restatement. Against the same rules written in the reference's own Blitz / C++
@@ -44,6 +46,28 @@ def test_matches_reference_golden():
             k = "%d_%g" % (rule, f)
             assert np.array_equal(best, g["best_" + k]) and np.array_equal(dist, g["dist_" + k]), k
             assert np.array_equal(keep, g["keep_" + k]), k
+
+
+def test_mra_assign_matches_reference_golden():
+    g = np.load(GOLDEN)
+    assert np.array_equal(clustering.mra_assign(g["S"]), g["mra_labels"])
+
+
+@pytest.mark.parametrize("V,R", [(1, 1), (9, 2), (200, 5)])
+def test_mra_assign(V, R):
+    rng = np.random.default_rng(V + R)
+    S = rng.uniform(0.1, 1.0, (V, R, R)).astype(np.float32)
+    S[::4] = np.round(S[::4] * 3) / 3
+    labels = clustering.mra_assign(S)
+    sums = S.astype(np.float64).sum(axis=2).astype(np.float32)  # sum over the references, stored as float
+    assert np.array_equal(labels, np.argmin(sums, axis=1))
+    ref = pyoracle.ref_mra_assign(S)
+    if ref is not None:
+        assert np.array_equal(labels, ref)
+    bad = S.copy()
+    bad[0, 0, 0] = np.nan
+    with pytest.raises(Exception):
+        clustering.mra_assign(bad)
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
