@@ -1,0 +1,149 @@
+"""The global-average refinement loop (MPI_Classification running mode 0, src/MPI_Classification.cpp:914-1160)
+as ettk_gb300.classification.refine_global drives it: the order of the library calls, the weights of each
+average (top-fraction cutoff, distance <= cutoff), the composition of the transforms (T <- T A, or A when
+the alignments are reset), the cleaned list (distance < cutoff), the rotational symmetrisation of each
+average and the spherical wedge handed to the reference. A recording stand-in for the metric replaces the
+GPU; the GPU calls themselves have their own parity tests."""
+import numpy as np
+import pytest
+
+from ettk_gb300 import classification
+from ettk_gb300.metric import WedgedSubImage3D
+
+
+def rot_z(deg):
+    a = np.deg2rad(deg)
+    T = np.eye(4)
+    T[:2, :2] = [[np.cos(a), -np.sin(a)], [np.sin(a), np.cos(a)]]
+    return T
+
+
+class FakeMetric:
+    def __init__(self, V, wedge_compensation=True, N=8):
+        self.params = {"N": N, "wedge_compensation": wedge_compensation}
+        self.V = V
+        self.log = []
+        self.passes = 0
+        rng = np.random.default_rng(3)
+        # per pass: distances and a small rotation per volume
+        self.dist = [rng.uniform(0.2, 0.9, V).astype(np.float32) for _ in range(5)]
+        self.ang = [rng.uniform(-10, 10, V) for _ in range(5)]
+
+    def set_particles(self, vols):
+        self.log.append(("set_particles", [v.matrix.copy() for v in vols]))
+
+    def average(self, members, weights, mats):
+        self.log.append(("average", list(members), np.asarray(weights).copy(), [np.asarray(m).copy() for m in mats]))
+        return np.full((8, 8, 8), float(len(self.log)), np.float32)
+
+    def variance(self, members, weights, mats, avg):
+        self.log.append(("variance", avg[0, 0, 0]))
+        return np.zeros_like(avg)
+
+    def symmetrize_rotational(self, vol):
+        self.log.append(("symmetrize_rotational", vol[0, 0, 0]))
+        return vol * 2
+
+    def set_references(self, refs):
+        self.log.append(("set_references", refs[0].image[0, 0, 0], refs[0].lwedge, refs[0].uwedge))
+
+    def average_spherical_wedge(self, members, weights, mats):
+        self.log.append(("average_spherical_wedge", np.asarray(weights).copy()))
+        return np.ones((4, 4), np.float32), None
+
+    def set_reference_spherical_wedge(self, r, wedge):
+        self.log.append(("set_reference_spherical_wedge", r))
+
+    def getDistances(self, pairs):
+        k = self.passes
+        self.passes += 1
+        D = -np.ones((len(pairs), 17, 1), np.float32)
+        for i, (_, p) in enumerate(pairs):
+            D[i, 0, 0] = self.dist[k][p]
+            D[i, 1:17, 0] = rot_z(self.ang[k][p]).reshape(16)
+        self.log.append(("getDistances", len(pairs)))
+        return D
+
+
+def volumes(V):
+    rng = np.random.default_rng(1)
+    return [WedgedSubImage3D(np.zeros((8, 8, 8), np.float32), matrix=rot_z(rng.uniform(0, 90))) for _ in range(V)]
+
+
+def calls(m, name):
+    return [c for c in m.log if c[0] == name]
+
+
+def test_composition_and_call_order():
+    V, it = 6, 3
+    vols = volumes(V)
+    m = FakeMetric(V)
+    out = classification.refine_global(m, vols, it)
+    assert len(calls(m, "average")) == it + 1 and len(calls(m, "getDistances")) == it
+    # T <- T A after every pass
+    T = [v.matrix for v in vols]
+    for k in range(it):
+        T = [T[i] @ rot_z(m.ang[k][i]) for i in range(V)]
+    assert np.allclose(out["matrices"], np.stack(T))
+    assert np.array_equal(out["distances"], m.dist[it - 1])
+    # every average used all volumes with weight 1 and the transforms of that moment
+    for k, c in enumerate(calls(m, "average")):
+        assert (c[2] == 1).all()
+    # the reference is the average (full wedge) and carries the members' spherical wedge
+    assert all(c[2] == -90.0 and c[3] == 90.0 for c in calls(m, "set_references"))
+    assert len(calls(m, "set_reference_spherical_wedge")) == it
+    names = [c[0] for c in m.log]
+    first = names.index("getDistances")
+    assert names[:first] == ["set_particles", "average", "set_references", "average_spherical_wedge",
+                             "set_reference_spherical_wedge"]
+    # one upload per pass, carrying the transforms the alignment starts from
+    sets = calls(m, "set_particles")
+    assert len(sets) == it + 1 and all(np.allclose(a, b.matrix) for a, b in zip(sets[0][1], vols))
+
+
+def test_top_fraction_weights_and_clean_list():
+    V, it, f = 11, 2, 0.5
+    m = FakeMetric(V)
+    out = classification.refine_global(m, volumes(V), it, top_fraction=f)
+    avgs = calls(m, "average")
+    assert (avgs[0][2] == 1).all()  # alignments start at 1: every volume within the cutoff
+    for k in range(1, it + 1):
+        d = m.dist[k - 1]
+        cut = np.sort(d)[int(np.float32(f) * np.float32(V - 1))]
+        assert np.array_equal(avgs[k][2], (d <= cut).astype(np.float32))
+    d = m.dist[it - 1]
+    cut = np.sort(d)[int(np.float32(f) * np.float32(V - 1))]
+    assert np.array_equal(out["clean"], d < cut)
+    assert np.array_equal(out["weights"], (d <= cut).astype(np.float32))
+
+
+def test_reset_alignments():
+    V, it = 4, 2
+    m = FakeMetric(V)
+    out = classification.refine_global(m, volumes(V), it, reset_alignments=True)
+    assert np.allclose(out["matrices"], np.stack([rot_z(m.ang[it - 1][i]) for i in range(V)]))
+    # every pass aligns the particles from no transform; the averages still use the composed transforms
+    sets = calls(m, "set_particles")
+    assert all(np.allclose(mm, np.eye(4)) for s_ in sets for mm in s_[1])
+    avgs = calls(m, "average")
+    assert np.allclose(np.stack(avgs[1][3]), np.stack([rot_z(m.ang[0][i]) for i in range(V)]))
+
+
+def test_rotational_variance_and_no_wedge():
+    V, it = 3, 1
+    m = FakeMetric(V, wedge_compensation=False)
+    out = classification.refine_global(m, volumes(V), it, rotational=True, variance=True)
+    assert len(calls(m, "symmetrize_rotational")) == it + 1
+    assert len(out["variances"]) == it + 1
+    names = [c[0] for c in m.log]
+    # variance of the plain average, then the symmetrisation, and the reference is the symmetrised volume
+    assert names.index("variance") < names.index("symmetrize_rotational") < names.index("set_references")
+    sym = calls(m, "symmetrize_rotational")[0][1]
+    assert calls(m, "set_references")[0][1] == 2 * sym
+    assert not calls(m, "set_reference_spherical_wedge")
+    assert out["average"][0, 0, 0] == 2 * calls(m, "symmetrize_rotational")[-1][1]
+
+
+def test_rejects_nfold():
+    with pytest.raises(NotImplementedError):
+        classification.refine_global(FakeMetric(2), volumes(2), 1, fold=3)
