@@ -1046,14 +1046,16 @@ const std::vector<int> &ettk_ctx::representation_band() {
   const int H = N / 2 + 1;
   std::vector<float> fk(h3);
   CK(cudaMemcpy(fk.data(), filter.p, h3 * sizeof(float), cudaMemcpyDeviceToHost));
+  std::vector<int> band;
   for (int x = 0; x < N; ++x)
     for (int y = 0; y < N; ++y)
       for (int k = 0; k < H; ++k) {
         const int g = (k * N + x) * N + y;
-        if (std::fabs(fk[g]) > 0.5f) repr_idx.push_back(g);
+        if (std::fabs(fk[g]) > 0.5f) band.push_back(g);
       }
-  repr_idx_dev.ensure(std::max<size_t>(repr_idx.size(), 1));
-  CK(cudaMemcpy(repr_idx_dev.p, repr_idx.data(), repr_idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  repr_idx_dev.ensure(std::max<size_t>(band.size(), 1));
+  CK(cudaMemcpy(repr_idx_dev.p, band.data(), band.size() * sizeof(int), cudaMemcpyHostToDevice));
+  repr_idx.swap(band);  // cached only once the device copy is in place
   return repr_idx;
 }
 
