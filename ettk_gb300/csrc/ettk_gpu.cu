@@ -2508,6 +2508,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_sd.release();
   c->w_jobs.release();
   c->w_sjobs.release();
+  c->repr_idx_dev.release();
   c->w_plans.release();
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
