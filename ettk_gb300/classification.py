@@ -17,7 +17,7 @@ The n-fold branch (cluster.symmetrize with its default alignment of each rotated
 """
 import numpy as np
 
-from . import clustering
+from . import clustering, volume_list
 from .metric import WedgedSubImage3D
 
 _FULL = {"lwedge": -90.0, "uwedge": 90.0, "normal": (0.0, 0.0, 0.0)}
@@ -29,12 +29,25 @@ def _distance_table(dist):
     return D
 
 
+def _write_list(path, volumes, mats, cut_offsets, keep=None):
+    rows = []
+    for i, v in enumerate(volumes):
+        if keep is not None and not keep[i]:
+            continue
+        rows.append({"lwedge": v.lwedge, "uwedge": v.uwedge, "position": v.position, "normal": v.normal,
+                     "matrix": mats[i], "cut_offset": float(cut_offsets[i]), "filename": v.filename})
+    volume_list.write(path, rows)
+
+
 def refine_global(metric, volumes, iterations, top_fraction=1.0, rotational=False, fold=1, reset_alignments=False,
-                  variance=False):
+                  variance=False, list_prefix=None):
     """Runs `iterations` align passes against the global average (iterations + 1 averages). `volumes`: list of
     WedgedSubImage3D (their matrices are the starting transforms). Returns a dict with the final average
     ([z][y][x]), the transforms [V][4][4], the last distances, the weights of the final average, the cleaned-list
-    mask of the last pass and, with variance=True, the variance maps of every average."""
+    mask of the last pass and, with variance=True, the variance maps of every average. With `list_prefix`, each
+    pass writes the reference's volume lists (1110-1147): `<prefix>_volumes_pre_centered_<n>.txt` with the new
+    transforms and each volume's distance in the cut-offset column, and with a top fraction below 1 the cleaned
+    `<prefix>_volumes_pre_centered_clean_<n>.txt` (n = pass + 1)."""
     if fold > 1:
         raise NotImplementedError("n-fold symmetrisation of the global average (aligned copies) is not reproduced")
     V = len(volumes)
@@ -80,6 +93,10 @@ def refine_global(metric, volumes, iterations, top_fraction=1.0, rotational=Fals
         T = [A[i].copy() if reset_alignments else T[i] @ A[i] for i in range(V)]
         if top_fraction < 1:
             clean = clustering.best_alignment_and_clean(_distance_table(dist), 1, top_fraction, clustering.SELECT)[2]
+        if list_prefix is not None:
+            _write_list("%s_volumes_pre_centered_%d.txt" % (list_prefix, it + 1), volumes, T, dist)
+            if top_fraction < 1:
+                _write_list("%s_volumes_pre_centered_clean_%d.txt" % (list_prefix, it + 1), volumes, T, dist, clean)
     out = {"average": avg, "matrices": np.stack(T), "distances": dist, "weights": weights, "clean": clean}
     if variance:
         out["variances"] = variances

@@ -147,3 +147,23 @@ def test_rotational_variance_and_no_wedge():
 def test_rejects_nfold():
     with pytest.raises(NotImplementedError):
         classification.refine_global(FakeMetric(2), volumes(2), 1, fold=3)
+
+
+def test_volume_lists(tmp_path):
+    from ettk_gb300 import volume_list
+    V, it, f = 9, 2, 0.6
+    m = FakeMetric(V)
+    vols = volumes(V)
+    prefix = str(tmp_path / "run")
+    out = classification.refine_global(m, vols, it, top_fraction=f, list_prefix=prefix)
+    for n in range(1, it + 1):
+        rows = volume_list.read("%s_volumes_pre_centered_%d.txt" % (prefix, n))
+        assert len(rows) == V
+        # the distance of the pass in the cut-offset column (6 significant digits, as the reference prints)
+        assert np.allclose([r["cut_offset"] for r in rows], m.dist[n - 1], rtol=1e-5)
+        d = m.dist[n - 1]
+        cut = np.sort(d)[int(np.float32(f) * np.float32(V - 1))]
+        clean = volume_list.read("%s_volumes_pre_centered_clean_%d.txt" % (prefix, n))
+        assert len(clean) == int((d < cut).sum())
+    last = volume_list.read("%s_volumes_pre_centered_%d.txt" % (prefix, it))
+    assert np.allclose(np.stack([r["matrix"] for r in last]), out["matrices"], atol=1e-5)
