@@ -180,3 +180,28 @@ def test_soft_weights_radius_semantics():
     W, radii = clustering.soft_weights(D, 1)
     assert W[0, 0] == 0
     assert abs(radii[0] - (0.5 + 0.025 * np.log(0.01))) < 1e-7
+
+
+def test_host_entries_reject_bad_arguments():
+    import ctypes
+    from ettk_gb300 import _lib
+    L = _lib.load()
+    D, _ = table(4, 2)
+    buf_i = np.zeros(8, np.int32)
+    buf_f = np.zeros(8, np.float32)
+    cut = ctypes.c_float()
+    # class count, volume count, row stride and rule out of range; missing outputs
+    for R, V, ld, rule in [(0, 4, 17, 0), (2, 0, 17, 0), (2, 4, 0, 0), (2, 4, 17, 3), (2, 4, 17, -1)]:
+        assert L.ettk_gpu_outlier_cutoff(R, V, D.ctypes.data, ld, 0.5, rule, buf_i.ctypes.data, buf_f.ctypes.data,
+                                         buf_i.ctypes.data, ctypes.byref(cut)) == _lib.ETTK_ERR_ARG
+    assert L.ettk_gpu_outlier_cutoff(2, 4, D.ctypes.data, 17, 0.5, 0, None, buf_f.ctypes.data, buf_i.ctypes.data,
+                                     None) == _lib.ETTK_ERR_ARG
+    assert L.ettk_gpu_outlier_cutoff(2, 4, D.ctypes.data, 17, float("nan"), 0, buf_i.ctypes.data, buf_f.ctypes.data,
+                                     buf_i.ctypes.data, None) == _lib.ETTK_ERR_NAN
+    W = np.zeros(16, np.float32)
+    assert L.ettk_gpu_soft_weights(0, 4, D.ctypes.data, 17, W.ctypes.data, None) == _lib.ETTK_ERR_ARG
+    assert L.ettk_gpu_soft_weights(2, 4, D.ctypes.data, 17, None, None) == _lib.ETTK_ERR_ARG
+    S = np.ones((4, 2, 2), np.float32)
+    assert L.ettk_gpu_mra_assign(2, 4, S.ctypes.data, None) == _lib.ETTK_ERR_ARG
+    assert L.ettk_gpu_mra_assign(0, 4, S.ctypes.data, buf_i.ctypes.data) == _lib.ETTK_ERR_ARG
+    assert L.ettk_gpu_mra_assign(2, 4, S.ctypes.data, buf_i.ctypes.data) == _lib.ETTK_OK
