@@ -1102,6 +1102,42 @@ int oracle_representation(const OracleParams *P, const OracleVolume *v, int fold
   return 0;
 }
 
+/* nbfFourierImageMetric::getLowDimensionRepresentationReal (inc/em/nbfFourierImageMetric.h:2375-2533) with
+ * bin_factor 1 and no mask file (the image filter's own mask): A = getImage of the volume; A = C2R(filter *
+ * R2C(A * shift)) * shift / N^3 (nbfFourierFilter::executeHalf on a real array, inc/em/nbfFourierFilter.h:654-672);
+ * with fold > 1 nbfImageFilter::symmetrize(A, fold) (as oracle_representation does it); the kept values are
+ * those where the mask exceeds 0.5, in the [x][y][z] order of the array. C (optional): K doubles; *K their
+ * number. (The reference's n-fold branch first symmetrises through a one-member average, 2377-2439; that branch
+ * is not restated.) */
+int oracle_representation_real(const OracleParams *P, const OracleVolume *v, int fold, double *C, int *K) {
+  const int N = P->N, H = N / 2 + 1;
+  const long n3 = (long)N * N * N, h3 = (long)N * N * H;
+  if (fold > 1) return 1;
+  std::vector<double> a;
+  get_image(*v, N, nullptr, a);
+  auto shift = [&](long id) {
+    const long x = id / ((long)N * N), y = (id / N) % N, z = id % N;
+    return ((x + y + z) & 1) ? -1.0 : 1.0;
+  };
+  for (long i = 0; i < n3; ++i) a[i] *= shift(i);
+  std::vector<float> f, mask;
+  build_filter(*P, f);
+  build_mask(*P, mask);
+  std::vector<cplx> F(h3);
+  rfft3d(a.data(), F.data(), N, N, N);
+  for (long i = 0; i < h3; ++i) F[i] *= (double)f[i];
+  irfft3d(F.data(), a.data(), N, N, N);
+  for (long i = 0; i < n3; ++i) a[i] = a[i] * shift(i) / (double)n3;
+  int k = 0;
+  for (long i = 0; i < n3; ++i)
+    if (mask[i] > .5) {
+      if (C) C[k] = a[i];
+      ++k;
+    }
+  *K = k;
+  return 0;
+}
+
 /* nbfCorrelationImageMetric::getDistances(representationFile, D) (inc/em/nbfCorrelationImageMetric.h:1726-1871),
  * single-process branch, with Blitz 0.9's types: complex<float> products and differences, sum() of a float
  * expression accumulated in double, mean() in float, Pixel overlap stored as float. R(V, K, depth) C order;

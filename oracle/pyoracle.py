@@ -94,6 +94,7 @@ def lib():
         L.oracle_representation_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int,
                                                                             ctypes.c_void_p]
         L.oracle_representation.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.oracle_representation_real.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
@@ -276,6 +277,18 @@ def representation(params, vol, meta, fold=1):
     R = np.zeros((K.value, 3), np.float32)
     lib().oracle_representation(ctypes.byref(P), ctypes.byref(v), int(fold), R.ctypes.data, ctypes.byref(K))
     return R
+
+
+def representation_real(params, vol, meta):
+    """getLowDimensionRepresentationReal of one volume (bin factor 1, the image filter's mask): (K,) float64."""
+    P = make_params(params)
+    v = make_volume(vol, meta)
+    K = ctypes.c_int()
+    if lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), 1, None, ctypes.byref(K)) != 0:
+        raise ValueError("unsupported")
+    C = np.zeros(K.value, np.float64)
+    lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), 1, C.ctypes.data, ctypes.byref(K))
+    return C
 
 
 def representation_distances(R, normalized=True):

@@ -140,3 +140,23 @@ def test_gpu_representations(ds32):
     assert np.abs(g[:, :, :2] - o[:, :, :2]).max() <= 2e-5 * np.abs(o[:, :, :2]).max()
     Do = pyoracle.representation_distances(o, True)
     assert np.allclose(D, Do, rtol=1e-4, atol=1e-6 * Do.max())
+
+
+def test_oracle_real_representation(ds32):
+    """getLowDimensionRepresentationReal (bin factor 1, the image filter's mask): the band-pass-filtered image
+    (nbfFourierFilter::executeHalf on a real array: C2R(filter R2C(A shift)) shift / N^3) at the voxels where the
+    mask exceeds 0.5, against numpy's FFTs; invariant to an affine change of the input values up to the scale."""
+    p = ds32.params
+    N = p["N"]
+    C = pyoracle.representation_real(p, ds32.particles[0], ds32.meta[0])
+    img = pyoracle.get_image(p, ds32.particles[0], ds32.meta[0])  # [x][y][z]
+    m, _, f = pyoracle.masks(p)
+    x, y, z = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    s = np.where((x + y + z) % 2, -1.0, 1.0)
+    F = np.fft.rfftn(img * s) * f
+    e = np.fft.irfftn(F, s=(N, N, N), axes=(0, 1, 2)) * s
+    expect = e[m > 0.5]
+    assert C.shape == expect.shape
+    assert np.abs(C - expect).max() <= 1e-9 * np.abs(expect).max()
+    C2 = pyoracle.representation_real(p, 3 * ds32.particles[0] + 1.5, ds32.meta[0])
+    assert np.abs(C2 - 3 * C).max() <= 1e-6 * np.abs(C).max()
