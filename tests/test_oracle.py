@@ -91,3 +91,21 @@ def test_alignment_golden():
         o = pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
         assert abs(o["distance"] - g["distance"][i]) <= 1e-6 * abs(g["distance"][i])
         assert np.allclose(o["matrix"], g["matrix"][i], atol=1e-9)
+
+
+def test_ccf_restriction_zero_scores_the_pose():
+    """getDistances type 2 at translation restriction 0 (doMra's scoring): the restriction is max(0 * 2, 1) = 1 on
+    the 2x grid (inc/em/nbfFourierImageMetric.h:1224-1225), so the shift moves by at most half a voxel per axis;
+    with the search open (restriction 6) the same offset pose is pulled back by about the 2-voxel offset."""
+    from ettk_gb300 import synthetic
+    ds = synthetic.generate("align32_b16", n_particles=1)
+    T = np.eye(4)
+    T[:3, :3] = ds.truth[0]["rotation"]
+    T[:3, 3] = ds.truth[0]["shift"]
+    T[0, 3] += 2.0
+    p0 = dict(ds.params, restrict_translation=0.0)
+    d0, t0 = pyoracle.ccf(p0, ds.references[0], ds.ref_meta[0], ds.particles[0], ds.meta[0], T)
+    d6, t6 = pyoracle.ccf(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[0], ds.meta[0], T)
+    assert np.abs(t0[:3, 3] - T[:3, 3]).max() <= 0.5
+    assert t6[0, 3] - T[0, 3] < -1.5
+    assert d6 < d0
