@@ -264,7 +264,10 @@ __global__ void k_combine(const PairPlan *__restrict__ plans, float *__restrict_
 
 // 3x3x3 ">=" local maxima with a -FLT_MAX border (localMaxima3D3x3, inc/em/nbfProjectionRotationMetric3D.h:67-79,
 // BordStrategyConst inc/bs/nbfBordStrategyConst.h:67-83); entries with |value| > 0 appended to the
-// item's list (order fixed on the host by sorting on the cell index).
+// item's list (order fixed on the host by sorting on the cell index). Cells inside the -FLT_MAX plateau of a
+// restricted rotation search (execute 602) are maxima of value -FLT_MAX for the reference too; they enter its
+// queues as FLT_MAX sentinels, which sort after every real candidate, lose every duplicate comparison and stop
+// the candidate loop only once no real candidate is left (697-701), so leaving them out changes no result.
 __global__ void k_local_max(const float *__restrict__ C, int n, const int *__restrict__ active, int cap, int *counts,
                             int2 *lists) {
   const long n3 = (long)n * n * n;
@@ -287,7 +290,7 @@ __global__ void k_local_max(const float *__restrict__ C, int n, const int *__res
             break;
           }
         }
-    if (ismax && fabsf(v) > 0.f) {
+    if (ismax && fabsf(v) > 0.f && v != -FLT_MAX) {
       int slot = atomicAdd(&counts[item], 1);
       if (slot < cap) lists[(long)item * cap + slot] = make_int2((int)id, __float_as_int(v));
     }
@@ -536,6 +539,17 @@ struct ettk_ctx {
     CK(cudaStreamSynchronize(st));
     if (prof) prof_flush();
   }
+  // Blocking copies ordered on the context stream. The stream is non-blocking, so a plain cudaMemcpy (legacy
+  // stream) would not be ordered with its kernels; a pageable host-to-device copy may also return before its
+  // DMA lands. Both helpers return with the copy complete, so the host buffer may go out of scope.
+  void h2d(void *dst, const void *src, size_t bytes) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  void d2h(void *dst, const void *src, size_t bytes) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
   void post_launch() {
     ++launches;
     CK(cudaGetLastError());
@@ -765,6 +779,10 @@ struct ettk_ctx {
     }
   }
   void align(int npairs, const int *pairs, float *D, int cols, int ncand);
+  // nbfCorrelationImageMetric::getWedgeOverlap(T) of each request: sum(w1 w2 filter) / sum(filter) over the
+  // half spectrum with the wedges of the effective sides only, 1 when neither side's wedge is effective
+  DevBuf<double> w_ovl;
+  std::vector<float> wedge_overlaps(const std::vector<EvalReq> &req);
   void soft_diag(const float *F1, const float *F2, int scaled, float *C);
 
   // ---------------------------------------------------------------- continuous pose refinement
@@ -1045,7 +1063,7 @@ const std::vector<int> &ettk_ctx::representation_band() {
   if (!repr_idx.empty()) return repr_idx;
   const int H = N / 2 + 1;
   std::vector<float> fk(h3);
-  CK(cudaMemcpy(fk.data(), filter.p, h3 * sizeof(float), cudaMemcpyDeviceToHost));
+  d2h(fk.data(), filter.p, h3 * sizeof(float));
   std::vector<int> band;
   for (int x = 0; x < N; ++x)
     for (int y = 0; y < N; ++y)
@@ -1054,7 +1072,7 @@ const std::vector<int> &ettk_ctx::representation_band() {
         if (std::fabs(fk[g]) > 0.5f) band.push_back(g);
       }
   repr_idx_dev.ensure(std::max<size_t>(band.size(), 1));
-  CK(cudaMemcpy(repr_idx_dev.p, band.data(), band.size() * sizeof(int), cudaMemcpyHostToDevice));
+  h2d(repr_idx_dev.p, band.data(), band.size() * sizeof(int));
   repr_idx.swap(band);  // cached only once the device copy is in place
   return repr_idx;
 }
@@ -1435,11 +1453,11 @@ void ettk_ctx::init_tables() {
   mask.ensure(n3);
   maskfft.ensure(n3);
   filter.ensure(h3);
-  CK(cudaMemcpy(mask.p, m.data(), n3 * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(maskfft.p, mf.data(), n3 * 4, cudaMemcpyHostToDevice));
+  h2d(mask.p, m.data(), n3 * 4);
+  h2d(maskfft.p, mf.data(), n3 * 4);
   {
     std::vector<float> fk = to_kz_major(f.data(), N);
-    CK(cudaMemcpy(filter.p, fk.data(), h3 * 4, cudaMemcpyHostToDevice));
+    h2d(filter.p, fk.data(), h3 * 4);
   }
   // wedge smoothing weights: std 2, radius int(2*0.5)=1, clipped renormalised kernels
   {
@@ -1486,8 +1504,8 @@ void ettk_ctx::init_tables() {
   }
   lw.ensure(hlw.size());
   plm.ensure(hplm.size());
-  CK(cudaMemcpy(lw.p, hlw.data(), hlw.size() * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(plm.p, hplm.data(), hplm.size() * 4, cudaMemcpyHostToDevice));
+  h2d(lw.p, hlw.data(), hlw.size() * 4);
+  h2d(plm.p, hplm.data(), hplm.size() * 4);
   int ncell = (2 * B - 1) * (2 * B - 1);
   std::vector<int> off(ncell);
   long total = 0;
@@ -1513,16 +1531,16 @@ void ettk_ctx::init_tables() {
   }
   dtab.ensure(total);
   doff.ensure(ncell);
-  CK(cudaMemcpy(dtab.p, hd.data(), total * 4, cudaMemcpyHostToDevice));
+  h2d(dtab.p, hd.data(), total * 4);
   if (!hd64.empty()) {
     dtab64.ensure(total);
-    CK(cudaMemcpy(dtab64.p, hd64.data(), total * 8, cudaMemcpyHostToDevice));
+    h2d(dtab64.p, hd64.data(), total * 8);
   }
-  CK(cudaMemcpy(doff.p, off.data(), ncell * 4, cudaMemcpyHostToDevice));
+  h2d(doff.p, off.data(), ncell * 4);
   std::vector<float> hs(n);
   for (int j = 0; j < n; ++j) hs[j] = (float)sin(M_PI * (2 * j + 1) / 4 / (double)(float)B);
   sinth.ensure(n);
-  CK(cudaMemcpy(sinth.p, hs.data(), n * 4, cudaMemcpyHostToDevice));
+  h2d(sinth.p, hs.data(), n * 4);
   // spherical sampling directions (vtkSphericalTransform, origin pi/4B, spacing 2pi/4B and pi/B)
   std::vector<float4> dv(nn);
   double oy = M_PI / 4.0 / (double)(float)B, sy = 2.0 * M_PI / 4.0 / (double)(float)B, sz = M_PI / (double)(float)B;
@@ -1532,7 +1550,7 @@ void ettk_ctx::init_tables() {
       dv[(size_t)j * n + k] = make_float4((float)(sin(ph) * cos(t2)), (float)(sin(ph) * sin(t2)), (float)cos(ph), 0.f);
     }
   dirs.ensure(nn);
-  CK(cudaMemcpy(dirs.p, dv.data(), nn * sizeof(float4), cudaMemcpyHostToDevice));
+  h2d(dirs.p, dv.data(), nn * sizeof(float4));
   int N2 = 2 * N;
   float lowCut = band ? p.bp_low : 0.0f, highCut = band ? p.bp_high : 1.0f;
   bandL = std::max(4, (int)ceilf(lowCut * (float)(N2 - 1)));
@@ -2200,9 +2218,14 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
           if (!Q.empty() && Q.top().v[3] == FLT_MAX) ps[i].done[q] = true;
         }
     }
-    // 5. final selection (execute 786-907) and output rows (getDistances 1962-2002)
-    std::vector<EvalReq> fallback;
-    std::vector<int> fb_pair;
+    // 5. final selection (execute 786-907) and output rows (getDistances 1962-2002). With one candidate the
+    // row holds the best distance, scale 1 (nbfFourierImageMetric's correlationScale) and getWedgeOverlap at
+    // the final transform; otherwise column 0 of every slot is first set to FLT_MAX (1985) and slot c holds
+    // candidate c with scale 1 and overlap 1 (candidateWedgeOverlaps, execute 880). Slots past ncand are not
+    // written (the reference would write past the end of D).
+    const bool multi = p.number_of_candidates != 1;
+    std::vector<EvalReq> finals(P);
+    std::vector<float> final_d(P);
     for (int i = 0; i < P; ++i) {
       std::vector<Cand> comb = ps[i].combined[0];
       comb.insert(comb.end(), ps[i].combined[1].begin(), ps[i].combined[1].end());
@@ -2212,8 +2235,10 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
       PQ pc;
       eliminate_equivalent(comb, pc, 2.5f);
       float best = FLT_MAX;
-      int row = todo[b0 + i];
-      for (int k = 0; k < ncand; ++k) D[((long)row * cols + 0) * ncand + k] = FLT_MAX;
+      const int row = todo[b0 + i];
+      auto at = [&](int col, int k) -> float & { return D[((long)row * cols + col) * ncand + k]; };
+      if (multi)
+        for (int k = 0; k < ncand; ++k) at(0, k) = FLT_MAX;
       int index = 0;
       Mat4 bestT = Mat4::eye();
       while (!pc.empty() && index < p.number_of_candidates) {
@@ -2231,24 +2256,74 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
           best = r.dist;
           bestT = r.t;
         }
-        if (index < ncand && ncand > 1) {
+        if (multi && index < ncand) {
           int off = 1;
-          D[((long)row * cols + 0) * ncand + index] = r.dist;
-          if (cols > 17) D[((long)row * cols + 1) * ncand + index] = 1.0f, off = 2;
-          if (cols > 18) D[((long)row * cols + 2) * ncand + index] = 1.0f, off = 3;
-          for (int m = 0; m < 16; ++m) D[((long)row * cols + m + off) * ncand + index] = (float)r.t.e[m];
+          at(0, index) = r.dist;
+          if (cols > 17) at(1, index) = 1.0f, off = 2;
+          if (cols > 18) at(2, index) = 1.0f, off = 3;
+          for (int m = 0; m < 16; ++m) at(m + off, index) = (float)r.t.e[m];
         }
         ++index;
       }
-      if (ncand == 1 || p.number_of_candidates == 1) {
+      finals[i] = {pr[i], pp[i], bestT};
+      final_d[i] = best;
+    }
+    if (!multi) {
+      std::vector<float> ovl;
+      if (cols > 18) ovl = wedge_overlaps(finals);
+      for (int i = 0; i < P; ++i) {
+        const int row = todo[b0 + i];
+        auto at = [&](int col) -> float & { return D[((long)row * cols + col) * ncand + 0]; };
         int off = 1;
-        D[((long)row * cols + 0) * ncand + 0] = best;
-        if (cols > 17) D[((long)row * cols + 1) * ncand + 0] = 1.0f, off = 2;
-        if (cols > 18) D[((long)row * cols + 2) * ncand + 0] = 1.0f, off = 3;
-        for (int m = 0; m < 16; ++m) D[((long)row * cols + m + off) * ncand + 0] = (float)bestT.e[m];
+        at(0) = final_d[i];
+        if (cols > 17) at(1) = 1.0f, off = 2;
+        if (cols > 18) at(2) = ovl[i], off = 3;
+        for (int m = 0; m < 16; ++m) at(m + off) = (float)finals[i].t.e[m];
       }
     }
   }
+}
+
+std::vector<float> ettk_ctx::wedge_overlaps(const std::vector<EvalReq> &req) {
+  const long E = (long)req.size();
+  std::vector<float> out(E, 1.0f);
+  std::vector<WedgeVecs> wv;
+  std::vector<int> ref, slot;
+  for (long e = 0; e < E; ++e) {
+    const VolumeGeom &g2 = partg[req[e].part];
+    const bool eff1 = !refg[req[e].ref].full_wedge(), eff2 = !g2.full_wedge();
+    if (!eff1 && !eff2) continue;  // getWedgeOverlap returns 1
+    WedgeVecs w{};
+    w.full = eff2 ? 0 : 1;
+    if (eff2) wedge_vectors(g2, &req[e].t, w.v1, w.v2);
+    wv.push_back(w);
+    ref.push_back(req[e].ref);
+    slot.push_back((int)e);
+  }
+  const long M = (long)wv.size();
+  if (M == 0) return out;
+  const int ACC = 8;
+  w_wv.ensure(M);
+  w_idx.ensure(M);
+  w_fw.ensure(M * h3);
+  w_ovl.ensure(M * ACC);
+  CK(cudaMemcpyAsync(w_wv.p, wv.data(), M * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_idx.p, ref.data(), M * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_ovl.p, 0, M * ACC * sizeof(double), st));
+  {
+    Scope sc_w(this, "wedge", 4.0 * M * h3);
+    switch (N) {
+      case 16: wedge_t<16>(M, w_ovl.p, ACC); break;
+      case 32: wedge_t<32>(M, w_ovl.p, ACC); break;
+      case 64: wedge_t<64>(M, w_ovl.p, ACC); break;
+      case 128: wedge_t<128>(M, w_ovl.p, ACC); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+    }
+  }
+  std::vector<double> acc(M * ACC);
+  read_back(acc.data(), w_ovl.p, M * ACC * sizeof(double));
+  for (long m = 0; m < M; ++m) out[slot[m]] = (float)(acc[m * ACC + 6] / sum_filter);
+  return out;
 }
 
 void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C) {
@@ -2524,7 +2599,7 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     c->refg.resize(R);
     c->useW1.resize(R);
     c->refvol.ensure(R * n3);
-    CK(cudaMemcpy(c->refvol.p, vols, R * n3 * 4, cudaMemcpyHostToDevice));
+    c->h2d(c->refvol.p, vols, R * n3 * 4);
     c->upload_maps(c->refvol.p, R, c->tm_ref, c->tm_ref_ok);
     std::vector<ResliceItem> items(R);
     std::vector<float> w1h((size_t)R * h3), w1s((size_t)R * c->nn);
@@ -2547,8 +2622,8 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     }
     c->W1half.ensure(R * h3);
     c->W1sph.ensure(R * c->nn);
-    CK(cudaMemcpy(c->W1half.p, w1h.data(), R * h3 * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->W1sph.p, w1s.data(), R * c->nn * 4, cudaMemcpyHostToDevice));
+    c->h2d(c->W1half.p, w1h.data(), R * h3 * 4);
+    c->h2d(c->W1sph.p, w1s.data(), R * c->nn * 4);
     // I1 = getImage(reference): reslice, mean of valid voxels removed; F_I1 = R2C(I1 maskfft shift)
     c->w_v.ensure(R * n3);
     c->w_acc.ensure(R * 2);
@@ -2741,7 +2816,7 @@ int ettk_gpu_classify(ettk_ctx *c, int iterations, int *labels, float *refs_out,
         }
       if (mem.empty()) {  // an empty class keeps its reference
         rc = guarded(c, [&] {
-          CK(cudaMemcpy(avg.data() + (size_t)r * n3, c->refvol.p + (size_t)r * n3, n3 * 4, cudaMemcpyDeviceToHost));
+          c->d2h(avg.data() + (size_t)r * n3, c->refvol.p + (size_t)r * n3, n3 * 4);
         });
         if (rc != ETTK_OK) return rc;
         continue;
@@ -2918,7 +2993,7 @@ int ettk_gpu_set_reference_spherical_wedge(ettk_ctx *c, int r, const float *wedg
     int use = 0;
     condition_spherical_host(w, c->B, use);
     c->sync();
-    CK(cudaMemcpy(c->W1sph.p + (long)r * c->nn, w.data(), (size_t)n * n * sizeof(float), cudaMemcpyHostToDevice));
+    c->h2d(c->W1sph.p + (long)r * c->nn, w.data(), (size_t)n * n * sizeof(float));
     c->useW1[r] = use;
   });
 }

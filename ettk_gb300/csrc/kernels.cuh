@@ -400,7 +400,8 @@ __global__ void __launch_bounds__(256, 3) k_wedge_roll(const WedgeVecs *__restri
       const int k = t / N, j = t - k * N;
       const int r = j * H + k;
       const float vm = q > 0 ? rm[r] : 0.f, vp = q < N - 1 ? rp[r] : 0.f;
-      const float v = smooth3v(sw, vm, r0[r], vp, q, N);
+      // a full wedge is the constant 1, unsmoothed (nbfWedge3D::getImageHalf, inc/em/nbfWedge3D.h:316-317)
+      const float v = w.full ? 1.f : smooth3v(sw, vm, r0[r], vp, q, N);
       const long g = ((long)k * N + q) * N + j;
       const float fw = filter[g] * (v * W1[g]);
       o[g] = fw;

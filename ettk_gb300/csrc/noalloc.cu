@@ -14,7 +14,10 @@
 //    call before starting any stream capture on the device;
 //  - all calls share the array and it keeps the previous call's contents: buffers that must start
 //    at zero are cleared by each call, and calls whose GPU work overlaps (other streams, other
-//    threads) race on the array, so callers must serialise them.
+//    threads) race on the array, so callers must serialise them;
+//  - the array's address and tables are set up once per device ordinal for the life of the process:
+//    do not use the entry point across a cudaDeviceReset (or a torn-down and recreated primary
+//    context) of that device.
 #include "../../include/ettk_gpu.h"
 #include "kernels.cuh"
 
@@ -164,6 +167,9 @@ int setup_device(int dev, unsigned char **out) {
   }
   static const SynthJob job{0, 1};
   if (cudaMemcpy(ptr + kLayout.jobs, &job, sizeof(job), cudaMemcpyHostToDevice) != cudaSuccess) return ETTK_ERR_CUDA;
+  // A pageable host-to-device cudaMemcpy may return before its DMA lands, and a caller's non-blocking stream
+  // is not ordered after the legacy stream: wait for the tables before any call may use them.
+  if (cudaDeviceSynchronize() != cudaSuccess) return ETTK_ERR_CUDA;
   g_dev_ptr[dev] = ptr;
   *out = ptr;
   return ETTK_OK;

@@ -80,7 +80,10 @@ int ettk_gpu_set_references(ettk_ctx *ctx, int R, const float *volumes, const et
 /* Replaces the list2 side: V particle volumes and metadata (host memory). */
 int ettk_gpu_set_particles(ettk_ctx *ctx, int V, const float *volumes, const ettk_volume_meta *meta);
 
-/* Same as ettk_gpu_set_particles with `volumes` already in device memory of the context's GPU. */
+/* As ettk_gpu_set_particles with `volumes` already in device memory of the context's GPU. The buffer is
+ * borrowed, not copied: it must hold the complete volumes when the call is made (the caller synchronises
+ * whatever stream wrote them), stay unchanged and allocated until the next set_particles call or
+ * ettk_gpu_destroy, since every later alignment reads it on the context's stream. */
 int ettk_gpu_set_particles_device(ettk_ctx *ctx, int V, const float *d_volumes, const ettk_volume_meta *meta);
 
 /* Particles cut from one tomogram (nbfWedgedSubImage3D::getImage's tomogram path,
@@ -238,8 +241,9 @@ int ettk_gpu_soft(ettk_ctx *ctx, const float *F1, const float *F2, int scaled, f
  * (a cudaStream_t, NULL = default stream) and the call returns without waiting for it.
  * Every intermediate lives in one 2 MiB file-scope device array of the library, so only B = 8 and
  * B = 16 are accepted (ETTK_ERR_ARG otherwise). The first call on a device sets that device's array
- * up (address and tables); make it before any stream capture on the device. All calls share the
- * array: calls whose GPU work overlaps race, so serialise them. */
+ * up (address and tables, then a device-wide synchronisation); make it before any stream capture on
+ * the device, and do not use the entry point across a cudaDeviceReset of that device. All calls share
+ * the array: calls whose GPU work overlaps race, so serialise them. */
 int ettk_gpu_soft_noalloc(int B, const float *d_F1, const float *d_F2, float *d_C, void *stream);
 
 /* Number of kernels this library launched since the context was created. */

@@ -4,7 +4,6 @@
 #include <cstdlib>
 #include <cstdio>
 #include <map>
-#include <mutex>
 
 namespace oracle {
 
@@ -17,10 +16,9 @@ struct Twiddles {
   std::vector<int> rev;    /* bit reversal permutation */
 };
 
+/* per-thread cache: callers on many host threads never contend for it */
 const Twiddles &twiddles(int n) {
-  static std::map<int, Twiddles> cache;
-  static std::mutex mu;
-  std::lock_guard<std::mutex> lock(mu);
+  thread_local std::map<int, Twiddles> cache;
   auto it = cache.find(n);
   if (it != cache.end()) return it->second;
   Twiddles t;

@@ -67,6 +67,7 @@ typedef struct {
   int n_peaks_q1, n_peaks_q2; /* queue sizes after equivalent-angle elimination */
   int use_window1, use_window2;
   int best_cell[3];           /* SO(3) grid cell (alpha, beta, gamma indices) of the best rotation */
+  float wedge_overlap;        /* getWedgeOverlap(getTransform()) */
 } OracleResult;
 
 } // extern "C"
@@ -645,6 +646,8 @@ struct CCF {
   }
 };
 
+float wedge_overlap(const OracleParams &P, const OracleVolume &ref, const OracleVolume &part, const M4 &t);
+
 /* nbfProjectionRotationMetric3D::execute (inc/em/nbfProjectionRotationMetric3D.h:415-907),
  * alignment_mode 3 (refinement off). */
 void align(const OracleParams &P, const OracleVolume &ref, const OracleVolume &part, OracleResult &res) {
@@ -785,6 +788,27 @@ void align(const OracleParams &P, const OracleVolume &ref, const OracleVolume &p
   res.distance = bestDistance;
   memcpy(res.matrix, bestT.e, sizeof(bestT.e));
   res.n_ccf = ccf.ncalls;
+  res.wedge_overlap = wedge_overlap(P, ref, part, bestT);
+}
+
+/* nbfCorrelationImageMetric::getWedgeOverlap (inc/em/nbfCorrelationImageMetric.h:532-565): the half-spectrum
+ * wedges of the sides whose wedge is effective (nbfWedge3D::isEffective, inc/em/nbfWedge3D.h:70: limits other
+ * than (-90, 90)), the particle's under t, summed as float(float(w1 w2) filter) in double over the
+ * updateFilterHalf filter and divided by the filter's sum; 1 when neither wedge is effective. */
+float wedge_overlap(const OracleParams &P, const OracleVolume &ref, const OracleVolume &part, const M4 &t) {
+  const bool e1 = !make_wedge(ref.lwedge, ref.uwedge).full(), e2 = !make_wedge(part.lwedge, part.uwedge).full();
+  if (!e1 && !e2) return 1.0f;
+  std::vector<float> w1, w2, filter;
+  if (e1) wedge_half(ref, P.N, nullptr, w1);
+  if (e2) wedge_half(part, P.N, &t, w2);
+  build_filter(P, filter);
+  double num = 0, den = 0;
+  for (size_t i = 0; i < filter.size(); ++i) {
+    float w = e1 && e2 ? w1[i] * w2[i] : (e1 ? w1[i] : w2[i]);
+    num += (double)(w * filter[i]);
+    den += (double)filter[i];
+  }
+  return (float)(num / den);
 }
 
 /* nbfWedgedAverageImage3D::getImageMPI + getImage with NBF_AVERAGE_IN_RECIPROCAL_SPACE

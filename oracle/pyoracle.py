@@ -47,16 +47,16 @@ class OracleResult(ctypes.Structure):
         ("cand_matrix", (ctypes.c_double * 16) * 8), ("n_ccf", ctypes.c_int),
         ("n_peaks_q1", ctypes.c_int), ("n_peaks_q2", ctypes.c_int),
         ("use_window1", ctypes.c_int), ("use_window2", ctypes.c_int),
-        ("best_cell", ctypes.c_int * 3),
+        ("best_cell", ctypes.c_int * 3), ("wedge_overlap", ctypes.c_float),
     ]
 
 
 def build():
-    """Compile the oracle library (and, when the reference tree is present, SOFT under _ref)."""
+    """Compile the oracle library, then run oracle/build_ref.sh, the recipe that compiles the reference's own
+    SOFT sources and Blitz harnesses under _ref where the reference tree is present (it names the tree's
+    location, overridable with ETTK_REFERENCE_ROOT, and skips cleanly where the tree is absent)."""
     subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
-    if os.path.isdir(os.environ.get("ETTK_REFERENCE_ROOT", "/root/reference")):
-        subprocess.run([os.path.join(HERE, "build_ref.sh")], check=True,
-                       stdout=subprocess.DEVNULL)
+    subprocess.run([os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
 
 
 _lib = None
@@ -146,6 +146,8 @@ def align(params, ref, ref_meta, part, part_meta):
         "use_window1": out.use_window1, "use_window2": out.use_window2,
         "best_cell": tuple(out.best_cell[:]),
         "cand_distance": list(out.cand_distance[:out.n_candidates]),
+        "cand_matrix": [np.array(out.cand_matrix[i][:]).reshape(4, 4) for i in range(out.n_candidates)],
+        "wedge_overlap": out.wedge_overlap,
     }
 
 

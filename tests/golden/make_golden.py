@@ -34,7 +34,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pyoracle  # noqa: E402
 from ettk_gb300 import synthetic  # noqa: E402
 
-REF = os.environ.get("ETTK_REFERENCE_ROOT", "/root/reference")
+# The reference tree (read in place for SOFT's own test signals): ETTK_REFERENCE_ROOT must name it.
+REF = os.environ.get("ETTK_REFERENCE_ROOT")
 
 
 def read_s2(path):
@@ -130,6 +131,8 @@ def main(which):
     R = pyoracle.ref_lib()
     if R is None:
         raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+    if not REF:
+        raise SystemExit("set ETTK_REFERENCE_ROOT to the reference tree (SOFT's test signals are read from it)")
     soft_dir = os.path.join(REF, "external", "soft-1.0")
     sig = read_s2(os.path.join(soft_dir, "randomS2sig_bw8.dat"))
     pat = read_s2(os.path.join(soft_dir, "randomS2sigA_bw8.dat"))
