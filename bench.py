@@ -44,6 +44,12 @@ def parse():
                     help="plain grid search vs grid search + adjoint refinement on the 64^3 B=32 workload: "
                          "alignments/s and error against the generating poses (one JSON line)")
     ap.add_argument("--refine-iterations", type=int, default=15)
+    ap.add_argument("--fast-study", action="store_true",
+                    help="plain form against the fast form (coarse SO(3) hit, one CCF per kept peak, local refinement) "
+                         "on the 64^3 B=32 workload: alignments/s, stage times and errors against the generating poses")
+    ap.add_argument("--fast-iterations", type=int, default=12)
+    ap.add_argument("--fast-peaks", type=int, default=1)
+    ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
     ap.add_argument("--repr-study", action="store_true",
                     help="unsupervised-classification step on the 64^3 workload: low-dimensional representations "
                          "of --study-pairs particles and the distance matrix between them (one JSON line)")
@@ -258,6 +264,83 @@ def adjoint_study(a):
     print(json.dumps(line), flush=True)
 
 
+def pose_errors(D, truth, off=1):
+    """Geodesic rotation error (degrees) and shift error (voxels) of slot 0 of every row against the generating
+    poses."""
+    import numpy as np
+    rot, sh = [], []
+    for i in range(D.shape[0]):
+        T = D[i, off:off + 16, 0].reshape(4, 4).astype(np.float64)
+        Rt = np.asarray(truth[i]["rotation"])
+        c = np.clip((np.trace(T[:3, :3] @ Rt.T) - 1) / 2, -1, 1)
+        rot.append(np.degrees(np.arccos(c)))
+        sh.append(np.linalg.norm(T[:3, 3] - np.asarray(truth[i]["shift"])))
+    return np.array(rot), np.array(sh)
+
+
+def error_summary(rot, sh, hit):
+    import numpy as np
+    return {"rotation_deg_median": float(np.median(rot[hit])), "rotation_deg_mean": float(np.mean(rot[hit])),
+            "shift_vox_median": float(np.median(sh[hit])), "shift_vox_mean": float(np.mean(sh[hit])),
+            "within_0.5deg_0.1vox": float(np.mean((rot < 0.5) & (sh < 0.1))), "basin_hits": int(hit.sum())}
+
+
+def fast_study(a):
+    """Plain form (SO(3) grid + CCF candidates with mirrors, FP32 Wigner) against the fast form (split-BF16 Wigner,
+    one CCF per kept peak, batched local refinement) on the same pairs: alignments/s of each (device-resident
+    particles, CUDA-synchronised wall time, after one warm-up call of each), the library's stage times, and the
+    rotation/shift errors against the generating poses over the pairs whose plain grid hit is within 20 degrees."""
+    import numpy as np
+    import torch
+    from ettk_gb300 import synthetic
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+
+    P = a.pairs
+    ds = synthetic.generate(WORKLOAD, n_particles=P)
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    vols = [WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in kw}) for i in range(P)]
+    ref = WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})
+    pairs = [(0, i) for i in range(P)]
+    out = {}
+    for form, prec in (("plain", 0), ("fast", a.fast_precision)):
+        m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec))
+        m.set_references([ref])
+        m.set_particles(vols)
+
+        def run(sub):
+            if form == "plain":
+                return m.getDistances(sub)
+            return m.getDistancesRefined(sub, iterations=a.fast_iterations, peaks=a.fast_peaks)
+        run(pairs[:8])
+        m.set_particles(vols)  # drop the cached spherical projections of the warm-up pairs
+        torch.cuda.synchronize()
+        m.profile(True)
+        t0 = time.perf_counter()
+        D = run(pairs)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        prof = m.profile_read()
+        m.profile(False)
+        m.close()
+        out[form] = (D, P / (t1 - t0), prof)
+    rp, sp = pose_errors(out["plain"][0], ds.truth)
+    rf, sf = pose_errors(out["fast"][0], ds.truth)
+    hit = rp < 20.0
+    stages = ("stage_so3", "stage_ccf", "stage_coarse_ccf", "stage_local_refine", "host_align_wall")
+    line = {"fast_study": {
+        "plain": dict(alignments_per_s=out["plain"][1], **error_summary(rp, sp, hit),
+                      stages_ms={k: round(v["ms"], 3) for k, v in out["plain"][2].items() if k in stages}),
+        "fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, hit),
+                     basin_hits_fast=int((rf < 20.0).sum()),
+                     stages_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items() if k in stages},
+                     families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()}),
+        "speedup": out["fast"][1] / out["plain"][1]},
+        "config": {"workload": WORKLOAD, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
+                   "fast_wigner_precision": a.fast_precision,
+                   "errors": "against the generating poses, over pairs whose plain grid hit is within 20 degrees"}}
+    print(json.dumps(line), flush=True)
+
+
 def repr_study(a):
     """getLowDimensionRepresentationHalf of V 64^3 particles and the V x V distance matrix of
     nbfCorrelationImageMetric::getDistances between them, each timed once after one small warm-up call
@@ -303,6 +386,9 @@ def main():
     a = parse()
     if a.repr_study:
         repr_study(a)
+        return
+    if a.fast_study:
+        fast_study(a)
         return
     if a.adjoint_study:
         adjoint_study(a)

@@ -18,6 +18,7 @@
 #include "fft2d.cuh"
 #include "wigner_tc.cuh"
 #include "refine.cuh"
+#include "local_refine.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -623,10 +624,10 @@ struct ettk_ctx {
     }
   }
   template <int NN, class Pre>
-  void r2c_z_t(Pre pre, float2 *out, long lines) {
+  void r2c_z_t(Pre pre, float2 *out, long lines, const char *family = "fft_r2c_z") {
     constexpr int L = reg_lines<NN>();
     long tiles = (lines + 2 * L - 1) / (2 * L);
-    Scope sc(this, "fft_r2c_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
+    Scope sc(this, family, 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
     bool streamed = false;
     if constexpr (has_stream<Pre>::value) {
       const unsigned long long sa = (unsigned long long)pre.stream_src(), aa = (unsigned long long)pre.stream_aux();
@@ -665,13 +666,13 @@ struct ettk_ctx {
     return g;
   }
   template <class Pre>
-  void r2c_z(int len, Pre pre, float2 *out, long lines) {
+  void r2c_z(int len, Pre pre, float2 *out, long lines, const char *family = "fft_r2c_z") {
     switch (len) {
-      case 16: r2c_z_t<16>(pre, out, lines); break;
-      case 32: r2c_z_t<32>(pre, out, lines); break;
-      case 64: r2c_z_t<64>(pre, out, lines); break;
-      case 128: r2c_z_t<128>(pre, out, lines); break;
-      case 256: r2c_z_t<256>(pre, out, lines); break;
+      case 16: r2c_z_t<16>(pre, out, lines, family); break;
+      case 32: r2c_z_t<32>(pre, out, lines, family); break;
+      case 64: r2c_z_t<64>(pre, out, lines, family); break;
+      case 128: r2c_z_t<128>(pre, out, lines, family); break;
+      case 256: r2c_z_t<256>(pre, out, lines, family); break;
       default: throw CudaError(ETTK_ERR_ARG, "unsupported FFT length");
     }
   }
@@ -779,6 +780,35 @@ struct ettk_ctx {
     }
   }
   void align(int npairs, const int *pairs, float *D, int cols, int ncand);
+  // ---------------------------------------------------------------- fast form: coarse SO(3) hit + local refinement
+  DevBuf<LRItem> lr_items;
+  DevBuf<LRState> lr_state;
+  DevBuf<float> lr_zm, lr_maps, lr_ip;
+  DevBuf<int> lr_src;
+  std::vector<int> lr_slot;  // particle -> slot of its band-passed copy in lr_ip (-1: none)
+  // band-passed copies of the fixed-image particles `parts` (filter of the metric, the particle's own frame)
+  void lr_filter_particles(const std::vector<int> &parts);
+  DevBuf<double> lr_acc;
+  double lr_C0 = 0, lr_C1 = 0;  // sum m, sum m^2 of the spherical mask
+  double lr_radius() const { return 0.6 * (p.mask_radius > 0 ? p.mask_radius : 0.5 * N); }
+  // zm of every request (reference filtered with the wedges at the request's pose, times the mask), the
+  // refinement states at the requests' poses and their index maps
+  void lr_setup(const std::vector<EvalReq> &req);
+  // iterations + 1 evaluations of every pair's objective, each followed by the per-pair update
+  void lr_run(long P, int iterations);
+  template <int NN>
+  void lr_eval_t(long E) {
+    constexpr int SLAB = NN >= 64 ? 4 : (NN >= 32 ? 8 : 16);
+    Scope sc(this, "local_refine", 4.0 * E * (double)n3 * 2);
+    k_lr_eval<NN, SLAB><<<dim3(NN / SLAB, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, mask.p, lr_acc.p);
+    post_launch();
+  }
+  void lr_eval(long E) { with_n(N, [&](auto nn) { lr_eval_t<decltype(nn)::value>(E); }); }
+  void align_refined(int npairs, const int *pairs, float *D, int cols, int ncand, int iterations, int peaks);
+  void refined_objective(int npairs, const int *pairs, const double *poses, const double *theta, double *rho,
+                         double *grad);
+  void so3_queues(int P, const std::vector<int> &pr, const std::vector<int> &pp, std::vector<PairPlan> &plans,
+                  std::vector<PQ> &q1, std::vector<PQ> &q2);
   // nbfCorrelationImageMetric::getWedgeOverlap(T) of each request: sum(w1 w2 filter) / sum(filter) over the
   // half spectrum with the wedges of the effective sides only, 1 when neither side's wedge is effective
   DevBuf<double> w_ovl;
@@ -1454,6 +1484,11 @@ void ettk_ctx::init_tables() {
   maskfft.ensure(n3);
   filter.ensure(h3);
   h2d(mask.p, m.data(), n3 * 4);
+  lr_C0 = lr_C1 = 0;
+  for (long i = 0; i < n3; ++i) {
+    lr_C0 += (double)m[i];
+    lr_C1 += (double)m[i] * (double)m[i];
+  }
   h2d(maskfft.p, mf.data(), n3 * 4);
   {
     std::vector<float> fk = to_kz_major(f.data(), N);
@@ -1590,7 +1625,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   CK(cudaMemcpyAsync(w_items.p, items.data(), P * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(sp_acc.p, 0, P * 4 * sizeof(double), st));
   {
-    Scope sc(this, "reslice", 8.0 * P * n3);
+    Scope sc(this, "sphere_reslice", 8.0 * P * n3);
     reslice(w_items.p, sp_v.p, sp_acc.p, 4, nullptr, P);
   }
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
@@ -1598,12 +1633,12 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   PrePadded pre{sp_v.p, mask.p, sp_acc.p, 4, N};
   k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
   post_launch();
-  r2c_z(N2, pre, sp_F.p, P * N2 * N2);
+  r2c_z(N2, pre, sp_F.p, P * N2 * N2, "sphere_fft");
   // (x, y) passes storing |F| directly (the complex spectrum is not used again)
   switch (N2) {
-    case 32: fft2d_t<32>(OpPaddedMagnitude<32>{sp_F.p, sp_M.p}, P); break;
-    case 64: fft2d_t<64>(OpPaddedMagnitude<64>{sp_F.p, sp_M.p}, P); break;
-    case 128: fft2d_t<128>(OpPaddedMagnitude<128>{sp_F.p, sp_M.p}, P); break;
+    case 32: fft2d_t<32>(OpPaddedMagnitude<32>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
+    case 64: fft2d_t<64>(OpPaddedMagnitude<64>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
+    case 128: fft2d_t<128>(OpPaddedMagnitude<128>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
     default: {
       xy_kxy(N2, sp_F.p, P, -1);
       k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
@@ -1930,6 +1965,226 @@ void eliminate_equivalent(std::vector<Cand> &pos, PQ &pq, float tol, const std::
 
 }  // namespace
 
+// Stages 1-3 of execute for a batch of P pairs (reference pr[i], particle pp[i]): spherical projections of the
+// particles not yet projected (cartesianToSpherical, inc/em/nbfProjectionRotationMetric3D.h:264-413), every SO(3)
+// correlation of the batch's window branches (468-584, 629), the beta restriction and 3x3x3 local maxima (602-646)
+// and the per-pair candidate queues after eliminateEquivalentAngles (1592-1702): q1 of the (windowed) correlation,
+// q2 of the unwindowed one where a window is used.
+void ettk_ctx::so3_queues(int P, const std::vector<int> &pr, const std::vector<int> &pp, std::vector<PairPlan> &plans,
+                          std::vector<PQ> &q1, std::vector<PQ> &q2) {
+  // 1. spherical projections of particles not yet projected
+  {
+    std::vector<ResliceItem> items;
+    std::vector<int> ids;
+    for (int i = 0; i < P; ++i)
+      if (!pp2_ready[pp[i]] && std::find(ids.begin(), ids.end(), pp[i]) == ids.end()) ids.push_back(pp[i]);
+    const int chunk = 256;
+    for (size_t c0 = 0; c0 < ids.size(); c0 += chunk) {
+      items.clear();
+      size_t c1 = std::min(ids.size(), c0 + chunk);
+      for (size_t c = c0; c < c1; ++c) {
+        ResliceItem it;
+        it.vol = part_vol(ids[c]);
+        it.tmap = part_map(ids[c]);
+        part_dims(it.dims);
+        double m12[12];
+        reslice_index(partg[ids[c]], N, nullptr, m12);
+        set_map(it, m12);
+        items.push_back(it);
+      }
+      w_sig.ensure(items.size() * nn);
+      spherical_projection(items, w_sig.p);
+      for (size_t c = c0; c < c1; ++c) {
+        CK(cudaMemcpyAsync(Pp2.p + (long)ids[c] * nn, w_sig.p + (c - c0) * nn, nn * 4, cudaMemcpyDeviceToDevice, st));
+        pp2_ready[ids[c]] = 1;
+      }
+    }
+  }
+  // 2. SO(3) plans: signals, correlation jobs, scaled jobs
+  std::vector<SigDesc> sd;
+  std::vector<SynthJob> jobs;
+  std::vector<ScaledJob> sjobs;
+  plans.assign(P, PairPlan{});
+  std::vector<int> jscaled;
+  auto sig = [&](int pair, int kind) {
+    sd.push_back({pair, kind});
+    return (int)sd.size() - 1;
+  };
+  auto corr = [&](PairPlan &pl, int slot, int pair, int k1, int k2, bool scaled) {
+    int f = sig(pair, k1), h = sig(pair, k2);
+    jobs.push_back({f, h});
+    pl.job[slot] = (int)jobs.size() - 1;
+    pl.scaled[slot] = scaled;
+    pl.sjob[slot] = -1;
+    if (scaled) {
+      sjobs.push_back({h, f, (int)jobs.size() - 1});
+      pl.sjob[slot] = (int)sjobs.size() - 1;
+    }
+  };
+  for (int i = 0; i < P; ++i) {
+    PairPlan &pl = plans[i];
+    for (int s = 0; s < 5; ++s) pl.job[s] = -1, pl.scaled[s] = 0, pl.sjob[s] = -1;
+    bool u1 = p.wedge_compensation && useW1[pr[i]], u2 = p.wedge_compensation && useW2[pp[i]];
+    if (u1 && u2) {
+      pl.branch = 1;
+      corr(pl, 0, i, K_PP1SQ_W1, K_W2, true);
+      corr(pl, 1, i, K_W1, K_PP2SQ_W2, true);
+      corr(pl, 2, i, K_PP1_W1, K_PP2_W2, true);
+      corr(pl, 3, i, K_W1, K_W2, true);
+    } else if (u1) {
+      pl.branch = 2;
+      corr(pl, 0, i, K_W1, K_PP2SQ, true);
+      corr(pl, 1, i, K_W1_PP1, K_PP2, true);
+    } else if (u2) {
+      pl.branch = 3;
+      corr(pl, 0, i, K_PP1SQ, K_W2, true);
+      corr(pl, 1, i, K_PP1, K_W2_PP2, true);
+    } else {
+      pl.branch = 4;
+      corr(pl, 0, i, K_PP1, K_PP2, false);
+    }
+    if (u1 || u2) corr(pl, 4, i, K_PP1, K_PP2, false);
+  }
+  long NS = (long)sd.size(), NJ = (long)jobs.size(), NSJ = (long)sjobs.size();
+  w_sd.ensure(NS);
+  w_jobs.ensure(NJ);
+  w_sjobs.ensure(std::max(1L, NSJ));
+  w_plans.ensure(P);
+  w_pair_ref.ensure(P);
+  w_pair_pp2.ensure(P);
+  w_pair_part.ensure(P);
+  w_sig.ensure(NS * nn);
+  w_coef.ensure(NS * B * B);
+  w_S.ensure(NJ * nso3);
+  w_C.ensure(NJ * nso3);
+  w_mm.ensure(NJ * 2);
+  w_w.ensure(std::max(1L, NSJ) * 2);
+  w_q1.ensure((long)P * nso3);
+  w_q2.ensure((long)P * nso3);
+  CK(cudaMemcpyAsync(w_sd.p, sd.data(), NS * sizeof(SigDesc), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_jobs.p, jobs.data(), NJ * sizeof(SynthJob), cudaMemcpyHostToDevice, st));
+  if (NSJ) CK(cudaMemcpyAsync(w_sjobs.p, sjobs.data(), NSJ * sizeof(ScaledJob), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_plans.p, plans.data(), P * sizeof(PairPlan), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_pair_ref.p, pr.data(), P * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_pair_pp2.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_pair_part.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
+  {
+    Scope sc_sig(this, "so3_signals", 4.0 * NS * nn * 2);
+    k_build_signals<<<NS, 256, 0, st>>>(w_sd.p, w_pair_ref.p, w_pair_pp2.p, Pp1.p, Pp2.p, W1sph.p, W2sph.p,
+                                        w_pair_part.p, (int)nn, w_sig.p);
+    post_launch();
+  }
+  size_t smem_sht = (n / 2 + (size_t)n * n) * sizeof(float2);
+  switch (B) {
+#define SO3_CASE(BB)                                                                                                  \
+case BB: {                                                                                                            \
+  if (smem_sht > 48 * 1024)                                                                                           \
+    CK(cudaFuncSetAttribute(k_sht<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sht));                  \
+  {                                                                                                                   \
+    Scope sc_sh(this, "sht", 4.0 * NS * nn + 8.0 * NS * B * B);                                                       \
+    k_sht<BB><<<NS, 256, smem_sht, st>>>(w_sig.p, lw.p, w_coef.p);                                                    \
+    post_launch();                                                                                                    \
+  }                                                                                                                   \
+  CK(cudaMemsetAsync(w_S.p, 0, NJ * nso3 * sizeof(float2), st));                                                      \
+  {                                                                                                                   \
+    Scope sc_s(this, "so3_synth", 8.0 * NJ * nso3 + 4.0 * dtab.n);                                                    \
+    synth<BB>(NJ);                                                                                                    \
+  }                                                                                                                   \
+  fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, 1, (long)n, 0, 1}, -1);                                              \
+  fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n, (long)n * n, 1, (long)n}, -1);                                    \
+  CK(cudaMemsetAsync(w_mm.p, 0, NJ * 2 * sizeof(unsigned long long), st));                                            \
+  {                                                                                                                   \
+    Scope sc_r(this, "so3_real", 12.0 * NJ * nso3);                                                                   \
+    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), NJ), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);                     \
+    post_launch();                                                                                                    \
+  }                                                                                                                   \
+  if (NSJ) {                                                                                                          \
+    Scope sc_w(this, "so3_weights", 4.0 * NSJ * nn);                                                                  \
+    k_so3_weights<BB><<<dim3(NSJ, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p,             \
+                                                    plm.p, sinth.p, w_w.p);                                           \
+    post_launch();                                                                                                    \
+  }                                                                                                                   \
+} break;
+    SO3_CASE(8)
+    SO3_CASE(16)
+    SO3_CASE(32)
+    SO3_CASE(64)
+#undef SO3_CASE
+    default:
+      throw CudaError(ETTK_ERR_ARG, "unsupported bandwidth");
+  }
+  {
+  Scope sc_c(this, "combine", 4.0 * (NJ + 2.0 * P) * nso3);
+  k_combine<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_plans.p, w_C.p, w_mm.p, w_w.p, n, rstart,
+                                                                      w_q1.p, w_q2.p);
+  post_launch();
+  }
+  // 3. local maxima -> host queues
+  const int cap = 8192;
+  w_cnt.ensure(2 * P);
+  w_active.ensure(2 * P);
+  w_lists.ensure((long)2 * P * cap);
+  std::vector<int> act(2 * P);
+  for (int i = 0; i < P; ++i) {
+    act[i] = 1;
+    act[P + i] = plans[i].job[4] >= 0;
+  }
+  CK(cudaMemcpyAsync(w_active.p, act.data(), 2 * P * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_cnt.p, 0, 2 * P * 4, st));
+  // q1 and q2 buffers are contiguous when allocated back to back; launch separately
+  {
+  Scope sc_lm(this, "local_max", 8.0 * P * nso3);
+  k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q1.p, n, w_active.p, cap, w_cnt.p, w_lists.p);
+  post_launch();
+  k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q2.p, n, w_active.p + P, cap, w_cnt.p + P,
+                                                                     w_lists.p + (long)P * cap);
+  post_launch();
+  }
+  std::vector<int> cnt(2 * P);
+  read_back(cnt.data(), w_cnt.p, 2 * P * 4);
+  int maxc = 0;
+  for (int q = 0; q < 2 * P; ++q) {
+    if (cnt[q] > cap) throw CudaError(ETTK_ERR_ARG, "too many SO(3) local maxima");
+    maxc = std::max(maxc, cnt[q]);
+  }
+  // the first maxc entries of every list, packed at pitch maxc (list q at lists[q * maxc])
+  std::vector<int2> lists((size_t)2 * P * std::max(maxc, 1));
+  if (maxc) {
+    HostScope hs(this, "host_wait");
+    CK(cudaMemcpy2DAsync(lists.data(), maxc * sizeof(int2), w_lists.p, cap * sizeof(int2), maxc * sizeof(int2),
+                         2 * P, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  q1.assign(P, PQ());
+  q2.assign(P, PQ());
+  {
+  HostScope hs_q(this, "host_queues");
+  // queues are independent: build them on the host cores
+  auto build_queue = [&](int q) {
+    int c = std::min(cnt[q], cap);
+    std::vector<int2> L(lists.begin() + (long)q * maxc, lists.begin() + (long)q * maxc + c);
+    std::sort(L.begin(), L.end(), [](const int2 &a, const int2 &b) { return a.x < b.x; });
+    std::vector<Cand> pos;
+    std::vector<Mat4> mats;
+    for (auto &e : L) {
+      int a = e.x / (n * n), bb = (e.x / n) % n, g = e.x % n;
+      float val = __builtin_bit_cast(float, e.y);
+      float alpha = (float)(a / (double)B * 180.0);
+      float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
+      if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
+      float gamma = (float)(g / (double)B * 180.0);
+      const Mat4 m = euler_candidate(alpha, beta, gamma);
+      if (transform_valid(p, m)) {
+        pos.push_back({{alpha, beta, gamma, -val}, -1});
+        mats.push_back(m);
+      }
+    }
+    eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f, &mats);
+  };
+  parallel_for(2 * P, build_queue);
+  }
+}
+
 void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand) {
   HostScope hs_all(this, "host_align_wall");
   int maxb = p.max_batch > 0 ? p.max_batch : 512;
@@ -1944,206 +2199,13 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
       pp[i] = pairs[2 * todo[b0 + i] + 1];
       if (pr[i] < 0 || pr[i] >= R || pp[i] < 0 || pp[i] >= V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
     }
-    // 1. spherical projections of particles not yet projected
+    std::vector<PairPlan> plans;
+    std::vector<PQ> q1, q2;
     {
-      std::vector<ResliceItem> items;
-      std::vector<int> ids;
-      for (int i = 0; i < P; ++i)
-        if (!pp2_ready[pp[i]] && std::find(ids.begin(), ids.end(), pp[i]) == ids.end()) ids.push_back(pp[i]);
-      const int chunk = 256;
-      for (size_t c0 = 0; c0 < ids.size(); c0 += chunk) {
-        items.clear();
-        size_t c1 = std::min(ids.size(), c0 + chunk);
-        for (size_t c = c0; c < c1; ++c) {
-          ResliceItem it;
-          it.vol = part_vol(ids[c]);
-          it.tmap = part_map(ids[c]);
-          part_dims(it.dims);
-          double m12[12];
-          reslice_index(partg[ids[c]], N, nullptr, m12);
-          set_map(it, m12);
-          items.push_back(it);
-        }
-        w_sig.ensure(items.size() * nn);
-        spherical_projection(items, w_sig.p);
-        for (size_t c = c0; c < c1; ++c) {
-          CK(cudaMemcpyAsync(Pp2.p + (long)ids[c] * nn, w_sig.p + (c - c0) * nn, nn * 4, cudaMemcpyDeviceToDevice, st));
-          pp2_ready[ids[c]] = 1;
-        }
-      }
+      HostScope hs_so3(this, "stage_so3");
+      so3_queues(P, pr, pp, plans, q1, q2);
     }
-    // 2. SO(3) plans: signals, correlation jobs, scaled jobs
-    std::vector<SigDesc> sd;
-    std::vector<SynthJob> jobs;
-    std::vector<ScaledJob> sjobs;
-    std::vector<PairPlan> plans(P);
-    std::vector<int> jscaled;
-    auto sig = [&](int pair, int kind) {
-      sd.push_back({pair, kind});
-      return (int)sd.size() - 1;
-    };
-    auto corr = [&](PairPlan &pl, int slot, int pair, int k1, int k2, bool scaled) {
-      int f = sig(pair, k1), h = sig(pair, k2);
-      jobs.push_back({f, h});
-      pl.job[slot] = (int)jobs.size() - 1;
-      pl.scaled[slot] = scaled;
-      pl.sjob[slot] = -1;
-      if (scaled) {
-        sjobs.push_back({h, f, (int)jobs.size() - 1});
-        pl.sjob[slot] = (int)sjobs.size() - 1;
-      }
-    };
-    for (int i = 0; i < P; ++i) {
-      PairPlan &pl = plans[i];
-      for (int s = 0; s < 5; ++s) pl.job[s] = -1, pl.scaled[s] = 0, pl.sjob[s] = -1;
-      bool u1 = p.wedge_compensation && useW1[pr[i]], u2 = p.wedge_compensation && useW2[pp[i]];
-      if (u1 && u2) {
-        pl.branch = 1;
-        corr(pl, 0, i, K_PP1SQ_W1, K_W2, true);
-        corr(pl, 1, i, K_W1, K_PP2SQ_W2, true);
-        corr(pl, 2, i, K_PP1_W1, K_PP2_W2, true);
-        corr(pl, 3, i, K_W1, K_W2, true);
-      } else if (u1) {
-        pl.branch = 2;
-        corr(pl, 0, i, K_W1, K_PP2SQ, true);
-        corr(pl, 1, i, K_W1_PP1, K_PP2, true);
-      } else if (u2) {
-        pl.branch = 3;
-        corr(pl, 0, i, K_PP1SQ, K_W2, true);
-        corr(pl, 1, i, K_PP1, K_W2_PP2, true);
-      } else {
-        pl.branch = 4;
-        corr(pl, 0, i, K_PP1, K_PP2, false);
-      }
-      if (u1 || u2) corr(pl, 4, i, K_PP1, K_PP2, false);
-    }
-    long NS = (long)sd.size(), NJ = (long)jobs.size(), NSJ = (long)sjobs.size();
-    w_sd.ensure(NS);
-    w_jobs.ensure(NJ);
-    w_sjobs.ensure(std::max(1L, NSJ));
-    w_plans.ensure(P);
-    w_pair_ref.ensure(P);
-    w_pair_pp2.ensure(P);
-    w_pair_part.ensure(P);
-    w_sig.ensure(NS * nn);
-    w_coef.ensure(NS * B * B);
-    w_S.ensure(NJ * nso3);
-    w_C.ensure(NJ * nso3);
-    w_mm.ensure(NJ * 2);
-    w_w.ensure(std::max(1L, NSJ) * 2);
-    w_q1.ensure((long)P * nso3);
-    w_q2.ensure((long)P * nso3);
-    CK(cudaMemcpyAsync(w_sd.p, sd.data(), NS * sizeof(SigDesc), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w_jobs.p, jobs.data(), NJ * sizeof(SynthJob), cudaMemcpyHostToDevice, st));
-    if (NSJ) CK(cudaMemcpyAsync(w_sjobs.p, sjobs.data(), NSJ * sizeof(ScaledJob), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w_plans.p, plans.data(), P * sizeof(PairPlan), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w_pair_ref.p, pr.data(), P * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w_pair_pp2.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w_pair_part.p, pp.data(), P * 4, cudaMemcpyHostToDevice, st));
-    k_build_signals<<<NS, 256, 0, st>>>(w_sd.p, w_pair_ref.p, w_pair_pp2.p, Pp1.p, Pp2.p, W1sph.p, W2sph.p,
-                                        w_pair_part.p, (int)nn, w_sig.p);
-    post_launch();
-    size_t smem_sht = (n / 2 + (size_t)n * n) * sizeof(float2);
-    switch (B) {
-#define SO3_CASE(BB)                                                                                          \
-  case BB: {                                                                                                  \
-    if (smem_sht > 48 * 1024)                                                                                 \
-      CK(cudaFuncSetAttribute(k_sht<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sht));        \
-    k_sht<BB><<<NS, 256, smem_sht, st>>>(w_sig.p, lw.p, w_coef.p);                                            \
-    post_launch();                                                                                            \
-    CK(cudaMemsetAsync(w_S.p, 0, NJ * nso3 * sizeof(float2), st));                                           \
-    {                                                                                                         \
-    Scope sc_s(this, "so3_synth", 8.0 * NJ * nso3 + 4.0 * dtab.n);                                           \
-    synth<BB>(NJ);                                                                                            \
-    }                                                                                                         \
-    fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, 1, (long)n, 0, 1}, -1);                                    \
-    fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n, (long)n * n, 1, (long)n}, -1);                          \
-    CK(cudaMemsetAsync(w_mm.p, 0, NJ * 2 * sizeof(unsigned long long), st));                                  \
-    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), NJ), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);            \
-    post_launch();                                                                                            \
-    if (NSJ) {                                                                                                \
-      k_so3_weights<BB><<<dim3(NSJ, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p,    \
-                                                      plm.p, sinth.p, w_w.p);                                 \
-      post_launch();                                                                                          \
-    }                                                                                                         \
-  } break;
-      SO3_CASE(8)
-      SO3_CASE(16)
-      SO3_CASE(32)
-      SO3_CASE(64)
-#undef SO3_CASE
-      default:
-        throw CudaError(ETTK_ERR_ARG, "unsupported bandwidth");
-    }
-    {
-    Scope sc_c(this, "combine", 4.0 * (NJ + 2.0 * P) * nso3);
-    k_combine<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_plans.p, w_C.p, w_mm.p, w_w.p, n, rstart,
-                                                                        w_q1.p, w_q2.p);
-    post_launch();
-    }
-    // 3. local maxima -> host queues
-    const int cap = 8192;
-    w_cnt.ensure(2 * P);
-    w_active.ensure(2 * P);
-    w_lists.ensure((long)2 * P * cap);
-    std::vector<int> act(2 * P);
-    for (int i = 0; i < P; ++i) {
-      act[i] = 1;
-      act[P + i] = plans[i].job[4] >= 0;
-    }
-    CK(cudaMemcpyAsync(w_active.p, act.data(), 2 * P * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(w_cnt.p, 0, 2 * P * 4, st));
-    // q1 and q2 buffers are contiguous when allocated back to back; launch separately
-    {
-    Scope sc_lm(this, "local_max", 8.0 * P * nso3);
-    k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q1.p, n, w_active.p, cap, w_cnt.p, w_lists.p);
-    post_launch();
-    k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q2.p, n, w_active.p + P, cap, w_cnt.p + P,
-                                                                       w_lists.p + (long)P * cap);
-    post_launch();
-    }
-    std::vector<int> cnt(2 * P);
-    read_back(cnt.data(), w_cnt.p, 2 * P * 4);
-    std::vector<int2> lists((long)2 * P * cap);
-    int maxc = 0;
-    for (int q = 0; q < 2 * P; ++q) {
-      if (cnt[q] > cap) throw CudaError(ETTK_ERR_ARG, "too many SO(3) local maxima");
-      maxc = std::max(maxc, cnt[q]);
-    }
-    if (maxc) {
-      // one strided copy of the first maxc entries of every list
-      HostScope hs(this, "host_wait");
-      CK(cudaMemcpy2DAsync(lists.data(), cap * sizeof(int2), w_lists.p, cap * sizeof(int2), maxc * sizeof(int2),
-                           2 * P, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-    }
-    std::vector<PQ> q1(P), q2(P);
-    {
-    HostScope hs_q(this, "host_queues");
-    // queues are independent: build them on the host cores
-    auto build_queue = [&](int q) {
-      int c = std::min(cnt[q], cap);
-      std::vector<int2> L(lists.begin() + (long)q * cap, lists.begin() + (long)q * cap + c);
-      std::sort(L.begin(), L.end(), [](const int2 &a, const int2 &b) { return a.x < b.x; });
-      std::vector<Cand> pos;
-      std::vector<Mat4> mats;
-      for (auto &e : L) {
-        int a = e.x / (n * n), bb = (e.x / n) % n, g = e.x % n;
-        float val = __builtin_bit_cast(float, e.y);
-        float alpha = (float)(a / (double)B * 180.0);
-        float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
-        if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
-        float gamma = (float)(g / (double)B * 180.0);
-        const Mat4 m = euler_candidate(alpha, beta, gamma);
-        if (transform_valid(p, m)) {
-          pos.push_back({{alpha, beta, gamma, -val}, -1});
-          mats.push_back(m);
-        }
-      }
-      eliminate_equivalent(pos, q < P ? q1[q] : q2[q - P], 0.25f, &mats);
-    };
-    parallel_for(2 * P, build_queue);
-    }
+    HostScope hs_ccf(this, "stage_ccf");  // candidate rounds and final selection
     // 4. candidate rounds (execute 678-776): direct and mirror CCF per popped candidate
     struct PairState {
       int index[2] = {0, 0};
@@ -2281,6 +2343,225 @@ void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand
         for (int m = 0; m < 16; ++m) at(m + off) = (float)finals[i].t.e[m];
       }
     }
+  }
+}
+
+void ettk_ctx::lr_setup(const std::vector<EvalReq> &req) {
+  const long P = (long)req.size();
+  const int ACC = 8;
+  w_wv.ensure(P);
+  w_idx.ensure(P);
+  w_fw.ensure(P * h3);
+  w_cA.ensure(P * h3);
+  w_acc.ensure(P * ACC);
+  lr_zm.ensure(P * n3);
+  lr_items.ensure(P);
+  lr_state.ensure(P);
+  lr_maps.ensure(P * 12);
+  lr_acc.ensure(P * LR_NACC);
+  std::vector<WedgeVecs> wv(P);
+  std::vector<int> refidx(P);
+  std::vector<LRItem> items(P);
+  std::vector<LRState> sts(P);
+  std::vector<float> maps(P * 12);
+  for (long e = 0; e < P; ++e) {
+    const VolumeGeom &g = partg[req[e].part];
+    WedgeVecs w{};
+    w.full = g.full_wedge() ? 1 : 0;
+    if (!w.full) wedge_vectors(g, &req[e].t, w.v1, w.v2);
+    wv[e] = w;
+    refidx[e] = req[e].ref;
+    LRItem it;
+    const int slot = req[e].part < (int)lr_slot.size() ? lr_slot[req[e].part] : -1;
+    it.vol = slot >= 0 ? lr_ip.p + (long)slot * n3 : part_vol(req[e].part);
+    part_dims(it.dims);
+    it.zm_index = (int)e;
+    items[e] = it;
+    LRState S{};
+    reslice_index(g, N, &req[e].t, S.base);
+    S.rho = -1e308;
+    S.alpha = 0.5;
+    sts[e] = S;
+    for (int k = 0; k < 12; ++k) maps[e * 12 + k] = (float)S.base[k];
+  }
+  CK(cudaMemcpyAsync(w_wv.p, wv.data(), P * sizeof(WedgeVecs), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w_idx.p, refidx.data(), P * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(lr_items.p, items.data(), P * sizeof(LRItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(lr_state.p, sts.data(), P * sizeof(LRState), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(lr_maps.p, maps.data(), P * 12 * sizeof(float), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, P * ACC * sizeof(double), st));
+  if (p.wedge_compensation) {
+    Scope sc_w(this, "wedge", 4.0 * P * h3);
+    with_n(N, [&](auto nn) { wedge_t<decltype(nn)::value>(P, w_acc.p, ACC); });
+  } else {
+    for (long e = 0; e < P; ++e) CK(cudaMemcpyAsync(w_fw.p + e * h3, filter.p, h3 * 4, cudaMemcpyDeviceToDevice, st));
+  }
+  // y1 = K(I1): F1 = FI1 fw (DC removed), inverse (x, y) passes, C2R z pass storing m * y1 (centring sign undone)
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, w_fw.p, w_cA.p, HalfSums<NN>{w_acc.p, ACC, 2}}, P, "local_refine_setup",
+                20.0);
+  });
+  c2r_z(N, w_cA.p, PostStoreZm{lr_zm.p, mask.p, N}, P * N * N);
+  k_lr_consts<<<(unsigned)P, 256, 0, st>>>(lr_zm.p, n3, lr_state.p);
+  post_launch();
+}
+
+void ettk_ctx::lr_filter_particles(const std::vector<int> &parts) {
+  lr_slot.assign(V, -1);
+  if (from_tomo || parts.empty()) return;
+  std::vector<int> u;
+  for (int q : parts)
+    if (lr_slot[q] < 0) {
+      lr_slot[q] = (int)u.size();
+      u.push_back(q);
+    }
+  const long M = (long)u.size();
+  lr_ip.ensure(M * n3);
+  lr_src.ensure(M);
+  w_cB.ensure(M * h3);
+  CK(cudaMemcpyAsync(lr_src.p, u.data(), M * sizeof(int), cudaMemcpyHostToDevice, st));
+  r2c_z(N, PreSignVol{partptr, lr_src.p, N}, w_cB.p, M * N * N);
+  xy_kxy(N, w_cB.p, M, -1);
+  with_n(N, [&](auto nn) {
+    constexpr int NN = decltype(nn)::value;
+    fft2d_t<NN>(OpFilterShared<NN>{w_cB.p, filter.p}, M, "local_refine_setup", 16.0);
+  });
+  c2r_z(N, w_cB.p, PostStoreSigned{lr_ip.p, N}, M * N * N);
+}
+
+void ettk_ctx::lr_run(long P, int iterations) {
+  for (int it = 0; it <= iterations; ++it) {
+    CK(cudaMemsetAsync(lr_acc.p, 0, P * LR_NACC * sizeof(double), st));
+    lr_eval(P);
+    k_lr_update<<<(unsigned)((P + 127) / 128), 128, 0, st>>>(lr_state.p, lr_acc.p, (int)P, (double)N, lr_C0, lr_C1,
+                                                              lr_radius(), 1e-3, lr_maps.p);
+    post_launch();
+  }
+}
+
+// Fast form: stages 1-3 as the plain form, then per pair one CCF evaluation (executeFourierNewHalf, the integer
+// half-voxel shift) of each of the `peaks` best candidates of the windowed queue and the best of the unwindowed
+// queue (no mirror evaluations), the best valid one refined by gradient ascent of the masked normalised
+// correlation (local_refine.cuh) in continuous rotation and shift.
+void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, int ncand, int iterations, int peaks) {
+  HostScope hs_all(this, "host_align_wall");
+  const int maxb = p.max_batch > 0 ? p.max_batch : 512;
+  std::vector<int> todo;
+  for (int i = 0; i < npairs; ++i)
+    if (D[(long)i * cols * ncand] == -1) todo.push_back(i);
+  for (size_t b0 = 0; b0 < todo.size(); b0 += maxb) {
+    const int P = (int)std::min<size_t>(maxb, todo.size() - b0);
+    std::vector<int> pr(P), pp(P);
+    for (int i = 0; i < P; ++i) {
+      pr[i] = pairs[2 * todo[b0 + i]];
+      pp[i] = pairs[2 * todo[b0 + i] + 1];
+      if (pr[i] < 0 || pr[i] >= R || pp[i] < 0 || pp[i] >= V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+    }
+    std::vector<PairPlan> plans;
+    std::vector<PQ> q1, q2;
+    {
+      HostScope hs_so3(this, "stage_so3");
+      so3_queues(P, pr, pp, plans, q1, q2);
+    }
+    std::vector<EvalReq> req;
+    std::vector<int> owner;
+    {
+      HostScope hs_c(this, "stage_coarse_ccf");
+      for (int i = 0; i < P; ++i)
+        for (int q = 0; q < 2; ++q) {
+          PQ &Q = q == 0 ? q1[i] : q2[i];
+          const int take = q == 0 ? peaks : 1;
+          for (int t = 0; t < take && !Q.empty() && Q.top().v[3] != FLT_MAX; ++t) {
+            const Cand c = Q.top();
+            Q.pop();
+            req.push_back({pr[i], pp[i], euler_candidate(c.v[0], c.v[1], c.v[2])});
+            owner.push_back(i);
+          }
+        }
+      std::vector<EvalRes> res;
+      eval_batch(req, res);
+      std::vector<int> best(P, -1);
+      for (size_t k = 0; k < req.size(); ++k) {
+        const int i = owner[k];
+        if (!transform_valid(p, res[k].t)) continue;
+        if (best[i] < 0 || res[k].dist < res[best[i]].dist) best[i] = (int)k;
+      }
+      std::vector<EvalReq> fb;
+      std::vector<int> fbi;
+      for (int i = 0; i < P; ++i)
+        if (best[i] < 0) {  // no valid candidate: the reference's fallback rotation (0, 0, 0) (execute 786-804)
+          fb.push_back({pr[i], pp[i], Mat4::eye()});
+          fbi.push_back(i);
+        }
+      std::vector<EvalRes> fres;
+      if (!fb.empty()) eval_batch(fb, fres);
+      std::vector<EvalReq> finals(P);
+      for (int i = 0; i < P; ++i) finals[i] = {pr[i], pp[i], best[i] >= 0 ? res[best[i]].t : Mat4::eye()};
+      for (size_t k = 0; k < fb.size(); ++k) finals[fbi[k]].t = fres[k].t;
+      req.swap(finals);
+    }
+    std::vector<LRState> sts(P);
+    {
+      HostScope hs_r(this, "stage_local_refine");
+      lr_filter_particles(pp);
+      lr_setup(req);
+      lr_run(P, iterations);
+      read_back(sts.data(), lr_state.p, P * sizeof(LRState));
+      check_status();
+    }
+    std::vector<EvalReq> fin(P);
+    for (int i = 0; i < P; ++i) fin[i] = {pr[i], pp[i], pose_from_index(partg[pp[i]], N, sts[i].base)};
+    std::vector<float> ovl;
+    if (cols > 18) ovl = wedge_overlaps(fin);
+    for (int i = 0; i < P; ++i) {
+      const int row = todo[b0 + i];
+      auto at = [&](int col, int k) -> float & { return D[((long)row * cols + col) * ncand + k]; };
+      for (int k = 1; k < ncand; ++k) at(0, k) = FLT_MAX;
+      int off = 1;
+      at(0, 0) = (float)(1.0 - sts[i].rho);
+      if (cols > 17) at(1, 0) = 1.0f, off = 2;
+      if (cols > 18) at(2, 0) = ovl[i], off = 3;
+      for (int m = 0; m < 16; ++m) at(m + off, 0) = (float)fin[i].t.e[m];
+    }
+  }
+}
+
+// The fast form's objective and gradient at T_i perturbed by theta_i, with zm built at T_i (checks only).
+void ettk_ctx::refined_objective(int npairs, const int *pairs, const double *poses, const double *theta, double *rho,
+                                 double *grad) {
+  std::vector<EvalReq> req(npairs);
+  for (int i = 0; i < npairs; ++i) {
+    req[i].ref = pairs[2 * i];
+    req[i].part = pairs[2 * i + 1];
+    if (req[i].ref < 0 || req[i].ref >= R || req[i].part < 0 || req[i].part >= V)
+      throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+    memcpy(req[i].t.e, poses + 16 * i, 16 * sizeof(double));
+  }
+  {
+    std::vector<int> parts(npairs);
+    for (int i = 0; i < npairs; ++i) parts[i] = req[i].part;
+    lr_filter_particles(parts);
+  }
+  lr_setup(req);
+  std::vector<LRState> sts(npairs);
+  read_back(sts.data(), lr_state.p, npairs * sizeof(LRState));
+  std::vector<float> maps(npairs * 12);
+  for (int i = 0; i < npairs; ++i) {
+    double m[12];
+    lr_perturb(sts[i].base, (double)N, theta + 6 * i, m);
+    for (int k = 0; k < 12; ++k) maps[i * 12 + k] = (float)m[k];
+  }
+  CK(cudaMemcpyAsync(lr_maps.p, maps.data(), npairs * 12 * sizeof(float), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(lr_acc.p, 0, npairs * LR_NACC * sizeof(double), st));
+  lr_eval(npairs);
+  std::vector<double> acc(npairs * LR_NACC);
+  read_back(acc.data(), lr_acc.p, acc.size() * sizeof(double));
+  for (int i = 0; i < npairs; ++i) {
+    double g[6];
+    rho[i] = lr_objective(acc.data() + (long)i * LR_NACC, lr_C0, lr_C1, sts[i].czm, sts[i].czz, g);
+    if (grad)
+      for (int k = 0; k < 6; ++k) grad[6 * i + k] = g[k];
   }
 }
 
@@ -2721,6 +3002,22 @@ int ettk_gpu_align_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, in
     return fail(c, ETTK_ERR_ARG, "invalid align arguments");
   if (c->R == 0 || c->V == 0) return fail(c, ETTK_ERR_STATE, "references and particles must be set first");
   return guarded(c, [&] { c->align(npairs, pairs, D, cols, ncand); });
+}
+
+int ettk_gpu_align_pairs_refined(ettk_ctx *c, int npairs, const int *pairs, float *D, int cols, int ncand,
+                                 int iterations, int peaks) {
+  if (!c || npairs < 0 || (npairs && (!pairs || !D)) || cols < 17 || ncand < 1 || iterations < 0 || peaks < 0 ||
+      iterations > 1000 || peaks > 64)
+    return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
+  return guarded(c, [&] { c->align_refined(npairs, pairs, D, cols, ncand, iterations, peaks ? peaks : 1); });
+}
+
+int ettk_gpu_refined_objective(ettk_ctx *c, int npairs, const int *pairs, const double *poses, const double *theta,
+                               double *rho, double *grad) {
+  if (!c || npairs <= 0 || !pairs || !poses || !theta || !rho) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
+  return guarded(c, [&] { c->refined_objective(npairs, pairs, poses, theta, rho, grad); });
 }
 
 int ettk_gpu_ccf(ettk_ctx *c, int r, int p, double *t, float *dist) {

@@ -266,6 +266,34 @@ class ProjectionRotationMetric3D:
                     "refine_objective")
         return (rho, g) if grad else rho
 
+    # -- fast form: coarse SO(3) hit + local refinement (no counterpart in the reference) -------
+    def getDistancesRefined(self, indexes, D=None, cols=17, ncand=1, iterations=12, peaks=1):
+        """As getDistances, through the fast form (ettk_gpu_align_pairs_refined): CCF of the `peaks` best
+        windowed candidates and the best unwindowed one, then `iterations` steps of continuous refinement;
+        column 0 is 1 - rho at the refined pose."""
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        n = idx.shape[0]
+        if D is None:
+            D = -np.ones((n, cols, ncand), np.float32)
+        assert D.dtype == np.float32 and D.flags.c_contiguous and D.shape[0] == n
+        self._check(self.L.ettk_gpu_align_pairs_refined(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1],
+                                                        D.shape[2], int(iterations), int(peaks)), "align_pairs_refined")
+        return D
+
+    def refined_objective(self, indexes, poses, theta, grad=True):
+        """The fast form's rho (and d rho / d(w, d)) with the reference filtered at poses (n x 4 x 4) and the
+        particle at those poses perturbed by theta (n x 6: rotation vector in radians, shift in voxels)."""
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        n = idx.shape[0]
+        T = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(n, 16))
+        th = np.ascontiguousarray(np.asarray(theta, np.float64).reshape(n, 6))
+        rho = np.zeros(n)
+        g = np.zeros((n, 6)) if grad else None
+        self._check(self.L.ettk_gpu_refined_objective(self._ctx, n, idx.ctypes.data, T.ctypes.data, th.ctypes.data,
+                                                      rho.ctypes.data, g.ctypes.data if grad else None),
+                    "refined_objective")
+        return (rho, g) if grad else rho
+
     # -- diagnostics ---------------------------------------------------------------------------
     def ccf(self, r, p, T):
         t = np.ascontiguousarray(np.asarray(T, np.float64).reshape(16)).copy()

@@ -213,6 +213,28 @@ int ettk_gpu_classify(ettk_ctx *ctx, int iterations, int *labels, float *refs_ou
 int ettk_gpu_refine_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
                           int iterations);
 
+/* Fast alignment form (no counterpart in the reference; it takes the place of getDistances with typeOfMetric 0,
+   whose Powell refinement, inc/em/nbfFourierImageMetric.h:1701-1809, and whose mirror and candidate CCF loop,
+   inc/em/nbfProjectionRotationMetric3D.h:678-901, it replaces): the same spherical projections, SO(3) correlations
+   (in the context's wigner_precision) and candidate queues as ettk_gpu_align_pairs, then per pair one CCF
+   (executeFourierNewHalf: integer half-voxel shift) of each of the `peaks` best candidates of the windowed queue
+   and of the best candidate of the unwindowed one, no mirror evaluations, and the best valid result refined in
+   continuous rotation and shift by `iterations` steps of gradient ascent of the masked normalised correlation
+   between the wedge- and band-limited reference (the CCF's filter times both wedges at the coarse pose) and the
+   particle (trilinear interpolation, analytic gradient). D has the layout of ettk_gpu_align_pairs; column 0 holds
+   1 - rho at the refined pose, the matrix the refined pose (continuous), scale 1 and the wedge overlap as there;
+   candidate slots past the first get FLT_MAX in column 0. Rows whose D[i][0][0] != -1 are skipped.
+   iterations 0 keeps the coarse pose (rho evaluated there); peaks 0 = 1. */
+int ettk_gpu_align_pairs_refined(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
+                                 int iterations, int peaks);
+
+/* The fast form's objective and gradient (for checks): for pair i, the reference filtered with the wedges at
+   pose T = poses[16 i..], and the particle at T perturbed by theta[6 i..] = (rotation vector w in radians about
+   the box centre, shift d in voxels) of the output grid: rho[i] and, when grad is non-null, grad[6 i..] =
+   d rho / d(w, d) at that perturbed pose. */
+int ettk_gpu_refined_objective(ettk_ctx *ctx, int npairs, const int *pairs, const double *poses, const double *theta,
+                               double *rho, double *grad);
+
 /* The refinement objective and its gradient (for checks): for pair i at pose T = poses[16 i..] perturbed by
    theta[6 i..] = (rotation vector w in radians about the box centre, shift d in voxels) of the output grid,
    rho[i] and, when grad is non-null, grad[6 i..] = d rho / d(w, d) at that perturbed pose. */

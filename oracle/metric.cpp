@@ -1047,6 +1047,170 @@ double oracle_refine_objective(const OracleParams *P, const OracleVolume *ref, c
   return (sgg > 0 && syy > 0) ? syg / sqrt(sgg * syy) : 0.0;
 }
 
+/* The fast form's local-refinement objective (no counterpart in the reference), restated in FP64 with its
+ * analytic gradient for the checks of the GPU's: zm = m1 * y1, y1 = K(I1) = C2R(R2C(I1 maskfft shift) fw) shift
+ * with fw = wedge1 * wedge2(t) * filter and the DC zeroed; the particle (a fixed image of edge N) band-passed in
+ * its own frame, C2R(R2C(I shift) filter) shift, and sampled as I by trilinear interpolation at
+ * the index map of t perturbed on the right by exp([w]x) about the box centre and the shift d (theta = w[3],
+ * d[3]), coordinates clamped to the volume; mu = sum m1 I / sum m1; rho = sum zm (I - mu) /
+ * sqrt(sum m1^2 (I - mu)^2 sum zm^2); grad = d rho / d(w, d) with dI/dd = G, dI/dw = (x - c) x G,
+ * G = M^T grad_p I (zero along a clamped axis). Returns rho; grad (6) may be NULL. */
+double oracle_refined_objective(const OracleParams *P, const OracleVolume *ref, const OracleVolume *part,
+                                const double *t16, const double *theta, double *grad) {
+  CCF ccf(*P, *ref, *part);
+  const int N = P->N, H = N / 2 + 1;
+  const long n3 = (long)N * N * N, h3 = (long)N * N * H;
+  M4 t;
+  memcpy(t.e, t16, sizeof(t.e));
+  std::vector<double> fw(h3);
+  {
+    std::vector<float> w2;
+    if (P->wedge_compensation) wedge_half(*part, N, &t, w2);
+    for (long i = 0; i < h3; ++i) fw[i] = P->wedge_compensation ? (double)(ccf.filter[i] * (w2[i] * ccf.wedge1[i]))
+                                                                 : (double)ccf.filter[i];
+    fw[((long)(N / 2) * N + N / 2) * H + (H - 1)] = 0;
+  }
+  auto shift = [&](long id) {
+    const int i = (int)(id / ((long)N * N)), j = (int)((id / N) % N), k = (int)(id % N);
+    return ((i + j + k) % 2) ? -1.0 : 1.0;
+  };
+  std::vector<double> zm(n3);
+  {
+    std::vector<cplx> F(h3);
+    for (long id = 0; id < n3; ++id) zm[id] = ccf.I1[id] * (double)ccf.maskfft[id] * shift(id);
+    rfft3d(zm.data(), F.data(), N, N, N);
+    for (long i = 0; i < h3; ++i) F[i] *= fw[i];
+    irfft3d(F.data(), zm.data(), N, N, N);
+    for (long id = 0; id < n3; ++id) zm[id] *= shift(id) * (double)ccf.mask[id];
+  }
+  /* index map of t (reslice_index), perturbed on the right */
+  M4 local = local_matrix(*part), fin;
+  m4_mul(local.e, t.e, fin.e);
+  if (m4_det(fin.e) == 0) fin = m4_identity();
+  double inM[16], outM[16], tmp[16], idx[16];
+  for (int i = 0; i < 16; ++i) inM[i] = outM[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  for (int i = 0; i < 3; ++i) {
+    inM[4 * i + 3] = (double)part->position[i];
+    outM[4 * i + 3] = -(double)(float)N / 2.0 - (i == 2 ? part->cut_offset : 0.0);
+  }
+  m4_mul(inM, fin.e, tmp);
+  m4_mul(tmp, outM, idx);
+  const double *w = theta, *d = theta + 3;
+  const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (th > 0) {
+    const double k[3] = {w[0] / th, w[1] / th, w[2] / th}, sn = sin(th), c1 = 1 - cos(th);
+    const double K[9] = {0, -k[2], k[1], k[2], 0, -k[0], -k[1], k[0], 0};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double k2 = 0;
+        for (int q = 0; q < 3; ++q) k2 += K[3 * i + q] * K[3 * q + j];
+        R[3 * i + j] += sn * K[3 * i + j] + c1 * k2;
+      }
+  }
+  const double c = 0.5 * N;
+  double M[9], o[3], Mp[9], op[3], tv[3];
+  for (int i = 0; i < 3; ++i) {
+    o[i] = idx[4 * i + 3];
+    for (int col = 0; col < 3; ++col) M[3 * i + col] = idx[4 * i + col];
+  }
+  for (int i = 0; i < 3; ++i) tv[i] = c - (R[3 * i] + R[3 * i + 1] + R[3 * i + 2]) * c + d[i];
+  for (int i = 0; i < 3; ++i) {
+    op[i] = o[i] + M[3 * i] * tv[0] + M[3 * i + 1] * tv[1] + M[3 * i + 2] * tv[2];
+    for (int col = 0; col < 3; ++col) Mp[3 * i + col] = M[3 * i] * R[col] + M[3 * i + 1] * R[3 + col] + M[3 * i + 2] * R[6 + col];
+  }
+  const int dims[3] = {part->dims[0], part->dims[1], part->dims[2]};
+  const long sy = dims[0], sz = (long)dims[0] * dims[1];
+  /* the particle band-passed in its own frame (its N^3 fixed image, [z][y][x]) by the metric's filter */
+  std::vector<double> ip((long)dims[0] * dims[1] * dims[2]);
+  {
+    std::vector<cplx> F(h3);
+    for (long id = 0; id < n3; ++id) ip[id] = (double)part->data[id] * shift(id);
+    rfft3d(ip.data(), F.data(), N, N, N);
+    for (long i = 0; i < h3; ++i) F[i] *= (double)ccf.filter[i];
+    irfft3d(F.data(), ip.data(), N, N, N);
+    for (long id = 0; id < n3; ++id) ip[id] *= shift(id);
+  }
+  double S[4] = {0, 0, 0, 0}, T[4][6] = {{0}}, C0 = 0, C1 = 0, czm = 0, czz = 0;
+  for (long id = 0; id < n3; ++id) {
+    const double m = ccf.mask[id];
+    C0 += m;
+    C1 += m * m;
+    czm += zm[id];
+    czz += zm[id] * zm[id];
+  }
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b)
+      for (int cz = 0; cz < N; ++cz) {
+        const long id = ((long)a * N + b) * N + cz;
+        const double m = ccf.mask[id];
+        if (m == 0) continue;
+        double pp[3], q[3], f[3], gr[3];
+        int i0[3];
+        bool in[3];
+        for (int i = 0; i < 3; ++i) {
+          pp[i] = op[i] + a * Mp[3 * i] + b * Mp[3 * i + 1] + cz * Mp[3 * i + 2];
+          const double hi = dims[i] - 1;
+          q[i] = std::min(std::max(pp[i], 0.0), hi);
+          in[i] = pp[i] > 0 && pp[i] < hi;
+          i0[i] = std::min((int)q[i], dims[i] - 2);
+          f[i] = q[i] - i0[i];
+        }
+        const double *base = ip.data() + i0[0] + i0[1] * sy + i0[2] * sz;
+        double v[2][2][2];
+        for (int z = 0; z < 2; ++z)
+          for (int y = 0; y < 2; ++y)
+            for (int x = 0; x < 2; ++x) v[z][y][x] = base[x + y * sy + z * sz];
+        double I = 0;
+        gr[0] = gr[1] = gr[2] = 0;
+        for (int z = 0; z < 2; ++z)
+          for (int y = 0; y < 2; ++y)
+            for (int x = 0; x < 2; ++x) {
+              const double wx = x ? f[0] : 1 - f[0], wy = y ? f[1] : 1 - f[1], wz = z ? f[2] : 1 - f[2];
+              const double sx = x ? 1 : -1, sy_ = y ? 1 : -1, sz_ = z ? 1 : -1;
+              I += wx * wy * wz * v[z][y][x];
+              gr[0] += sx * wy * wz * v[z][y][x];
+              gr[1] += wx * sy_ * wz * v[z][y][x];
+              gr[2] += wx * wy * sz_ * v[z][y][x];
+            }
+        for (int i = 0; i < 3; ++i)
+          if (!in[i]) gr[i] = 0;
+        double G[3];
+        for (int col = 0; col < 3; ++col) G[col] = Mp[col] * gr[0] + Mp[3 + col] * gr[1] + Mp[6 + col] * gr[2];
+        const double r[3] = {a - c, b - c, cz - c};
+        const double Dk[6] = {r[1] * G[2] - r[2] * G[1], r[2] * G[0] - r[0] * G[2], r[0] * G[1] - r[1] * G[0],
+                              G[0], G[1], G[2]};
+        const double z = zm[id];
+        S[0] += m * I;
+        S[1] += m * m * I;
+        S[2] += m * m * I * I;
+        S[3] += z * I;
+        for (int k = 0; k < 6; ++k) {
+          T[0][k] += m * Dk[k];
+          T[1][k] += m * m * Dk[k];
+          T[2][k] += m * m * I * Dk[k];
+          T[3][k] += z * Dk[k];
+        }
+      }
+  const double mu = S[0] / C0;
+  const double num = S[3] - mu * czm;
+  const double den2 = S[2] - 2.0 * mu * S[1] + mu * mu * C1;
+  if (!(den2 > 0) || !(czz > 0)) {
+    if (grad)
+      for (int k = 0; k < 6; ++k) grad[k] = 0;
+    return 0;
+  }
+  const double den = sqrt(den2 * czz), rho = num / den;
+  if (grad)
+    for (int k = 0; k < 6; ++k) {
+      const double dmu = T[0][k] / C0;
+      const double dnum = T[3][k] - dmu * czm;
+      const double dden2 = 2.0 * T[2][k] - 2.0 * dmu * S[1] - 2.0 * mu * T[1][k] + 2.0 * mu * dmu * C1;
+      grad[k] = dnum / den - 0.5 * rho * dden2 / den2;
+    }
+  return rho;
+}
+
 /* nbfImageFilter::symmetrize (inc/em/nbfImageFilter.h:527-554): the mean over i < fold of getImage of the
  * volume as a fixed image (position dims/2, identity matrix, no normal) under RotateZ(i * 360 / fold), each a
  * tricubic reslice with the mean of its valid voxels removed and invalid voxels zero (inc/em/nbfWedgedAverageImage3D.h

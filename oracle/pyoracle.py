@@ -86,6 +86,8 @@ def lib():
         L.oracle_ccf.restype = ctypes.c_float
         L.oracle_refine_objective.argtypes = [P, V, V, dp, dp]
         L.oracle_refine_objective.restype = ctypes.c_double
+        L.oracle_refined_objective.argtypes = [P, V, V, dp, dp, ctypes.c_void_p]
+        L.oracle_refined_objective.restype = ctypes.c_double
         L.oracle_average.argtypes = [P, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp]
         L.oracle_symmetrize.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p]
         L.oracle_variance.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5
@@ -169,6 +171,19 @@ def refine_objective(params, ref, ref_meta, part, part_meta, T, theta):
     t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16))
     th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(6))
     return float(lib().oracle_refine_objective(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t, th))
+
+
+def refined_objective(params, ref, ref_meta, part, part_meta, T, theta):
+    """FP64 objective of the fast form's local refinement (the reference filtered with the wedges at pose T, the
+    particle at T perturbed by theta) and its analytic gradient: (rho, grad[6])."""
+    P = make_params(params)
+    r = make_volume(ref, ref_meta)
+    q = make_volume(part, part_meta)
+    t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16))
+    th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(6))
+    g = np.zeros(6)
+    rho = lib().oracle_refined_objective(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t, th, g.ctypes.data)
+    return float(rho), g
 
 
 def get_image(params, vol, meta, T=None):
