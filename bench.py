@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--fast-iterations", type=int, default=12)
     ap.add_argument("--fast-peaks", type=int, default=1)
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
+    ap.add_argument("--fast-only", action="store_true",
+                    help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")
     ap.add_argument("--repr-study", action="store_true",
                     help="unsupervised-classification step on the 64^3 workload: low-dimensional representations "
                          "of --study-pairs particles and the distance matrix between them (one JSON line)")
@@ -302,7 +304,8 @@ def fast_study(a):
     ref = WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})
     pairs = [(0, i) for i in range(P)]
     out = {}
-    for form, prec in (("plain", 0), ("fast", a.fast_precision)):
+    forms = (("fast", a.fast_precision),) if a.fast_only else (("plain", 0), ("fast", a.fast_precision))
+    for form, prec in forms:
         m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec))
         m.set_references([ref])
         m.set_particles(vols)
@@ -311,7 +314,7 @@ def fast_study(a):
             if form == "plain":
                 return m.getDistances(sub)
             return m.getDistancesRefined(sub, iterations=a.fast_iterations, peaks=a.fast_peaks)
-        run(pairs[:8])
+        run(pairs if a.fast_only else pairs[:8])
         m.set_particles(vols)  # drop the cached spherical projections of the warm-up pairs
         torch.cuda.synchronize()
         m.profile(True)
@@ -323,6 +326,14 @@ def fast_study(a):
         m.profile(False)
         m.close()
         out[form] = (D, P / (t1 - t0), prof)
+    if a.fast_only:
+        rf, sf = pose_errors(out["fast"][0], ds.truth)
+        line = {"fast_study": {"fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, rf < 20.0),
+                                            families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()})},
+                "config": {"workload": WORKLOAD, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
+                           "fast_wigner_precision": a.fast_precision}}
+        print(json.dumps(line), flush=True)
+        return
     rp, sp = pose_errors(out["plain"][0], ds.truth)
     rf, sf = pose_errors(out["fast"][0], ds.truth)
     hit = rp < 20.0

@@ -217,83 +217,100 @@ __global__ void k_build_signals(const SigDesc *__restrict__ sd, const int *__res
   }
 }
 
-// softScaled rescale + branch combination + beta restriction (execute 526-602):
-// out[pair] = combination of the pair's correlation jobs; slot 4 (unwindowed) restricted in place.
+// The SO(3) correlation jobs of one pair and how execute combines them (526-602).
 struct PairPlan {
   int branch;   // 1 both windows, 2 only window 1, 3 only window 2, 4 none
   int job[5];   // correlation job per slot (-1 unused)
   int scaled[5];
   int sjob[5];  // scaled-job index for weights (-1 if unscaled)
 };
-__global__ void k_combine(const PairPlan *__restrict__ plans, float *__restrict__ C, const unsigned long long *__restrict__ mm,
-                          const double *__restrict__ w, int n, int rstart, float *__restrict__ q1, float *__restrict__ q2) {
-  const PairPlan P = plans[blockIdx.y];
-  const long n3 = (long)n * n * n;
-  float lo[5], sc[5], wl[5];
-  for (int s = 0; s < 5; ++s) {
-    lo[s] = 0.f;
-    sc[s] = 1.f;
-    wl[s] = 0.f;
-    if (P.job[s] >= 0 && P.scaled[s]) {
-      float mn = ordered_to_float(~(uint32_t)(mm[2 * P.job[s]] >> 32));
-      float mx = ordered_to_float((uint32_t)(mm[2 * P.job[s] + 1] >> 32));
-      double wmin = w[2 * P.sjob[s]], wmax = w[2 * P.sjob[s] + 1];
-      lo[s] = mn;
-      sc[s] = (float)((wmax - wmin) / ((double)mx - (double)mn));
-      wl[s] = (float)wmin;
+// Branch combination and local maxima in one pass (execute 526-646): each CTA owns an 8^3 tile of one pair's
+// (2B)^3 grid, forms q1 (and q2 where the pair has the unwindowed correlation) on the tile and its one-cell halo in shared memory, then applies
+// the 3x3x3 ">=" test with the -FLT_MAX border on the interior (localMaxima3D3x3, inc/em/nbfProjectionRotationMetric3D.h:
+// 67-79; BordStrategyConst, inc/bs/nbfBordStrategyConst.h:67-83) and appends the maxima (cell index, value) to the
+// pair's lists (order fixed on the host by sorting on the cell index); q1 and q2 are never written to memory.
+// Per cell: the softScaled rescale of each scaled job to [wmin, wmax] (1297-1319), the branch formula of execute
+// (526-584) and -FLT_MAX on the beta rows from rstart (602). Cells inside the -FLT_MAX plateau of a restricted
+// rotation search are maxima of value -FLT_MAX for the reference too; they enter its queues as FLT_MAX sentinels,
+// which sort after every real candidate, lose every duplicate comparison and stop the candidate loop only once no
+// real candidate is left (697-701), so leaving them out changes no result.
+constexpr int CP_T = 8, CP_H = CP_T + 2;
+__global__ void __launch_bounds__(256) k_combine_peaks(const PairPlan *__restrict__ plans, const float *__restrict__ C,
+                                                       const unsigned long long *__restrict__ mm,
+                                                       const double *__restrict__ w, int n, int rstart, int P, int cap,
+                                                       int *counts, int2 *lists) {
+  __shared__ float qs[2][CP_H * CP_H * CP_H];
+  __shared__ float lo[5], sc[5], wl[5];
+  __shared__ PairPlan Psh;
+  const int pair = blockIdx.y;
+  if (threadIdx.x == 0) {
+    const PairPlan Pl = plans[pair];
+    Psh = Pl;
+    for (int s = 0; s < 5; ++s) {
+      lo[s] = 0.f;
+      sc[s] = 1.f;
+      wl[s] = 0.f;
+      if (Pl.job[s] >= 0 && Pl.scaled[s]) {
+        const float mn = ordered_to_float(~(uint32_t)(mm[2 * Pl.job[s]] >> 32));
+        const float mx = ordered_to_float((uint32_t)(mm[2 * Pl.job[s] + 1] >> 32));
+        const double wmin = w[2 * Pl.sjob[s]], wmax = w[2 * Pl.sjob[s] + 1];
+        lo[s] = mn;
+        sc[s] = (float)((wmax - wmin) / ((double)mx - (double)mn));
+        wl[s] = (float)wmin;
+      }
     }
   }
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
-    int b = (int)((id / n) % n);
-    float c[5];
-    for (int s = 0; s < 5; ++s) c[s] = P.job[s] >= 0 ? (C[(long)P.job[s] * n3 + id] - lo[s]) * sc[s] + wl[s] : 0.f;
-    float r;
-    if (P.branch == 1) {
-      float c1 = sqrtf(c[0]) * sqrtf(c[1]);
-      c1 = 2.0f * (1.0f - c[2] / c1);
-      r = -c1 / c[3];
-    } else if (P.branch == 2 || P.branch == 3) {
-      r = c[1] / sqrtf(c[0]);
-    } else {
-      r = c[0];
+  __syncthreads();
+  const PairPlan &Pl = Psh;
+  const bool two = Pl.job[4] >= 0;
+  const int tpa = n / CP_T;
+  const int ta = blockIdx.x / (tpa * tpa), tb = (blockIdx.x / tpa) % tpa, tg = blockIdx.x % tpa;
+  const int a0 = ta * CP_T - 1, b0 = tb * CP_T - 1, g0 = tg * CP_T - 1;
+  const int n3 = n * n * n;
+  for (int v = threadIdx.x; v < CP_H * CP_H * CP_H; v += blockDim.x) {
+    const int la = v / (CP_H * CP_H), lb = (v / CP_H) % CP_H, lg = v % CP_H;
+    const int aa = a0 + la, bb = b0 + lb, g = g0 + lg;
+    float r1 = -FLT_MAX, r2 = -FLT_MAX;
+    if (aa >= 0 && bb >= 0 && g >= 0 && aa < n && bb < n && g < n && bb < rstart) {
+      const int id = (aa * n + bb) * n + g;
+      float c[5];
+#pragma unroll
+      for (int s = 0; s < 5; ++s) c[s] = Pl.job[s] >= 0 ? (C[(long)Pl.job[s] * n3 + id] - lo[s]) * sc[s] + wl[s] : 0.f;
+      if (Pl.branch == 1) {
+        float c1 = sqrtf(c[0]) * sqrtf(c[1]);
+        c1 = 2.0f * (1.0f - c[2] / c1);
+        r1 = -c1 / c[3];
+      } else if (Pl.branch == 2 || Pl.branch == 3) {
+        r1 = c[1] / sqrtf(c[0]);
+      } else {
+        r1 = c[0];
+      }
+      r2 = c[4];
     }
-    if (b >= rstart) r = -FLT_MAX;
-    q1[(long)blockIdx.y * n3 + id] = r;
-    if (P.job[4] >= 0) q2[(long)blockIdx.y * n3 + id] = (b >= rstart) ? -FLT_MAX : c[4];
+    qs[0][v] = r1;
+    qs[1][v] = r2;
   }
-}
-
-// 3x3x3 ">=" local maxima with a -FLT_MAX border (localMaxima3D3x3, inc/em/nbfProjectionRotationMetric3D.h:67-79,
-// BordStrategyConst inc/bs/nbfBordStrategyConst.h:67-83); entries with |value| > 0 appended to the
-// item's list (order fixed on the host by sorting on the cell index). Cells inside the -FLT_MAX plateau of a
-// restricted rotation search (execute 602) are maxima of value -FLT_MAX for the reference too; they enter its
-// queues as FLT_MAX sentinels, which sort after every real candidate, lose every duplicate comparison and stop
-// the candidate loop only once no real candidate is left (697-701), so leaving them out changes no result.
-__global__ void k_local_max(const float *__restrict__ C, int n, const int *__restrict__ active, int cap, int *counts,
-                            int2 *lists) {
-  const long n3 = (long)n * n * n;
-  const int item = blockIdx.y;
-  if (!active[item]) return;
-  const float *c = C + (long)item * n3;
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n3; id += (long)gridDim.x * blockDim.x) {
-    int a = (int)(id / ((long)n * n)), b = (int)((id / n) % n), g = (int)(id % n);
-    float v = c[id];
-    bool ismax = true;
-    for (int da = -1; da <= 1 && ismax; ++da)
-      for (int db = -1; db <= 1 && ismax; ++db)
-        for (int dg = -1; dg <= 1; ++dg) {
-          if (!da && !db && !dg) continue;
-          int aa = a + da, bb = b + db, gg = g + dg;
-          float nb = (aa < 0 || bb < 0 || gg < 0 || aa >= n || bb >= n || gg >= n) ? -FLT_MAX
-                                                                                      : c[((long)aa * n + bb) * n + gg];
-          if (!(v >= nb)) {
-            ismax = false;
-            break;
-          }
-        }
-    if (ismax && fabsf(v) > 0.f && v != -FLT_MAX) {
-      int slot = atomicAdd(&counts[item], 1);
-      if (slot < cap) lists[(long)item * cap + slot] = make_int2((int)id, __float_as_int(v));
+  __syncthreads();
+  for (int q = 0; q < (two ? 2 : 1); ++q) {
+    const float *Q = qs[q];
+    for (int v = threadIdx.x; v < CP_T * CP_T * CP_T; v += blockDim.x) {
+      const int la = v / (CP_T * CP_T) + 1, lb = (v / CP_T) % CP_T + 1, lg = v % CP_T + 1;
+      const int c0 = (la * CP_H + lb) * CP_H + lg;
+      const float val = Q[c0];
+      bool ismax = fabsf(val) > 0.f && val != -FLT_MAX;
+      for (int da = -1; da <= 1 && ismax; ++da)
+        for (int db = -1; db <= 1 && ismax; ++db)
+          for (int dg = -1; dg <= 1; ++dg)
+            if ((da | db | dg) && !(val >= Q[c0 + (da * CP_H + db) * CP_H + dg])) {
+              ismax = false;
+              break;
+            }
+      if (ismax) {
+        const int item = q * P + pair;
+        const int slot = atomicAdd(&counts[item], 1);
+        const int id = ((a0 + la) * n + (b0 + lb)) * n + (g0 + lg);
+        if (slot < cap) lists[(long)item * cap + slot] = make_int2(id, __float_as_int(val));
+      }
     }
   }
 }
@@ -407,7 +424,7 @@ struct ettk_ctx {
   std::vector<VolumeGeom> partg;
   std::vector<int> useW2, pp2_ready;
   // work buffers
-  DevBuf<float> w_r, w_v, w_fw, w_tmp, w_C, w_q1, w_q2, w_sig, w_norm, w_norm2, sp_v, sp_M, sp_padc;
+  DevBuf<float> w_r, w_v, w_fw, w_tmp, w_C, w_sig, w_norm, w_norm2, sp_v, sp_M, sp_padc;
   DevBuf<float2> w_cA, w_cB, w_cC, w_p1, w_p2, w_coef, w_S, sp_F;
   DevBuf<double> w_acc, w_w, sp_acc;
   DevBuf<unsigned long long> w_peak, w_mm;
@@ -448,7 +465,7 @@ struct ettk_ctx {
     }
   }
   DevBuf<WedgeVecs> w_wv;
-  DevBuf<int> w_idx, w_idx2, w_cnt, w_active, w_pair_ref, w_pair_pp2, w_pair_part, w_i1;
+  DevBuf<int> w_idx, w_idx2, w_cnt, w_pair_ref, w_pair_pp2, w_pair_part, w_i1;
   DevBuf<int2> w_lists;
   DevBuf<EvalOut> w_out;
   DevBuf<SigDesc> w_sd;
@@ -763,7 +780,8 @@ struct ettk_ctx {
 
   // ---------------------------------------------------------------- setup
   void init_tables();
-  void spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out /*device, items*nn*/);
+  // |F| spherical projections of the items into Pp_out[out_index[i] * nn] (device; out_index null: [i * nn])
+  void spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out, const int *out_index = nullptr);
   void eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> &res);
   // executeFourierNewHalf for any number of requests, in device chunks of at most 4096 evaluations at 64^3
   // (scaled by 64^3 / N^3, 256 to 8192; about 6.4 MB of scratch per 64^3 evaluation): fewer chunks mean
@@ -1408,6 +1426,7 @@ void ettk_ctx::init_tables() {
   status.ensure(1);
   CK(cudaMemset(status.p, 0, sizeof(int)));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_so3_weights<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)so3_weights_smem<64>()));
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CK(cudaFuncSetAttribute(k_reslice_brick<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
@@ -1611,7 +1630,7 @@ void ettk_ctx::init_tables() {
 }
 
 // cartesianToSpherical for a batch of volumes (inc/em/nbfProjectionRotationMetric3D.h:264-413)
-void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out) {
+void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out, const int *out_index) {
   long P = (long)items.size();
   if (P == 0) return;
   int N2 = 2 * N;
@@ -1650,7 +1669,7 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
 #define SS_CASE(NN)                                                                                              \
   case NN:                                                                                                       \
     k_sphere_sample<NN><<<dim3(nblocks<int>(nn, 128), P), 128, 0, st>>>(sp_M.p, dirs.p, (int)nn, bandL, bandU,   \
-                                                                        sp_padc.p, Pp_out);                     \
+                                                                        sp_padc.p, Pp_out, out_index);          \
     break;
     SS_CASE(16)
     SS_CASE(32)
@@ -1992,12 +2011,10 @@ void ettk_ctx::so3_queues(int P, const std::vector<int> &pr, const std::vector<i
         set_map(it, m12);
         items.push_back(it);
       }
-      w_sig.ensure(items.size() * nn);
-      spherical_projection(items, w_sig.p);
-      for (size_t c = c0; c < c1; ++c) {
-        CK(cudaMemcpyAsync(Pp2.p + (long)ids[c] * nn, w_sig.p + (c - c0) * nn, nn * 4, cudaMemcpyDeviceToDevice, st));
-        pp2_ready[ids[c]] = 1;
-      }
+      w_idx2.ensure(c1 - c0);
+      CK(cudaMemcpyAsync(w_idx2.p, ids.data() + c0, (c1 - c0) * sizeof(int), cudaMemcpyHostToDevice, st));
+      spherical_projection(items, Pp2.p, w_idx2.p);  // straight into the particles' rows of Pp2
+      for (size_t c = c0; c < c1; ++c) pp2_ready[ids[c]] = 1;
     }
   }
   // 2. SO(3) plans: signals, correlation jobs, scaled jobs
@@ -2059,8 +2076,6 @@ void ettk_ctx::so3_queues(int P, const std::vector<int> &pr, const std::vector<i
   w_C.ensure(NJ * nso3);
   w_mm.ensure(NJ * 2);
   w_w.ensure(std::max(1L, NSJ) * 2);
-  w_q1.ensure((long)P * nso3);
-  w_q2.ensure((long)P * nso3);
   CK(cudaMemcpyAsync(w_sd.p, sd.data(), NS * sizeof(SigDesc), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(w_jobs.p, jobs.data(), NJ * sizeof(SynthJob), cudaMemcpyHostToDevice, st));
   if (NSJ) CK(cudaMemcpyAsync(w_sjobs.p, sjobs.data(), NSJ * sizeof(ScaledJob), cudaMemcpyHostToDevice, st));
@@ -2100,7 +2115,7 @@ case BB: {                                                                      
   }                                                                                                                   \
   if (NSJ) {                                                                                                          \
     Scope sc_w(this, "so3_weights", 4.0 * NSJ * nn);                                                                  \
-    k_so3_weights<BB><<<dim3(NSJ, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p,             \
+    k_so3_weights<BB><<<dim3(NSJ, 2), 256, so3_weights_smem<BB>(), st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p,             \
                                                     plm.p, sinth.p, w_w.p);                                           \
     post_launch();                                                                                                    \
   }                                                                                                                   \
@@ -2113,32 +2128,17 @@ case BB: {                                                                      
     default:
       throw CudaError(ETTK_ERR_ARG, "unsupported bandwidth");
   }
-  {
-  Scope sc_c(this, "combine", 4.0 * (NJ + 2.0 * P) * nso3);
-  k_combine<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_plans.p, w_C.p, w_mm.p, w_w.p, n, rstart,
-                                                                      w_q1.p, w_q2.p);
-  post_launch();
-  }
-  // 3. local maxima -> host queues
+  // 3. branch combination, beta restriction and local maxima -> host queues
   const int cap = 8192;
   w_cnt.ensure(2 * P);
-  w_active.ensure(2 * P);
   w_lists.ensure((long)2 * P * cap);
-  std::vector<int> act(2 * P);
-  for (int i = 0; i < P; ++i) {
-    act[i] = 1;
-    act[P + i] = plans[i].job[4] >= 0;
-  }
-  CK(cudaMemcpyAsync(w_active.p, act.data(), 2 * P * 4, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(w_cnt.p, 0, 2 * P * 4, st));
-  // q1 and q2 buffers are contiguous when allocated back to back; launch separately
   {
-  Scope sc_lm(this, "local_max", 8.0 * P * nso3);
-  k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q1.p, n, w_active.p, cap, w_cnt.p, w_lists.p);
-  post_launch();
-  k_local_max<<<dim3(nblocks<int>(nso3, 256, 256), P), 256, 0, st>>>(w_q2.p, n, w_active.p + P, cap, w_cnt.p + P,
-                                                                     w_lists.p + (long)P * cap);
-  post_launch();
+    Scope sc_c(this, "combine_peaks", 4.0 * NJ * nso3);
+    const int tiles = (n / CP_T) * (n / CP_T) * (n / CP_T);
+    k_combine_peaks<<<dim3(tiles, P), 256, 0, st>>>(w_plans.p, w_C.p, w_mm.p, w_w.p, n, rstart, P, cap, w_cnt.p,
+                                                   w_lists.p);
+    post_launch();
   }
   std::vector<int> cnt(2 * P);
   read_back(cnt.data(), w_cnt.p, 2 * P * 4);
@@ -2639,7 +2639,7 @@ void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C)
     k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), 1), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);         \
     post_launch();                                                                                        \
     if (scaled) {                                                                                         \
-      k_so3_weights<BB><<<dim3(1, 2), 256, 0, st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p, \
+      k_so3_weights<BB><<<dim3(1, 2), 256, so3_weights_smem<BB>(), st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p, \
                                                     plm.p, sinth.p, w_w.p);                               \
       post_launch();                                                                                      \
     }                                                                                                     \
@@ -2827,7 +2827,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
                          &c->W1half, &c->Pp1, &c->W1sph, &c->partvol, &c->W2sph, &c->Pp2, &c->w_r, &c->w_v,
-                         &c->w_fw, &c->w_tmp, &c->w_C, &c->w_q1, &c->w_q2, &c->w_sig, &c->w_norm,
+                         &c->w_fw, &c->w_tmp, &c->w_C, &c->w_sig, &c->w_norm,
                          &c->w_norm2, &c->sp_v, &c->sp_M, &c->sp_padc};
   for (auto b : fb) b->release();
   DevBuf<float2> *cb[] = {&c->Fm1, &c->FI1, &c->w_cA, &c->w_cB, &c->w_cC, &c->w_p1, &c->w_p2, &c->w_coef, &c->w_S, &c->sp_F};
@@ -2854,7 +2854,6 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_idx.release();
   c->w_idx2.release();
   c->w_cnt.release();
-  c->w_active.release();
   c->w_pair_ref.release();
   c->w_pair_pp2.release();
   c->w_pair_part.release();

@@ -1124,7 +1124,7 @@ static __global__ void k_magnitude(const float2 *__restrict__ F, float *__restri
 template <int N>
 __global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs,
                                                        int n_dirs, int bandL, int bandU, const float *__restrict__ padc,
-                                                       float *__restrict__ Pp) {
+                                                       float *__restrict__ Pp, const int *__restrict__ out_index) {
   constexpr int N2 = 2 * N, H = N + 1, MSK = N2 - 1;
   const int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= n_dirs) return;
@@ -1180,7 +1180,7 @@ __global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__
     }
     acc += v;
   }
-  Pp[(long)e * n_dirs + d] = acc;
+  Pp[(long)(out_index ? out_index[e] : e) * n_dirs + d] = acc;
 }
 
 // Corner value of the windowed image (the pad constant).
@@ -1296,12 +1296,25 @@ static __global__ void k_so3_real(const float2 *__restrict__ S, float *__restric
       bmin = kn > bmin ? kn : bmin;
     }
   }
-  if (mm) {
+  if (mm) {  // one pair of atomics per block
+    __shared__ unsigned long long red[2][32];
     bmax = warp_max_u64(bmax);
     bmin = warp_max_u64(bmin);
-    if ((threadIdx.x & 31) == 0) {
-      atomicMax(&mm[2 * job + 0], bmin);
-      atomicMax(&mm[2 * job + 1], bmax);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+      red[0][wid] = bmin;
+      red[1][wid] = bmax;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      bmin = lane < nw ? red[0][lane] : 0ull;
+      bmax = lane < nw ? red[1][lane] : 0ull;
+      bmin = warp_max_u64(bmin);
+      bmax = warp_max_u64(bmax);
+      if (lane == 0) {
+        atomicMax(&mm[2 * job + 0], bmin);
+        atomicMax(&mm[2 * job + 1], bmax);
+      }
     }
   }
 }
@@ -1316,56 +1329,82 @@ struct ScaledJob {
   int job;    // correlation job (for the min/max cells)
 };
 template <int B>
-static __global__ void k_so3_weights(const ScaledJob *__restrict__ sj, const unsigned long long *__restrict__ mm,
-                              const float2 *__restrict__ coef, const float *__restrict__ sig,
-                              const float *__restrict__ dtab, const int *__restrict__ doff, const float *__restrict__ plm,
-                              const float *__restrict__ sinth, double *w) {
+constexpr size_t so3_weights_smem() { return (size_t)3 * B * B * sizeof(float2); }
+template <int B>
+static __global__ void __launch_bounds__(256) k_so3_weights(const ScaledJob *__restrict__ sj,
+                                                            const unsigned long long *__restrict__ mm,
+                                                            const float2 *__restrict__ coef,
+                                                            const float *__restrict__ sig,
+                                                            const float *__restrict__ dtab, const int *__restrict__ doff,
+                                                            const float *__restrict__ plm,
+                                                            const float *__restrict__ sinth, double *w) {
   constexpr int n = 2 * B;
-  __shared__ float2 g[B * B];
+  extern __shared__ float2 wsm2[];   // so3_weights_smem<B>() bytes
+  float2 *g = wsm2;                  // rotated coefficients g(l, m), m >= 0: [l][m]
+  float2 *Hs = wsm2 + B * B;         // H(j, m) = sum_l g(l, m) P~_l^m(theta_j): [j][m]
+  __shared__ float2 ea[B], eg[2 * B - 1], ep[n];
   __shared__ double sh[32];
   const ScaledJob J = sj[blockIdx.x];
   const int which = blockIdx.y;
-  unsigned long long key = mm[2 * J.job + which];
-  uint32_t pos = 0xffffffffu - (uint32_t)(key & 0xffffffffu);
-  int a = pos / (n * n), b = (pos / n) % n, gg = pos % n;
-  float alpha = (float)(a / (double)B * 3.141592653589793), gamma = (float)(gg / (double)B * 3.141592653589793);
+  const unsigned long long key = mm[2 * J.job + which];
+  const uint32_t pos = 0xffffffffu - (uint32_t)(key & 0xffffffffu);
+  const int a = pos / (n * n), b = (pos / n) % n, gg = pos % n;
+  const float alpha = (float)(a / (double)B * 3.141592653589793), gamma = (float)(gg / (double)B * 3.141592653589793);
+  // phase tables: e^{-i m alpha} (m >= 0), e^{-i m' gamma} (|m'| < B), e^{2 pi i t / n}
+  for (int t = threadIdx.x; t < 2 * B - 1; t += blockDim.x) {
+    float s1, c1;
+    sincosf(-((t - (B - 1)) * gamma), &s1, &c1);
+    eg[t] = make_float2(c1, s1);
+    if (t < B) {
+      sincosf(-(t * alpha), &s1, &c1);
+      ea[t] = make_float2(c1, s1);
+    }
+  }
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    float s1, c1;
+    sincospif(2.0f * t / n, &s1, &c1);
+    ep[t] = make_float2(c1, s1);
+  }
+  __syncthreads();
   const float2 *h = coef + (long)J.h * B * B;
   for (int idx = threadIdx.x; idx < B * B; idx += blockDim.x) {
-    int l = idx / B, m = idx - l * B;
+    const int l = idx / B, m = idx - l * B;
     float2 acc = make_float2(0.f, 0.f);
     if (m <= l) {
-      float nl = rsqrtf((2.0f * l + 1.0f) * 0.5f);
+      const float nl = rsqrtf((2.0f * l + 1.0f) * 0.5f);
       for (int mp = -l; mp <= l; ++mp) {
-        int cell = (m + B - 1) * (2 * B - 1) + (mp + B - 1);
-        int l0 = max(abs(m), abs(mp));
-        float dv = dtab[doff[cell] + (l - l0) * n + b] * nl;
-        float s1, c1;
-        sincosf(-(m * alpha + mp * gamma), &s1, &c1);
-        acc = cadd(acc, cscale(cmul(make_float2(c1, s1), coef_at(h, B, l, mp)), dv));
+        const int cell = (m + B - 1) * (2 * B - 1) + (mp + B - 1);
+        const int l0 = max(abs(m), abs(mp));
+        const float dv = dtab[doff[cell] + (l - l0) * n + b] * nl;
+        acc = cadd(acc, cscale(cmul(eg[mp + B - 1], coef_at(h, B, l, mp)), dv));
       }
+      acc = cmul(ea[m], acc);
     }
     g[idx] = acc;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) {
+    const int j = idx / B, m = idx - j * B;
+    float2 hm = make_float2(0.f, 0.f);
+    for (int l = m; l < B; ++l) hm = cadd(hm, cscale(g[l * B + m], plm[((long)m * B + l) * n + j]));
+    Hs[idx] = hm;
   }
   __syncthreads();
   const float *F1 = sig + (long)J.f1sig * n * n;
   double s = 0;
   const float inv = 0.3989422804014327f;
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-    int j = idx / n, k = idx - j * n;
-    float phi = 2.0f * 3.14159265358979f * k / n;
-    float r = 0.f;
-    for (int m = 0; m < B; ++m) {
-      float2 hm = make_float2(0.f, 0.f);
-      for (int l = m; l < B; ++l) hm = cadd(hm, cscale(g[l * B + m], plm[((long)m * B + l) * n + j]));
-      float sn, cs;
-      sincosf(m * phi, &sn, &cs);
-      float re = hm.x * cs - hm.y * sn;
-      r += (m == 0) ? re : 2.f * re;
+    const int j = idx / n, k = idx - j * n;
+    const float2 *Hj = Hs + j * B;
+    float r = Hj[0].x;
+    for (int m = 1; m < B; ++m) {
+      const float2 e = ep[(m * k) & (n - 1)];
+      r += 2.f * (Hj[m].x * e.x - Hj[m].y * e.y);
     }
     r *= inv;
     s += (double)F1[idx] * (double)r * (double)sinth[j];
   }
-  double bsum = block_sum(s, sh);
+  const double bsum = block_sum(s, sh);
   if (threadIdx.x == 0) w[2 * blockIdx.x + which] = bsum;
 }
 
