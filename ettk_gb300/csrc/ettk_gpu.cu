@@ -2105,12 +2105,12 @@ case BB: {                                                                      
     Scope sc_s(this, "so3_synth", 8.0 * NJ * nso3 + 4.0 * dtab.n);                                                    \
     synth<BB>(NJ);                                                                                                    \
   }                                                                                                                   \
-  fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, 1, (long)n, 0, 1}, -1);                                              \
+  fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n * n, (long)n * n * n, 1, (long)n * n}, -1);                        \
   fft_strided(2 * BB, w_S.p, LineMap{NJ * n * n, n, (long)n * n, 1, (long)n}, -1);                                    \
   CK(cudaMemsetAsync(w_mm.p, 0, NJ * 2 * sizeof(unsigned long long), st));                                            \
   {                                                                                                                   \
     Scope sc_r(this, "so3_real", 12.0 * NJ * nso3);                                                                   \
-    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), NJ), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);                     \
+    k_so3_real<BB><<<dim3(n, NJ), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);                                                \
     post_launch();                                                                                                    \
   }                                                                                                                   \
   if (NSJ) {                                                                                                          \
@@ -2633,10 +2633,10 @@ void ettk_ctx::soft_diag(const float *F1, const float *F2, int scaled, float *C)
     post_launch();                                                                                        \
     CK(cudaMemsetAsync(w_S.p, 0, nso3 * sizeof(float2), st));                                            \
     synth<BB>(1);                                                                                         \
-    fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, 1, (long)n, 0, 1}, -1);                               \
+    fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, n * n, (long)n * n * n, 1, (long)n * n}, -1);         \
     fft_strided(2 * BB, w_S.p, LineMap{(long)n * n, n, (long)n * n, 1, (long)n}, -1);                     \
     CK(cudaMemsetAsync(w_mm.p, 0, 2 * sizeof(unsigned long long), st));                                   \
-    k_so3_real<BB><<<dim3(nblocks<int>(nso3, 256, 256), 1), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);         \
+    k_so3_real<BB><<<dim3(n, 1), 256, 0, st>>>(w_S.p, w_C.p, w_mm.p);                                    \
     post_launch();                                                                                        \
     if (scaled) {                                                                                         \
       k_so3_weights<BB><<<dim3(1, 2), 256, so3_weights_smem<BB>(), st>>>(w_sjobs.p, w_mm.p, w_coef.p, w_sig.p, dtab.p, doff.p, \

@@ -1266,32 +1266,38 @@ static __global__ void k_so3_synth(const float2 *__restrict__ coef, const SynthJ
       float2 acc = make_float2(0.f, 0.f);
       for (int t = 0; t < L; ++t) acc = cadd(acc, cscale(sF[jl][t], sd[t * n + b]));
       int mm1 = (m1 + n) % n, mm2 = (m2 + n) % n;
-      S[(((long)(j0 + jl) * n + b) * n + mm1) * n + mm2] = acc;
+      S[(((long)(j0 + jl) * n + mm1) * n + mm2) * n + b] = acc;
     }
   }
 }
 
-// Real part and scale (1/2B)(B/pi) of the alpha/gamma-transformed synthesis into C[job][a][b][g]
-// (soft_fftw.c:1913-1920; nbfProjectionRotationMetric3D.h:1254-1265), with packed min/max per job
-// in memory order (rotatedSphericalImageMinMax, 1557-1589).
+// Real part and scale (1/2B)(B/pi) of the alpha/gamma-transformed synthesis S[job][a][g][b] into
+// C[job][a][b][g] (soft_fftw.c:1913-1920; nbfProjectionRotationMetric3D.h:1254-1265), with packed min/max per job
+// in the memory order of C (rotatedSphericalImageMinMax, 1557-1589). One CTA per (a, job) transposes the (g, b)
+// plane through shared memory in blocks of 32 g rows (coalesced reads along b, writes along g).
 template <int B>
-static __global__ void k_so3_real(const float2 *__restrict__ S, float *__restrict__ C, unsigned long long *mm) {
-  constexpr int n = 2 * B;
-  const long n3 = (long)n * n * n;
-  const int job = blockIdx.y;
+static __global__ void __launch_bounds__(256) k_so3_real(const float2 *__restrict__ S, float *__restrict__ C,
+                                                         unsigned long long *mm) {
+  constexpr int n = 2 * B, GT = 32 < n ? 32 : n;
+  __shared__ float tile[GT][n + 1];
+  const int a = blockIdx.x, job = blockIdx.y;
   const float scale = (1.0f / n) * ((float)B / 3.14159265358979f);
+  const float2 *Sa = S + ((long)job * n + a) * n * n;
+  float *Ca = C + ((long)job * n + a) * n * n;
   unsigned long long bmax = 0, bmin = 0;
-  // four consecutive gamma per thread and step: two 16-byte reads of S, one 16-byte store of C
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < (int)(n3 / 4); q += gridDim.x * blockDim.x) {
-    const int id = 4 * q;
-    const int a = id / (n * n), b = (id / n) & (n - 1), g = id & (n - 1);
-    const float4 *s4 = reinterpret_cast<const float4 *>(S + (((long)job * n + b) * n + a) * n + g);
-    const float4 p0 = s4[0], p1 = s4[1];
-    const float v[4] = {p0.x * scale, p0.z * scale, p1.x * scale, p1.z * scale};
-    reinterpret_cast<float4 *>(C + (long)job * n3)[q] = make_float4(v[0], v[1], v[2], v[3]);
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      unsigned long long kx = pack_max(v[t], (uint32_t)(id + t)), kn = pack_min(v[t], (uint32_t)(id + t));
+  for (int g0 = 0; g0 < n; g0 += GT) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < GT * n; i += blockDim.x) {
+      const int gl = i / n, bb = i - gl * n;
+      tile[gl][bb] = Sa[(long)(g0 + gl) * n + bb].x * scale;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < GT * n; i += blockDim.x) {
+      const int bb = i / GT, gl = i - bb * GT;
+      const float v = tile[gl][bb];
+      Ca[(long)bb * n + g0 + gl] = v;
+      const uint32_t id = (uint32_t)((a * n + bb) * n + g0 + gl);
+      const unsigned long long kx = pack_max(v, id), kn = pack_min(v, id);
       bmax = kx > bmax ? kx : bmax;
       bmin = kn > bmin ? kn : bmin;
     }

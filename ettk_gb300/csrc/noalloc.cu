@@ -195,11 +195,12 @@ int run(unsigned char *base, const float *F1, const float *F2, float *C, cudaStr
   k_so3_synth<B><<<(2 * B - 1) * (2 * B - 1), 256, 0, st>>>(coef, jobs, 1, dtab, doff, S);
   constexpr int L = 16;
   size_t sm = (n / 2 + (size_t)L * n) * sizeof(float2);
-  LineMap m2{(long)n * n, 1, (long)n, 0, 1};
-  LineMap m1{(long)n * n, n, (long)n * n, 1, (long)n};
+  // S is [m1][m2][beta]: transforms along m2 (lines (m1, beta)) then along m1 (lines (m2, beta))
+  LineMap m2{(long)n * n, n, (long)n * n, 1, (long)n};
+  LineMap m1{(long)n * n, n * n, (long)n * n * n, 1, (long)n * n};
   k_fft_strided<n, L><<<(int)((m2.n_lines + L - 1) / L), 256, sm, st>>>(S, m2, -1, nullptr, 1);
   k_fft_strided<n, L><<<(int)((m1.n_lines + L - 1) / L), 256, sm, st>>>(S, m1, -1, nullptr, 1);
-  k_so3_real<B><<<dim3(((long)n * n * n + 255) / 256, 1), 256, 0, st>>>(S, C, nullptr);
+  k_so3_real<B><<<dim3(n, 1), 256, 0, st>>>(S, C, nullptr);
   return cudaGetLastError() == cudaSuccess ? ETTK_OK : ETTK_ERR_CUDA;
 }
 

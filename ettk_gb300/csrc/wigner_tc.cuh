@@ -36,6 +36,7 @@ struct WigTC {
   static constexpr size_t CAP = (size_t)228 * 1024 * NCOL / 512 + 1024;
   static constexpr size_t SMEM = OPS > CAP ? OPS : CAP;
   static_assert(n % 16 == 0 && n <= 256, "tensor-core N");
+  static_assert(SMEM >= (size_t)64 * 16 * 2 * sizeof(float), "epilogue staging fits the operand area");
 };
 
 // kind::f16 / kind::tf32 instruction descriptor: D f32 (bits 4-5), A/B format (7-9, 10-12: BF16 1, TF32 2),
@@ -86,7 +87,7 @@ ETTK_DEV void wig_store(void *base, int idx, float x, int part) {
   }
 }
 
-// grid (cells, ceil(n_jobs / 64)), 128 threads; coef [signal][l][m >= 0], S [job][b][m1 mod n][m2 mod n].
+// grid (cells, ceil(n_jobs / 64)), 128 threads; coef [signal][l][m >= 0], S [job][m1 mod n][m2 mod n][b].
 // A barrier that does not complete within the poll limit sets *status and leaves this tile's output unwritten.
 template <int B, int MODE>
 __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__ coef, const SynthJob *__restrict__ jobs,
@@ -162,13 +163,17 @@ __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(&bar))
                  : "memory");
   }
-  const bool ok = mbar_wait(&bar, 0, 1 << 22);
-  if (!ok && lane == 0) atomicExch(status, 1);
+  const bool mine = mbar_wait(&bar, 0, 1 << 22);
+  if (!mine && lane == 0) atomicExch(status, 1);
+  const bool ok = __syncthreads_and(mine);  // block-uniform: the epilogue below synchronises the CTA
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const int row = warp * 32 + lane, jl = row & 63, j = j0 + jl, comp = row >> 6;
+    // 16 accumulator columns (beta) at a time: tcgen05.ld of the thread's row (job jl, real or imaginary part),
+    // staged in the operand area (free once the MMAs completed) as [jl][beta][re, im], then written as whole
+    // 128-byte runs S[job][m1][m2][beta .. beta + 15]
+    const int row = warp * 32 + lane, jl = row & 63, comp = row >> 6;
     const int mm1 = (m1 + n) % n, mm2 = (m2 + n) % n;
-    float *Sf = reinterpret_cast<float *>(S);
+    float *stg = reinterpret_cast<float *>(wig_sm);
 #pragma unroll 1
     for (int c0 = 0; c0 < n; c0 += 16) {
       uint32_t r[16];
@@ -179,10 +184,14 @@ __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__
             "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
           : "r"(addr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (j < n_jobs) {
+      __syncthreads();  // the previous chunk's stores have read the staging area
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-          Sf[((((long)j * n + c0 + q) * n + mm1) * n + mm2) * 2 + comp] = __uint_as_float(r[q]);
+      for (int q = 0; q < 16; ++q) stg[(jl * 16 + q) * 2 + comp] = __uint_as_float(r[q]);
+      __syncthreads();
+      for (int t = tid; t < 64 * 16; t += blockDim.x) {
+        const int jt = t >> 4, q = t & 15, j = j0 + jt;
+        if (j < n_jobs)
+          S[(((long)j * n + mm1) * n + mm2) * n + c0 + q] = make_float2(stg[(jt * 16 + q) * 2], stg[(jt * 16 + q) * 2 + 1]);
       }
     }
   }
@@ -217,7 +226,7 @@ __global__ void __launch_bounds__(256) k_so3_synth_f64(const float2 *__restrict_
       re += fr * d[t * n + b];
       im += fi * d[t * n + b];
     }
-    S[(((long)j * n + b) * n + mm1) * n + mm2] = make_float2((float)re, (float)im);
+    S[(((long)j * n + mm1) * n + mm2) * n + b] = make_float2((float)re, (float)im);
   }
 }
 
