@@ -48,7 +48,7 @@ def parse():
                     help="plain form against the fast form (coarse SO(3) hit, one CCF per kept peak, local refinement) "
                          "on the 64^3 B=32 workload: alignments/s, stage times and errors against the generating poses")
     ap.add_argument("--fast-iterations", type=int, default=12)
-    ap.add_argument("--fast-peaks", type=int, default=1)
+    ap.add_argument("--fast-peaks", type=int, default=0, help="0: the metric's candidate_peaks")
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
     ap.add_argument("--fast-only", action="store_true",
                     help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")

@@ -146,6 +146,10 @@ struct DevBuf {
     p = nullptr;
     n = 0;
   }
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }  // buffers of a context are freed with it (ettk_gpu_destroy makes the device current)
 };
 
 // Rotation search bookkeeping (TinyVector<float,4>: alpha, beta, gamma, value) with an index that
@@ -312,6 +316,18 @@ __global__ void __launch_bounds__(256) k_combine_peaks(const PairPlan *__restric
         if (slot < cap) lists[(long)item * cap + slot] = make_int2(id, __float_as_int(val));
       }
     }
+  }
+}
+
+// Centred half spectra of M volumes of edge N (kz-major [e][kz][x][y], DC at (N/2, N/2, kz = N/2)) cut down to the
+// frequencies of edge N/2 (|f| < N/4 on x and y, -N/4 <= f <= 0 on kz): the Fourier crop of a 2x decimation.
+__global__ void k_spectrum_crop(const float2 *__restrict__ in, int N, long M, float2 *__restrict__ out) {
+  const int n = N / 2, h = n / 2 + 1, H = N / 2 + 1, q = N / 4;
+  const long total = M * h * (long)n * n;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+    const int y = (int)(id % n), x = (int)((id / n) % n), kz = (int)((id / ((long)n * n)) % h);
+    const long e = id / ((long)h * n * n);
+    out[id] = in[((e * H + kz + q) * N + x + q) * N + y + q];
   }
 }
 
@@ -804,8 +820,9 @@ struct ettk_ctx {
   DevBuf<float> lr_zm, lr_maps, lr_ip;
   DevBuf<int> lr_src;
   std::vector<int> lr_slot;  // particle -> slot of its band-passed copy in lr_ip (-1: none)
-  // band-passed copies of the fixed-image particles `parts` (filter of the metric, the particle's own frame)
-  void lr_filter_particles(const std::vector<int> &parts);
+  // band-passed copies of the fixed-image particles `parts` (filter of the metric, the particle's own frame) in
+  // lr_ip at slot lr_slot[particle]; with_half also their Fourier crops to edge N/2 in dec_vol, same slots
+  void lr_filter_particles(const std::vector<int> &parts, bool with_half = false);
   DevBuf<double> lr_acc;
   double lr_C0 = 0, lr_C1 = 0;  // sum m, sum m^2 of the spherical mask
   double lr_radius() const { return 0.6 * (p.mask_radius > 0 ? p.mask_radius : 0.5 * N); }
@@ -823,6 +840,19 @@ struct ettk_ctx {
   }
   void lr_eval(long E) { with_n(N, [&](auto nn) { lr_eval_t<decltype(nn)::value>(E); }); }
   void align_refined(int npairs, const int *pairs, float *D, int cols, int ncand, int iterations, int peaks);
+  // Candidate screening of the fast form on 2x decimated volumes: a child context of edge N/2 (the metric's
+  // parameters rescaled to the half grid) holding the Fourier-cropped references and, per batch, particles.
+  ettk_ctx *half = nullptr;
+  bool half_refs_ok = false;
+  DevBuf<float> dec_vol;
+  DevBuf<int> dec_src;
+  // Fourier crop of M fixed-image volumes vols + src[e] N^3 (device) to edge N/2, into out (M (N/2)^3, x fastest)
+  void decimate(const float *vols, const std::vector<int> &src, float *out);
+  void half_setup();  // creates the child context and gives it the decimated references (once per reference set)
+  // best CCF candidate per pair scored on the decimated volumes (particles prepared by lr_filter_particles with
+  // with_half): full-grid transform (translation doubled)
+  void half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
+                   const std::vector<int> &owner, std::vector<EvalReq> &finals);
   void refined_objective(int npairs, const int *pairs, const double *poses, const double *theta, double *rho,
                          double *grad);
   void so3_queues(int P, const std::vector<int> &pr, const std::vector<int> &pp, std::vector<PairPlan> &plans,
@@ -2407,7 +2437,115 @@ void ettk_ctx::lr_setup(const std::vector<EvalReq> &req) {
   post_launch();
 }
 
-void ettk_ctx::lr_filter_particles(const std::vector<int> &parts) {
+void ettk_ctx::decimate(const float *vols, const std::vector<int> &src, float *out) {
+  const long M = (long)src.size();
+  const int n = N / 2;
+  const long hh = (long)n * n * (n / 2 + 1);
+  dec_src.ensure(M);
+  w_cB.ensure(M * h3);
+  w_cA.ensure(M * hh);
+  CK(cudaMemcpyAsync(dec_src.p, src.data(), M * sizeof(int), cudaMemcpyHostToDevice, st));
+  r2c_z(N, PreSignVol{vols, dec_src.p, N}, w_cB.p, M * N * N);
+  xy_kxy(N, w_cB.p, M, -1);
+  k_spectrum_crop<<<nblocks<int>(M * hh, 256), 256, 0, st>>>(w_cB.p, N, M, w_cA.p);
+  post_launch();
+  xy_kxy(n, w_cA.p, M, +1);
+  c2r_z(n, w_cA.p, PostStoreSigned{out, n}, M * n * n);
+}
+
+// The volume-list row of a geometry on the half grid: positions, cut offset and the matrix translation halved.
+static ettk_volume_meta half_meta(const VolumeGeom &g) {
+  ettk_volume_meta m{};
+  m.lwedge = g.lwedge;
+  m.uwedge = g.uwedge;
+  for (int i = 0; i < 3; ++i) {
+    m.normal[i] = g.normal[i];
+    m.position[i] = 0.5f * g.position[i];
+  }
+  m.cut_offset = 0.5f * g.cut_offset;
+  memcpy(m.matrix, g.matrix, sizeof(m.matrix));
+  m.matrix[3] *= 0.5;
+  m.matrix[7] *= 0.5;
+  m.matrix[11] *= 0.5;
+  return m;
+}
+
+void ettk_ctx::half_setup() {
+  if (!half) {
+    ettk_params hp = p;
+    hp.N = N / 2;
+    hp.B = 8;  // the child runs no SO(3) search
+    hp.mask_radius = 0.5f * p.mask_radius;
+    hp.mask_sigma = 0.5f * p.mask_sigma;
+    hp.square_mask_size = 0.5f * p.square_mask_size;
+    // normalised frequencies double on the half grid; exp(-b r^2) keeps its value with b / 4
+    hp.bp_low = 2.f * p.bp_low;
+    hp.bp_high = 2.f * p.bp_high;
+    hp.bp_low_sigma = 2.f * p.bp_low_sigma;
+    hp.bp_high_sigma = 2.f * p.bp_high_sigma;
+    hp.bfactor = 0.25f * p.bfactor;
+    hp.restrict_translation = 0.5f * p.restrict_translation;
+    hp.wigner_precision = 0;
+    ettk_ctx *h = nullptr;
+    const int rc = ettk_gpu_create(device, &hp, &h);
+    if (rc != ETTK_OK) throw CudaError(rc, "half-grid screening context could not be created");
+    half = h;
+    half_refs_ok = false;
+  }
+  if (!half_refs_ok) {
+    const int n = N / 2;
+    std::vector<int> src(R);
+    for (int r = 0; r < R; ++r) src[r] = r;
+    DevBuf<float> dref;  // once per reference set (dec_vol may hold the batch's particles)
+    dref.ensure((long)R * n * n * n);
+    decimate(refvol.p, src, dref.p);
+    std::vector<float> host((size_t)R * n * n * n);
+    d2h(host.data(), dref.p, host.size() * sizeof(float));
+    std::vector<ettk_volume_meta> meta(R);
+    for (int r = 0; r < R; ++r) meta[r] = half_meta(refg[r]);
+    const int rc = ettk_gpu_set_references(half, R, host.data(), meta.data());
+    if (rc != ETTK_OK) throw CudaError(rc, "half-grid references: " + half->err);
+    half_refs_ok = true;
+  }
+}
+
+void ettk_ctx::half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
+                           const std::vector<int> &owner, std::vector<EvalReq> &finals) {
+  half_setup();
+  const int P = (int)pr.size();
+  std::vector<int> u;  // the batch's particles in the slot order of lr_filter_particles (dec_vol)
+  for (int q : pp)
+    if (lr_slot[q] == (int)u.size()) u.push_back(q);
+  const long M = (long)u.size();
+  sync();  // the child reads the decimated particles on its own stream
+  std::vector<ettk_volume_meta> meta(M);
+  for (long i = 0; i < M; ++i) meta[i] = half_meta(partg[u[i]]);
+  int rc = ettk_gpu_set_particles_device(half, (int)M, dec_vol.p, meta.data());
+  if (rc != ETTK_OK) throw CudaError(rc, "half-grid particles: " + half->err);
+  std::vector<EvalReq> hreq(cand.size());
+  for (size_t k = 0; k < cand.size(); ++k) hreq[k] = {cand[k].ref, lr_slot[cand[k].part], cand[k].t};
+  std::vector<EvalRes> res;
+  half->eval_batch(hreq, res);
+  std::vector<int> best(P, -1);
+  for (size_t k = 0; k < cand.size(); ++k) {
+    const int i = owner[k];
+    if (!transform_valid(half->p, res[k].t)) continue;
+    if (best[i] < 0 || res[k].dist < res[best[i]].dist) best[i] = (int)k;
+  }
+  finals.resize(P);
+  for (int i = 0; i < P; ++i) {
+    Mat4 t = Mat4::eye();
+    if (best[i] >= 0) {
+      t = res[best[i]].t;
+      t.e[3] *= 2.0;
+      t.e[7] *= 2.0;
+      t.e[11] *= 2.0;
+    }
+    finals[i] = {pr[i], pp[i], t};
+  }
+}
+
+void ettk_ctx::lr_filter_particles(const std::vector<int> &parts, bool with_half) {
   lr_slot.assign(V, -1);
   if (from_tomo || parts.empty()) return;
   std::vector<int> u;
@@ -2423,6 +2561,16 @@ void ettk_ctx::lr_filter_particles(const std::vector<int> &parts) {
   CK(cudaMemcpyAsync(lr_src.p, u.data(), M * sizeof(int), cudaMemcpyHostToDevice, st));
   r2c_z(N, PreSignVol{partptr, lr_src.p, N}, w_cB.p, M * N * N);
   xy_kxy(N, w_cB.p, M, -1);
+  if (with_half) {  // the same spectra, cropped to edge N/2, are the particles of the half-grid screening
+    const int n = N / 2;
+    const long hh = (long)n * n * (n / 2 + 1);
+    w_cA.ensure(M * hh);
+    dec_vol.ensure(M * n * n * n);
+    k_spectrum_crop<<<nblocks<int>(M * hh, 256), 256, 0, st>>>(w_cB.p, N, M, w_cA.p);
+    post_launch();
+    xy_kxy(n, w_cA.p, M, +1);
+    c2r_z(n, w_cA.p, PostStoreSigned{dec_vol.p, n}, M * n * n);
+  }
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
     fft2d_t<NN>(OpFilterShared<NN>{w_cB.p, filter.p}, M, "local_refine_setup", 16.0);
@@ -2441,9 +2589,12 @@ void ettk_ctx::lr_run(long P, int iterations) {
 }
 
 // Fast form: stages 1-3 as the plain form, then per pair one CCF evaluation (executeFourierNewHalf, the integer
-// half-voxel shift) of each of the `peaks` best candidates of the windowed queue and the best of the unwindowed
-// queue (no mirror evaluations), the best valid one refined by gradient ascent of the masked normalised
-// correlation (local_refine.cuh) in continuous rotation and shift.
+// shift of its upsampled grid) of each of the `peaks` best candidates of the windowed queue and the peaks / 3
+// (at least one) best of the unwindowed queue, as the candidate loop takes them, but with no mirror evaluations;
+// for boxes of edge 32 and more the CCF runs on the volumes Fourier-cropped to half the edge (the metric's band-pass
+// keeps little above half the Nyquist frequency, so the cropped CCF ranks the candidates as the full one does at an
+// eighth of the work); the best valid candidate is refined by gradient ascent of the masked normalised correlation
+// (local_refine.cuh) in continuous rotation and shift.
 void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, int ncand, int iterations, int peaks) {
   HostScope hs_all(this, "host_align_wall");
   const int maxb = p.max_batch > 0 ? p.max_batch : 512;
@@ -2458,6 +2609,11 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
       pp[i] = pairs[2 * todo[b0 + i] + 1];
       if (pr[i] < 0 || pr[i] >= R || pp[i] < 0 || pp[i] >= V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
     }
+    const bool use_half = N >= 32 && !from_tomo;
+    {
+      HostScope hs_p(this, "stage_particle_spectra");
+      lr_filter_particles(pp, use_half);  // device work queued ahead of the SO(3) stage
+    }
     std::vector<PairPlan> plans;
     std::vector<PQ> q1, q2;
     {
@@ -2471,7 +2627,7 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
       for (int i = 0; i < P; ++i)
         for (int q = 0; q < 2; ++q) {
           PQ &Q = q == 0 ? q1[i] : q2[i];
-          const int take = q == 0 ? peaks : 1;
+          const int take = q == 0 ? peaks : std::max(1, peaks / 3);
           for (int t = 0; t < take && !Q.empty() && Q.top().v[3] != FLT_MAX; ++t) {
             const Cand c = Q.top();
             Q.pop();
@@ -2479,6 +2635,14 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
             owner.push_back(i);
           }
         }
+    }
+    if (use_half) {
+      HostScope hs_c(this, "stage_coarse_ccf");
+      std::vector<EvalReq> finals;
+      half_screen(pr, pp, req, owner, finals);
+      req.swap(finals);
+    } else {
+      HostScope hs_c(this, "stage_coarse_ccf");
       std::vector<EvalRes> res;
       eval_batch(req, res);
       std::vector<int> best(P, -1);
@@ -2504,7 +2668,6 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
     std::vector<LRState> sts(P);
     {
       HostScope hs_r(this, "stage_local_refine");
-      lr_filter_particles(pp);
       lr_setup(req);
       lr_run(P, iterations);
       read_back(sts.data(), lr_state.p, P * sizeof(LRState));
@@ -2823,6 +2986,8 @@ int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **out) {
 
 int ettk_gpu_destroy(ettk_ctx *c) {
   if (!c) return ETTK_OK;
+  if (c->half) ettk_gpu_destroy(c->half);
+  c->half = nullptr;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
   DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
@@ -2873,6 +3038,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
 int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_volume_meta *meta) {
   if (!c || R <= 0 || !vols || !meta) return fail(c, ETTK_ERR_ARG, "invalid reference arguments");
   if (!finite_volume(vols, (long)R * c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite reference volume");
+  c->half_refs_ok = false;
   return guarded(c, [&] {
     long n3 = c->n3, h3 = c->h3;
     c->R = R;
@@ -3009,7 +3175,9 @@ int ettk_gpu_align_pairs_refined(ettk_ctx *c, int npairs, const int *pairs, floa
       iterations > 1000 || peaks > 64)
     return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
-  return guarded(c, [&] { c->align_refined(npairs, pairs, D, cols, ncand, iterations, peaks ? peaks : 1); });
+  return guarded(c, [&] {
+    c->align_refined(npairs, pairs, D, cols, ncand, iterations, peaks ? peaks : c->p.candidate_peaks);
+  });
 }
 
 int ettk_gpu_refined_objective(ettk_ctx *c, int npairs, const int *pairs, const double *poses, const double *theta,

@@ -267,10 +267,10 @@ class ProjectionRotationMetric3D:
         return (rho, g) if grad else rho
 
     # -- fast form: coarse SO(3) hit + local refinement (no counterpart in the reference) -------
-    def getDistancesRefined(self, indexes, D=None, cols=17, ncand=1, iterations=12, peaks=1):
+    def getDistancesRefined(self, indexes, D=None, cols=17, ncand=1, iterations=12, peaks=0):
         """As getDistances, through the fast form (ettk_gpu_align_pairs_refined): CCF of the `peaks` best
-        windowed candidates and the best unwindowed one, then `iterations` steps of continuous refinement;
-        column 0 is 1 - rho at the refined pose."""
+        windowed candidates (0: candidate_peaks) and peaks / 3 unwindowed ones, then `iterations` steps of
+        continuous refinement; column 0 is 1 - rho at the refined pose."""
         idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
         n = idx.shape[0]
         if D is None:

@@ -217,14 +217,16 @@ int ettk_gpu_refine_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D,
    whose Powell refinement, inc/em/nbfFourierImageMetric.h:1701-1809, and whose mirror and candidate CCF loop,
    inc/em/nbfProjectionRotationMetric3D.h:678-901, it replaces): the same spherical projections, SO(3) correlations
    (in the context's wigner_precision) and candidate queues as ettk_gpu_align_pairs, then per pair one CCF
-   (executeFourierNewHalf: integer half-voxel shift) of each of the `peaks` best candidates of the windowed queue
-   and of the best candidate of the unwindowed one, no mirror evaluations, and the best valid result refined in
+   (executeFourierNewHalf) of each of the `peaks` best candidates of the windowed queue and of the peaks / 3 (at
+   least one) best of the unwindowed one, no mirror evaluations, computed for boxes of edge 32 and more on the
+   volumes Fourier-cropped to half the edge (the band-pass keeps little above half the Nyquist frequency), and the
+   best valid result refined in
    continuous rotation and shift by `iterations` steps of gradient ascent of the masked normalised correlation
    between the wedge- and band-limited reference (the CCF's filter times both wedges at the coarse pose) and the
    particle (trilinear interpolation, analytic gradient). D has the layout of ettk_gpu_align_pairs; column 0 holds
    1 - rho at the refined pose, the matrix the refined pose (continuous), scale 1 and the wedge overlap as there;
    candidate slots past the first get FLT_MAX in column 0. Rows whose D[i][0][0] != -1 are skipped.
-   iterations 0 keeps the coarse pose (rho evaluated there); peaks 0 = 1. */
+   iterations 0 keeps the coarse pose (rho evaluated there); peaks 0 = the context's candidate_peaks. */
 int ettk_gpu_align_pairs_refined(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
                                  int iterations, int peaks);
 
