@@ -314,7 +314,7 @@ def fast_study(a):
             if form == "plain":
                 return m.getDistances(sub)
             return m.getDistancesRefined(sub, iterations=a.fast_iterations, peaks=a.fast_peaks)
-        run(pairs if a.fast_only else pairs[:8])
+        run(pairs)  # warm-up at full size (buffers, tables, the half-grid references)
         m.set_particles(vols)  # drop the cached spherical projections of the warm-up pairs
         torch.cuda.synchronize()
         m.profile(True)

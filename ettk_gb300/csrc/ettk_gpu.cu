@@ -765,9 +765,9 @@ struct ettk_ctx {
   // (x, y) passes of a 3-D transform of `items` kz-major spectra [len/2+1][len][len]: one CTA per kz plane
   // (k_fft2d) up to len = 128, two strided register passes beyond.
   template <int NN, class Op>
-  void fft2d_t(Op op, long items, const char *family = "fft_xy", double bytes_per_elem = 16.0) {
+  void fft2d_t(Op op, long items, const char *family = "fft_xy", double bytes_per_elem = 16.0, int planes = NN / 2 + 1) {
     constexpr size_t smem = fft2d_smem<NN>();
-    constexpr long H2 = NN / 2 + 1;
+    const long H2 = planes;  // kz planes transformed (blockIdx.x), from the op's first plane
     Scope sc(this, family, bytes_per_elem * items * H2 * NN * NN);
     static bool attr_set = false;  // per instantiation, once per process
     if (!attr_set) {
@@ -796,6 +796,26 @@ struct ettk_ctx {
 
   // ---------------------------------------------------------------- setup
   void init_tables();
+  // (x, y) passes of the padded spherical-projection spectra sp_F storing |F| into sp_M: the planes kz < N2/2
+  // by k_fft2d_padded (half-row shared memory), the last plane by k_fft2d
+  template <int N2>
+  void padded_magnitude_t(long P) {
+    constexpr size_t smem = fft2d_padded_smem<N2>();
+    {
+      Scope sc(this, "sphere_fft", 16.0 * P * (N2 / 2) * N2 * N2);
+      static bool attr_set = false;  // per instantiation, once per process
+      if (!attr_set) {
+        CK(cudaFuncSetAttribute(k_fft2d_padded<N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaFuncSetAttribute(k_fft2d_padded<N2>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        attr_set = true;
+      }
+      k_fft2d_padded<N2><<<dim3(N2 / 2, (unsigned)P), 256, smem, st>>>(sp_F.p, sp_M.p);
+      post_launch();
+    }
+    OpPaddedMagnitude<N2> last{sp_F.p, sp_M.p};
+    last.kz0 = N2 / 2;
+    fft2d_t<N2>(last, P, "sphere_fft", 16.0, 1);
+  }
   // |F| spherical projections of the items into Pp_out[out_index[i] * nn] (device; out_index null: [i * nn])
   void spherical_projection(const std::vector<ResliceItem> &items, float *Pp_out, const int *out_index = nullptr);
   void eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> &res);
@@ -849,8 +869,11 @@ struct ettk_ctx {
   // Fourier crop of M fixed-image volumes vols + src[e] N^3 (device) to edge N/2, into out (M (N/2)^3, x fastest)
   void decimate(const float *vols, const std::vector<int> &src, float *out);
   void half_setup();  // creates the child context and gives it the decimated references (once per reference set)
-  // best CCF candidate per pair scored on the decimated volumes (particles prepared by lr_filter_particles with
-  // with_half): full-grid transform (translation doubled)
+  // hands the batch's decimated particles (lr_filter_particles with with_half, queued on st) to the child: host
+  // set-up only, the child's stream waits for dec_ev before its first kernel
+  cudaEvent_t dec_ev = nullptr;
+  void half_particles(const std::vector<int> &pp);
+  // best CCF candidate per pair scored on the decimated volumes: full-grid transform (translation doubled)
   void half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
                    const std::vector<int> &owner, std::vector<EvalReq> &finals);
   void refined_objective(int npairs, const int *pairs, const double *poses, const double *theta, double *rho,
@@ -1680,14 +1703,15 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   k_mean_all<<<dim3(nblocks<int>(n3, 256, 256), P), 256, 0, st>>>(sp_v.p, sp_acc.p, 4, N, sp_acc.p, 2);
   post_launch();
   PrePadded pre{sp_v.p, mask.p, sp_acc.p, 4, N};
+  pre.nyquist_only = N2 <= 128;  // k_fft2d_padded consumes the spectra (larger boxes transform every plane)
   k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
   post_launch();
   r2c_z(N2, pre, sp_F.p, P * N2 * N2, "sphere_fft");
   // (x, y) passes storing |F| directly (the complex spectrum is not used again)
   switch (N2) {
-    case 32: fft2d_t<32>(OpPaddedMagnitude<32>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
-    case 64: fft2d_t<64>(OpPaddedMagnitude<64>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
-    case 128: fft2d_t<128>(OpPaddedMagnitude<128>{sp_F.p, sp_M.p}, P, "sphere_fft"); break;
+    case 32: padded_magnitude_t<32>(P); break;
+    case 64: padded_magnitude_t<64>(P); break;
+    case 128: padded_magnitude_t<128>(P); break;
     default: {
       xy_kxy(N2, sp_F.p, P, -1);
       k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
@@ -2509,23 +2533,38 @@ void ettk_ctx::half_setup() {
   }
 }
 
-void ettk_ctx::half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
-                           const std::vector<int> &owner, std::vector<EvalReq> &finals) {
+void ettk_ctx::half_particles(const std::vector<int> &pp) {
   half_setup();
-  const int P = (int)pr.size();
+  if (!dec_ev) CK(cudaEventCreateWithFlags(&dec_ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(dec_ev, st));
   std::vector<int> u;  // the batch's particles in the slot order of lr_filter_particles (dec_vol)
   for (int q : pp)
     if (lr_slot[q] == (int)u.size()) u.push_back(q);
   const long M = (long)u.size();
-  sync();  // the child reads the decimated particles on its own stream
   std::vector<ettk_volume_meta> meta(M);
   for (long i = 0; i < M; ++i) meta[i] = half_meta(partg[u[i]]);
-  int rc = ettk_gpu_set_particles_device(half, (int)M, dec_vol.p, meta.data());
+  const int rc = ettk_gpu_set_particles_device(half, (int)M, dec_vol.p, meta.data());
   if (rc != ETTK_OK) throw CudaError(rc, "half-grid particles: " + half->err);
+}
+
+void ettk_ctx::half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
+                           const std::vector<int> &owner, std::vector<EvalReq> &finals) {
+  const int P = (int)pr.size();
+  CK(cudaStreamWaitEvent(half->st, dec_ev, 0));  // the decimated particles are written on st
   std::vector<EvalReq> hreq(cand.size());
   for (size_t k = 0; k < cand.size(); ++k) hreq[k] = {cand[k].ref, lr_slot[cand[k].part], cand[k].t};
+  half->prof = prof;
   std::vector<EvalRes> res;
   half->eval_batch(hreq, res);
+  if (prof) {  // the child's kernel families, reported under "half:"
+    for (auto &kv : half->prof_agg) {
+      ProfAgg &g = prof_agg["half:" + kv.first];
+      g.n += kv.second.n;
+      g.ms += kv.second.ms;
+      g.bytes += kv.second.bytes;
+    }
+    half->prof_agg.clear();
+  }
   std::vector<int> best(P, -1);
   for (size_t k = 0; k < cand.size(); ++k) {
     const int i = owner[k];
@@ -2613,6 +2652,7 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
     {
       HostScope hs_p(this, "stage_particle_spectra");
       lr_filter_particles(pp, use_half);  // device work queued ahead of the SO(3) stage
+      if (use_half) half_particles(pp);   // the child's host set-up while the device works
     }
     std::vector<PairPlan> plans;
     std::vector<PQ> q1, q2;
@@ -2989,6 +3029,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   if (c->half) ettk_gpu_destroy(c->half);
   c->half = nullptr;
   cudaSetDevice(c->device);
+  if (c->dec_ev) cudaEventDestroy(c->dec_ev);
   if (c->st) cudaStreamSynchronize(c->st);
   DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
                          &c->W1half, &c->Pp1, &c->W1sph, &c->partvol, &c->W2sph, &c->Pp2, &c->w_r, &c->w_v,

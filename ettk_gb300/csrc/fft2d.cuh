@@ -147,19 +147,81 @@ struct OpPaddedMagnitude {
   const float2 *d;
   float *mag;
   int sign = -1;
+  int kz0 = 0;  // plane of blockIdx.x = 0 (the launch for the last plane alone uses kz0 = N2 / 2)
   ETTK_DEV void begin() {}
   ETTK_DEV void rows(int kz, int &r0, int &r1) const {
-    if (kz < KXY<N2>::H - 1) {
+    if (kz + kz0 < KXY<N2>::H - 1) {
       r0 = 0;
       r1 = N2 / 2;
     }
   }
-  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N2>::at(e, kz, i)]; }
+  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N2>::at(e, kz + kz0, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
-    mag[KXY<N2>::at(e, kz, i)] = sqrtf(v.x * v.x + v.y * v.y);
+    mag[KXY<N2>::at(e, kz + kz0, i)] = sqrtf(v.x * v.x + v.y * v.y);
   }
   ETTK_DEV void end(int, int) {}
 };
+
+// The planes kz < N2/2 of the same pass in less shared memory: there only the rows x < R = N2/2 are nonzero, and
+// their entries y >= R too (the z transforms of the padding lines vanish below kz = N2/2), so after the row
+// transforms every column is a length-N2 transform of R values followed by zeros, computed as two R-point
+// transforms (even outputs: the column; odd outputs: the column times e^{-2 pi i j / N2}). Shared memory holds
+// the R nonzero rows and the twiddled copy of half of the columns at a time, so that two CTAs share an SM.
+template <int N2>
+constexpr size_t fft2d_padded_smem() {
+  return ((size_t)(N2 / 2) * (N2 + 1) + (size_t)(N2 / 2) * (N2 / 2 + 1)) * sizeof(float2);
+}
+template <int N2>
+__global__ void __launch_bounds__(256, 2) k_fft2d_padded(const float2 *__restrict__ d, float *__restrict__ mag) {
+  constexpr int R = N2 / 2, PA = N2 + 1, PB = R + 1;
+  constexpr int G1 = MaxAB<N2>::v, GR1 = 256 / G1, WG1 = 32 / G1;
+  constexpr int G2 = MaxAB<R>::v, GR2 = 256 / G2, WG2 = 32 / G2;
+  extern __shared__ float2 pdm[];
+  float2 *A = pdm, *Bm = pdm + R * PA;
+  __shared__ float2 tw1[N2], tw2[R];
+  load_full_twiddles<N2>(tw1);
+  load_full_twiddles<R>(tw2);
+  const int kz = blockIdx.x, e = blockIdx.y;
+  for (int i = threadIdx.x; i < R * N2; i += blockDim.x) {
+    const int x = i / N2, y = i - x * N2;
+    A[x * PA + y] = y < R ? d[KXY<N2>::at(e, kz, x * N2 + y)] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  {  // row transforms (y lines), lines of one warp 8 apart as in k_fft2d
+    const int grp = threadIdx.x / G1, lane = threadIdx.x % G1;
+    const int sub = (grp % WG1) * (GR1 / WG1) + grp / WG1;
+    for (int r0 = 0; r0 < R; r0 += GR1) {
+      const int r = r0 + sub;
+      group_fft<N2>(A + (r < R ? r : 0) * PA, 1, lane, r < R, -1, tw1);
+    }
+  }
+  __syncthreads();
+  for (int h = 0; h < 2; ++h) {
+    const int c0 = h * R;
+    for (int i = threadIdx.x; i < R * R; i += blockDim.x) {
+      const int j = i / R, c = i - j * R;
+      Bm[j * PB + c] = cmul(A[j * PA + c0 + c], tw1[j]);
+    }
+    __syncthreads();
+    {  // column transforms: A's columns c0 .. c0 + R - 1 (even outputs) and Bm's (odd outputs)
+      const int grp = threadIdx.x / G2, lane = threadIdx.x % G2;
+      const int sub = (grp % WG2) * (GR2 / WG2) + grp / WG2;
+      for (int q0 = 0; q0 < 2 * R; q0 += GR2) {
+        const int q = q0 + sub;
+        const bool act = q < 2 * R;
+        float2 *line = !act ? A : (q < R ? A + c0 + q : Bm + (q - R));
+        group_fft<R>(line, q < R || !act ? PA : PB, lane, act, -1, tw2);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < N2 * R; i += blockDim.x) {
+      const int x = i / R, c = i - x * R;
+      const float2 v = (x & 1) ? Bm[(x >> 1) * PB + c] : A[(x >> 1) * PA + c0 + c];
+      mag[KXY<N2>::at(e, kz, x * N2 + c0 + c)] = sqrtf(v.x * v.x + v.y * v.y);
+    }
+    __syncthreads();
+  }
+}
 
 // Sums of |v|^2 of a normalizeFourierHalf (inc/em/nbfCorrelationImageMetric.h:497-530): kz < H-1 into
 // acc[e][slot], the kz = H-1 plane into acc[e][slot+1]; per-thread FP32 partials, FP64 across threads.

@@ -200,8 +200,9 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
     float c0, s0;
     const long lt = l_base + (threadIdx.x % RL);
     if (__syncthreads_and(lt >= n_lines || pre.pad_line(lt, c0, s0))) {
-      for (int idx = threadIdx.x; idx < H * RL; idx += blockDim.x) {
+      for (int idx = pre.nyquist_only ? (N / 2) * RL + threadIdx.x : threadIdx.x; idx < H * RL; idx += blockDim.x) {
         const int k = idx / RL, rl = idx - k * RL;
+        if (pre.nyquist_only && k != N / 2) break;  // the consumer never reads the zero planes of padding lines
         const long l = l_base + rl;
         if (l < n_lines) {
           float2 v = make_float2(0.f, 0.f);

@@ -1077,6 +1077,9 @@ struct PrePadded {
     return (img - meanAll) * mask[id] + meanAll;
   }
   static constexpr bool kPadLines = true;
+  // the z pass of a padding line writes only its kz = N2/2 entry (the padded magnitude pass of k_fft2d_padded
+  // reads no other plane of such a line)
+  bool nyquist_only = false;
   // line (x, y) with x >= N or y >= N lies wholly in the padding: r[z] = c (-1)^(x+y+z)
   ETTK_DEV bool pad_line(long line, float &c, float &sign_xy) {
     const int N2 = 2 * N;
