@@ -6,6 +6,9 @@ translational CCF candidates, alignment_mode 3) through the library's getDistanc
   value : pairs/s with the particle volumes already resident in HBM (set_particles_device + align)
   e2e   : pairs/s through the host-buffer API: pinned host volumes copied in every step
           (ettk_gpu_set_particles) and the result rows read back (ettk_gpu_align_pairs)
+  fast_form : the same pairs through the fast form (ettk_gpu_align_pairs_refined: split-BF16 Wigner contraction,
+          half-grid candidate screening, local refinement): alignments/s, speed-up over the plain form, e2e, and
+          both forms' rotation/shift errors against the generating poses
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank aligns its own batch on its own GPU (independent replicas, no collective
@@ -25,6 +28,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "align64_b32"
+FAST_PRECISION = 2   # split-BF16 Wigner-d contraction on the tensor cores
+FAST_ITERATIONS = 6  # local refinement steps of the fast form
 METRIC = "alignments/s at 64^3 bw=32: plain GPU vs batched+adjoint form at <=0.5deg/0.1 vox"
 
 
@@ -47,7 +52,8 @@ def parse():
     ap.add_argument("--fast-study", action="store_true",
                     help="plain form against the fast form (coarse SO(3) hit, one CCF per kept peak, local refinement) "
                          "on the 64^3 B=32 workload: alignments/s, stage times and errors against the generating poses")
-    ap.add_argument("--fast-iterations", type=int, default=12)
+    ap.add_argument("--fast-iterations", type=int, default=6)
+    ap.add_argument("--workload", default=WORKLOAD, help="workload of the studies (align64_b32, refine64_b32)")
     ap.add_argument("--fast-peaks", type=int, default=0, help="0: the metric's candidate_peaks")
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
     ap.add_argument("--fast-only", action="store_true",
@@ -298,7 +304,7 @@ def fast_study(a):
     from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
 
     P = a.pairs
-    ds = synthetic.generate(WORKLOAD, n_particles=P)
+    ds = synthetic.generate(a.workload, n_particles=P)
     kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
     vols = [WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in kw}) for i in range(P)]
     ref = WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})
@@ -330,7 +336,7 @@ def fast_study(a):
         rf, sf = pose_errors(out["fast"][0], ds.truth)
         line = {"fast_study": {"fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, rf < 20.0),
                                             families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()})},
-                "config": {"workload": WORKLOAD, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
+                "config": {"workload": a.workload, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
                            "fast_wigner_precision": a.fast_precision}}
         print(json.dumps(line), flush=True)
         return
@@ -346,7 +352,7 @@ def fast_study(a):
                      stages_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items() if k in stages},
                      families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()}),
         "speedup": out["fast"][1] / out["plain"][1]},
-        "config": {"workload": WORKLOAD, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
+        "config": {"workload": a.workload, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
                    "fast_wigner_precision": a.fast_precision,
                    "errors": "against the generating poses, over pairs whose plain grid hit is within 20 degrees"}}
     print(json.dumps(line), flush=True)
@@ -466,16 +472,17 @@ def main():
         m.set_particles(vols, stacked=parts_host.numpy())
         return m.getDistances(pairs)
 
-    def timed(fn, steps):
+    def timed(fn, steps, strm=None):
+        strm = strm or stream
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        e0.record(strm)
         for _ in range(steps):
             fn()
-        e1.record(stream)
+        e1.record(strm)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         if world > 1:
@@ -495,7 +502,32 @@ def main():
     prof = m.profile_read()
     m.profile(False)
     ms_e2e = timed(step_e2e, a.steps)
+    D_plain = step_device()
+    # the fast form on the same pairs: split-BF16 Wigner contraction, half-grid candidate screening, local refinement
+    mf = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=FAST_PRECISION), device=local)
+    mf.set_references([WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})])
+    fstream = torch.cuda.ExternalStream(mf.stream())
+
+    def step_fast():
+        mf.set_particles_device(parts_dev.data_ptr(), metas)
+        return mf.getDistancesRefined(pairs, iterations=FAST_ITERATIONS)
+
+    def step_fast_e2e():
+        mf.set_particles(vols, stacked=parts_host.numpy())
+        return mf.getDistancesRefined(pairs, iterations=FAST_ITERATIONS)
+
+    for _ in range(a.warmup):
+        step_fast()
+    fl0 = mf.kernel_launches()
+    ms_fast = timed(step_fast, a.steps, fstream)
+    fast_launches = mf.kernel_launches() - fl0
+    ms_fast_e2e = timed(step_fast_e2e, a.steps, fstream)
+    D_fast = step_fast()
+    mf.close()
     clk = clocks.stop()
+    rp, sp = pose_errors(D_plain, ds.truth)
+    rf, sf = pose_errors(D_fast, ds.truth)
+    hit = rp < 20.0
 
     hbm, tflops, peak_kind = peaks()
     kernels = {k: v for k, v in prof.items() if not k.startswith("host_")}
@@ -525,6 +557,19 @@ def main():
         "e2e": {"value": e2e, "unit": "alignments/s", "h2d_bytes_per_step": P * N ** 3 * 4,
                 "d2h_bytes_per_step": P * 17 * 4},
         "gpu_launches": launches,
+        "fast_form": {
+            "value": world * P * a.steps / (ms_fast * 1e-3), "unit": "alignments/s", "ms_per_step": ms_fast / a.steps,
+            "speedup_vs_plain": ms / ms_fast,
+            "e2e": {"value": world * P * a.steps / (ms_fast_e2e * 1e-3), "unit": "alignments/s",
+                    "h2d_bytes_per_step": P * N ** 3 * 4, "d2h_bytes_per_step": P * 17 * 4},
+            "gpu_launches": fast_launches,
+            "method": "SO(3) grid with split-BF16 tcgen05 Wigner contraction, CCF of the candidatePeaks + 1 best "
+                      "candidates on half-grid Fourier crops, %d steps of local 6-DOF refinement by the analytic "
+                      "gradient of the masked normalised correlation" % FAST_ITERATIONS,
+            "errors": {"plain": error_summary(rp, sp, hit), "fast": dict(error_summary(rf, sf, hit),
+                                                                         basin_hits_fast=int((rf < 20.0).sum())),
+                       "note": "against the generating poses; medians and means over the pairs whose plain grid hit "
+                               "is within 20 degrees"}},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_per_launch,

@@ -6,7 +6,8 @@ workload definitions:
 
 * a reference = sum of isotropic Gaussian blobs on a centred N^3 grid;
 * a particle = the reference rotated by a uniform SO(3) rotation (trilinear
-  interpolation), shifted by an integer offset, multiplied in Fourier space by a
+  interpolation), shifted by an integer offset (or, for the local-refinement workload, a continuous one), multiplied
+  in Fourier space by a
   single-axis missing wedge about Y (the binary plane test of nbfWedge3D,
   inc/em/nbfWedge3D.h:351-356), plus white Gaussian noise at the requested SNR;
 * metadata in the reference's volume-list vocabulary: lwedge/uwedge = -tilt/+tilt,
@@ -48,6 +49,7 @@ class Workload:
     restrict_translation: float
     n_refs: int = 1
     shared_fraction: float = 0.0
+    continuous_shift: bool = False  # shifts uniform in [-shift, shift] (sub-voxel) instead of integers
 
 
 WORKLOADS = {
@@ -60,6 +62,9 @@ WORKLOADS = {
     # 64^3, 10 references with 30% shared blobs
     "mra64_b32": Workload("mra64_b32", 2, 64, 32, 8000, 40, (3.0, 6.0), 20.0, (0.5, 1.0), 8, 0.05,
                           (45.0, 70.0), True, 10.0, n_refs=10, shared_fraction=0.3),
+    # 64^3 local-refinement workload: continuous poses and sub-voxel shifts uniform in +-8, per-particle wedges
+    "refine64_b32": Workload("refine64_b32", 3, 64, 32, 4000, 40, (3.0, 6.0), 20.0, (0.5, 1.0), 8, 0.05,
+                             (45.0, 70.0), True, 10.0, continuous_shift=True),
     # 32^3, 3 references with 30% shared blobs (small multireference classification case for tests)
     "mra32_b16": Workload("mra32_b16", 5, 32, 16, 60, 20, (1.5, 3.0), 10.0, (0.5, 1.0), 4, 0.1,
                           (60.0, 60.0), False, 6.0, n_refs=3, shared_fraction=0.3),
@@ -195,7 +200,10 @@ def generate(name, n_particles=None, seed=None):
     meta, truth = [], []
     for i in range(P):
         G = random_rotation(r_poses)
-        s = r_shifts.integers(-w.shift, w.shift + 1, 3).astype(np.float64)
+        if w.continuous_shift:
+            s = r_shifts.uniform(-w.shift, w.shift, 3)
+        else:
+            s = r_shifts.integers(-w.shift, w.shift + 1, 3).astype(np.float64)
         tilt = w.tilt[0] if w.tilt[0] == w.tilt[1] else r_wedges.uniform(w.tilt[0], w.tilt[1])
         phi = r_wedges.uniform(0.0, 360.0) if w.inplane else 0.0
         lw, uw = -float(np.float32(tilt)), float(np.float32(tilt))

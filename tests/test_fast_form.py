@@ -142,3 +142,69 @@ def test_fast_form_resume_rule(ds64):
     assert np.all(D[2] == 5.0)
     others = [i for i in range(n) if i != 2]
     assert np.all(D[others, 0, 0] < 1.0)
+
+
+def _rodrigues(w):
+    t = np.linalg.norm(w)
+    if t == 0:
+        return np.eye(3)
+    k = w / t
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * K @ K
+
+
+def _ascend(m, pair, T, radius, iters=30):
+    """Gradient ascent of the fast form's objective from pose T (step rule of the library's optimizer), evaluated
+    through the C ABI; returns the final pose and rho."""
+    rho, g = m.refined_objective([pair], [T], np.zeros((1, 6)))
+    rho, g = rho[0], g[0]
+    alpha = 0.5
+    for _ in range(iters):
+        gu = np.concatenate([g[:3] / radius, g[3:]])
+        nrm = np.linalg.norm(gu)
+        if not nrm > 0 or alpha < 1e-3:
+            break
+        Q = np.eye(4)
+        Q[:3, :3] = _rodrigues(gu[:3] / nrm * alpha / radius)
+        Q[:3, 3] = gu[3:] / nrm * alpha
+        Tt = T @ Q
+        rt, gt = m.refined_objective([pair], [Tt], np.zeros((1, 6)))
+        if rt[0] > rho:
+            T, rho, g, alpha = Tt, rt[0], gt[0], min(alpha * 1.6, 4.0)
+        else:
+            alpha *= 0.35
+    return T, rho
+
+
+def test_error_floor_of_the_objective():
+    """Where the objective itself puts the pose at this signal-to-noise ratio: ascent started at the generating
+    poses of the continuous-pose, sub-voxel-shift workload ends away from them, at a correlation at least that of
+    the generating pose; the fast form's poses lie within twice that floor's median error of the generating ones.
+    The floor (printed) bounds what any optimiser of this objective can reach on these data."""
+    ds = synthetic.generate("refine64_b32", n_particles=16)
+    n = 16
+    m = metric(ds, n)
+    radius = 0.6 * ds.params["mask_radius"]
+    try:
+        floor_rot, floor_sh = [], []
+        for i in range(n):
+            T0 = np.eye(4)
+            T0[:3, :3] = ds.truth[i]["rotation"]
+            T0[:3, 3] = ds.truth[i]["shift"]
+            r0 = m.refined_objective([(0, i)], [T0], np.zeros((1, 6)), grad=False)[0]
+            T, rho = _ascend(m, (0, i), T0, radius)
+            assert rho >= r0
+            c = np.clip((np.trace(T[:3, :3] @ T0[:3, :3].T) - 1) / 2, -1, 1)
+            floor_rot.append(np.degrees(np.arccos(c)))
+            floor_sh.append(np.linalg.norm(T[:3, 3] - T0[:3, 3]))
+        Df = m.getDistancesRefined([(0, i) for i in range(n)], iterations=16)
+    finally:
+        m.close()
+    rf, sf = errors(Df, ds)
+    hit = rf < 20.0
+    fr, fs = float(np.median(floor_rot)), float(np.median(floor_sh))
+    print("objective error floor: median %.3f deg, %.3f voxel; fast form: %.3f deg, %.3f voxel"
+          % (fr, fs, np.median(rf[hit]), np.median(sf[hit])))
+    assert hit.sum() >= n // 2
+    assert np.median(rf[hit]) <= 2.0 * fr + 0.5
+    assert np.median(sf[hit]) <= 2.0 * fs + 0.1
