@@ -670,7 +670,12 @@ static __global__ void k_score(const double *acc, int acc_stride, const unsigned
   if (overlap && use_wedge) pk = fmax(0.0, (double)k1_m - (double)T) / a[6] * sum_filter;
   else pk = fmax(0.0, (double)k1_m - (double)T);
   EvalOut o;
-  o.dist = (float)(pk / big / big);
+  // the peak is stored in the reference's float correlationPeak, then divided twice in float by the int size of
+  // the upsampled grid (inc/em/nbfFourierImageMetric.h:1250-1258)
+  const float bigf = (float)big;
+  float cp = (float)pk;
+  cp = cp / bigf;
+  o.dist = cp / bigf;
   int X = idx / (W * W), Y = (idx / W) % W, Z = idx % W;
   o.shift[0] = (float)((X - (W - 1) / 2.0) / 2.0f);
   o.shift[1] = (float)((Y - (W - 1) / 2.0) / 2.0f);

@@ -24,12 +24,14 @@ g++ -O2 -fPIC -std=c++17 -c "$HERE/fft64.cpp" -o "$OUT/obj/fft64.o" &
 wait
 g++ -shared -o "$OUT/libsoft_ref.so" "$OUT"/obj/*.o -lm
 echo "built $OUT/libsoft_ref.so"
-# The reference's cylindrical-domain classes (header-only), the representation-distance loop and the
-# class-selection rules, on its vendored Blitz 0.9, behind C harnesses.
+# The reference's cylindrical-domain classes (header-only), the representation-distance loop, the class-selection
+# rules and the Fourier filter / spectrum normalisation / CCF distance expressions, on its vendored Blitz 0.9,
+# behind C harnesses.
 BLITZ="$REF/external/blitz-0.9"
 if [ -d "$BLITZ/blitz" ]; then
   g++ -O2 -fPIC -std=c++11 -w -ffp-contract=off -shared -I"$BLITZ" -I"$REF/inc" \
     "$HERE/shim/cyl_ref_wrap.cpp" "$HERE/shim/repr_blitz_wrap.cpp" "$HERE/shim/clustering_blitz_wrap.cpp" \
+    "$HERE/shim/filter_blitz_wrap.cpp" \
     -o "$OUT/libblitz_ref.so"
   echo "built $OUT/libblitz_ref.so"
 fi

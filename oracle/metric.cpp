@@ -481,6 +481,38 @@ int peaks_to_queue(const OracleParams &P, std::vector<double> &C, PQ &pq) {
 
 /* ---------------------------------------------------------------- translational CCF */
 
+/* normalizeFourierHalf (inc/em/nbfCorrelationImageMetric.h:497-530): DC zeroed, norm = float(2 * sum |F|^2 over
+ * kz < H-1), then float(sqrt((norm + sum over kz = H-1) / (N N 2 (H-1)))), F /= norm. F is [N][N][H]. */
+float normalize_half(int N, cplx *F) {
+  const int H = N / 2 + 1;
+  F[((long)(N / 2) * N + N / 2) * H + (H - 1)] = 0;
+  double s1 = 0, s2 = 0;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < H; ++k) {
+        cplx f = F[((long)i * N + j) * H + k];
+        double m = (f * std::conj(f)).real();
+        if (k < H - 1) s1 += m; else s2 += m;
+      }
+  float norm = (float)(2 * s1);
+  norm = (float)sqrt((norm + s2) / (1.0 * N * N * 2 * (H - 1)));
+  const long h3 = (long)N * N * H;
+  for (long i = 0; i < h3; ++i) F[i] /= (double)norm;
+  return norm;
+}
+
+/* The distance of executeFourierNewHalf (inc/em/nbfFourierImageMetric.h:1249-1258): the peak (double expression)
+ * stored in the float correlationPeak, then divided twice in float by the int size (2N)^3 of the upsampled grid. */
+float ccf_distance(float k1_m, double maxT, double sum_wf, double sum_f, bool overlap, int N) {
+  const double peak = overlap ? std::max(0.0, (double)k1_m - maxT) / sum_wf * sum_f : std::max(0.0, (double)k1_m - maxT);
+  float cp = (float)peak;
+  const int big = 8 * N * N * N;
+  cp = cp / (float)big;
+  cp = cp / (float)big;
+  return cp;
+}
+
+
 struct CCF {
   const OracleParams &P;
   const OracleVolume &ref, &part;
@@ -498,23 +530,7 @@ struct CCF {
     wedge_half(ref, P.N, nullptr, wedge1);
   }
 
-  /* normalizeFourierHalf (inc/em/nbfCorrelationImageMetric.h:497-530) */
-  float normalize(std::vector<cplx> &F) {
-    int N = P.N, H = N / 2 + 1;
-    F[((long)(N / 2) * N + N / 2) * H + (H - 1)] = 0;
-    double s1 = 0, s2 = 0;
-    for (int i = 0; i < N; ++i)
-      for (int j = 0; j < N; ++j)
-        for (int k = 0; k < H; ++k) {
-          cplx f = F[((long)i * N + j) * H + k];
-          double m = (f * std::conj(f)).real();
-          if (k < H - 1) s1 += m; else s2 += m;
-        }
-    float norm = (float)(2 * s1);
-    norm = (float)sqrt((norm + s2) / (1.0 * N * N * 2 * (H - 1)));
-    for (auto &f : F) f /= (double)norm;
-    return norm;
-  }
+  float normalize(std::vector<cplx> &F) { return normalize_half(P.N, F.data()); }
 
   /* executeFourierNewHalf (inc/em/nbfFourierImageMetric.h:1077-1323); t is updated in place */
   float execute(M4 &t) {
@@ -623,15 +639,10 @@ struct CCF {
           if (!(radius < restriction * restriction)) T = -DBL_MAX;
           if (T > best) { best = T; bi = i; bj = j; bk = k; }
         }
-    double peak;
-    if (P.overlap_normalized && useWedge) {
-      double sw = 0;
+    double sw = 0;
+    if (P.overlap_normalized && useWedge)
       for (long i = 0; i < h3; ++i) sw += (double)(wedge[i] * filter[i]);
-      peak = std::max(0.0, (double)k1_m - best) / sw * sumFilter;
-    } else {
-      peak = std::max(0.0, (double)k1_m - best);
-    }
-    float correlationPeak = (float)(peak / big / big);
+    float correlationPeak = ccf_distance(k1_m, best, sw, sumFilter, P.overlap_normalized && useWedge, N);
     float sh[3] = {(float)((bi - (ext - 1) / 2.0) / 2.0f), (float)((bj - (ext - 1) / 2.0) / 2.0f),
                    (float)((bk - (ext - 1) / 2.0) / 2.0f)};
     double tr[16];
@@ -1519,6 +1530,15 @@ int oracle_average(const OracleParams *P, int M, const OracleVolume *vols, const
   average(*P, M, vols, weights, mats, a);
   memcpy(out, a.data(), sizeof(double) * a.size());
   return 0;
+}
+
+int oracle_normalize_half(int N, double *FRI, float *norm) {
+  *norm = normalize_half(N, reinterpret_cast<cplx *>(FRI));
+  return 0;
+}
+
+float oracle_ccf_distance(float k1_m, double maxT, double sum_wf, double sum_f, int overlap, int N) {
+  return ccf_distance(k1_m, maxT, sum_wf, sum_f, overlap != 0, N);
 }
 
 int oracle_rfft3d(int n0, int n1, int n2, const double *in, double *outRI) {

@@ -98,6 +98,10 @@ def lib():
         L.oracle_representation.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.oracle_representation_real.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
+        L.oracle_normalize_half.argtypes = [ctypes.c_int, dp, ctypes.POINTER(ctypes.c_float)]
+        L.oracle_ccf_distance.argtypes = [ctypes.c_float, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int]
+        L.oracle_ccf_distance.restype = ctypes.c_float
         L.oracle_irfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         _lib = L
     return _lib
@@ -369,6 +373,19 @@ def variance(params, vols, metas, weights, mats, avg_xyz):
     return out.reshape(N, N, N)
 
 
+def normalize_half(F):
+    """normalizeFourierHalf of a complex [N][N][N/2+1] half spectrum (a copy): (normalised spectrum, norm)."""
+    N = F.shape[0]
+    a = np.ascontiguousarray(np.stack([F.real, F.imag], -1), np.float64)
+    norm = ctypes.c_float()
+    lib().oracle_normalize_half(N, a, ctypes.byref(norm))
+    return a[..., 0] + 1j * a[..., 1], norm.value
+
+
+def ccf_distance(k1_m, maxT, sum_wf, sum_f, overlap, N):
+    return lib().oracle_ccf_distance(k1_m, maxT, sum_wf, sum_f, int(bool(overlap)), N)
+
+
 def rfft3d(x):
     x = np.ascontiguousarray(x, np.float64)
     n0, n1, n2 = x.shape
@@ -419,6 +436,12 @@ def blitz_ref_lib():
         L.repr_ref_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.clustering_ref_soft_weights.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
         L.clustering_ref_mra_assign.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.filter_ref_half.argtypes = [ctypes.c_int] + [ctypes.c_float] * 5 + [ctypes.c_void_p]
+        L.normalize_ref_half.argtypes = [ctypes.c_int, ctypes.c_void_p]
+        L.normalize_ref_half.restype = ctypes.c_float
+        L.distance_ref.argtypes = [ctypes.c_float, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_int]
+        L.distance_ref.restype = ctypes.c_float
         L.clustering_ref_cutoff.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _blitz_ref = L
@@ -481,6 +504,35 @@ def ref_cutoff(d, fraction, rule):
     L.clustering_ref_cutoff(R, V, d.ctypes.data, float(fraction), int(rule), best.ctypes.data, dist.ctypes.data,
                             keep.ctypes.data)
     return best, dist, keep.astype(bool)
+
+
+def ref_filter_half(params):
+    """The half-grid Fourier filter in the reference's Blitz expressions ([N][N][N/2+1]); None when absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    N = params["N"]
+    out = np.zeros((N, N, N // 2 + 1), np.float32)
+    L.filter_ref_half(N, params["bp_low"], params["bp_high"], params["bp_low_sigma"], params["bp_high_sigma"],
+                      params.get("bfactor", 0.0), out.ctypes.data)
+    return out
+
+
+def ref_normalize_half(F):
+    """normalizeFourierHalf in the reference's Blitz expressions (a copy): (spectrum, norm); None when absent."""
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    a = np.ascontiguousarray(np.stack([F.real, F.imag], -1), np.float64)
+    norm = L.normalize_ref_half(F.shape[0], a.ctypes.data)
+    return a[..., 0] + 1j * a[..., 1], norm
+
+
+def ref_ccf_distance(k1_m, maxT, sum_wf, sum_f, overlap, N):
+    L = blitz_ref_lib()
+    if L is None:
+        return None
+    return L.distance_ref(k1_m, maxT, sum_wf, sum_f, int(bool(overlap)), N)
 
 
 def ref_mra_assign(S):

@@ -14,11 +14,13 @@ rotsym_n16.npz the rotational-symmetry step of the classification loop run by th
 clustering.npz soft class weights, outlier cutoffs (three rules, several fractions) and the MRA class
                choice of seeded distance tables with ties, from the class-selection rules in the reference's expressions
                (oracle/_ref/libblitz_ref.so).
+filter_pins.npz the half-grid Fourier filters (band-pass, B-factor), normalizeFourierHalf of seeded spectra and the
+               CCF distance of seeded peak inputs, in the reference's own Blitz expressions (oracle/_ref/libblitz_ref.so).
 repr_dist.npz  distance matrices between seeded low-dimensional representations (depth 3 with wedge bits,
                and depth 1) from the representation-distance loop in the reference's Blitz expressions
                (oracle/_ref/libblitz_ref.so), overlap-normalised and averaged.
 
-Usage: python make_golden.py [soft|align32|align128|rotsym|repr|clustering ...]   (no argument: all)
+Usage: python make_golden.py [soft|align32|align128|rotsym|repr|clustering|pins ...]   (no argument: all)
 """
 import hashlib
 import os
@@ -92,7 +94,42 @@ def mra_inputs():
     return S
 
 
+# Fourier filters (N, low, high, low sigma, high sigma, bfactor) of the filter pin: the workloads' band-passes with and
+# without a B-factor, another band, and no band-pass at all
+FILTER_CASES = [(32, .01, .5, .01, .05, 0.0), (64, .01, .5, .01, .05, 0.0), (64, .01, .5, .01, .05, 2.0),
+                (32, .05, .3, .02, .08, .5), (16, 0.0, 1.0, .1, .1, 0.0)]
+
+
+def pin_inputs():
+    """Seeded half spectra for the normalisation pin and CCF peak inputs for the distance pin."""
+    rng = np.random.default_rng(20261204)
+    spectra = [rng.standard_normal((N, N, N // 2 + 1)) + 1j * rng.standard_normal((N, N, N // 2 + 1)) for N in (8, 16)]
+    n = 64
+    dist = {"k1_m": rng.uniform(0.5, 3.0, n).astype(np.float32), "maxT": rng.uniform(-1.0, 3.0, n),
+            "sum_wf": rng.uniform(1e3, 1e5, n), "sum_f": rng.uniform(1e5, 2e5, n),
+            "overlap": rng.integers(0, 2, n).astype(np.int32), "N": rng.choice([16, 32, 64, 128], n).astype(np.int32)}
+    return spectra, dist
+
+
 def main(which):
+    if "pins" in which:
+        spectra, dist = pin_inputs()
+        out = {}
+        for c, (N, lo, hi, lv, hv, bf) in enumerate(FILTER_CASES):
+            f = pyoracle.ref_filter_half(dict(N=N, bp_low=lo, bp_high=hi, bp_low_sigma=lv, bp_high_sigma=hv, bfactor=bf))
+            if f is None:
+                raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+            out["filter_%d" % c] = f
+        for k, F in enumerate(spectra):
+            G, norm = pyoracle.ref_normalize_half(F)
+            out["spectrum_%d" % k], out["normalized_%d" % k], out["norm_%d" % k] = F, G, np.float32(norm)
+        for key, v in dist.items():
+            out["dist_" + key] = v
+        out["distance"] = np.array([pyoracle.ref_ccf_distance(float(dist["k1_m"][i]), float(dist["maxT"][i]),
+                                                              float(dist["sum_wf"][i]), float(dist["sum_f"][i]),
+                                                              int(dist["overlap"][i]), int(dist["N"][i]))
+                                    for i in range(len(dist["N"]))], np.float32)
+        np.savez_compressed(os.path.join(HERE, "filter_pins.npz"), **out)
     if "clustering" in which:
         d = clustering_inputs()
         sw = pyoracle.ref_soft_weights(d)
@@ -146,4 +183,4 @@ def main(which):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym", "repr", "clustering"])
+    main(sys.argv[1:] or ["soft", "align32", "align128", "rotsym", "repr", "clustering", "pins"])
