@@ -62,7 +62,8 @@ SYMBOLS = [
     "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
     "ettk_gpu_representation_distances", "ettk_gpu_representations", "ettk_gpu_mra_assign",
-    "ettk_gpu_align_pairs_refined", "ettk_gpu_refined_objective",
+    "ettk_gpu_align_pairs_refined", "ettk_gpu_refined_objective", "ettk_gpu_score_pairs",
+    "ettk_gpu_average_partial", "ettk_gpu_average_finish",
 ]
 
 _lib = None
@@ -101,6 +102,9 @@ def load(path=None):
     L.ettk_gpu_align_pairs_refined.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int]
     L.ettk_gpu_refined_objective.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
+    L.ettk_gpu_score_pairs.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+    L.ettk_gpu_average_partial.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
+    L.ettk_gpu_average_finish.argtypes = [vp, vp, vp, vp, vp]
     L.ettk_gpu_classify.argtypes = [vp, ctypes.c_int, vp, vp, vp]
     L.ettk_gpu_variance.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_symmetrize.argtypes = [vp, vp, ctypes.c_int, vp]

@@ -834,6 +834,20 @@ struct ettk_ctx {
     }
   }
   void align(int npairs, const int *pairs, float *D, int cols, int ncand);
+  // translational search window of the CCF on the upsampled grid for a translation restriction
+  // (nbfFourierImageMetric.h:1216-1232): first index lo, width W, squared radius rr2
+  void set_window(float restrict_translation) {
+    const int N2 = 2 * N;
+    const float center = (float)(N2 / 2.0);
+    float restriction = center;
+    if (restrict_translation < FLT_MAX) restriction = (float)std::max((double)restrict_translation * 2.0f, 1.0);
+    lo = (int)std::max(0.0, (double)center - floor(restriction));
+    const int hi = (int)std::min((double)center + floor(restriction), (double)(N2 - 1));
+    W = hi - lo + 1;
+    rr2 = restriction * restriction;
+  }
+  // getDistances with typeOfMetric 2: one CCF per pair at the particle's own alignment
+  void score(int npairs, const int *pairs, float *D, int cols, int ncand, float restrict_translation);
   // ---------------------------------------------------------------- fast form: coarse SO(3) hit + local refinement
   DevBuf<LRItem> lr_items;
   DevBuf<LRState> lr_state;
@@ -896,6 +910,8 @@ struct ettk_ctx {
                    std::vector<double> &rho, std::vector<double> &g6);
   void refine(const std::vector<EvalReq> &req, int iterations, std::vector<Mat4> &out, std::vector<double> &rho);
   void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
+  void average_accumulate(int M, const int *parts, const float *weights, const double *mats);
+  void average_finish(float *avg);
   void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
   void symmetrize(const float *vol, int fold, float *out);
   void symmetrize_rotational(const float *vol, float *out);
@@ -915,6 +931,13 @@ struct ettk_ctx {
 // own matrix reset to identity (inc/em/nbfWedgedAverageImage3D.h:313-319), R2C, |F|-weighted FP64
 // accumulation in member order, normalised inverse, RMS scaling.
 void ettk_ctx::average(int M, const int *parts, const float *weights, const double *mats, float *avg) {
+  average_accumulate(M, parts, weights, mats);
+  average_finish(avg);
+}
+
+// Members resliced (exact coordinates, own matrix reset), transformed and accumulated in FP64 into w_w = [acc | re |
+// im | sumsq] (kz-major, h3 each), the getImageMPI accumulators (inc/em/nbfWedgedAverageImage3D.h:260-356).
+void ettk_ctx::average_accumulate(int M, const int *parts, const float *weights, const double *mats) {
   std::vector<int> idx;
   for (int i = 0; i < M; ++i) {
     if (parts[i] < 0 || parts[i] >= V) throw CudaError(ETTK_ERR_ARG, "member index out of range");
@@ -964,6 +987,13 @@ void ettk_ctx::average(int M, const int *parts, const float *weights, const doub
       post_launch();
     }
   }
+}
+
+// getImage's reciprocal-space average from the accumulators in w_w (inc/em/nbfWedgedAverageImage3D.h:216-258):
+// (re, im) / acc where acc > 0, DC zero, C2R, centring shift, RMS 1; avg N^3 floats on the host.
+void ettk_ctx::average_finish(float *avg) {
+  DevBuf<double> &ac = w_w;
+  CK(cudaMemsetAsync(ac.p + 3 * h3, 0, sizeof(double), st));
   w_cB.ensure(h3);
   w_r.ensure(n3);
   k_avg_spectrum<<<nblocks<int>(h3, 256, 4096), 256, 0, st>>>(ac.p, ac.p + h3, ac.p + 2 * h3, N, w_cB.p);
@@ -1664,14 +1694,7 @@ void ettk_ctx::init_tables() {
   bandU = (int)ceil(std::min(.5, (double)highCut) * (N2 - 1));
   double rs = floor((double)(p.restrict_rotation * (float)B) / 90.0 - 1.0);
   rstart = (int)std::max(1.0, std::min(rs, (double)(n - 1)));
-  // translational search window on the upsampled grid (nbfFourierImageMetric.h:1216-1232)
-  float center = (float)(N2 / 2.0);
-  float restriction = center;
-  if (p.restrict_translation < FLT_MAX) restriction = (float)std::max((double)p.restrict_translation * 2.0f, 1.0);
-  lo = (int)std::max(0.0, (double)center - floor(restriction));
-  int hi = (int)std::min((double)center + floor(restriction), (double)(N2 - 1));
-  W = hi - lo + 1;
-  rr2 = restriction * restriction;
+  set_window(p.restrict_translation);
   // F(m1*shift)
   Fm1.ensure(h3);
   PreProductShift pre{mask.p, nullptr, N};
@@ -2768,6 +2791,52 @@ void ettk_ctx::refined_objective(int npairs, const int *pairs, const double *pos
   }
 }
 
+// nbfFourierImageMetricCore::execute (inc/em/nbfFourierImageMetricCore.h:35-66) as getDistances runs it for
+// typeOfMetric 2 (inc/em/nbfCorrelationImageMetric.h:1912-1976): per pair one executeFourierNewHalf at the identity
+// transform of the particle (its own matrix is the alignment under test) with the given translation restriction;
+// the transform keeps the found shift when isTransformValid accepts it, else stays the identity. The core metric
+// has one candidate, so only slot 0 of each row is written (distance, scale 1, getWedgeOverlap, transform).
+void ettk_ctx::score(int npairs, const int *pairs, float *D, int cols, int ncand, float restrict_translation) {
+  HostScope hs_all(this, "host_score_wall");
+  std::vector<int> todo;
+  for (int i = 0; i < npairs; ++i)
+    if (D[(long)i * cols * ncand] == -1) todo.push_back(i);
+  if (todo.empty()) return;
+  std::vector<EvalReq> req(todo.size());
+  for (size_t k = 0; k < todo.size(); ++k) {
+    const int r = pairs[2 * todo[k]], v = pairs[2 * todo[k] + 1];
+    if (r < 0 || r >= R || v < 0 || v >= V) throw CudaError(ETTK_ERR_ARG, "pair index out of range");
+    req[k] = {r, v, Mat4::eye()};
+  }
+  // the restriction in force for this call (the reference sets the metric's and restores it afterwards)
+  struct WindowGuard {
+    ettk_ctx *c;
+    float keep;
+    ~WindowGuard() {
+      c->p.restrict_translation = keep;
+      c->set_window(keep);
+    }
+  } guard{this, p.restrict_translation};
+  if (restrict_translation >= 0) {
+    p.restrict_translation = restrict_translation;
+    set_window(restrict_translation);
+  }
+  std::vector<EvalRes> res;
+  eval_batch(req, res);
+  std::vector<EvalReq> fin(req.size());
+  for (size_t k = 0; k < req.size(); ++k) fin[k] = {req[k].ref, req[k].part, transform_valid(p, res[k].t) ? res[k].t : Mat4::eye()};
+  std::vector<float> ovl;
+  if (cols > 18) ovl = wedge_overlaps(fin);
+  for (size_t k = 0; k < req.size(); ++k) {
+    auto at = [&](int col) -> float & { return D[((long)todo[k] * cols + col) * ncand]; };
+    int off = 1;
+    at(0) = res[k].dist;
+    if (cols > 17) at(1) = 1.0f, off = 2;
+    if (cols > 18) at(2) = ovl[k], off = 3;
+    for (int m = 0; m < 16; ++m) at(m + off) = (float)fin[k].t.e[m];
+  }
+}
+
 std::vector<float> ettk_ctx::wedge_overlaps(const std::vector<EvalReq> &req) {
   const long E = (long)req.size();
   std::vector<float> out(E, 1.0f);
@@ -3210,6 +3279,14 @@ int ettk_gpu_align_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, in
   return guarded(c, [&] { c->align(npairs, pairs, D, cols, ncand); });
 }
 
+int ettk_gpu_score_pairs(ettk_ctx *c, int npairs, const int *pairs, float *D, int cols, int ncand,
+                         float restrict_translation) {
+  if (!c || npairs < 0 || (npairs && (!pairs || !D)) || cols < 17 || ncand < 1 || !(restrict_translation == restrict_translation))
+    return fail(c, ETTK_ERR_ARG, "invalid score arguments");
+  if (c->R == 0 || c->V == 0) return fail(c, ETTK_ERR_STATE, "references and particles must be set first");
+  return guarded(c, [&] { c->score(npairs, pairs, D, cols, ncand, restrict_translation); });
+}
+
 int ettk_gpu_align_pairs_refined(ettk_ctx *c, int npairs, const int *pairs, float *D, int cols, int ncand,
                                  int iterations, int peaks) {
   if (!c || npairs < 0 || (npairs && (!pairs || !D)) || cols < 17 || ncand < 1 || iterations < 0 || peaks < 0 ||
@@ -3411,6 +3488,48 @@ int ettk_gpu_average(ettk_ctx *c, int M, const int *particles, const float *weig
   if (!c || M < 0 || (M && (!particles || !weights || !matrices)) || !avg) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (c->V == 0) return fail(c, ETTK_ERR_STATE, "particles must be set first");
   return guarded(c, [&] { c->average(M, particles, weights, matrices, avg); });
+}
+
+// [x][y][kz] (the reference's half-spectrum arrays) <-> kz-major [kz][x][y]
+static void half_to_kz_major(const double *src, int N, double *dst) {
+  const int H = N / 2 + 1;
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int k = 0; k < H; ++k) dst[((size_t)k * N + x) * N + y] = src[((size_t)x * N + y) * H + k];
+}
+static void kz_major_to_half(const double *src, int N, double *dst) {
+  const int H = N / 2 + 1;
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y)
+      for (int k = 0; k < H; ++k) dst[((size_t)x * N + y) * H + k] = src[((size_t)k * N + x) * N + y];
+}
+
+int ettk_gpu_average_partial(ettk_ctx *c, int M, const int *particles, const float *weights, const double *matrices,
+                             double *re, double *im, double *acc) {
+  if (!c || M < 0 || (M && (!particles || !weights || !matrices)) || !re || !im || !acc)
+    return fail(c, ETTK_ERR_ARG, "invalid average arguments");
+  if (c->V == 0) return fail(c, ETTK_ERR_STATE, "particles must be set first");
+  return guarded(c, [&] {
+    c->average_accumulate(M, particles, weights, matrices);
+    std::vector<double> h(3 * c->h3);
+    c->d2h(h.data(), c->w_w.p, h.size() * sizeof(double));
+    kz_major_to_half(h.data(), c->N, acc);
+    kz_major_to_half(h.data() + c->h3, c->N, re);
+    kz_major_to_half(h.data() + 2 * c->h3, c->N, im);
+  });
+}
+
+int ettk_gpu_average_finish(ettk_ctx *c, const double *re, const double *im, const double *acc, float *avg) {
+  if (!c || !re || !im || !acc || !avg) return fail(c, ETTK_ERR_ARG, "invalid average arguments");
+  return guarded(c, [&] {
+    std::vector<double> h(3 * c->h3);
+    half_to_kz_major(acc, c->N, h.data());
+    half_to_kz_major(re, c->N, h.data() + c->h3);
+    half_to_kz_major(im, c->N, h.data() + 2 * c->h3);
+    c->w_w.ensure(3 * c->h3 + 1);
+    c->h2d(c->w_w.p, h.data(), h.size() * sizeof(double));
+    c->average_finish(avg);
+  });
 }
 
 int ettk_gpu_variance(ettk_ctx *c, int M, const int *parts, const float *weights, const double *mats,

@@ -1,9 +1,13 @@
-"""Replica sharding of alignment pairs across ranks (one GPU per rank).
+"""Replica sharding across ranks (one GPU per rank).
 
 The reference distributes (reference, particle) pairs to MPI workers in bundles
 (inc/em/nbfCorrelationImageMetric.h:2010-2282); pairs are independent, so here every rank aligns
 a disjoint, contiguous share of the pair list on its own GPU and rank 0 gathers the result rows
 (torch.distributed point-to-point of the small D rows; no collective on the data path).
+
+Class averages are the one place with an exchange: each rank accumulates its share of the members
+(getImageMPI's three half-spectrum accumulators) and one sum across ranks precedes the average
+(getImage), the reduction the reference performs over MPI (inc/em/nbfWedgedAverageImage3D.h:216-356).
 """
 import numpy as np
 
@@ -34,3 +38,20 @@ def gather_rows(D_local, n_pairs, rank, world, dist):
     if D_local.shape[0]:
         dist.send(torch.from_numpy(np.ascontiguousarray(D_local, np.float32)), dst=0)
     return None
+
+
+def average_across_ranks(metric, particles, weights, matrices, rank, world, dist):
+    """Class average of members spread over the ranks: this rank's contiguous share of (particles, weights,
+    matrices) accumulated by metric.average_partial, the three accumulators summed over the ranks
+    (dist.all_reduce), and the average finished on every rank by metric.average_finish."""
+    import torch
+    s, e = shard(len(particles), rank, world)
+    parts = metric.average_partial(list(particles[s:e]), list(weights[s:e]), list(matrices[s:e]))
+    summed = []
+    for a in parts:
+        t = torch.from_numpy(np.ascontiguousarray(a, np.float64))
+        if dist.get_backend() == "nccl":  # NCCL reduces device tensors
+            t = t.cuda()
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        summed.append(t.cpu().numpy())
+    return metric.average_finish(*summed)

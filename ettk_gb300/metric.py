@@ -120,16 +120,24 @@ class ProjectionRotationMetric3D:
         return self.transform
 
     # -- nbfCorrelationImageMetric::getDistances (core overload) ---------------------------------
-    def getDistances(self, indexes, D=None, cols=17, ncand=1):
+    def getDistances(self, indexes, D=None, cols=17, ncand=1, typeOfMetric=3, restrict_translation=-1.0):
         """indexes: sequence of (reference index, particle index). D: float32 (npairs, cols, ncand),
-        rows pre-filled with -1 are computed (others skipped)."""
+        rows pre-filled with -1 are computed (others skipped). typeOfMetric 3: the alignment (SO(3) search and
+        CCF candidates); 2: one CCF per pair at the particle's own alignment matrix (nbfFourierImageMetricCore) with
+        the translation restriction restrict_translation (negative: the metric's)."""
         idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
         n = idx.shape[0]
         if D is None:
             D = -np.ones((n, cols, ncand), np.float32)
         assert D.dtype == np.float32 and D.flags.c_contiguous and D.shape[0] == n
-        self._check(self.L.ettk_gpu_align_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1], D.shape[2]),
-                    "align_pairs")
+        if typeOfMetric == 2:
+            self._check(self.L.ettk_gpu_score_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1],
+                                                    D.shape[2], float(restrict_translation)), "score_pairs")
+        elif typeOfMetric == 3:
+            self._check(self.L.ettk_gpu_align_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1],
+                                                    D.shape[2]), "align_pairs")
+        else:
+            raise ValueError("typeOfMetric 2 or 3 (0, refinement on, is the fast form: getDistancesRefined)")
         return D
 
     # -- nbfWedgedAverageImage3D::setAlignments + getImage ----------------------------------------
@@ -144,6 +152,29 @@ class ProjectionRotationMetric3D:
         out = np.zeros((N, N, N), np.float32)
         self._check(self.L.ettk_gpu_average(self._ctx, n, idx.ctypes.data, w.ctypes.data, M.ctypes.data,
                                             out.ctypes.data), "average")
+        return out
+
+    def average_partial(self, particles, weights, matrices):
+        """getImageMPI's accumulators (re, im, acc), each float64 [x][y][kz] (N, N, N/2 + 1), for summing across
+        contexts or processes before average_finish."""
+        n = len(particles)
+        N = self.params["N"]
+        idx = np.ascontiguousarray(particles, np.int32)
+        w = np.ascontiguousarray(weights, np.float32)
+        M = np.ascontiguousarray(np.asarray(matrices, np.float64).reshape(n, 16))
+        out = [np.zeros((N, N, N // 2 + 1), np.float64) for _ in range(3)]
+        self._check(self.L.ettk_gpu_average_partial(self._ctx, n, idx.ctypes.data, w.ctypes.data, M.ctypes.data,
+                                                    out[0].ctypes.data, out[1].ctypes.data, out[2].ctypes.data),
+                    "average_partial")
+        return tuple(out)
+
+    def average_finish(self, re, im, acc):
+        """The class average ([z][y][x] float32, RMS 1) from summed accumulators."""
+        N = self.params["N"]
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (re, im, acc)]
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_average_finish(self._ctx, arrs[0].ctypes.data, arrs[1].ctypes.data,
+                                                   arrs[2].ctypes.data, out.ctypes.data), "average_finish")
         return out
 
     # -- nbfWedgedAverageImage3D::getImageVarianceMPI / nbfImageFilter::symmetrize -------------------------

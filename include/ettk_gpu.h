@@ -108,6 +108,16 @@ int ettk_gpu_align_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, 
 int ettk_gpu_average(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
                      float *avg);
 
+/* The class average split for members spread over several contexts or processes (getImageMPI returns its three
+ * accumulators for the caller to sum across MPI ranks before getImage, inc/em/nbfWedgedAverageImage3D.h:216-356):
+ * ettk_gpu_average_partial accumulates the members as ettk_gpu_average does and writes, in the reference's
+ * [x][y][kz] half-spectrum order (N * N * (N/2 + 1) doubles each), re = sum w |F| Re F, im = sum w |F| Im F and
+ * acc = sum |w| |F|; ettk_gpu_average_finish turns summed accumulators into the average (RMS 1, N^3 floats, x
+ * fastest). Partial over all members followed by finish gives ettk_gpu_average's result. */
+int ettk_gpu_average_partial(ettk_ctx *ctx, int M, const int *particles, const float *weights, const double *matrices,
+                             double *re, double *im, double *acc);
+int ettk_gpu_average_finish(ettk_ctx *ctx, const double *re, const double *im, const double *acc, float *avg);
+
 /* Variance of class members about an average (nbfWedgedAverageImage3D::getImageVarianceMPI after
    setAverageImage, inc/em/nbfWedgedAverageImage3D.h:440-493): var = sum over members with weight != 0 of
    |w| (T - avg)^2 / sum |w|, T the member resampled as ettk_gpu_average resamples it (getImage, mean of valid
@@ -212,6 +222,18 @@ int ettk_gpu_classify(ettk_ctx *ctx, int iterations, int *labels, float *refs_ou
    and shift, continuous). Writes the refined 4x4 pose and distance 1 - rho into the row. */
 int ettk_gpu_refine_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
                           int iterations);
+
+/* Replaces getDistances(list1, list2, indexes, D, type=2) (inc/em/nbfCorrelationImageMetric.h:1912-1976) with its
+ * nbfFourierImageMetricCore (inc/em/nbfFourierImageMetricCore.h:35-66): per pair one translational CCF
+ * (executeFourierNewHalf) of the particle under its own alignment matrix (the volume-list matrix, as doMra gives each
+ * duplicate volume one of its alignments, inc/em/nbfLoopClustering.h:1523-1561) against the reference, with the
+ * translation restriction restrict_translation (negative: the context's; doMra uses 0, which scores the given pose on
+ * the 3-point window of the upsampled grid). D as in ettk_gpu_align_pairs; only candidate slot 0 is written
+ * (the core metric keeps one candidate): the distance, scale 1, the wedge overlap at the transform, and the
+ * transform (the found shift when isTransformValid accepts it, else the identity). Rows whose D[i][0][0] != -1
+ * are skipped. */
+int ettk_gpu_score_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, int cols, int ncand,
+                         float restrict_translation);
 
 /* Fast alignment form (no counterpart in the reference; it takes the place of getDistances with typeOfMetric 0,
    whose Powell refinement, inc/em/nbfFourierImageMetric.h:1701-1809, and whose mirror and candidate CCF loop,

@@ -1532,6 +1532,12 @@ int oracle_average(const OracleParams *P, int M, const OracleVolume *vols, const
   return 0;
 }
 
+float oracle_wedge_overlap(const OracleParams *P, const OracleVolume *ref, const OracleVolume *part, const double *t16) {
+  M4 t;
+  memcpy(t.e, t16, sizeof(t.e));
+  return wedge_overlap(*P, *ref, *part, t);
+}
+
 int oracle_normalize_half(int N, double *FRI, float *norm) {
   *norm = normalize_half(N, reinterpret_cast<cplx *>(FRI));
   return 0;

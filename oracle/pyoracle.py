@@ -99,6 +99,8 @@ def lib():
         L.oracle_representation_real.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_normalize_half.argtypes = [ctypes.c_int, dp, ctypes.POINTER(ctypes.c_float)]
+        L.oracle_wedge_overlap.argtypes = [P, V, V, dp]
+        L.oracle_wedge_overlap.restype = ctypes.c_float
         L.oracle_ccf_distance.argtypes = [ctypes.c_float, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_int, ctypes.c_int]
         L.oracle_ccf_distance.restype = ctypes.c_float
@@ -164,6 +166,15 @@ def ccf(params, ref, ref_meta, part, part_meta, T):
     t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16)).copy()
     d = lib().oracle_ccf(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t)
     return float(d), t.reshape(4, 4)
+
+
+def wedge_overlap(params, ref, ref_meta, part, part_meta, T):
+    """getWedgeOverlap(T) of the pair (the D column of 19-column rows)."""
+    P = make_params(params)
+    r = make_volume(ref, ref_meta)
+    q = make_volume(part, part_meta)
+    t = np.ascontiguousarray(np.asarray(T, dtype=np.float64).reshape(16))
+    return float(lib().oracle_wedge_overlap(ctypes.byref(P), ctypes.byref(r), ctypes.byref(q), t))
 
 
 def refine_objective(params, ref, ref_meta, part, part_meta, T, theta):
