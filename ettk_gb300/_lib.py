@@ -63,7 +63,7 @@ SYMBOLS = [
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
     "ettk_gpu_representation_distances", "ettk_gpu_representations", "ettk_gpu_mra_assign",
     "ettk_gpu_align_pairs_refined", "ettk_gpu_refined_objective", "ettk_gpu_score_pairs",
-    "ettk_gpu_average_partial", "ettk_gpu_average_finish",
+    "ettk_gpu_average_partial", "ettk_gpu_average_finish", "ettk_gpu_wait_probe",
 ]
 
 _lib = None
@@ -105,6 +105,7 @@ def load(path=None):
     L.ettk_gpu_score_pairs.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
     L.ettk_gpu_average_partial.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
     L.ettk_gpu_average_finish.argtypes = [vp, vp, vp, vp, vp]
+    L.ettk_gpu_wait_probe.argtypes = [vp, ctypes.c_int]
     L.ettk_gpu_classify.argtypes = [vp, ctypes.c_int, vp, vp, vp]
     L.ettk_gpu_variance.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.ettk_gpu_symmetrize.argtypes = [vp, vp, ctypes.c_int, vp]

@@ -477,7 +477,7 @@ struct ettk_ctx {
     CK(cudaStreamSynchronize(st));
     if (h) {
       CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
-      throw CudaError(ETTK_ERR_TIMEOUT, "a bulk tensor copy did not complete in time");
+      throw CudaError(ETTK_ERR_TIMEOUT, "a bounded device wait (bulk tensor copy or tensor-core commit) ran out");
     }
   }
   DevBuf<WedgeVecs> w_wv;
@@ -809,11 +809,12 @@ struct ettk_ctx {
         CK(cudaFuncSetAttribute(k_fft2d_padded<N2>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         attr_set = true;
       }
-      k_fft2d_padded<N2><<<dim3(N2 / 2, (unsigned)P), 256, smem, st>>>(sp_F.p, sp_M.p);
+      k_fft2d_padded<N2><<<dim3(N2 / 2, (unsigned)P), 256, smem, st>>>(sp_F.p, sp_M.p, p.mutual_correlation ? 1 : 0);
       post_launch();
     }
     OpPaddedMagnitude<N2> last{sp_F.p, sp_M.p};
     last.kz0 = N2 / 2;
+    last.mutual = p.mutual_correlation ? 1 : 0;
     fft2d_t<N2>(last, P, "sphere_fft", 16.0, 1);
   }
   // |F| spherical projections of the items into Pp_out[out_index[i] * nn] (device; out_index null: [i * nn])
@@ -1737,7 +1738,8 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
     case 128: padded_magnitude_t<128>(P); break;
     default: {
       xy_kxy(N2, sp_F.p, P, -1);
-      k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h);
+      k_magnitude<<<nblocks<int>(P * big_h, 256, 8192), 256, 0, st>>>(sp_F.p, sp_M.p, P * big_h,
+                                                                        p.mutual_correlation ? 1 : 0);
       post_launch();
     }
   }
@@ -1918,7 +1920,9 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   r2c_z(N, pp, w_cB.p, E * N * N);
   with_n(N, [&](auto nn) {
     constexpr int NN = decltype(nn)::value;
-    fft2d_t<NN>(OpFwdFilter<NN>{w_cB.p, w_fw.p, HalfSums<NN>{acc2, ACC, 2}, i1}, E, "fft_xy", 20.0);
+    OpFwdFilter<NN> op{w_cB.p, w_fw.p, HalfSums<NN>{acc2, ACC, 2}, i1};
+    op.mutual = p.mutual_correlation ? 1 : 0;
+    fft2d_t<NN>(op, E, "fft_xy", 20.0);
   });
   k_norms<<<nblocks<int>(E, 128), 128, 0, st>>>(acc2, ACC, 2, N, (int)E, w_norm2.p, nullptr);
   post_launch();
@@ -3073,7 +3077,7 @@ int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **out) {
   *out = nullptr;
   const ettk_params &p = *params;
   if (!pow2(p.N) || p.N < 16 || p.N > 128 || !(p.B == 8 || p.B == 16 || p.B == 32 || p.B == 64) ||
-      p.mutual_correlation != 0 || p.candidate_peaks < 1 || p.number_of_candidates < 1 || p.wigner_precision < 0 ||
+      p.candidate_peaks < 1 || p.number_of_candidates < 1 || p.wigner_precision < 0 ||
       p.wigner_precision > WIG_FP64)
     return ETTK_ERR_ARG;
   ettk_ctx *c = new (std::nothrow) ettk_ctx;
@@ -3191,6 +3195,10 @@ int ettk_gpu_set_references(ettk_ctx *c, int R, const float *vols, const ettk_vo
     PreParticle pre{c->w_v.p, c->maskfft.p, c->w_acc.p, 2, c->N};
     c->r2c_z(c->N, pre, c->FI1.p, (long)R * c->N * c->N);
     c->xy_kxy(c->N, c->FI1.p, R, -1);
+    if (c->p.mutual_correlation) {  // executeHalf's F / |F|^(1/2), ahead of every filter the I1 branch applies
+      k_mutual_scale<<<nblocks<int>((long)R * h3, 256, 8192), 256, 0, c->st>>>(c->FI1.p, (long)R * h3);
+      c->post_launch();
+    }
     // Pp1 = cartesianToSpherical(I1)
     c->Pp1.ensure(R * c->nn);
     c->spherical_projection(items, c->Pp1.p);
@@ -3303,6 +3311,16 @@ int ettk_gpu_refined_objective(ettk_ctx *c, int npairs, const int *pairs, const 
   if (!c || npairs <= 0 || !pairs || !poses || !theta || !rho) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
   return guarded(c, [&] { c->refined_objective(npairs, pairs, poses, theta, rho, grad); });
+}
+
+int ettk_gpu_wait_probe(ettk_ctx *c, int max_iter) {
+  if (!c || max_iter < 1 || max_iter > (1 << 24)) return fail(c, ETTK_ERR_ARG, "invalid wait probe arguments");
+  return guarded(c, [&] {
+    k_wait_probe<<<1, 32, 0, c->st>>>(max_iter, c->status.p);
+    c->post_launch();
+    c->sync();
+    c->check_status();
+  });
 }
 
 int ettk_gpu_ccf(ettk_ctx *c, int r, int p, double *t, float *dist) {

@@ -148,6 +148,7 @@ struct OpPaddedMagnitude {
   float *mag;
   int sign = -1;
   int kz0 = 0;  // plane of blockIdx.x = 0 (the launch for the last plane alone uses kz0 = N2 / 2)
+  int mutual = 0;  // store |F|^(1/2) (mutual correlation)
   ETTK_DEV void begin() {}
   ETTK_DEV void rows(int kz, int &r0, int &r1) const {
     if (kz + kz0 < KXY<N2>::H - 1) {
@@ -157,7 +158,7 @@ struct OpPaddedMagnitude {
   }
   ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N2>::at(e, kz + kz0, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
-    mag[KXY<N2>::at(e, kz + kz0, i)] = sqrtf(v.x * v.x + v.y * v.y);
+    mag[KXY<N2>::at(e, kz + kz0, i)] = spectrum_magnitude(v, mutual);
   }
   ETTK_DEV void end(int, int) {}
 };
@@ -172,7 +173,8 @@ constexpr size_t fft2d_padded_smem() {
   return ((size_t)(N2 / 2) * (N2 + 1) + (size_t)(N2 / 2) * (N2 / 2 + 1)) * sizeof(float2);
 }
 template <int N2>
-__global__ void __launch_bounds__(256, 2) k_fft2d_padded(const float2 *__restrict__ d, float *__restrict__ mag) {
+__global__ void __launch_bounds__(256, 2) k_fft2d_padded(const float2 *__restrict__ d, float *__restrict__ mag,
+                                                          int mutual) {
   constexpr int R = N2 / 2, PA = N2 + 1, PB = R + 1;
   constexpr int G1 = MaxAB<N2>::v, GR1 = 256 / G1, WG1 = 32 / G1;
   constexpr int G2 = MaxAB<R>::v, GR2 = 256 / G2, WG2 = 32 / G2;
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(256, 2) k_fft2d_padded(const float2 *__restric
     for (int i = threadIdx.x; i < N2 * R; i += blockDim.x) {
       const int x = i / R, c = i - x * R;
       const float2 v = (x & 1) ? Bm[(x >> 1) * PB + c] : A[(x >> 1) * PA + c0 + c];
-      mag[KXY<N2>::at(e, kz, x * N2 + c0 + c)] = sqrtf(v.x * v.x + v.y * v.y);
+      mag[KXY<N2>::at(e, kz, x * N2 + c0 + c)] = spectrum_magnitude(v, mutual);
     }
     __syncthreads();
   }
@@ -268,10 +270,12 @@ struct OpFwdFilter {
   HalfSums<N> sums;
   const int *fw_index = nullptr;  // item whose wedge * filter applies (null: the item itself)
   int sign = -1;
+  int mutual = 0;  // F / |F|^(1/2) before the filter (executeHalf with mutual correlation)
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N>::at(e, kz, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
     const long g = KXY<N>::at(e, kz, i);
+    if (mutual) v = mutual_scale(v);
     v = cscale(v, fw[fw_index ? KXY<N>::at(fw_index[e], kz, i) : g]);
     if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
     sums.add(v);

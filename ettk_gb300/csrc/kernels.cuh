@@ -7,6 +7,16 @@
 namespace ettk {
 
 // Per-item reslice input: the fixed image, its dims and the output-index -> input-index map.
+// Diagnostic of the bounded waits: an mbarrier that nothing arrives at, polled max_iter times; the wait gives up,
+// sets *status and the kernel returns, as every bounded wait of the library does when its copy or MMA never
+// completes (the host then reports ETTK_ERR_TIMEOUT and the context stays usable).
+static __global__ void k_wait_probe(int max_iter, int *status) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (!mbar_wait(&bar, 0, max_iter) && threadIdx.x == 0) atomicExch(status, 1);
+}
+
 struct ResliceItem {
   const float *vol;
   int dims[3];
@@ -140,7 +150,8 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   const int o0 = geo[0], o1 = geo[1], o2 = geo[2], e0 = geo[3], e1 = geo[4], e2 = geo[5], mode = geo[6];
   const long n3 = (long)N * N * N;
   const int nxa = RB + ea, nxb = RB + eb, nxc = RB + ec, n_ext = (ea | eb | ec) ? nxa * nxb * nxc : 0;
-  if (mode == 2) {  // every voxel lies outside the volume: background, nothing staged, nothing summed
+  // the brick (and its faces) as background: nothing staged, nothing summed
+  auto background = [&]() {
     for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x)
       out[(long)eidx * n3 + ((long)(bx * RB + (v >> 6)) * N + (by * RB + ((v >> 3) & 7))) * N + bz * RB + (v & 7)] =
           -FLT_MAX;
@@ -149,6 +160,9 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
       if (la < RB && lb < RB && lc < RB) continue;
       it.faces[face_index(bx * RB + la, by * RB + lb, bz * RB + lc, N)] = -FLT_MAX;
     }
+  };
+  if (mode == 2) {  // every voxel lies outside the volume
+    background();
     return;
   }
   const int x0 = o0 & ~3;                        // floor to a multiple of 4
@@ -167,9 +181,14 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
       mbar_expect_tx(&tma_bar, RT_X * RT_Y * RT_Z * (uint32_t)sizeof(float));
       tma_load_3d(box4, it.tmap, x0, o1, o2, &tma_bar);
     }
-    if (!mbar_wait(&tma_bar, 0, RT_WAIT)) {
+    bool landed = mbar_wait(&tma_bar, 0, RT_WAIT);
+    if (!landed) {
       atomicExch(status, 1);
-      mbar_wait(&tma_bar, 0, RT_WAIT);  // the copy may still land: wait again (bounded) before the buffer is reused
+      landed = mbar_wait(&tma_bar, 0, RT_WAIT);  // the copy may still land: wait again (bounded)
+    }
+    if (!__syncthreads_and(landed)) {  // the box never arrived: background (the status makes the call fail), no read
+      background();
+      return;
     }
   } else if (staged) {
     // flat index -> (row, group) and row -> (y, z) by multiply-high (exact for divisors <= 64, index < 2^16)
@@ -1115,12 +1134,25 @@ struct PrePadded {
   }
 };
 
-// |F| of the (2N)^3 half spectrum (inc/em/nbfProjectionRotationMetric3D.h:321-325)
-static __global__ void k_magnitude(const float2 *__restrict__ F, float *__restrict__ M, long n) {
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-    float2 f = F[id];
-    M[id] = sqrtf(f.x * f.x + f.y * f.y);
-  }
+// |F| of the (2N)^3 half spectrum, or |F|^(1/2) with mutual correlation (inc/em/nbfProjectionRotationMetric3D.h:318-325)
+ETTK_DEV float spectrum_magnitude(float2 f, int mutual) {
+  const float m = sqrtf(f.x * f.x + f.y * f.y);
+  return mutual ? sqrtf(m) : m;
+}
+static __global__ void k_magnitude(const float2 *__restrict__ F, float *__restrict__ M, long n, int mutual) {
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x)
+    M[id] = spectrum_magnitude(F[id], mutual);
+}
+
+// nbfFourierFilter::executeHalf with mutual correlation (inc/em/nbfFourierFilter.h:590-595): F / |F|^(1/2) where
+// |F| > 0, on n spectrum values in place
+ETTK_DEV float2 mutual_scale(float2 f) {
+  const float C = sqrtf(sqrtf(f.x * f.x + f.y * f.y));
+  return C > 0.f ? make_float2(f.x / C, f.y / C) : f;
+}
+static __global__ void k_mutual_scale(float2 *__restrict__ F, long n) {
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x)
+    F[id] = mutual_scale(F[id]);
 }
 
 // Cubic resampling on radial shells through vtkSphericalTransform with wrap, summed over the

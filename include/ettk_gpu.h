@@ -28,7 +28,7 @@ enum {
   ETTK_ERR_OOM = 2,      /* device or host allocation failed (the reference exit(1)s instead,
                             inc/em/nbfProjectionRotationMetric3D.h:1093-1104) */
   ETTK_ERR_CUDA = 3,     /* a CUDA runtime call failed */
-  ETTK_ERR_TIMEOUT = 4,  /* reserved: a bounded device wait gave up */
+  ETTK_ERR_TIMEOUT = 4,  /* a bounded device wait (bulk copy, tensor-core commit) gave up; the context stays usable */
   ETTK_ERR_NAN = 5,      /* non-finite input volume */
   ETTK_ERR_STATE = 6     /* references or particles not set */
 };
@@ -51,7 +51,7 @@ typedef struct {
   int number_of_candidates;     /* nbfCorrelationImageMetric::setNumberOfCandidates */
   int wedge_compensation;       /* nbfImageMetric::setMissingWedgeCompensation */
   int overlap_normalized;       /* nbfImageMetric::setToComputeOverlapNormalizedDistances */
-  int mutual_correlation;       /* nbfImageMetric::setToUseMutualCorrelation (must be 0) */
+  int mutual_correlation;       /* nbfImageMetric::setToUseMutualCorrelation: |F|^(1/2) spherical projections, F/|F|^(1/2) in the CCF */
   int max_batch;                /* pairs aligned per device batch (0 = automatic) */
   int wigner_precision;         /* Wigner-d contraction of the SO(3) correlation (no reference setting; the
                                    reference contracts in FP64): 0 FP32 (default, parity), 1 BF16 tensor cores,
@@ -264,6 +264,11 @@ int ettk_gpu_refined_objective(ettk_ctx *ctx, int npairs, const int *pairs, cons
    rho[i] and, when grad is non-null, grad[6 i..] = d rho / d(w, d) at that perturbed pose. */
 int ettk_gpu_refine_objective(ettk_ctx *ctx, int npairs, const int *pairs, const double *poses,
                               const double *theta, double *rho, double *grad);
+
+/* Diagnostic of the bounded device waits (no counterpart in the reference): one kernel polls an mbarrier that
+ * nothing arrives at max_iter times (1 .. 2^24), gives up and flags it; the call returns ETTK_ERR_TIMEOUT, as any
+ * call whose bulk copy or tensor-core commit never completes does, and the context stays usable. */
+int ettk_gpu_wait_probe(ettk_ctx *ctx, int max_iter);
 
 /* Diagnostics (staged parity checks; no counterpart in the reference API):
  * one executeFourierNewHalf call (inc/em/nbfFourierImageMetric.h:1077-1323) of particle p against

@@ -44,6 +44,7 @@ typedef struct {
   int number_of_candidates;   /* nbfCorrelationImageMetric::numberOfCandidates */
   int wedge_compensation;     /* useMissingWedgeCompensation */
   int overlap_normalized;     /* overlapNormalizedDistances */
+  int mutual_correlation;     /* useMutualCorrelation */
 } OracleParams;
 
 typedef struct {
@@ -329,7 +330,8 @@ void cartesian_to_spherical(const OracleParams &P, const std::vector<float> &mas
         long id = x + (long)N2 * (y + (long)N2 * z);
         if (z <= N) {
           cplx f = F[((long)x * N2 + y) * H + z];
-          M[id] = sqrt((f * std::conj(f)).real());
+          /* |F|, or with mutual correlation |F|^(1/2) (cartesianToSpherical, 318-322) */
+          M[id] = P.mutual_correlation ? sqrt(sqrt((f * std::conj(f)).real())) : sqrt((f * std::conj(f)).real());
         } else {
           M[id] = A[((long)x * N2 + y) * N2 + z];
         }
@@ -547,6 +549,13 @@ struct CCF {
     }
     auto shift = [&](int i, int j, int k) { return ((i + j + k) % 2) ? -1.0 : 1.0; };
     auto apply_filter = [&](std::vector<cplx> &F) {
+      /* nbfFourierFilter::executeHalf (inc/em/nbfFourierFilter.h:586-606): with mutual correlation F / |F|^(1/2)
+       * where |F| > 0, then the filter (times the wedge) */
+      if (P.mutual_correlation)
+        for (long i = 0; i < h3; ++i) {
+          const double C = pow((F[i] * std::conj(F[i])).real(), .25);
+          if (C > 0) F[i] /= C;
+        }
       for (long i = 0; i < h3; ++i) {
         float fw = useWedge ? filter[i] * wedge[i] : filter[i];
         F[i] *= (double)fw;

@@ -27,6 +27,7 @@ class OracleParams(ctypes.Structure):
         ("restrict_translation", ctypes.c_float), ("restrict_rotation", ctypes.c_float),
         ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
         ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
+        ("mutual_correlation", ctypes.c_int),
     ]
 
 
@@ -118,7 +119,8 @@ def make_params(p):
         bp_high_sigma=p["bp_high_sigma"], bfactor=p.get("bfactor", 0.0),
         restrict_translation=p["restrict_translation"], restrict_rotation=p["restrict_rotation"],
         candidate_peaks=p["candidate_peaks"], number_of_candidates=p["number_of_candidates"],
-        wedge_compensation=int(p["wedge_compensation"]), overlap_normalized=int(p["overlap_normalized"]))
+        wedge_compensation=int(p["wedge_compensation"]), overlap_normalized=int(p["overlap_normalized"]),
+        mutual_correlation=int(bool(p.get("mutual_correlation", False))))
 
 
 def make_volume(data, meta):

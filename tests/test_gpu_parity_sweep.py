@@ -13,6 +13,8 @@ branch of the getDistances path:
   rows cut from the SO(3) peak search, inc/em/nbfProjectionRotationMetric3D.h:602);
 - a B-factor (buildBFactorHalf, inc/em/nbfFourierFilter.h:778-797);
 - distances not normalised by the overlap, and missing-wedge compensation off (inc/em/nbfImageMetric.h:151-158);
+- mutual correlation (|F|^(1/2) spherical projections, inc/em/nbfProjectionRotationMetric3D.h:318-325; F / |F|^(1/2)
+  before the CCF filter, inc/em/nbfFourierFilter.h:586-606);
 - the resume rule: rows of D whose first entry is not -1 are left as they are (getDistances 1944-1946).
 
 Criterion per pair (the parity bar of this path): the same SO(3) grid cell (rotation entries equal to 1e-5;
@@ -123,6 +125,7 @@ BRANCHES = {
     "overlap_normalisation_off": dict(overlap_normalized=False),
     "wedge_compensation_off": dict(wedge_compensation=False),
     "candidate_peaks_3": dict(candidate_peaks=3),
+    "mutual_correlation": dict(mutual_correlation=True),
 }
 
 
