@@ -156,8 +156,9 @@ def cpu_baseline(n_pairs):
     wall = time.perf_counter() - t0
     busy = max(r[0] for r in res)
     return {"value": n_pairs / busy, "unit": "alignments/s", "cores": cores, "kind": "port",
-            "sample": "%d pairs of the %s workload (64^3, B=32), one oracle process per core, %.1f s wall"
-                      % (n_pairs, WORKLOAD, wall)}
+            "sample": "%d pairs of the %s workload (64^3, B=32), one oracle process per core, %.1f s wall; "
+                      "the oracle is built -O3 and transforms with its own radix-2 FFT (the reference's FFTW3 is not "
+                      "in the image)" % (n_pairs, WORKLOAD, wall)}
 
 
 # ------------------------------------------------------------------------------- clocks
@@ -530,13 +531,14 @@ def main():
     hit = rp < 20.0
 
     hbm, tflops, peak_kind = peaks()
-    kernels = {k: v for k, v in prof.items() if not k.startswith("host_")}
+    # device families only: host_* scopes are wall-clock host time, stage_* scopes bracket several families
+    kernels = {k: v for k, v in prof.items() if not k.startswith(("host_", "stage_"))}
     dom_name, dom = max(kernels.items(), key=lambda kv: kv[1]["ms"])
     achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
     total_prof_ms = sum(v["ms"] for v in kernels.values())
     # DRAM bytes per launch of the dominant kernel: the ncu figure per volume (profiles/roofline_traffic.json,
     # dram__bytes_read.sum + dram__bytes_write.sum of a capture) scaled to this run's volumes per launch
-    traffic, alg_per_launch = None, dom["bytes"] / max(1, dom["launches"])
+    traffic, alg_per_launch, rec = None, dom["bytes"] / max(1, dom["launches"]), None
     try:
         with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
             rec = json.load(f).get(dom_name)
@@ -544,6 +546,23 @@ def main():
             traffic = rec["dram_bytes_per_volume"] * alg_per_launch / (8.0 * N ** 3)
     except (OSError, ValueError, KeyError):
         traffic = None
+    smem = None
+    if dom_name == "reslice":
+        # The tricubic gather reads 64 taps per output voxel from the staged footprint: with one shared-memory
+        # wavefront per clock per SM, a conflict-free gather takes N^3 * 64 / 32 wavefronts per volume. floor_ms is
+        # that count over the SMs at the sampled clock; frac = floor_ms / the family's time. The ncu count of shared
+        # load wavefronts per volume (bank conflicts and the staging included) gives the pipe's utilisation.
+        vols = dom["bytes"] / (8.0 * N ** 3)
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+        ideal = N ** 3 * 64 / 32
+        floor_ms = vols * ideal / (sms * mhz * 1e6) * 1e3
+        smem = {"basis": "shared-memory wavefronts, 1 per clock per SM", "ideal_wavefronts_per_volume": ideal,
+                "volumes": vols, "sms": sms, "sm_mhz": mhz, "floor_ms": floor_ms, "frac": floor_ms / dom["ms"]}
+        if rec and rec.get("smem_ld_wavefronts_per_volume"):
+            w = rec["smem_ld_wavefronts_per_volume"]
+            smem["measured_wavefronts_per_volume"] = w
+            smem["pipe_utilisation"] = vols * w / (sms * mhz * 1e6) * 1e3 / dom["ms"]
     value = world * P * a.steps / (ms * 1e-3)
     e2e = world * P * a.steps / (ms_e2e * 1e-3)
     out = {
@@ -573,7 +592,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_per_launch,
-                     "kernel_share": dom["ms"] / total_prof_ms if total_prof_ms else None,
+                     "kernel_share": dom["ms"] / total_prof_ms if total_prof_ms else None, "smem": smem,
                      "families": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                                       "GBps": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None}
                                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}},

@@ -913,6 +913,7 @@ struct ettk_ctx {
   void average(int M, const int *parts, const float *weights, const double *mats, float *avg);
   void average_accumulate(int M, const int *parts, const float *weights, const double *mats);
   void average_finish(float *avg);
+  void average_finish_device(bool xfast);
   void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
   void symmetrize(const float *vol, int fold, float *out);
   void symmetrize_rotational(const float *vol, float *out);
@@ -923,6 +924,14 @@ struct ettk_ctx {
   DevBuf<int> repr_idx_dev;
   const std::vector<int> &representation_band();
   void representations(int M, const int *parts, int fold, float *R);
+  // kept voxels ([x][y][z] offsets) of the real-space representation for a bin factor, cached
+  std::vector<int> real_idx;
+  int real_bin = 0;
+  DevBuf<int> real_idx_dev;
+  DevBuf<float> w_real;
+  const std::vector<int> &representation_real_band(int bin);
+  void real_filtered(const float *src, int E, float *dst);
+  void representations_real(int M, const int *parts, int fold, int bin, float *R);
   // members resliced as the average resamples them (own matrix reset, Euler(normal) * alignment), exact
   // coordinates, into w_v [E][x][y][z] with their valid-value sums in w_acc [E][2]
   void reslice_members(const int *idx, int E, const int *parts, const double *mats);
@@ -993,6 +1002,14 @@ void ettk_ctx::average_accumulate(int M, const int *parts, const float *weights,
 // getImage's reciprocal-space average from the accumulators in w_w (inc/em/nbfWedgedAverageImage3D.h:216-258):
 // (re, im) / acc where acc > 0, DC zero, C2R, centring shift, RMS 1; avg N^3 floats on the host.
 void ettk_ctx::average_finish(float *avg) {
+  average_finish_device(true);
+  CK(cudaMemcpyAsync(avg, w_tmp.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+  sync();
+  check_status();
+}
+
+// The same average left in w_tmp (N^3 floats, x fastest when xfast, else [x][y][z]).
+void ettk_ctx::average_finish_device(bool xfast) {
   DevBuf<double> &ac = w_w;
   CK(cudaMemsetAsync(ac.p + 3 * h3, 0, sizeof(double), st));
   w_cB.ensure(h3);
@@ -1004,11 +1021,8 @@ void ettk_ctx::average_finish(float *avg) {
   k_avg_shift_sumsq<<<nblocks<int>(n3, 256, 1024), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3);
   post_launch();
   w_tmp.ensure(n3);
-  k_avg_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3, w_tmp.p);
+  k_avg_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_r.p, N, ac.p + 3 * h3, w_tmp.p, xfast ? 1 : 0);
   post_launch();
-  CK(cudaMemcpyAsync(avg, w_tmp.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-  sync();
-  check_status();
 }
 
 void ettk_ctx::reslice_members(const int *idx, int E, const int *parts, const double *mats) {
@@ -1320,6 +1334,166 @@ void ettk_ctx::representations(int M, const int *parts, int fold, float *R) {
         r[3 * q + 2] = (F > 1 || w[((size_t)x * N + y) * H + kz] > .5f) ? 1.f : 0.f;
       }
     });
+  }
+}
+
+// The voxels kept by getLowDimensionRepresentationReal (inc/em/nbfFourierImageMetric.h:2482-2523): with an integer
+// bin factor vtkImageResample (magnification 1 / bin, cubic) samples both the image and the mask at the input
+// indices bin * i, i = 0 .. floor((N - 1) / bin), integer positions where the tricubic kernel is the voxel itself;
+// the values where the (binned) mask exceeds 0.5 are kept in the [x][y][z] order of the binned array.
+const std::vector<int> &ettk_ctx::representation_real_band(int bin) {
+  if (real_bin == bin) return real_idx;
+  std::vector<float> mh(n3);
+  d2h(mh.data(), mask.p, n3 * sizeof(float));
+  const int nb = (N - 1) / bin + 1;
+  std::vector<int> band;
+  for (int x = 0; x < nb; ++x)
+    for (int y = 0; y < nb; ++y)
+      for (int z = 0; z < nb; ++z) {
+        const int id = (x * bin * N + y * bin) * N + z * bin;
+        if (mh[id] > .5f) band.push_back(id);
+      }
+  real_idx_dev.ensure(std::max<size_t>(band.size(), 1));
+  h2d(real_idx_dev.p, band.data(), band.size() * sizeof(int));
+  real_idx.swap(band);
+  real_bin = bin;
+  return real_idx;
+}
+
+// nbfFourierFilter::executeHalf of E real images ([e][x][y][z], centring sign not applied) without a wedge:
+// dst = C2R(filter * R2C(src * shift)) * shift / N^3, [e][x][y][z].
+void ettk_ctx::real_filtered(const float *src, int E, float *dst) {
+  w_cA.ensure((long)E * h3);
+  r2c_z(N, PreProductShift{src, nullptr, N}, w_cA.p, (long)E * N * N);
+  xy_kxy(N, w_cA.p, E, -1);
+  switch (N) {
+    case 16: fft2d_t<16>(OpFilterShared<16>{w_cA.p, filter.p}, E); break;
+    case 32: fft2d_t<32>(OpFilterShared<32>{w_cA.p, filter.p}, E); break;
+    case 64: fft2d_t<64>(OpFilterShared<64>{w_cA.p, filter.p}, E); break;
+    case 128: fft2d_t<128>(OpFilterShared<128>{w_cA.p, filter.p}, E); break;
+    default: throw CudaError(ETTK_ERR_ARG, "unsupported box size for representations");
+  }
+  c2r_z(N, w_cA.p, PostStoreScaledSigned{dst, N, 1.0f / (float)n3}, (long)E * N * N);
+}
+
+// nbfFourierImageMetric::getLowDimensionRepresentationReal (inc/em/nbfFourierImageMetric.h:2375-2533), no mask file,
+// integer bin factor, for M particles. fold <= 1: A = getImage of the particle (own geometry, valid voxels minus their
+// mean, 0 elsewhere). fold > 1 (2377-2439): A = the wedged average of the particle alone under its matrix times
+// RotateZ(f * 360 / fold), f < fold, weights 1 / fold (the class average of ettk_gpu_average). A is band-pass
+// filtered (executeHalf on the real array); with fold > 1 it is then symmetrised n-fold about z
+// (nbfImageFilter::symmetrize: the mean of its getImage values as a fixed image under RotateZ(i * 360 / fold));
+// R[m][q] = A at the q-th kept voxel (representation_real_band).
+void ettk_ctx::representations_real(int M, const int *parts, int fold, int bin, float *R) {
+  const std::vector<int> &band = representation_real_band(bin);
+  const int K = (int)band.size();
+  std::vector<float> vals;
+  if (fold <= 1) {
+    const int chunk = (int)std::max(16L, std::min(256L, 256L * 64 * 64 * 64 / n3));
+    for (int c0 = 0; c0 < M; c0 += chunk) {
+      const int E = std::min(chunk, M - c0);
+      std::vector<ResliceItem> items(E);
+      for (int e = 0; e < E; ++e) {
+        const int p = parts[c0 + e];
+        double m12[12];
+        reslice_index(partg[p], N, nullptr, m12);
+        items[e].vol = part_vol(p);
+        items[e].tmap = part_map(p);
+        part_dims(items[e].dims);
+        set_map(items[e], m12);
+      }
+      w_items.ensure(E);
+      w_v.ensure((long)E * n3);
+      w_r.ensure((long)E * n3);
+      w_acc.ensure(2L * E);
+      w_real.ensure(std::max(1L, (long)E * K));
+      CK(cudaMemcpyAsync(w_items.p, items.data(), E * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+      CK(cudaMemsetAsync(w_acc.p, 0, 2L * E * sizeof(double), st));
+      reslice(w_items.p, w_v.p, w_acc.p, 2, nullptr, E);
+      // getImage values (valid voxels minus their mean, 0 elsewhere), still [e][x][y][z]
+      w_tmp.ensure((long)E * n3);
+      k_getimage_values<<<nblocks<int>((long)E * n3, 256, 8192), 256, 0, st>>>(w_v.p, w_acc.p, E, N, w_tmp.p);
+      post_launch();
+      real_filtered(w_tmp.p, E, w_r.p);
+      if (K) {
+        k_real_gather<<<nblocks<int>((long)E * K, 256, 4096), 256, 0, st>>>(w_r.p, E, n3, real_idx_dev.p, K, w_real.p);
+        post_launch();
+      }
+      vals.resize((size_t)E * K);
+      CK(cudaMemcpyAsync(vals.data(), w_real.p, vals.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+      sync();
+      check_status();
+      std::copy(vals.begin(), vals.end(), R + (size_t)c0 * K);
+    }
+    return;
+  }
+  const int F = fold;
+  std::vector<int> pp(F);
+  std::vector<float> w(F, 1.0f / (float)F);
+  std::vector<double> mats(16L * F);
+  // the rotations of the symmetrisation, applied to the filtered image as a fixed image centred at N/2
+  VolumeGeom g{};
+  g.lwedge = -90.f;
+  g.uwedge = 90.f;
+  for (int k = 0; k < 3; ++k) g.position[k] = (float)(N / 2.0);
+  for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+  std::vector<ResliceItem> sym(F);
+  for (int i = 0; i < F; ++i) {
+    Mat4 t = Mat4::eye();
+    rotate(t, i * 360.0 / F, 0, 0, 1);
+    double m12[12];
+    reslice_index(g, N, &t, m12);
+    sym[i].dims[0] = sym[i].dims[1] = sym[i].dims[2] = N;
+    sym[i].tmap = nullptr;
+    set_map(sym[i], m12);
+  }
+  const std::vector<double> acc0 = {0.0, 1.0};  // every value valid, nothing to remove
+  DevBuf<double> dacc0;
+  dacc0.ensure(2);
+  h2d(dacc0.p, acc0.data(), 2 * sizeof(double));
+  DevBuf<float> filt, fixed;
+  filt.ensure(n3);
+  fixed.ensure(n3);
+  w_real.ensure(std::max<long>(1, K));
+  vals.resize(K);
+  for (int m = 0; m < M; ++m) {
+    const int p = parts[m];
+    Mat4 own;
+    memcpy(own.e, partg[p].matrix, sizeof(own.e));
+    for (int f = 0; f < F; ++f) {
+      Mat4 t = Mat4::eye();
+      rotate(t, f * 360.0 / F, 0, 0, 1);
+      const Mat4 mf = mul(own, t);  // vtkMatrix4x4::Multiply4x4(matrix, rotation)
+      memcpy(mats.data() + 16L * f, mf.e, sizeof(mf.e));
+      pp[f] = p;
+    }
+    average_accumulate(F, pp.data(), w.data(), mats.data());
+    average_finish_device(false);  // w_tmp: the average, [x][y][z]
+    real_filtered(w_tmp.p, 1, filt.p);
+    // the filtered image as a fixed image (x fastest), resliced under the F rotations; the mean of their getImage values
+    k_getimage_fixed<<<nblocks<int>(n3, 256, 8192), 256, 0, st>>>(filt.p, dacc0.p, 1, N, fixed.p);
+    post_launch();
+    for (int i = 0; i < F; ++i) sym[i].vol = fixed.p;
+    w_items.ensure(F);
+    w_v.ensure((long)F * n3);
+    w_acc.ensure(2L * F);
+    CK(cudaMemcpyAsync(w_items.p, sym.data(), F * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w_acc.p, 0, 2L * F * sizeof(double), st));
+    {
+      Scope sc(this, "reslice", 8.0 * F * n3);
+      k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), (unsigned)F), 256, RS_SMEM, st>>>(
+          w_items.p, N, w_v.p, w_acc.p, 2, status.p, nullptr);
+      post_launch();
+    }
+    k_sym_mean<<<nblocks<int>(n3, 256, 8192), 256, 0, st>>>(w_v.p, w_acc.p, F, 1, N, filt.p);
+    post_launch();
+    if (K) {
+      k_real_gather<<<nblocks<int>((long)K, 256, 4096), 256, 0, st>>>(filt.p, 1, n3, real_idx_dev.p, K, w_real.p);
+      post_launch();
+    }
+    CK(cudaMemcpyAsync(vals.data(), w_real.p, (size_t)K * sizeof(float), cudaMemcpyDeviceToHost, st));
+    sync();
+    check_status();
+    std::copy(vals.begin(), vals.end(), R + (size_t)m * K);
   }
 }
 
@@ -3143,6 +3317,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_jobs.release();
   c->w_sjobs.release();
   c->repr_idx_dev.release();
+  c->real_idx_dev.release();
   c->w_plans.release();
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
@@ -3614,6 +3789,21 @@ int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int fold,
     for (int i = 0; i < M; ++i)
       if (particles[i] < 0 || particles[i] >= c->V) throw CudaError(ETTK_ERR_ARG, "particle index out of range");
     c->representations(M, particles, fold, R);
+  });
+}
+
+int ettk_gpu_representations_real(ettk_ctx *c, int M, const int *particles, int fold, int bin_factor, int *K,
+                                  float *R) {
+  if (!c || !K || fold < 1 || fold > 360 || bin_factor < 1 || bin_factor > 64) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (R && (M < 1 || !particles)) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] {
+    if (c->mask.p == nullptr) throw CudaError(ETTK_ERR_STATE, "context not initialised");
+    *K = (int)c->representation_real_band(bin_factor).size();
+    if (!R) return;
+    if (c->V < 1) throw CudaError(ETTK_ERR_STATE, "set particles first");
+    for (int i = 0; i < M; ++i)
+      if (particles[i] < 0 || particles[i] >= c->V) throw CudaError(ETTK_ERR_ARG, "particle index out of range");
+    c->representations_real(M, particles, fold, bin_factor, R);
   });
 }
 

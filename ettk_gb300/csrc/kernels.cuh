@@ -38,20 +38,25 @@ __host__ __device__ inline long face_index(int a, int b, int c, int N) {
 // -FLT_MAX outside [-0.5, dim-0.5] (vtkImageReslice border 1, clamp mode), plus per-item sums
 // of valid values and their count into acc[item*acc_stride + 0/1].
 //
-// One 8x8x8 output brick per CTA. The input footprint of the brick (its corner coordinates widened by
-// the cubic support and a rounding margin) is staged in shared memory. A brick whose footprint misses the
-// volume on some axis, or whose corners all lie more than a voxel beyond the valid range on one axis, is
-// background throughout and stages nothing. When the item has a tensor map and the fixed
-// RT_X x RT_Y x RT_Z box at (x0, o1, o2) lies inside the volume and holds the footprint, one bulk tensor copy
-// (TMA) stages it (bricks at the edge of the volume are faster with the tight 16-byte staging below than with
-// a zero-filled box copy and a clamping pass). Otherwise the threads stage it with 16-byte loads: the x range starts at a
-// multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge value (the clamp
-// border of the reference, exact because the x extent is a multiple of 4). For a rotation the footprint is
-// at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned volumes)
-// read the taps from global memory. A copy that does not complete sets *status (the host reports a
-// timeout) instead of waiting forever. The 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block, whose
-// rotated taps spread over more banks than a 1 x 4 x 8 row; the brick's outputs go through a small shared
-// buffer so that the stores are whole 32-byte rows.
+// One 8x8x8 output brick per CTA of 256 threads (two voxels per thread). The input footprint of the brick (its
+// corner coordinates widened by the cubic support and a rounding margin) is staged in shared memory. A brick whose
+// footprint misses the volume on some axis, or whose corners all lie more than a voxel beyond the valid range on one
+// axis, is background throughout and stages nothing. When the item has a tensor map and the fixed
+// RT_X x RT_Y x RT_Z box at (x0, o1, o2) holds the footprint, one bulk tensor copy (TMA) stages it, also at the
+// edge of the volume: the copy reads zeros outside the volume, and the voxels whose taps reach past a face read the
+// clamped positions instead (the clamp border of the reference). Items without a tensor map are staged with 16-byte
+// loads: the x range starts at a multiple of 4, and a 4-wide group that lies wholly outside the volume takes the edge
+// value (exact because the x extent is a multiple of 4), so every tap reads the box as it is. For a rotation the
+// footprint is at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned
+// volumes) read the taps from global memory. A copy that does not complete sets *status (the host reports a
+// timeout) instead of waiting forever. The 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block, whose rotated
+// taps spread over more banks than a 1 x 4 x 8 row; a thread whose two voxels both read the box as it is sums them
+// together in packed FP32x2 arithmetic; the brick's outputs go through a small shared buffer so that the stores are
+// whole 32-byte rows.
+// CTAs per SM the FP32-coordinate reslice is compiled for (four: 64 registers per thread)
+#ifndef ETTK_RESLICE_MIN_BLOCKS
+#define ETTK_RESLICE_MIN_BLOCKS 4
+#endif
 constexpr int RB = 8;             // brick edge
 constexpr int RS_MAX = 11760;     // staged floats (45.9 KiB of dynamic shared memory, four CTAs per SM)
 constexpr size_t RS_SMEM = RS_MAX * sizeof(float);
@@ -62,33 +67,181 @@ constexpr int RT_X = 28, RT_Y = 21, RT_Z = 20;
 static_assert(RT_X * RT_Y * RT_Z <= RS_MAX, "tensor box exceeds the staging buffer");
 constexpr int RT_WAIT = 1 << 22;  // polls of the copy barrier before the kernel reports a timeout
 
-// Tricubic sum with clamped taps read from global memory (bricks whose footprint is not staged).
-static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz, int ix, int iy, int iz,
-                                              float wx0, float wx1, float wx2, float wx3, float wy0, float wy1, float wy2,
-                                              float wy3, float wz0, float wz1, float wz2, float wz3) {
-  const float wy[4] = {wy0, wy1, wy2, wy3}, wz[4] = {wz0, wz1, wz2, wz3};
-  const int x_0 = min(max(ix - 1, 0), dx - 1), x_1 = min(max(ix, 0), dx - 1), x_2 = min(max(ix + 1, 0), dx - 1),
-            x_3 = min(max(ix + 2, 0), dx - 1);
+// Positions of a thread's two output voxels in the fixed image: integer cells, tricubic weights (voxel u in
+// component u of each float2, so that the pair's sums run in packed FP32x2 arithmetic) and the valid-range tests.
+struct TapPair {
+  int ix[2], iy[2], iz[2];
+  float2 wx[4], wy[4], wz[4];
+  bool inside[2];
+};
+ETTK_DEV float comp(float2 v, int u) { return u ? v.y : v.x; }
+ETTK_DEV void set_comp(float2 &v, int u, float x) {
+  if (u) v.y = x; else v.x = x;
+}
+
+// Voxel (a, b, cz) of the output as component u of T. PRECISE: the voxel coordinate follows the reference's FP64
+// sequence ((origin + c*z) + b*y) + a*x without FMA contraction and is rounded to the 2^-16 grid in FP64 (used
+// where 1e-5 output parity matters); otherwise the same sequence runs in FP32. CLAMP_ALL: every position is inside.
+template <bool PRECISE, bool CLAMP_ALL>
+ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, int b, int cz, TapPair &T, int u) {
+  float fx, fy, fz;
+  int ix, iy, iz;
+  bool inside;
+  if (PRECISE) {
+    double q[3];
+    for (int k = 0; k < 3; ++k) {
+      double w = __dadd_rn(it.md[k], __dmul_rn((double)cz, it.md[9 + k]));
+      w = __dadd_rn(w, __dmul_rn((double)b, it.md[6 + k]));
+      q[k] = __dadd_rn(w, __dmul_rn((double)a, it.md[3 + k]));
+    }
+    inside = CLAMP_ALL || !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 ||
+                            q[2] > dz - 0.5);
+    const long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0),
+                    r2 = __double2ll_rn(q[2] * 65536.0);
+    ix = (int)(r0 >> 16);
+    fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
+    iy = (int)(r1 >> 16);
+    fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
+    iz = (int)(r2 >> 16);
+    fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
+  } else {
+    float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
+    p0 = p0 + b * it.m[6];
+    p1 = p1 + b * it.m[7];
+    p2 = p2 + b * it.m[8];
+    p0 = p0 + a * it.m[3];
+    p1 = p1 + a * it.m[4];
+    p2 = p2 + a * it.m[5];
+    inside = CLAMP_ALL || !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
+    ix = vtk_floor(p0, fx);
+    iy = vtk_floor(p1, fy);
+    iz = vtk_floor(p2, fz);
+  }
+  T.ix[u] = ix;
+  T.iy[u] = iy;
+  T.iz[u] = iz;
+  T.inside[u] = inside;
+  float w[4];
+  cubic_weights(w, fx);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) set_comp(T.wx[i], u, w[i]);
+  // The reference uses only the middle row/plane when fy/fz == 0; the full 4x4x4 sum with the
+  // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
+  cubic_weights(w, fy);
+  if (!((dy > 1) && (fy != 0.f))) { w[0] = 0.f; w[1] = 1.f; w[2] = 0.f; w[3] = 0.f; }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) set_comp(T.wy[i], u, w[i]);
+  cubic_weights(w, fz);
+  if (!((dz > 1) && (fz != 0.f))) { w[0] = 0.f; w[1] = 1.f; w[2] = 0.f; w[3] = 0.f; }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) set_comp(T.wz[i], u, w[i]);
+}
+
+// The tricubic sum of every path below, in one fixed order: per row (z plane k, y row j)
+// xs = ((wx0 r0 + wx1 r1) + wx2 r2) + wx3 r3 (fused), acc += (wz_k wy_j) xs (fused).
+// Voxel u's taps read from the staged box at unclamped positions: row pitch P, plane pitch PE (floats),
+// b0 = tap (0, 0, 0).
+ETTK_DEV float tap_sum_box(const float *b0, int P, int PE, const TapPair &T, int u) {
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float *r = b0 + k * PE + j * P;
+      float xs = __fmul_rn(comp(T.wx[0], u), r[0]);
+      xs = __fmaf_rn(comp(T.wx[1], u), r[1], xs);
+      xs = __fmaf_rn(comp(T.wx[2], u), r[2], xs);
+      xs = __fmaf_rn(comp(T.wx[3], u), r[3], xs);
+      acc = __fmaf_rn(__fmul_rn(comp(T.wz[k], u), comp(T.wy[j], u)), xs, acc);
+    }
+  return acc;
+}
+// The same sum for both voxels at once in packed FP32x2 arithmetic (one instruction per pair of operations).
+ETTK_DEV float2 tap_sum_box_pair(const float *pa, const float *pb, int P, int PE, const TapPair &T) {
+  float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float *ra = pa + k * PE + j * P, *rb = pb + k * PE + j * P;
+      float2 xs = __fmul2_rn(T.wx[0], make_float2(ra[0], rb[0]));
+      xs = __ffma2_rn(T.wx[1], make_float2(ra[1], rb[1]), xs);
+      xs = __ffma2_rn(T.wx[2], make_float2(ra[2], rb[2]), xs);
+      xs = __ffma2_rn(T.wx[3], make_float2(ra[3], rb[3]), xs);
+      acc = __ffma2_rn(__fmul2_rn(T.wz[k], T.wy[j]), xs, acc);
+    }
+  return acc;
+}
+// Voxel u's taps clamped to the volume (the reference's clamp border) and read from the staged box, whose origin
+// is (x0, o1, o2): used for voxels within two voxels of a face when the box copy filled positions outside the volume.
+ETTK_DEV float tap_sum_clamped(const float *box, int x0, int o1, int o2, int P, int PE, int dx, int dy, int dz,
+                               const TapPair &T, int u) {
+  int xo[4], yo[4], zo[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    xo[i] = min(max(T.ix[u] - 1 + i, 0), dx - 1) - x0;
+    yo[i] = (min(max(T.iy[u] - 1 + i, 0), dy - 1) - o1) * P;
+    zo[i] = (min(max(T.iz[u] - 1 + i, 0), dz - 1) - o2) * PE;
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float *r = box + zo[k] + yo[j];
+      float xs = __fmul_rn(comp(T.wx[0], u), r[xo[0]]);
+      xs = __fmaf_rn(comp(T.wx[1], u), r[xo[1]], xs);
+      xs = __fmaf_rn(comp(T.wx[2], u), r[xo[2]], xs);
+      xs = __fmaf_rn(comp(T.wx[3], u), r[xo[3]], xs);
+      acc = __fmaf_rn(__fmul_rn(comp(T.wz[k], u), comp(T.wy[j], u)), xs, acc);
+    }
+  return acc;
+}
+// One voxel's cell and weights, for the global-memory path (passed by value to a function that is not inlined).
+struct ResliceTap {
+  int ix, iy, iz;
+  float wx[4], wy[4], wz[4];
+};
+ETTK_DEV ResliceTap single_tap(const TapPair &T, int u) {
+  ResliceTap t;
+  t.ix = T.ix[u];
+  t.iy = T.iy[u];
+  t.iz = T.iz[u];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    t.wx[i] = comp(T.wx[i], u);
+    t.wy[i] = comp(T.wy[i], u);
+    t.wz[i] = comp(T.wz[i], u);
+  }
+  return t;
+}
+// Taps clamped to the volume and read from global memory (bricks whose footprint is not staged).
+static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz,
+                                                     ResliceTap t) {
+  const int x_0 = min(max(t.ix - 1, 0), dx - 1), x_1 = min(max(t.ix, 0), dx - 1), x_2 = min(max(t.ix + 1, 0), dx - 1),
+            x_3 = min(max(t.ix + 2, 0), dx - 1);
   float acc = 0.f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int z = min(max(iz - 1 + k, 0), dz - 1);
+    const int z = min(max(t.iz - 1 + k, 0), dz - 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int y = min(max(iy - 1 + j, 0), dy - 1);
+      const int y = min(max(t.iy - 1 + j, 0), dy - 1);
       const float *row = vol + ((long)z * dy + y) * dx;
-      acc += (wz[k] * wy[j]) * (wx0 * __ldg(row + x_0) + wx1 * __ldg(row + x_1) + wx2 * __ldg(row + x_2) + wx3 * __ldg(row + x_3));
+      float xs = __fmul_rn(t.wx[0], __ldg(row + x_0));
+      xs = __fmaf_rn(t.wx[1], __ldg(row + x_1), xs);
+      xs = __fmaf_rn(t.wx[2], __ldg(row + x_2), xs);
+      xs = __fmaf_rn(t.wx[3], __ldg(row + x_3), xs);
+      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), xs, acc);
     }
   }
   return acc;
 }
 
-// PRECISE: the voxel coordinate follows the reference's FP64 sequence ((origin + c*z) + b*y) + a*x
-// without FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5 output parity
-// matters); otherwise the same sequence runs in FP32.
-// CLAMP_ALL: every voxel takes the clamped tricubic value (no -max background), for the continuous refinement.
+// PRECISE: FP64 voxel coordinates (reslice_tap). CLAMP_ALL: every voxel takes the clamped tricubic value (no -max
+// background), for the continuous refinement.
 template <bool PRECISE, bool CLAMP_ALL = false>
-__global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
+__global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
                                                           float *__restrict__ out, double *acc, int acc_stride,
                                                           int *status, const int *__restrict__ item_index) {
   extern __shared__ __align__(128) float4 box4[];
@@ -139,10 +292,9 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
       const int x0 = o[0] & ~3;
       int mode = 0;
       if (outside) mode = 2;
-      else if (it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && x0 >= 0 && x0 + RT_X <= dx && o[1] >= 0 &&
-               o[1] + RT_Y <= dy && o[2] >= 0 && o[2] + RT_Z <= dz && o[0] + e[0] <= x0 + RT_X && e[1] <= RT_Y &&
+      else if (it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && o[0] + e[0] <= x0 + RT_X && e[1] <= RT_Y &&
                e[2] <= RT_Z)
-        mode = 1;  // the box lies inside the volume: one bulk copy, no clamping
+        mode = 1;  // the box holds the footprint: one bulk copy (positions outside the volume read as zero)
       geo[6] = mode;
     }
   }
@@ -208,94 +360,72 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : 4) k_reslice_brick(const Re
   __syncthreads();
   float s = 0.f;
   int cnt = 0;
-  // tricubic value of output voxel (a, b, cz) from the staged footprint (or global memory); inside: valid
-  auto voxel = [&](int a, int b, int cz, bool &inside) -> float {
-    int ix, iy, iz;
-    float fx, fy, fz;
-    if (PRECISE) {
-      double q[3];
-      for (int t = 0; t < 3; ++t) {
-        double w = __dadd_rn(it.md[t], __dmul_rn((double)cz, it.md[9 + t]));
-        w = __dadd_rn(w, __dmul_rn((double)b, it.md[6 + t]));
-        q[t] = __dadd_rn(w, __dmul_rn((double)a, it.md[3 + t]));
-      }
-      inside = CLAMP_ALL || !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 || q[2] > dz - 0.5);
-      const long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0),
-                      r2 = __double2ll_rn(q[2] * 65536.0);
-      ix = (int)(r0 >> 16);
-      fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
-      iy = (int)(r1 >> 16);
-      fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
-      iz = (int)(r2 >> 16);
-      fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
-    } else {
-      float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
-      p0 = p0 + b * it.m[6];
-      p1 = p1 + b * it.m[7];
-      p2 = p2 + b * it.m[8];
-      p0 = p0 + a * it.m[3];
-      p1 = p1 + a * it.m[4];
-      p2 = p2 + a * it.m[5];
-      inside = CLAMP_ALL || !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
-      ix = vtk_floor(p0, fx);
-      iy = vtk_floor(p1, fy);
-      iz = vtk_floor(p2, fz);
-    }
-    float val = -FLT_MAX;
-    if (inside) {
-      float wx[4], wy[4], wz[4];
-      cubic_weights(wx, fx);
-      cubic_weights(wy, fy);
-      cubic_weights(wz, fz);
-      // The reference uses only the middle row/plane when fy/fz == 0; the full 4x4x4 sum with the
-      // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
-      if (!((dy > 1) && (fy != 0.f))) { wy[0] = 0.f; wy[1] = 1.f; wy[2] = 0.f; wy[3] = 0.f; }
-      if (!((dz > 1) && (fz != 0.f))) { wz[0] = 0.f; wz[1] = 1.f; wz[2] = 0.f; wz[3] = 0.f; }
-      float acc2 = 0.f;
-      if (staged) {
-        const float *b0 = box + ((iz - 1 - o2) * E1 + (iy - 1 - o1)) * P + (ix - 1 - x0);
-        const int rz = E1 * P;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const float *row = b0 + k * rz + j * P;
-            acc2 += (wz[k] * wy[j]) * (wx[0] * row[0] + wx[1] * row[1] + wx[2] * row[2] + wx[3] * row[3]);
-          }
-        }
-      } else {
-        acc2 = tricubic_global(vol, dx, dy, dz, ix, iy, iz, wx[0], wx[1], wx[2], wx[3], wy[0], wy[1], wy[2], wy[3], wz[0],
-                               wz[1], wz[2], wz[3]);
-      }
-      val = acc2;
-    }
-    return val;
+  // Box offset of voxel u's tap (0, 0, 0) and whether its 4 x 4 x 4 taps can be read from the box as they are: the
+  // 16-byte staging stores clamped values beyond the volume, the bulk copy zeros there, so its voxels within two
+  // voxels of a face read clamped positions instead (tap_sum_clamped).
+  const int PE = E1 * P;
+  auto tap_off = [&](const TapPair &T, int u) {
+    return ((T.iz[u] - 1 - o2) * E1 + (T.iy[u] - 1 - o1)) * P + (T.ix[u] - 1 - x0);
   };
-#pragma unroll 1
-  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
-    const int w = v >> 5, ln = v & 31;
-    const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
-    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
-    bool inside;
-    const float val = voxel(a, b, cz, inside);
-    if (inside) {
-      s += val;
+  auto direct = [&](const TapPair &T, int u) {
+    return staged && (!use_tma || ((unsigned)(T.ix[u] - 1) <= (unsigned)(dx - 4) &&
+                                   (unsigned)(T.iy[u] - 1) <= (unsigned)(dy - 4) &&
+                                   (unsigned)(T.iz[u] - 1) <= (unsigned)(dz - 4)));
+  };
+  // tricubic value of voxel u (-FLT_MAX outside the valid range)
+  auto value = [&](const TapPair &T, int u) -> float {
+    if (!T.inside[u]) return -FLT_MAX;
+    if (!staged) return tricubic_global(vol, dx, dy, dz, single_tap(T, u));
+    if (!direct(T, u)) return tap_sum_clamped(box, x0, o1, o2, P, PE, dx, dy, dz, T, u);
+    return use_tma ? tap_sum_box(box + tap_off(T, u), RT_X, RT_X * RT_Y, T, u) : tap_sum_box(box + tap_off(T, u), P, PE, T, u);
+  };
+  // The thread's two voxels v = tid and tid + 256; the 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block.
+  auto brick_pos = [&](int u, int &la, int &lb, int &lc) {
+    const int v = threadIdx.x + 256 * u, w = v >> 5, ln = v & 31;
+    la = 4 * (w >> 3) + (ln >> 3);
+    lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3);
+    lc = 2 * (w & 3) + (ln & 1);
+  };
+  TapPair T;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    int la, lb, lc;
+    brick_pos(u, la, lb, lc);
+    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, bx * RB + la, by * RB + lb, bz * RB + lc, T, u);
+  }
+  float val[2];
+  if (T.inside[0] && T.inside[1] && direct(T, 0) && direct(T, 1)) {
+    const float2 r = use_tma ? tap_sum_box_pair(box + tap_off(T, 0), box + tap_off(T, 1), RT_X, RT_X * RT_Y, T)
+                             : tap_sum_box_pair(box + tap_off(T, 0), box + tap_off(T, 1), P, PE, T);
+    val[0] = r.x;
+    val[1] = r.y;
+  } else {
+    val[0] = value(T, 0);
+    val[1] = value(T, 1);
+  }
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    if (T.inside[u]) {
+      s += val[u];
       cnt += 1;
     }
-    obuf[la * 66 + lb * 8 + lc] = val;
+    int la, lb, lc;
+    brick_pos(u, la, lb, lc);
+    obuf[la * 66 + lb * 8 + lc] = val[u];
   }
   __syncthreads();
   for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
-    const int la = v >> 6, lb = (v >> 3) & 7, lc = v & 7;
-    out[(long)eidx * n3 + ((long)(bx * RB + la) * N + (by * RB + lb)) * N + bz * RB + lc] = obuf[la * 66 + lb * 8 + lc];
+    const int a = v >> 6, b = (v >> 3) & 7, c = v & 7;
+    out[(long)eidx * n3 + ((long)(bx * RB + a) * N + (by * RB + b)) * N + bz * RB + c] = obuf[a * 66 + b * 8 + c];
   }
   // faces one step past the box (not part of this item's output or sums)
   for (int i = threadIdx.x; i < n_ext; i += blockDim.x) {
-    const int la = i / (nxb * nxc), lb = (i / nxc) % nxb, lc = i % nxc;
-    if (la < RB && lb < RB && lc < RB) continue;
-    bool inside;
-    const int a = bx * RB + la, b = by * RB + lb, cz = bz * RB + lc;
-    it.faces[face_index(a, b, cz, N)] = voxel(a, b, cz, inside);
+    const int fa = i / (nxb * nxc), fb = (i / nxc) % nxb, fc = i % nxc;
+    if (fa < RB && fb < RB && fc < RB) continue;
+    TapPair F;
+    const int a = bx * RB + fa, b = by * RB + fb, cz = bz * RB + fc;
+    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, a, b, cz, F, 0);
+    it.faces[face_index(a, b, cz, N)] = value(F, 0);
   }
   if (acc) {
     double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
@@ -591,6 +721,20 @@ struct PostStore {
   ETTK_DEV void end() {}
   ETTK_DEV void operator()(long line, int k, float v) { y[line * N + k] = v; }
 };
+// Store of a C2R z pass with the centring sign undone and a scale: a = C2R(F) * shift / N^3 (nbfFourierFilter::executeHalf
+// on a real array, inc/em/nbfFourierFilter.h:654-672, with scale 1 / N^3).
+struct PostStoreScaledSigned {
+  float *y;
+  int N;
+  float scale;
+  ETTK_DEV void begin() {}
+  ETTK_DEV void end() {}
+  ETTK_DEV void operator()(long line, int k, float v) {
+    const int r = (int)(line % ((long)N * N));
+    const float w = v * scale;
+    y[line * N + k] = ((((r / N) + (r % N) + k) & 1) ? -w : w);
+  }
+};
 // Pruned inverse of the zero-padded (2N)^3 half spectrum, restricted to the search window
 // [lo, lo+W) on each axis (the reference computes the whole (2N)^3 C2R, nbfFourierImageMetric.h:1204-1232,
 // and reads only this window). Same FFTW order: complex inverse along x, then y (k_pruned_fft, 2N-point
@@ -753,12 +897,23 @@ static __global__ void k_avg_shift_sumsq(float *__restrict__ y, int N, double *a
 }
 
 // divide by the RMS (float, as varianceInside) and write x-fastest
-static __global__ void k_avg_finish(const float *__restrict__ y, int N, const double *sumsq, float *__restrict__ out) {
+// out = y / RMS(y), written x fastest ([z][y][x]) when xfast, else in y's [x][y][z] order
+static __global__ void k_avg_finish(const float *__restrict__ y, int N, const double *sumsq, float *__restrict__ out,
+                                    int xfast) {
   long n3 = (long)N * N * N;
   float rms = (float)sqrt(sumsq[0] / (double)n3);
   for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < (int)n3; id += gridDim.x * blockDim.x) {
     int x = id / (N * N), yy = (id / N) % N, z = id % N;
-    out[x + (long)N * (yy + (long)N * z)] = y[id] / rms;
+    out[xfast ? x + (long)N * (yy + (long)N * z) : (long)id] = y[id] / rms;
+  }
+}
+
+// R[e][q] = v[e][idx[q]] (the kept voxels of getLowDimensionRepresentationReal, v [e][x][y][z])
+static __global__ void k_real_gather(const float *__restrict__ v, int E, long n3, const int *__restrict__ idx, int K,
+                                     float *__restrict__ R) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (long)E * K; i += (long)gridDim.x * blockDim.x) {
+    const long e = i / K;
+    R[i] = v[e * n3 + idx[i - e * K]];
   }
 }
 
@@ -781,6 +936,14 @@ static __global__ void k_sym_finish(const float *__restrict__ v, const double *_
     const int x = (int)(id / ((long)N * N)), y = (int)((id / N) % N), z = (int)(id % N);
     out[x + (long)N * (y + (long)N * z)] = (float)(s / fold);
   }
+}
+
+// getImage values of E reslices ([e][x][y][z], sums in acc[e][0..1]), in the same order.
+static __global__ void k_getimage_values(const float *__restrict__ v, const double *__restrict__ acc, int E, int N,
+                                         float *__restrict__ out) {
+  const long n3 = (long)N * N * N;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < (long)E * n3; id += (long)gridDim.x * blockDim.x)
+    out[id] = (float)get_image_value(v[id], acc + 2 * (id / n3));
 }
 
 // getImage values of E reslices ([e][x][y][z], sums in acc[e][0..1]) as fixed images [e][z][y][x] (x fastest),

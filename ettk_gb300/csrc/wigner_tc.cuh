@@ -36,7 +36,7 @@ struct WigTC {
   static constexpr size_t CAP = (size_t)228 * 1024 * NCOL / 512 + 1024;
   static constexpr size_t SMEM = OPS > CAP ? OPS : CAP;
   static_assert(n % 16 == 0 && n <= 256, "tensor-core N");
-  static_assert(SMEM >= (size_t)64 * 16 * 2 * sizeof(float), "epilogue staging fits the operand area");
+  static_assert(SMEM >= (size_t)64 * 33 * sizeof(float), "epilogue staging fits the operand area");
 };
 
 // kind::f16 / kind::tf32 instruction descriptor: D f32 (bits 4-5), A/B format (7-9, 10-12: BF16 1, TF32 2),
@@ -52,12 +52,6 @@ ETTK_DEV uint64_t wig_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
          (1ull << 46);
 }
-// element (r, k) of an R x KP K-major operand in the core-matrix layout, cores ordered [r / 8][k / KE]
-template <int KP, int KE>
-ETTK_DEV int wig_core(int r, int k) {
-  return ((r >> 3) * (KP / KE) + k / KE) * (8 * KE) + (r & 7) * KE + (k % KE);
-}
-
 template <int MODE>
 ETTK_DEV void wig_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accumulate) {
   if (MODE == WIG_TF32)
@@ -74,28 +68,42 @@ ETTK_DEV void wig_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, u
         : "memory");
 }
 
-// value x as the hi (part 0) or lo (part 1) operand of the mode
-template <int MODE>
-ETTK_DEV void wig_store(void *base, int idx, float x, int part) {
+// KE consecutive K elements of one operand row (x[0..KE-1]) as the hi (part 0) or lo (part 1) copy of the mode,
+// packed into the 16-byte core-matrix row they occupy
+template <int MODE, int KE>
+ETTK_DEV uint4 wig_pack(const float *x, int part) {
+  uint32_t w[4];
   if (MODE == WIG_TF32) {
-    uint32_t t;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(x));
-    reinterpret_cast<uint32_t *>(base)[idx] = t;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(w[e]) : "f"(x[e]));
   } else {
-    const __nv_bfloat16 hi = __float2bfloat16(x);
-    reinterpret_cast<__nv_bfloat16 *>(base)[idx] = part == 0 ? hi : __float2bfloat16(x - __bfloat162float(hi));
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      __nv_bfloat16 h[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const float v = x[2 * e + u];
+        const __nv_bfloat16 hi = __float2bfloat16(v);
+        h[u] = part == 0 ? hi : __float2bfloat16(v - __bfloat162float(hi));
+      }
+      w[e] = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
+    }
   }
+  return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // grid (cells, ceil(n_jobs / 64)), 128 threads; coef [signal][l][m >= 0], S [job][m1 mod n][m2 mod n][b].
 // A barrier that does not complete within the poll limit sets *status and leaves this tile's output unwritten.
+// Every shared-memory store is bank-conflict free: each thread writes whole 16-byte core-matrix rows, the eight
+// lanes that fill one core matrix (rows r..r+7) covering its 128 contiguous bytes, and the epilogue staging rows
+// have a pitch of 33 floats.
 template <int B, int MODE>
 __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__ coef, const SynthJob *__restrict__ jobs,
                                                       int n_jobs, const float *__restrict__ dtab,
                                                       const int *__restrict__ doff, float2 *__restrict__ S,
                                                       int *status) {
   using T = WigTC<B, MODE>;
-  constexpr int n = T::n, KP = T::KP, KE = T::KE;
+  constexpr int n = T::n, KP = T::KP, KE = T::KE, KC = KP / KE;
   extern __shared__ __align__(1024) unsigned char wig_sm[];
   unsigned char *A0 = wig_sm, *A1 = wig_sm + T::A_BYTES;                                  // A1 only for WIG_SPLIT
   unsigned char *B0 = wig_sm + T::NOPS * T::A_BYTES, *B1 = B0 + T::B_BYTES;            // B1 only for WIG_SPLIT
@@ -112,34 +120,48 @@ __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) mbar_init(&bar, 1);
-  // A: F = f(l,-m1) conj(h(l,-m2)) (-1)^(m1+m2); rows 0..63 real, 64..127 imaginary; zero beyond L and n_jobs
+  // A: F = f(l,-m1) conj(h(l,-m2)) (-1)^(m1+m2); rows 0..63 real, 64..127 imaginary; zero beyond L and n_jobs.
+  // Item i: job row jl = i % 64 (fastest, so that eight lanes fill one core matrix), K chunk tc = i / 64.
   const float sgn = ((m1 + m2) & 1) ? -1.f : 1.f;
-  for (int i = tid; i < 64 * KP; i += blockDim.x) {
-    const int jl = i / KP, t = i - jl * KP, j = j0 + jl;
-    float2 F = make_float2(0.f, 0.f);
-    if (j < n_jobs && t < L) {
-      const SynthJob jb = jobs[j];
-      const int l = l0 + t;
-      const float2 a = coef_at(coef + (long)jb.f * B * B, B, l, -m1);
-      const float2 b = coef_at(coef + (long)jb.h * B * B, B, l, -m2);
-      F = cscale(cmul(a, cconj(b)), sgn);
+  for (int i = tid; i < 64 * KC; i += blockDim.x) {
+    const int jl = i & 63, tc = i >> 6, j = j0 + jl;
+    float re[KE], im[KE];
+    const bool live = j < n_jobs;
+    SynthJob jb{};
+    if (live) jb = jobs[j];
+#pragma unroll
+    for (int e = 0; e < KE; ++e) {
+      const int t = tc * KE + e;
+      float2 F = make_float2(0.f, 0.f);
+      if (live && t < L) {
+        const float2 a = coef_at(coef + (long)jb.f * B * B, B, l0 + t, -m1);
+        const float2 b = coef_at(coef + (long)jb.h * B * B, B, l0 + t, -m2);
+        F = cscale(cmul(a, cconj(b)), sgn);
+      }
+      re[e] = F.x;
+      im[e] = F.y;
     }
-    const int ir = wig_core<KP, KE>(jl, t), ii = wig_core<KP, KE>(64 + jl, t);
-    wig_store<MODE>(A0, ir, F.x, 0);
-    wig_store<MODE>(A0, ii, F.y, 0);
+    const int cr = ((jl >> 3) * KC + tc) * 8 + (jl & 7), ci = (((64 + jl) >> 3) * KC + tc) * 8 + (jl & 7);
+    reinterpret_cast<uint4 *>(A0)[cr] = wig_pack<MODE, KE>(re, 0);
+    reinterpret_cast<uint4 *>(A0)[ci] = wig_pack<MODE, KE>(im, 0);
     if (MODE == WIG_SPLIT) {
-      wig_store<MODE>(A1, ir, F.x, 1);
-      wig_store<MODE>(A1, ii, F.y, 1);
+      reinterpret_cast<uint4 *>(A1)[cr] = wig_pack<MODE, KE>(re, 1);
+      reinterpret_cast<uint4 *>(A1)[ci] = wig_pack<MODE, KE>(im, 1);
     }
   }
-  // B: d~^l(beta_b), row b, column t
+  // B: d~^l(beta_b), row b, column t; item i: b = i % n, K chunk tc = i / n
   const float *d = dtab + doff[cell];
-  for (int i = tid; i < n * KP; i += blockDim.x) {
-    const int b = i / KP, t = i - b * KP;
-    const float v = t < L ? d[t * n + b] : 0.f;
-    const int ib = wig_core<KP, KE>(b, t);
-    wig_store<MODE>(B0, ib, v, 0);
-    if (MODE == WIG_SPLIT) wig_store<MODE>(B1, ib, v, 1);
+  for (int i = tid; i < n * KC; i += blockDim.x) {
+    const int b = i % n, tc = i / n;
+    float v[KE];
+#pragma unroll
+    for (int e = 0; e < KE; ++e) {
+      const int t = tc * KE + e;
+      v[e] = t < L ? d[t * n + b] : 0.f;
+    }
+    const int cb = ((b >> 3) * KC + tc) * 8 + (b & 7);
+    reinterpret_cast<uint4 *>(B0)[cb] = wig_pack<MODE, KE>(v, 0);
+    if (MODE == WIG_SPLIT) reinterpret_cast<uint4 *>(B1)[cb] = wig_pack<MODE, KE>(v, 1);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -169,7 +191,8 @@ __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
     // 16 accumulator columns (beta) at a time: tcgen05.ld of the thread's row (job jl, real or imaginary part),
-    // staged in the operand area (free once the MMAs completed) as [jl][beta][re, im], then written as whole
+    // staged in the operand area (free once the MMAs completed) as [jl][beta][re, im] with a row pitch of 33 floats
+    // (the 32 lanes of a warp, 32 consecutive jl, store to 32 distinct banks), then written as whole
     // 128-byte runs S[job][m1][m2][beta .. beta + 15]
     const int row = warp * 32 + lane, jl = row & 63, comp = row >> 6;
     const int mm1 = (m1 + n) % n, mm2 = (m2 + n) % n;
@@ -186,12 +209,12 @@ __global__ void __launch_bounds__(128) k_so3_synth_tc(const float2 *__restrict__
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       __syncthreads();  // the previous chunk's stores have read the staging area
 #pragma unroll
-      for (int q = 0; q < 16; ++q) stg[(jl * 16 + q) * 2 + comp] = __uint_as_float(r[q]);
+      for (int q = 0; q < 16; ++q) stg[jl * 33 + q * 2 + comp] = __uint_as_float(r[q]);
       __syncthreads();
       for (int t = tid; t < 64 * 16; t += blockDim.x) {
         const int jt = t >> 4, q = t & 15, j = j0 + jt;
         if (j < n_jobs)
-          S[(((long)j * n + mm1) * n + mm2) * n + c0 + q] = make_float2(stg[(jt * 16 + q) * 2], stg[(jt * 16 + q) * 2 + 1]);
+          S[(((long)j * n + mm1) * n + mm2) * n + c0 + q] = make_float2(stg[jt * 33 + q * 2], stg[jt * 33 + q * 2 + 1]);
       }
     }
   }

@@ -211,6 +211,18 @@ class ProjectionRotationMetric3D:
                                                     R.ctypes.data), "representations")
         return R
 
+    def representations_real(self, particles, fold=1, bin_factor=1):
+        """getLowDimensionRepresentationReal of the given particles (the n-fold branch through the one-member wedged
+        average when fold > 1; integer bin factor): (M, K, 1) float32, the depth-1 representation array."""
+        p = np.ascontiguousarray(np.asarray(particles, np.int32))
+        K = ctypes.c_int()
+        self._check(self.L.ettk_gpu_representations_real(self._ctx, 0, None, int(fold), int(bin_factor),
+                                                         ctypes.byref(K), None), "representations_real")
+        R = np.zeros((len(p), K.value, 1), np.float32)
+        self._check(self.L.ettk_gpu_representations_real(self._ctx, len(p), p.ctypes.data, int(fold), int(bin_factor),
+                                                         ctypes.byref(K), R.ctypes.data), "representations_real")
+        return R
+
     def representation_distances(self, R, overlap_normalized=None):
         """nbfCorrelationImageMetric::getDistances(representations, D): R is (V, K, 3) (re, im, wedge bit) or
         (V, K, 1) float32; returns the symmetric (V, V) distance matrix."""

@@ -141,6 +141,20 @@ int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
    floats, the representation array R(M, K, 3) of ettk_gpu_representation_distances. */
 int ettk_gpu_representations(ettk_ctx *ctx, int M, const int *particles, int fold, int *K, float *R);
 
+/* Real-space low-dimensional representations of particles (nbfFourierImageMetric::getLowDimensionRepresentationReal,
+   inc/em/nbfFourierImageMetric.h:2375-2533, as nbfCorrelationImageMetric::getRepresentations collects them with
+   useRealRepresentation, inc/em/nbfCorrelationImageMetric.h:1341-1352; no mask file): per particle its image (own
+   geometry, mean of valid voxels removed) or, with fold > 1, the wedged average of the particle alone under its matrix
+   times RotateZ(f * 360 / fold) for f < fold (weights 1 / fold, as ettk_gpu_average); band-pass filtered
+   (nbfFourierFilter::executeHalf on the real array: C2R(filter R2C(A shift)) shift / N^3); with fold > 1 then
+   symmetrised n-fold about z (as ettk_gpu_symmetrize); binned by the integer bin_factor (vtkImageResample with
+   magnification 1 / bin_factor: samples at input indices bin_factor * i, i <= (N - 1) / bin_factor, of the image and
+   of the mask alike); the values where the binned mask exceeds 0.5 are kept in [x][y][z] order. fold 1..360,
+   bin_factor 1..64. *K receives K (the call with R = NULL only does that); R receives M * K floats, the depth-1
+   representation array R(M, K, 1) of ettk_gpu_representation_distances. */
+int ettk_gpu_representations_real(ettk_ctx *ctx, int M, const int *particles, int fold, int bin_factor, int *K,
+                                  float *R);
+
 /* Distance matrix between low-dimensional representations (nbfCorrelationImageMetric::getDistances(file, D),
    inc/em/nbfCorrelationImageMetric.h:1726-1871, the pairwise step of the unsupervised classification). R is
    the reference's representation array R(V, K, depth) in C order: depth 3 = (re, im, wedge bit) of the K kept

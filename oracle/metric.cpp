@@ -1310,19 +1310,37 @@ int oracle_representation(const OracleParams *P, const OracleVolume *v, int fold
   return 0;
 }
 
-/* nbfFourierImageMetric::getLowDimensionRepresentationReal (inc/em/nbfFourierImageMetric.h:2375-2533) with
- * bin_factor 1 and no mask file (the image filter's own mask): A = getImage of the volume; A = C2R(filter *
- * R2C(A * shift)) * shift / N^3 (nbfFourierFilter::executeHalf on a real array, inc/em/nbfFourierFilter.h:654-672);
- * with fold > 1 nbfImageFilter::symmetrize(A, fold) (as oracle_representation does it); the kept values are
- * those where the mask exceeds 0.5, in the [x][y][z] order of the array. C (optional): K doubles; *K their
- * number. (The reference's n-fold branch first symmetrises through a one-member average, 2377-2439; that branch
- * is not restated.) */
-int oracle_representation_real(const OracleParams *P, const OracleVolume *v, int fold, double *C, int *K) {
+/* nbfFourierImageMetric::getLowDimensionRepresentationReal (inc/em/nbfFourierImageMetric.h:2375-2533) with no mask
+ * file (the image filter's own mask):
+ *  - fold > 1 (2377-2439): A = the wedged average of the one volume under the fold alignments matrix * RotateZ(f * 360
+ *    / fold) (vtkMatrix4x4::Multiply4x4(matrix, rotation)), weights 1 / fold (float), as `average` computes it;
+ *    otherwise A = getImage of the volume;
+ *  - A = C2R(filter * R2C(A * shift)) * shift / N^3 (nbfFourierFilter::executeHalf on a real array,
+ *    inc/em/nbfFourierFilter.h:654-672);
+ *  - fold > 1: nbfImageFilter::symmetrize(A, fold) (A cast to float as a fixed image, as oracle_representation);
+ *  - binning by the integer factor bin (vtkImageResample with magnification 1 / bin, cubic: output extent
+ *    [0, floor((N - 1) / bin)], sample i at input index bin * i, an integer position where the tricubic kernel reduces
+ *    to the voxel itself), of A and of the mask alike;
+ *  - the kept values are those where the (binned) mask exceeds 0.5, in the [x][y][z] order of the array.
+ * C (optional): K doubles; *K their number. */
+int oracle_representation_real(const OracleParams *P, const OracleVolume *v, int fold, int bin, double *C, int *K) {
   const int N = P->N, H = N / 2 + 1;
   const long n3 = (long)N * N * N, h3 = (long)N * N * H;
-  if (fold > 1) return 1;
+  if (bin < 1) return 1;
   std::vector<double> a;
-  get_image(*v, N, nullptr, a);
+  if (fold > 1) {
+    std::vector<OracleVolume> vols(fold, *v);
+    std::vector<float> w(fold, 1.0f / (float)fold);
+    std::vector<double> mats(16L * fold);
+    for (int f = 0; f < fold; ++f) {
+      M4 t = m4_identity();
+      m4_rotate_pre(t, f * 360.0 / fold, 0, 0, 1);
+      m4_mul(v->matrix, t.e, mats.data() + 16L * f);
+    }
+    average(*P, fold, vols.data(), w.data(), mats.data(), a);
+  } else {
+    get_image(*v, N, nullptr, a);
+  }
   auto shift = [&](long id) {
     const long x = id / ((long)N * N), y = (id / N) % N, z = id % N;
     return ((x + y + z) & 1) ? -1.0 : 1.0;
@@ -1336,12 +1354,32 @@ int oracle_representation_real(const OracleParams *P, const OracleVolume *v, int
   for (long i = 0; i < h3; ++i) F[i] *= (double)f[i];
   irfft3d(F.data(), a.data(), N, N, N);
   for (long i = 0; i < n3; ++i) a[i] = a[i] * shift(i) / (double)n3;
+  if (fold > 1) {
+    std::vector<float> fx(n3);
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) fx[x + (long)N * (y + (long)N * z)] = (float)a[((long)x * N + y) * N + z];
+    OracleVolume fv;
+    memset(&fv, 0, sizeof(fv));
+    fv.data = fx.data();
+    fv.dims[0] = fv.dims[1] = fv.dims[2] = N;
+    fv.lwedge = -90.f;
+    fv.uwedge = 90.f;
+    for (int k = 0; k < 16; ++k) fv.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    for (int k = 0; k < 3; ++k) fv.position[k] = (float)(N / 2.0);
+    oracle_symmetrize(P, &fv, fold, a.data());
+  }
+  const int nb = (N - 1) / bin + 1;
   int k = 0;
-  for (long i = 0; i < n3; ++i)
-    if (mask[i] > .5) {
-      if (C) C[k] = a[i];
-      ++k;
-    }
+  for (int x = 0; x < nb; ++x)
+    for (int y = 0; y < nb; ++y)
+      for (int z = 0; z < nb; ++z) {
+        const long id = ((long)x * bin * N + (long)y * bin) * N + (long)z * bin;
+        if (mask[id] > .5) {
+          if (C) C[k] = a[id];
+          ++k;
+        }
+      }
   *K = k;
   return 0;
 }

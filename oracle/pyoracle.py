@@ -97,7 +97,8 @@ def lib():
         L.oracle_representation_distances.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int,
                                                                             ctypes.c_void_p]
         L.oracle_representation.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
-        L.oracle_representation_real.argtypes = [P, V, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.oracle_representation_real.argtypes = [P, V, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                 ctypes.POINTER(ctypes.c_int)]
         L.oracle_rfft3d.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.oracle_normalize_half.argtypes = [ctypes.c_int, dp, ctypes.POINTER(ctypes.c_float)]
         L.oracle_wedge_overlap.argtypes = [P, V, V, dp]
@@ -313,15 +314,18 @@ def representation(params, vol, meta, fold=1):
     return R
 
 
-def representation_real(params, vol, meta):
-    """getLowDimensionRepresentationReal of one volume (bin factor 1, the image filter's mask): (K,) float64."""
+def representation_real(params, vol, meta, fold=1, bin_factor=1):
+    """getLowDimensionRepresentationReal of one volume (the image filter's mask; n-fold branch through the one-member
+    wedged average; integer bin factor): (K,) float64."""
     P = make_params(params)
     v = make_volume(vol, meta)
     K = ctypes.c_int()
-    if lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), 1, None, ctypes.byref(K)) != 0:
+    if lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), int(fold), int(bin_factor), None,
+                                        ctypes.byref(K)) != 0:
         raise ValueError("unsupported")
     C = np.zeros(K.value, np.float64)
-    lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), 1, C.ctypes.data, ctypes.byref(K))
+    lib().oracle_representation_real(ctypes.byref(P), ctypes.byref(v), int(fold), int(bin_factor), C.ctypes.data,
+                                     ctypes.byref(K))
     return C
 
 

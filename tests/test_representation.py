@@ -160,3 +160,63 @@ def test_oracle_real_representation(ds32):
     assert np.abs(C - expect).max() <= 1e-9 * np.abs(expect).max()
     C2 = pyoracle.representation_real(p, 3 * ds32.particles[0] + 1.5, ds32.meta[0])
     assert np.abs(C2 - 3 * C).max() <= 1e-6 * np.abs(C).max()
+
+
+def _rot_z(deg):
+    """vtkTransform::RotateZ(deg) as a 4x4 matrix."""
+    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
+    T = np.eye(4)
+    T[:2, :2] = [[c, -s], [s, c]]
+    return T
+
+
+def test_oracle_real_representation_bin_and_fold(ds32):
+    """getLowDimensionRepresentationReal's other branches in the oracle: binning by 2 keeps the bin-1 image's values at
+    the even indices where the mask at those indices exceeds 0.5; the n-fold branch equals the composition of the
+    one-member wedged average (weights 1 / fold, matrix * RotateZ(f * 360 / fold)), the band-pass filter and the
+    n-fold symmetrisation of the filtered image."""
+    p = ds32.params
+    N = p["N"]
+    vol, meta = ds32.particles[1], ds32.meta[1]
+    m, _, f = pyoracle.masks(p)
+    x, y, z = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    s = np.where((x + y + z) % 2, -1.0, 1.0)
+
+    def filt(img):
+        return np.fft.irfftn(np.fft.rfftn(img * s) * f, s=(N, N, N), axes=(0, 1, 2)) * s
+
+    e = filt(pyoracle.get_image(p, vol, meta))
+    C2 = pyoracle.representation_real(p, vol, meta, bin_factor=2)
+    keep = m[::2, ::2, ::2] > 0.5
+    assert C2.shape == (int(keep.sum()),)
+    assert np.abs(C2 - e[::2, ::2, ::2][keep]).max() <= 1e-9 * np.abs(C2).max()
+    fold = 3
+    M0 = np.asarray(meta["matrix"], np.float64).reshape(4, 4)
+    mats = [M0 @ _rot_z(k * 360.0 / fold) for k in range(fold)]
+    avg = pyoracle.average(p, [vol] * fold, [meta] * fold, [np.float32(1.0 / fold)] * fold, mats)
+    fa = filt(avg)
+    sym = pyoracle.symmetrize(p, np.ascontiguousarray(fa.transpose(2, 1, 0)).astype(np.float32), fold)
+    C3 = pyoracle.representation_real(p, vol, meta, fold=fold)
+    assert np.abs(C3 - sym[m > 0.5]).max() <= 1e-6 * np.abs(C3).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fold,bin_factor", [(1, 1), (1, 2), (3, 1), (2, 2)])
+def test_gpu_representations_real(ds32, fold, bin_factor):
+    """ettk_gpu_representations_real against the oracle (FP32 transforms and reslices against FP64): within 5e-5 of
+    the largest value for the plain image, 2e-4 through the n-fold branch's average and symmetrisation; the kept voxels
+    (how many, in which order) exactly; distances of the depth-1 array bit-exact against the oracle's loop."""
+    n = len(ds32.meta)
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        m.set_particles([WedgedSubImage3D(ds32.particles[i], **{k: ds32.meta[i][k] for k in KW}) for i in range(n)])
+        g = m.representations_real([2, 0, 3], fold=fold, bin_factor=bin_factor)
+        D = m.representation_distances(g)
+    finally:
+        m.close()
+    o = np.stack([pyoracle.representation_real(ds32.params, ds32.particles[i], ds32.meta[i], fold=fold,
+                                               bin_factor=bin_factor) for i in (2, 0, 3)])
+    assert g.shape == o.shape + (1,)
+    tol = 5e-5 if fold == 1 else 2e-4
+    assert np.abs(g[:, :, 0] - o).max() <= tol * np.abs(o).max()
+    assert np.array_equal(D, pyoracle.representation_distances(g, True))
