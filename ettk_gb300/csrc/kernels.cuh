@@ -293,8 +293,14 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
       int mode = 0;
       if (outside) mode = 2;
       else if (it.tmap != nullptr && (smem_addr(box4) & 127) == 0 && o[0] + e[0] <= x0 + RT_X && e[1] <= RT_Y &&
-               e[2] <= RT_Z)
-        mode = 1;  // the box holds the footprint: one bulk copy (positions outside the volume read as zero)
+               e[2] <= RT_Z &&
+               (!CLAMP_ALL || (x0 >= 0 && x0 + RT_X <= dx && o[1] >= 0 && o[1] + RT_Y <= dy && o[2] >= 0 &&
+                               o[2] + RT_Z <= dz)))
+        // the box holds the footprint: one bulk copy (positions outside the volume read as zero). The clamped taps
+        // of a voxel in the valid range lie in [floor(p) - 1, floor(p) + 2] and so in the footprint; with CLAMP_ALL
+        // a voxel far outside the volume would clamp to positions outside the box, so there the box must lie inside
+        // the volume (every tap then reads the box as it is).
+        mode = 1;
       geo[6] = mode;
     }
   }
