@@ -916,6 +916,7 @@ struct ettk_ctx {
   void average_finish_device(bool xfast);
   void variance(int M, const int *parts, const float *weights, const double *mats, const float *avg, float *var);
   void symmetrize(const float *vol, int fold, float *out);
+  void mean_images(const float *vol, int n, const Mat4 *ts, float *out);
   void symmetrize_rotational(const float *vol, float *out);
   void average_spherical_wedge(int M, const int *parts, const float *weights, const double *mats, float *count,
                                float *wedge);
@@ -1092,6 +1093,18 @@ void ettk_ctx::symmetrize(const float *vol, int fold, float *out) {
     memcpy(out, vol, n3 * sizeof(float));
     return;
   }
+  std::vector<Mat4> ts(fold);
+  for (int i = 0; i < fold; ++i) {
+    ts[i] = Mat4::eye();
+    rotate(ts[i], i * 360.0 / fold, 0, 0, 1);
+  }
+  mean_images(vol, fold, ts.data(), out);
+}
+
+// The mean over n transforms of getImage of vol as a fixed image (nbfWedgedSubImage3D::getImage with
+// setFixedImage: position N/2, no normal, identity matrix, full wedge): each a tricubic reslice with the mean of its
+// valid voxels removed and the invalid ones 0, summed in order in FP64 and divided by n. vol and out are x fastest.
+void ettk_ctx::mean_images(const float *vol, int n, const Mat4 *ts, float *out) {
   w_tmp.ensure(n3);
   CK(cudaMemcpyAsync(w_tmp.p, vol, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
   VolumeGeom g{};  // fixed image: position N/2, no normal, identity matrix, no cut offset, full wedge
@@ -1099,30 +1112,28 @@ void ettk_ctx::symmetrize(const float *vol, int fold, float *out) {
   g.uwedge = 90.f;
   for (int k = 0; k < 3; ++k) g.position[k] = (float)(N / 2.0);
   for (int k = 0; k < 16; ++k) g.matrix[k] = (k % 5 == 0) ? 1.0 : 0.0;
-  std::vector<ResliceItem> items(fold);
-  for (int i = 0; i < fold; ++i) {
-    Mat4 t = Mat4::eye();
-    rotate(t, i * 360.0 / fold, 0, 0, 1);
+  std::vector<ResliceItem> items(n);
+  for (int i = 0; i < n; ++i) {
     double m12[12];
-    reslice_index(g, N, &t, m12);
+    reslice_index(g, N, &ts[i], m12);
     items[i].vol = w_tmp.p;
     items[i].tmap = nullptr;
     items[i].dims[0] = items[i].dims[1] = items[i].dims[2] = N;
     set_map(items[i], m12);
   }
-  w_items.ensure(fold);
-  w_v.ensure((long)fold * n3);
-  w_acc.ensure(2L * fold);
-  CK(cudaMemcpyAsync(w_items.p, items.data(), fold * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(w_acc.p, 0, 2L * fold * sizeof(double), st));
+  w_items.ensure(n);
+  w_v.ensure((long)n * n3);
+  w_acc.ensure(2L * n);
+  CK(cudaMemcpyAsync(w_items.p, items.data(), n * sizeof(ResliceItem), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(w_acc.p, 0, 2L * n * sizeof(double), st));
   {
-    Scope sc(this, "reslice", 8.0 * fold * n3);
-    k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), fold), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p,
-                                                                                           2, status.p, nullptr);
+    Scope sc(this, "reslice", 8.0 * n * n3);
+    k_reslice_brick<true><<<dim3((N / RB) * (N / RB) * (N / RB), n), 256, RS_SMEM, st>>>(w_items.p, N, w_v.p, w_acc.p,
+                                                                                        2, status.p, nullptr);
     post_launch();
   }
   w_r.ensure(n3);
-  k_sym_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_v.p, w_acc.p, fold, N, w_r.p);
+  k_sym_finish<<<nblocks<int>(n3, 256, 4096), 256, 0, st>>>(w_v.p, w_acc.p, n, N, w_r.p);
   post_launch();
   CK(cudaMemcpyAsync(out, w_r.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, st));
   sync();
@@ -3737,6 +3748,18 @@ int ettk_gpu_symmetrize(ettk_ctx *c, const float *vol, int fold, float *out) {
   if (!c || !vol || !out || fold < 1 || fold > 360) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
   return guarded(c, [&] { c->symmetrize(vol, fold, out); });
+}
+
+int ettk_gpu_mean_images(ettk_ctx *c, const float *vol, int n, const double *transforms, float *out) {
+  if (!c || !vol || !out || !transforms || n < 1 || n > 4096) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (!finite_volume(vol, c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite volume");
+  for (long k = 0; k < 16L * n; ++k)
+    if (!std::isfinite(transforms[k])) return fail(c, ETTK_ERR_NAN, "non-finite transform");
+  return guarded(c, [&] {
+    std::vector<Mat4> ts(n);
+    for (int i = 0; i < n; ++i) memcpy(ts[i].e, transforms + 16L * i, sizeof(ts[i].e));
+    c->mean_images(vol, n, ts.data(), out);
+  });
 }
 
 int ettk_gpu_representation_distances(ettk_ctx *c, int V, int K, int depth, const float *R, int overlap_normalized,

@@ -50,9 +50,8 @@ __host__ __device__ inline long face_index(int a, int b, int c, int N) {
 // footprint is at most 20 x 20 rows of 24 floats, which RS_MAX holds; other bricks (scaled matrices, unaligned
 // volumes) read the taps from global memory. A copy that does not complete sets *status (the host reports a
 // timeout) instead of waiting forever. The 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block, whose rotated
-// taps spread over more banks than a 1 x 4 x 8 row; a thread whose two voxels both read the box as it is sums them
-// together in packed FP32x2 arithmetic; the brick's outputs go through a small shared buffer so that the stores are
-// whole 32-byte rows.
+// taps spread over more banks than a 1 x 4 x 8 row; the brick's outputs go through a small shared buffer so that
+// the stores are whole 32-byte rows.
 // CTAs per SM the FP32-coordinate reslice is compiled for (four: 64 registers per thread)
 #ifndef ETTK_RESLICE_MIN_BLOCKS
 #define ETTK_RESLICE_MIN_BLOCKS 4
@@ -67,26 +66,19 @@ constexpr int RT_X = 28, RT_Y = 21, RT_Z = 20;
 static_assert(RT_X * RT_Y * RT_Z <= RS_MAX, "tensor box exceeds the staging buffer");
 constexpr int RT_WAIT = 1 << 22;  // polls of the copy barrier before the kernel reports a timeout
 
-// Positions of a thread's two output voxels in the fixed image: integer cells, tricubic weights (voxel u in
-// component u of each float2, so that the pair's sums run in packed FP32x2 arithmetic) and the valid-range tests.
-struct TapPair {
-  int ix[2], iy[2], iz[2];
-  float2 wx[4], wy[4], wz[4];
-  bool inside[2];
-};
-ETTK_DEV float comp(float2 v, int u) { return u ? v.y : v.x; }
-ETTK_DEV void set_comp(float2 &v, int u, float x) {
-  if (u) v.y = x; else v.x = x;
-}
-
-// Voxel (a, b, cz) of the output as component u of T. PRECISE: the voxel coordinate follows the reference's FP64
-// sequence ((origin + c*z) + b*y) + a*x without FMA contraction and is rounded to the 2^-16 grid in FP64 (used
-// where 1e-5 output parity matters); otherwise the same sequence runs in FP32. CLAMP_ALL: every position is inside.
-template <bool PRECISE, bool CLAMP_ALL>
-ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, int b, int cz, TapPair &T, int u) {
-  float fx, fy, fz;
+// Position of an output voxel in the fixed image: integer cell, tricubic weights and the valid-range test.
+struct ResliceTap {
   int ix, iy, iz;
+  float wx[4], wy[4], wz[4];
   bool inside;
+};
+
+// Voxel (a, b, cz) of the output. PRECISE: the voxel coordinate follows the reference's FP64 sequence
+// ((origin + c*z) + b*y) + a*x without FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5
+// output parity matters); otherwise the same sequence runs in FP32. CLAMP_ALL: every position is inside.
+template <bool PRECISE, bool CLAMP_ALL>
+ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, int b, int cz, ResliceTap &t) {
+  float fx, fy, fz;
   if (PRECISE) {
     double q[3];
     for (int k = 0; k < 3; ++k) {
@@ -94,15 +86,15 @@ ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, 
       w = __dadd_rn(w, __dmul_rn((double)b, it.md[6 + k]));
       q[k] = __dadd_rn(w, __dmul_rn((double)a, it.md[3 + k]));
     }
-    inside = CLAMP_ALL || !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 ||
-                            q[2] > dz - 0.5);
+    t.inside = CLAMP_ALL || !(q[0] < -0.5 || q[0] > dx - 0.5 || q[1] < -0.5 || q[1] > dy - 0.5 || q[2] < -0.5 ||
+                              q[2] > dz - 0.5);
     const long long r0 = __double2ll_rn(q[0] * 65536.0), r1 = __double2ll_rn(q[1] * 65536.0),
                     r2 = __double2ll_rn(q[2] * 65536.0);
-    ix = (int)(r0 >> 16);
+    t.ix = (int)(r0 >> 16);
     fx = (float)(r0 & 0xFFFF) * (1.0f / 65536.0f);
-    iy = (int)(r1 >> 16);
+    t.iy = (int)(r1 >> 16);
     fy = (float)(r1 & 0xFFFF) * (1.0f / 65536.0f);
-    iz = (int)(r2 >> 16);
+    t.iz = (int)(r2 >> 16);
     fz = (float)(r2 & 0xFFFF) * (1.0f / 65536.0f);
   } else {
     float p0 = it.m[0] + cz * it.m[9], p1 = it.m[1] + cz * it.m[10], p2 = it.m[2] + cz * it.m[11];
@@ -112,76 +104,48 @@ ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, 
     p0 = p0 + a * it.m[3];
     p1 = p1 + a * it.m[4];
     p2 = p2 + a * it.m[5];
-    inside = CLAMP_ALL || !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
-    ix = vtk_floor(p0, fx);
-    iy = vtk_floor(p1, fy);
-    iz = vtk_floor(p2, fz);
+    t.inside = CLAMP_ALL || !(p0 < -0.5f || p0 > dx - 0.5f || p1 < -0.5f || p1 > dy - 0.5f || p2 < -0.5f || p2 > dz - 0.5f);
+    t.ix = vtk_floor(p0, fx);
+    t.iy = vtk_floor(p1, fy);
+    t.iz = vtk_floor(p2, fz);
   }
-  T.ix[u] = ix;
-  T.iy[u] = iy;
-  T.iz[u] = iz;
-  T.inside[u] = inside;
-  float w[4];
-  cubic_weights(w, fx);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) set_comp(T.wx[i], u, w[i]);
+  cubic_weights(t.wx, fx);
+  cubic_weights(t.wy, fy);
+  cubic_weights(t.wz, fz);
   // The reference uses only the middle row/plane when fy/fz == 0; the full 4x4x4 sum with the
   // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
-  cubic_weights(w, fy);
-  if (!((dy > 1) && (fy != 0.f))) { w[0] = 0.f; w[1] = 1.f; w[2] = 0.f; w[3] = 0.f; }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) set_comp(T.wy[i], u, w[i]);
-  cubic_weights(w, fz);
-  if (!((dz > 1) && (fz != 0.f))) { w[0] = 0.f; w[1] = 1.f; w[2] = 0.f; w[3] = 0.f; }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) set_comp(T.wz[i], u, w[i]);
+  if (!((dy > 1) && (fy != 0.f))) { t.wy[0] = 0.f; t.wy[1] = 1.f; t.wy[2] = 0.f; t.wy[3] = 0.f; }
+  if (!((dz > 1) && (fz != 0.f))) { t.wz[0] = 0.f; t.wz[1] = 1.f; t.wz[2] = 0.f; t.wz[3] = 0.f; }
 }
 
 // The tricubic sum of every path below, in one fixed order: per row (z plane k, y row j)
 // xs = ((wx0 r0 + wx1 r1) + wx2 r2) + wx3 r3 (fused), acc += (wz_k wy_j) xs (fused).
-// Voxel u's taps read from the staged box at unclamped positions: row pitch P, plane pitch PE (floats),
-// b0 = tap (0, 0, 0).
-ETTK_DEV float tap_sum_box(const float *b0, int P, int PE, const TapPair &T, int u) {
+// Taps read from the staged box at unclamped positions: row pitch P, plane pitch PE (floats), b0 = tap (0, 0, 0).
+ETTK_DEV float tap_sum_box(const float *b0, int P, int PE, const ResliceTap &t) {
   float acc = 0.f;
 #pragma unroll
   for (int k = 0; k < 4; ++k)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float *r = b0 + k * PE + j * P;
-      float xs = __fmul_rn(comp(T.wx[0], u), r[0]);
-      xs = __fmaf_rn(comp(T.wx[1], u), r[1], xs);
-      xs = __fmaf_rn(comp(T.wx[2], u), r[2], xs);
-      xs = __fmaf_rn(comp(T.wx[3], u), r[3], xs);
-      acc = __fmaf_rn(__fmul_rn(comp(T.wz[k], u), comp(T.wy[j], u)), xs, acc);
+      float xs = __fmul_rn(t.wx[0], r[0]);
+      xs = __fmaf_rn(t.wx[1], r[1], xs);
+      xs = __fmaf_rn(t.wx[2], r[2], xs);
+      xs = __fmaf_rn(t.wx[3], r[3], xs);
+      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), xs, acc);
     }
   return acc;
 }
-// The same sum for both voxels at once in packed FP32x2 arithmetic (one instruction per pair of operations).
-ETTK_DEV float2 tap_sum_box_pair(const float *pa, const float *pb, int P, int PE, const TapPair &T) {
-  float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float *ra = pa + k * PE + j * P, *rb = pb + k * PE + j * P;
-      float2 xs = __fmul2_rn(T.wx[0], make_float2(ra[0], rb[0]));
-      xs = __ffma2_rn(T.wx[1], make_float2(ra[1], rb[1]), xs);
-      xs = __ffma2_rn(T.wx[2], make_float2(ra[2], rb[2]), xs);
-      xs = __ffma2_rn(T.wx[3], make_float2(ra[3], rb[3]), xs);
-      acc = __ffma2_rn(__fmul2_rn(T.wz[k], T.wy[j]), xs, acc);
-    }
-  return acc;
-}
-// Voxel u's taps clamped to the volume (the reference's clamp border) and read from the staged box, whose origin
-// is (x0, o1, o2): used for voxels within two voxels of a face when the box copy filled positions outside the volume.
+// Taps clamped to the volume (the reference's clamp border) and read from the staged box, whose origin is
+// (x0, o1, o2): used for voxels within two voxels of a face when the box copy filled positions outside the volume.
 ETTK_DEV float tap_sum_clamped(const float *box, int x0, int o1, int o2, int P, int PE, int dx, int dy, int dz,
-                               const TapPair &T, int u) {
+                               const ResliceTap &t) {
   int xo[4], yo[4], zo[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    xo[i] = min(max(T.ix[u] - 1 + i, 0), dx - 1) - x0;
-    yo[i] = (min(max(T.iy[u] - 1 + i, 0), dy - 1) - o1) * P;
-    zo[i] = (min(max(T.iz[u] - 1 + i, 0), dz - 1) - o2) * PE;
+    xo[i] = min(max(t.ix - 1 + i, 0), dx - 1) - x0;
+    yo[i] = (min(max(t.iy - 1 + i, 0), dy - 1) - o1) * P;
+    zo[i] = (min(max(t.iz - 1 + i, 0), dz - 1) - o2) * PE;
   }
   float acc = 0.f;
 #pragma unroll
@@ -189,50 +153,37 @@ ETTK_DEV float tap_sum_clamped(const float *box, int x0, int o1, int o2, int P, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float *r = box + zo[k] + yo[j];
-      float xs = __fmul_rn(comp(T.wx[0], u), r[xo[0]]);
-      xs = __fmaf_rn(comp(T.wx[1], u), r[xo[1]], xs);
-      xs = __fmaf_rn(comp(T.wx[2], u), r[xo[2]], xs);
-      xs = __fmaf_rn(comp(T.wx[3], u), r[xo[3]], xs);
-      acc = __fmaf_rn(__fmul_rn(comp(T.wz[k], u), comp(T.wy[j], u)), xs, acc);
+      float xs = __fmul_rn(t.wx[0], r[xo[0]]);
+      xs = __fmaf_rn(t.wx[1], r[xo[1]], xs);
+      xs = __fmaf_rn(t.wx[2], r[xo[2]], xs);
+      xs = __fmaf_rn(t.wx[3], r[xo[3]], xs);
+      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), xs, acc);
     }
   return acc;
 }
-// One voxel's cell and weights, for the global-memory path (passed by value to a function that is not inlined).
-struct ResliceTap {
-  int ix, iy, iz;
-  float wx[4], wy[4], wz[4];
-};
-ETTK_DEV ResliceTap single_tap(const TapPair &T, int u) {
-  ResliceTap t;
-  t.ix = T.ix[u];
-  t.iy = T.iy[u];
-  t.iz = T.iz[u];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    t.wx[i] = comp(T.wx[i], u);
-    t.wy[i] = comp(T.wy[i], u);
-    t.wz[i] = comp(T.wz[i], u);
-  }
-  return t;
-}
-// Taps clamped to the volume and read from global memory (bricks whose footprint is not staged).
-static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz,
-                                                     ResliceTap t) {
-  const int x_0 = min(max(t.ix - 1, 0), dx - 1), x_1 = min(max(t.ix, 0), dx - 1), x_2 = min(max(t.ix + 1, 0), dx - 1),
-            x_3 = min(max(t.ix + 2, 0), dx - 1);
+// Taps clamped to the volume and read from global memory (bricks whose footprint is not staged). Not inlined; its
+// arguments are scalars so that they pass in registers (a structure passed by reference would live in local memory
+// for every voxel of the calling kernel).
+static __device__ __noinline__ float tricubic_global(const float *__restrict__ vol, int dx, int dy, int dz, int ix, int iy,
+                                                     int iz, float wx0, float wx1, float wx2, float wx3, float wy0,
+                                                     float wy1, float wy2, float wy3, float wz0, float wz1, float wz2,
+                                                     float wz3) {
+  const float wx[4] = {wx0, wx1, wx2, wx3}, wy[4] = {wy0, wy1, wy2, wy3}, wz[4] = {wz0, wz1, wz2, wz3};
+  const int x_0 = min(max(ix - 1, 0), dx - 1), x_1 = min(max(ix, 0), dx - 1), x_2 = min(max(ix + 1, 0), dx - 1),
+            x_3 = min(max(ix + 2, 0), dx - 1);
   float acc = 0.f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int z = min(max(t.iz - 1 + k, 0), dz - 1);
+    const int z = min(max(iz - 1 + k, 0), dz - 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int y = min(max(t.iy - 1 + j, 0), dy - 1);
+      const int y = min(max(iy - 1 + j, 0), dy - 1);
       const float *row = vol + ((long)z * dy + y) * dx;
-      float xs = __fmul_rn(t.wx[0], __ldg(row + x_0));
-      xs = __fmaf_rn(t.wx[1], __ldg(row + x_1), xs);
-      xs = __fmaf_rn(t.wx[2], __ldg(row + x_2), xs);
-      xs = __fmaf_rn(t.wx[3], __ldg(row + x_3), xs);
-      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), xs, acc);
+      float xs = __fmul_rn(wx[0], __ldg(row + x_0));
+      xs = __fmaf_rn(wx[1], __ldg(row + x_1), xs);
+      xs = __fmaf_rn(wx[2], __ldg(row + x_2), xs);
+      xs = __fmaf_rn(wx[3], __ldg(row + x_3), xs);
+      acc = __fmaf_rn(__fmul_rn(wz[k], wy[j]), xs, acc);
     }
   }
   return acc;
@@ -366,58 +317,36 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
   __syncthreads();
   float s = 0.f;
   int cnt = 0;
-  // Box offset of voxel u's tap (0, 0, 0) and whether its 4 x 4 x 4 taps can be read from the box as they are: the
+  // Box offset of a voxel's tap (0, 0, 0) and whether its 4 x 4 x 4 taps can be read from the box as they are: the
   // 16-byte staging stores clamped values beyond the volume, the bulk copy zeros there, so its voxels within two
   // voxels of a face read clamped positions instead (tap_sum_clamped).
   const int PE = E1 * P;
-  auto tap_off = [&](const TapPair &T, int u) {
-    return ((T.iz[u] - 1 - o2) * E1 + (T.iy[u] - 1 - o1)) * P + (T.ix[u] - 1 - x0);
-  };
-  auto direct = [&](const TapPair &T, int u) {
-    return staged && (!use_tma || ((unsigned)(T.ix[u] - 1) <= (unsigned)(dx - 4) &&
-                                   (unsigned)(T.iy[u] - 1) <= (unsigned)(dy - 4) &&
-                                   (unsigned)(T.iz[u] - 1) <= (unsigned)(dz - 4)));
-  };
-  // tricubic value of voxel u (-FLT_MAX outside the valid range)
-  auto value = [&](const TapPair &T, int u) -> float {
-    if (!T.inside[u]) return -FLT_MAX;
-    if (!staged) return tricubic_global(vol, dx, dy, dz, single_tap(T, u));
-    if (!direct(T, u)) return tap_sum_clamped(box, x0, o1, o2, P, PE, dx, dy, dz, T, u);
-    return use_tma ? tap_sum_box(box + tap_off(T, u), RT_X, RT_X * RT_Y, T, u) : tap_sum_box(box + tap_off(T, u), P, PE, T, u);
+  // tricubic value of a voxel (-FLT_MAX outside the valid range)
+  auto value = [&](const ResliceTap &t) -> float {
+    if (!t.inside) return -FLT_MAX;
+    if (!staged)
+      return tricubic_global(vol, dx, dy, dz, t.ix, t.iy, t.iz, t.wx[0], t.wx[1], t.wx[2], t.wx[3], t.wy[0], t.wy[1],
+                             t.wy[2], t.wy[3], t.wz[0], t.wz[1], t.wz[2], t.wz[3]);
+    const int off = ((t.iz - 1 - o2) * E1 + (t.iy - 1 - o1)) * P + (t.ix - 1 - x0);
+    if (!use_tma) return tap_sum_box(box + off, P, PE, t);
+    if ((unsigned)(t.ix - 1) <= (unsigned)(dx - 4) && (unsigned)(t.iy - 1) <= (unsigned)(dy - 4) &&
+        (unsigned)(t.iz - 1) <= (unsigned)(dz - 4))
+      return tap_sum_box(box + off, RT_X, RT_X * RT_Y, t);
+    return tap_sum_clamped(box, x0, o1, o2, P, PE, dx, dy, dz, t);
   };
   // The thread's two voxels v = tid and tid + 256; the 32 voxels of a warp form a 4 (a) x 4 (b) x 2 (c) block.
-  auto brick_pos = [&](int u, int &la, int &lb, int &lc) {
-    const int v = threadIdx.x + 256 * u, w = v >> 5, ln = v & 31;
-    la = 4 * (w >> 3) + (ln >> 3);
-    lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3);
-    lc = 2 * (w & 3) + (ln & 1);
-  };
-  TapPair T;
-#pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    int la, lb, lc;
-    brick_pos(u, la, lb, lc);
-    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, bx * RB + la, by * RB + lb, bz * RB + lc, T, u);
-  }
-  float val[2];
-  if (T.inside[0] && T.inside[1] && direct(T, 0) && direct(T, 1)) {
-    const float2 r = use_tma ? tap_sum_box_pair(box + tap_off(T, 0), box + tap_off(T, 1), RT_X, RT_X * RT_Y, T)
-                             : tap_sum_box_pair(box + tap_off(T, 0), box + tap_off(T, 1), P, PE, T);
-    val[0] = r.x;
-    val[1] = r.y;
-  } else {
-    val[0] = value(T, 0);
-    val[1] = value(T, 1);
-  }
-#pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    if (T.inside[u]) {
-      s += val[u];
+#pragma unroll 1
+  for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
+    const int w = v >> 5, ln = v & 31;
+    const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
+    ResliceTap t;
+    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, bx * RB + la, by * RB + lb, bz * RB + lc, t);
+    const float val = value(t);
+    if (t.inside) {
+      s += val;
       cnt += 1;
     }
-    int la, lb, lc;
-    brick_pos(u, la, lb, lc);
-    obuf[la * 66 + lb * 8 + lc] = val[u];
+    obuf[la * 66 + lb * 8 + lc] = val;
   }
   __syncthreads();
   for (int v = threadIdx.x; v < RB * RB * RB; v += blockDim.x) {
@@ -428,10 +357,10 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
   for (int i = threadIdx.x; i < n_ext; i += blockDim.x) {
     const int fa = i / (nxb * nxc), fb = (i / nxc) % nxb, fc = i % nxc;
     if (fa < RB && fb < RB && fc < RB) continue;
-    TapPair F;
+    ResliceTap t;
     const int a = bx * RB + fa, b = by * RB + fb, cz = bz * RB + fc;
-    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, a, b, cz, F, 0);
-    it.faces[face_index(a, b, cz, N)] = value(F, 0);
+    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, a, b, cz, t);
+    it.faces[face_index(a, b, cz, N)] = value(t);
   }
   if (acc) {
     double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);

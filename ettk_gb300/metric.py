@@ -45,6 +45,7 @@ class ProjectionRotationMetric3D:
     def __init__(self, params, device=0):
         self.L = _lib.load()
         self.params = dict(params)
+        self.device = device
         self._ctx = ctypes.c_void_p()
         P = _lib.make_params(self.params)
         self._check(self.L.ettk_gpu_create(device, ctypes.byref(P), ctypes.byref(self._ctx)), "create")
@@ -197,6 +198,16 @@ class ProjectionRotationMetric3D:
         v = np.ascontiguousarray(vol, np.float32)
         out = np.zeros((N, N, N), np.float32)
         self._check(self.L.ettk_gpu_symmetrize(self._ctx, v.ctypes.data, int(fold), out.ctypes.data), "symmetrize")
+        return out
+
+    def mean_images(self, vol, transforms):
+        """Mean of getImage of a [z][y][x] fixed-image volume under each 4x4 transform; returns [z][y][x]."""
+        N = self.params["N"]
+        v = np.ascontiguousarray(vol, np.float32)
+        t = np.ascontiguousarray(np.asarray(transforms, np.float64).reshape(-1, 16))
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_mean_images(self._ctx, v.ctypes.data, len(t), t.ctypes.data, out.ctypes.data),
+                    "mean_images")
         return out
 
     def representations(self, particles, fold=1):

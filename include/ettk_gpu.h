@@ -130,6 +130,14 @@ int ettk_gpu_variance(ettk_ctx *ctx, int M, const int *particles, const float *w
    with the mean of its valid voxels removed. fold = 1 returns the volume unchanged. N^3 floats, x fastest. */
 int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
 
+/* The mean over n transforms (transforms: n row-major 4x4 matrices) of getImage of vol as a fixed image
+   (nbfWedgedSubImage3D::getImage after setFixedImage: centred at N/2, full wedge): each a tricubic resample under the
+   transform with the mean of its valid voxels removed and the invalid ones 0, summed in order in FP64 and divided by
+   n, as nbfLoopClustering::symmetrize accumulates reference.getImage(data, t) over the folds with the shifts the
+   CCF found (inc/em/nbfLoopClustering.h:5987-6042). ettk_gpu_symmetrize is the case t_i = RotateZ(i * 360 / fold).
+   vol and out: N^3 floats, x fastest. n 1..4096. */
+int ettk_gpu_mean_images(ettk_ctx *ctx, const float *vol, int n, const double *transforms, float *out);
+
 /* Low-dimensional representations of particles (nbfFourierImageMetric::getLowDimensionRepresentationHalf,
    inc/em/nbfFourierImageMetric.h:1967-2034, as nbfCorrelationImageMetric::getRepresentations collects them,
    inc/em/nbfCorrelationImageMetric.h:1323-1372; padding 1): per particle its image (own geometry, mean of

@@ -109,3 +109,53 @@ def test_variance(ds32):
     o = pyoracle.variance(ds32.params, [ds32.particles[i] for i in members], [ds32.meta[i] for i in members], weights,
                           mats, avg.transpose(2, 1, 0).astype(np.float64)).transpose(2, 1, 0)
     assert rel_rms(g, o) <= 1e-5, rel_rms(g, o)
+
+
+def _shifted_rot_z(deg, shift):
+    from ettk_gb300 import classification
+    T = classification._rot_z(deg)
+    S = np.eye(4)
+    S[:3, 3] = shift
+    return T @ S
+
+
+@pytest.mark.gpu
+def test_mean_images(ds32):
+    """ettk_gpu_mean_images: the mean of getImage of a fixed image under rotations with translations, against the
+    oracle's FP64 getImage (1e-5 relative RMS)."""
+    vol = ds32.references[0]
+    ts = [np.eye(4), _shifted_rot_z(120.0, (1.5, -0.5, 0.25)), _shifted_rot_z(240.0, (-1.0, 2.0, 0.5))]
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        g = m.mean_images(vol, ts)
+    finally:
+        m.close()
+    full = {"lwedge": -90.0, "uwedge": 90.0}
+    o = np.mean([pyoracle.get_image(ds32.params, vol, full, t) for t in ts], axis=0).transpose(2, 1, 0)
+    assert rel_rms(g, o) <= 1e-5, rel_rms(g, o)
+
+
+@pytest.mark.gpu
+def test_symmetrize_aligned(ds32):
+    """The aligned n-fold step of the global-average loop (nbfLoopClustering::symmetrize with alignment,
+    inc/em/nbfLoopClustering.h:5950-6076) on the GPU against the oracle: the same CCF transforms for every fold, and
+    the symmetrised image within 1e-5 relative RMS."""
+    from ettk_gb300 import classification
+    fold = 3
+    vol = ds32.references[0]
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        img, ts = classification.symmetrize_aligned(m, vol, fold)
+    finally:
+        m.close()
+    p = ds32.params
+    full = {"lwedge": -90.0, "uwedge": 90.0}
+    to = [np.eye(4)]
+    for f in range(1, fold):
+        _, t = pyoracle.ccf(p, vol, full, vol, full, classification._rot_z(f * 360.0 / fold))
+        to.append(t)
+    for a, b in zip(ts, to):
+        assert np.allclose(a, b, atol=1e-6), (a, b)
+    shifted = np.mean([pyoracle.get_image(p, vol, full, t) for t in to], axis=0)  # [x][y][z]
+    o = pyoracle.symmetrize(p, np.ascontiguousarray(shifted.transpose(2, 1, 0)).astype(np.float32), fold)
+    assert rel_rms(img, o.transpose(2, 1, 0)) <= 1e-5, rel_rms(img, o.transpose(2, 1, 0))

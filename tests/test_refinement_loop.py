@@ -144,9 +144,59 @@ def test_rotational_variance_and_no_wedge():
     assert out["average"][0, 0, 0] == 2 * calls(m, "symmetrize_rotational")[-1][1]
 
 
-def test_rejects_nfold():
-    with pytest.raises(NotImplementedError):
-        classification.refine_global(FakeMetric(2), volumes(2), 1, fold=3)
+class FakeSym:
+    """Stand-in for the n-fold step's context: the CCF adds a known translation to the transform it is given."""
+
+    def __init__(self):
+        self.log = []
+
+    def set_references(self, refs):
+        self.log.append(("set_references", refs[0].image[0, 0, 0], refs[0].lwedge))
+
+    def set_particles(self, vols):
+        self.log.append(("set_particles", vols[0].image[0, 0, 0]))
+
+    def ccf(self, r, p, T):
+        S = np.eye(4)
+        S[:3, 3] = (len(self.log), -1.0, 0.5)
+        self.log.append(("ccf", np.asarray(T).copy(), np.asarray(T) @ S))
+        return 0.5, np.asarray(T) @ S
+
+    def mean_images(self, vol, ts):
+        self.log.append(("mean_images", vol[0, 0, 0], [np.asarray(t).copy() for t in ts]))
+        return vol + 1
+
+    def symmetrize(self, vol, fold):
+        self.log.append(("symmetrize", vol[0, 0, 0], fold))
+        return vol * 3
+
+
+def test_nfold_branch():
+    """cluster.symmetrize with alignment (inc/em/nbfLoopClustering.h:5950-6076): fold - 1 CCFs of the average against
+    itself from RotateZ(f * 360 / fold), the mean of its images under the re-centred transforms, then the plain
+    n-fold symmetrisation; the reference is that image and its spherical wedge counts every member under T_i t_f."""
+    V, it, fold = 4, 2, 3
+    m, s = FakeMetric(V), FakeSym()
+    out = classification.refine_global(m, volumes(V), it, fold=fold, sym=s)
+    ccf = [c for c in s.log if c[0] == "ccf"]
+    assert len(ccf) == (fold - 1) * (it + 1)
+    for f in range(1, fold):
+        assert np.allclose(ccf[f - 1][1], rot_z(f * 360.0 / fold), atol=1e-12)
+    means = [c for c in s.log if c[0] == "mean_images"]
+    syms = [c for c in s.log if c[0] == "symmetrize"]
+    assert len(means) == len(syms) == it + 1 and all(c[2] == fold for c in syms)
+    ts = means[0][2]
+    assert len(ts) == fold and np.allclose(ts[0], np.eye(4))
+    # the transforms the mean uses are the CCF outputs
+    for f in range(1, fold):
+        assert np.allclose(ts[f], ccf[f - 1][2])
+    # the reference of the alignment is the symmetrised image
+    refs = calls(m, "set_references")
+    assert refs[0][1] == 9.0  # the first average holds 2: mean of images + 1, symmetrisation * 3
+    # the spherical wedge: every member once per fold, weight 1 each
+    w = calls(m, "average_spherical_wedge")
+    assert len(w) == it and len(w[0][1]) == V * fold
+    assert out["average"][0, 0, 0] == syms[-1][1] * 3
 
 
 def test_volume_lists(tmp_path):
