@@ -123,9 +123,15 @@ class ProjectionRotationMetric3D:
     # -- nbfCorrelationImageMetric::getDistances (core overload) ---------------------------------
     def getDistances(self, indexes, D=None, cols=17, ncand=1, typeOfMetric=3, restrict_translation=-1.0):
         """indexes: sequence of (reference index, particle index). D: float32 (npairs, cols, ncand),
-        rows pre-filled with -1 are computed (others skipped). typeOfMetric 3: the alignment (SO(3) search and
-        CCF candidates); 2: one CCF per pair at the particle's own alignment matrix (nbfFourierImageMetricCore) with
-        the translation restriction restrict_translation (negative: the metric's)."""
+        rows pre-filled with -1 are computed (others skipped). The metric types of nbfCorrelationImageMetric::
+        getDistances (inc/em/nbfCorrelationImageMetric.h:1918-1930):
+          3: the alignment, refinement off (SO(3) search and CCF candidates);
+          2: one CCF per pair at the particle's own alignment matrix (nbfFourierImageMetricCore) with the translation
+             restriction restrict_translation (negative: the metric's);
+          0: the alignment with refinement on; the Powell refinement of each candidate is replaced by the fast
+             form's batched gradient refinement (getDistancesRefined, default iterations);
+          1: refinement from the particle's own alignment (nbfFourierImageMetric): the type-2 CCF, then the
+             batched gradient refinement of that pose (refine)."""
         idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
         n = idx.shape[0]
         if D is None:
@@ -137,8 +143,18 @@ class ProjectionRotationMetric3D:
         elif typeOfMetric == 3:
             self._check(self.L.ettk_gpu_align_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1],
                                                     D.shape[2]), "align_pairs")
+        elif typeOfMetric == 0:
+            return self.getDistancesRefined(indexes, D=D)
+        elif typeOfMetric == 1:
+            todo = D[:, 0, 0] == -1
+            self._check(self.L.ettk_gpu_score_pairs(self._ctx, n, idx.ctypes.data, D.ctypes.data, D.shape[1],
+                                                    D.shape[2], float(restrict_translation)), "score_pairs")
+            if todo.any():
+                sub = np.ascontiguousarray(D[todo])
+                self.refine(idx[todo], sub)
+                D[todo] = sub
         else:
-            raise ValueError("typeOfMetric 2 or 3 (0, refinement on, is the fast form: getDistancesRefined)")
+            raise ValueError("typeOfMetric 0, 1, 2 or 3")
         return D
 
     # -- nbfWedgedAverageImage3D::setAlignments + getImage ----------------------------------------

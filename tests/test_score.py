@@ -96,3 +96,21 @@ def test_mra_scoring_and_class_choice():
                                               metas[v * R + r], np.eye(4))
     assert np.all(np.abs(S - So) <= 1e-4 * np.abs(So))
     assert np.array_equal(clustering.mra_assign(S), clustering.mra_assign(So))
+
+
+def test_metric_types_zero_and_one():
+    """getDistances' other metric types route to the batched forms: type 0 (refinement on) is getDistancesRefined,
+    type 1 (refinement from the own alignment) is the type-2 CCF followed by refine; same rows bit for bit."""
+    ds = synthetic.generate("align32_b16", n_particles=3)
+    m = ProjectionRotationMetric3D(ds.params)
+    try:
+        m.set_references([WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in KW + ("matrix",)})])
+        m.set_particles([WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in KW + ("matrix",)})
+                         for i in range(3)])
+        pairs = [(0, i) for i in range(3)]
+        assert np.array_equal(m.getDistances(pairs, typeOfMetric=0), m.getDistancesRefined(pairs))
+        D1 = m.getDistances(pairs, typeOfMetric=1)
+        D2 = m.refine(pairs, m.getDistances(pairs, typeOfMetric=2))
+        assert np.array_equal(D1, D2)
+    finally:
+        m.close()
