@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
     ap.add_argument("--fast-only", action="store_true",
                     help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")
+    ap.add_argument("--config-table", action="store_true",
+                    help="plain and fast form on every alignment configuration, the oracle beside each, one "
+                         "classification pass (--study-pairs particles x 10 references)")
     ap.add_argument("--repr-study", action="store_true",
                     help="unsupervised-classification step on the 64^3 workload: low-dimensional representations "
                          "of --study-pairs particles and the distance matrix between them (one JSON line)")
@@ -128,18 +131,18 @@ def precision_study(a):
 # ------------------------------------------------------------------------------- CPU (oracle) arm
 
 def _cpu_worker(args):
-    idx, n = args
+    idx, n, workload = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     from ettk_gb300 import synthetic
-    ds = synthetic.generate(WORKLOAD, n_particles=n)
+    ds = synthetic.generate(workload, n_particles=n)
     t0 = time.perf_counter()
     for i in idx:
         pyoracle.align(ds.params, ds.references[0], ds.ref_meta[0], ds.particles[i], ds.meta[i])
     return time.perf_counter() - t0, len(idx)
 
 
-def cpu_baseline(n_pairs):
+def cpu_baseline(n_pairs, workload=WORKLOAD):
     """The oracle (FP64 port of the reference path) on all host cores: one single-threaded process per
     core on a disjoint shard, as the reference runs one MPI worker per core. Returns pairs/s."""
     import multiprocessing as mp
@@ -152,13 +155,13 @@ def cpu_baseline(n_pairs):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(s, n_pairs) for s in shards if s])
+        res = pool.map(_cpu_worker, [(s, n_pairs, workload) for s in shards if s])
     wall = time.perf_counter() - t0
     busy = max(r[0] for r in res)
     return {"value": n_pairs / busy, "unit": "alignments/s", "cores": cores, "kind": "port",
-            "sample": "%d pairs of the %s workload (64^3, B=32), one oracle process per core, %.1f s wall; "
+            "sample": "%d pairs of the %s workload, one oracle process per core, %.1f s wall; "
                       "the oracle is built -O3 and transforms with its own radix-2 FFT (the reference's FFTW3 is not "
-                      "in the image)" % (n_pairs, WORKLOAD, wall)}
+                      "in the image)" % (n_pairs, workload, wall)}
 
 
 # ------------------------------------------------------------------------------- clocks
@@ -299,40 +302,11 @@ def fast_study(a):
     one CCF per kept peak, batched local refinement) on the same pairs: alignments/s of each (device-resident
     particles, CUDA-synchronised wall time, after one warm-up call of each), the library's stage times, and the
     rotation/shift errors against the generating poses over the pairs whose plain grid hit is within 20 degrees."""
-    import numpy as np
-    import torch
     from ettk_gb300 import synthetic
-    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
 
     P = a.pairs
     ds = synthetic.generate(a.workload, n_particles=P)
-    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
-    vols = [WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in kw}) for i in range(P)]
-    ref = WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})
-    pairs = [(0, i) for i in range(P)]
-    out = {}
-    forms = (("fast", a.fast_precision),) if a.fast_only else (("plain", 0), ("fast", a.fast_precision))
-    for form, prec in forms:
-        m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec))
-        m.set_references([ref])
-        m.set_particles(vols)
-
-        def run(sub):
-            if form == "plain":
-                return m.getDistances(sub)
-            return m.getDistancesRefined(sub, iterations=a.fast_iterations, peaks=a.fast_peaks)
-        run(pairs)  # warm-up at full size (buffers, tables, the half-grid references)
-        m.set_particles(vols)  # drop the cached spherical projections of the warm-up pairs
-        torch.cuda.synchronize()
-        m.profile(True)
-        t0 = time.perf_counter()
-        D = run(pairs)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        prof = m.profile_read()
-        m.profile(False)
-        m.close()
-        out[form] = (D, P / (t1 - t0), prof)
+    out = compare_forms(ds, P, a.fast_iterations, a.fast_peaks, a.fast_precision, a.fast_only)
     if a.fast_only:
         rf, sf = pose_errors(out["fast"][0], ds.truth)
         line = {"fast_study": {"fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, rf < 20.0),
@@ -357,6 +331,84 @@ def fast_study(a):
                    "fast_wigner_precision": a.fast_precision,
                    "errors": "against the generating poses, over pairs whose plain grid hit is within 20 degrees"}}
     print(json.dumps(line), flush=True)
+
+
+def compare_forms(ds, P, iterations, peaks, precision, fast_only=False):
+    """Plain and fast form on the first P particles of ds against its reference: per form (result rows,
+    alignments/s, the library's profile), timed after one warm-up call at full size."""
+    import torch
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    vols = [WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in kw}) for i in range(P)]
+    ref = WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})
+    pairs = [(0, i) for i in range(P)]
+    out = {}
+    forms = (("fast", precision),) if fast_only else (("plain", 0), ("fast", precision))
+    for form, prec in forms:
+        m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec))
+        m.set_references([ref])
+        m.set_particles(vols)
+
+        def run(sub):
+            if form == "plain":
+                return m.getDistances(sub)
+            return m.getDistancesRefined(sub, iterations=iterations, peaks=peaks)
+        run(pairs)  # warm-up at full size (buffers, tables, the half-grid references)
+        m.set_particles(vols)  # drop the cached spherical projections of the warm-up pairs
+        torch.cuda.synchronize()
+        m.profile(True)
+        t0 = time.perf_counter()
+        D = run(pairs)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        prof = m.profile_read()
+        m.profile(False)
+        m.close()
+        out[form] = (D, P / (t1 - t0), prof)
+    return out
+
+
+def config_table(a):
+    """The results table of the configurations: per alignment configuration the plain and the fast form
+    (alignments/s, errors against the generating poses) and the oracle on the host cores on a bounded sample;
+    for the classification configuration one classify pass (align all particles against all references, assign,
+    re-average) timed as pairs/s."""
+    import numpy as np
+    import torch
+    from ettk_gb300 import synthetic
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+    rows = {}
+    for name, P, cpu_n in (("align32_b16", 200, 64), ("align64_b32", 256, 32), ("refine64_b32", 256, 32),
+                           ("align128_b64", 32, 16)):
+        cpu = cpu_baseline(cpu_n, name)
+        ds = synthetic.generate(name, n_particles=P)
+        out = compare_forms(ds, P, FAST_ITERATIONS, 0, FAST_PRECISION)
+        rp, sp = pose_errors(out["plain"][0], ds.truth)
+        rf, sf = pose_errors(out["fast"][0], ds.truth)
+        hit = rp < 20.0
+        rows[name] = {"pairs": P, "cpu": cpu, "plain": dict(alignments_per_s=out["plain"][1], **error_summary(rp, sp, hit)),
+                      "fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, hit)),
+                      "speedup": out["fast"][1] / out["plain"][1]}
+        print(json.dumps({"config_row": name, **rows[name]}), flush=True)
+    # classification: V particles x R references, one pass
+    V = a.study_pairs
+    ds = synthetic.generate("mra64_b32", n_particles=V)
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    m = ProjectionRotationMetric3D(ds.params)
+    m.set_references([WedgedSubImage3D(r, **{k: rm[k] for k in kw}) for r, rm in zip(ds.references, ds.ref_meta)])
+    m.set_particles([WedgedSubImage3D(ds.particles[i], **{k: ds.meta[i][k] for k in kw}) for i in range(V)])
+    m.classify(1)  # warm-up
+    m.set_references([WedgedSubImage3D(r, **{k: rm[k] for k in kw}) for r, rm in zip(ds.references, ds.ref_meta)])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    labels, _, _ = m.classify(1)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    m.close()
+    R = len(ds.references)
+    rows["mra64_b32"] = {"particles": V, "references": R, "pairs_per_s": V * R / dt, "pass_s": dt,
+                         "classes_used": int(len(np.unique(labels)))}
+    print(json.dumps({"config_table": rows}), flush=True)
 
 
 def repr_study(a):
@@ -407,6 +459,9 @@ def main():
         return
     if a.fast_study:
         fast_study(a)
+        return
+    if a.config_table:
+        config_table(a)
         return
     if a.adjoint_study:
         adjoint_study(a)
