@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "align64_b32"
 FAST_PRECISION = 2   # split-BF16 Wigner-d contraction on the tensor cores
 FAST_ITERATIONS = 6  # local refinement steps of the fast form
+FAST_COARSE = 0  # 1: the fast form's SO(3) search on the half grid at B/2
 METRIC = "alignments/s at 64^3 bw=32: plain GPU vs batched+adjoint form at <=0.5deg/0.1 vox"
 
 
@@ -56,6 +57,8 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD, help="workload of the studies (align64_b32, refine64_b32)")
     ap.add_argument("--fast-peaks", type=int, default=0, help="0: the metric's candidate_peaks")
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
+    ap.add_argument("--fast-coarse", type=int, default=FAST_COARSE,
+                    help="1: the fast form's SO(3) search on the half grid at B/2")
     ap.add_argument("--fast-only", action="store_true",
                     help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")
     ap.add_argument("--config-table", action="store_true",
@@ -306,13 +309,13 @@ def fast_study(a):
 
     P = a.pairs
     ds = synthetic.generate(a.workload, n_particles=P)
-    out = compare_forms(ds, P, a.fast_iterations, a.fast_peaks, a.fast_precision, a.fast_only)
+    out = compare_forms(ds, P, a.fast_iterations, a.fast_peaks, a.fast_precision, a.fast_only, a.fast_coarse)
     if a.fast_only:
         rf, sf = pose_errors(out["fast"][0], ds.truth)
         line = {"fast_study": {"fast": dict(alignments_per_s=out["fast"][1], **error_summary(rf, sf, rf < 20.0),
                                             families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()})},
                 "config": {"workload": a.workload, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
-                           "fast_wigner_precision": a.fast_precision}}
+                           "fast_wigner_precision": a.fast_precision, "fast_coarse_so3": a.fast_coarse}}
         print(json.dumps(line), flush=True)
         return
     rp, sp = pose_errors(out["plain"][0], ds.truth)
@@ -328,12 +331,12 @@ def fast_study(a):
                      families_ms={k: round(v["ms"], 3) for k, v in out["fast"][2].items()}),
         "speedup": out["fast"][1] / out["plain"][1]},
         "config": {"workload": a.workload, "pairs": P, "iterations": a.fast_iterations, "peaks": a.fast_peaks,
-                   "fast_wigner_precision": a.fast_precision,
+                   "fast_wigner_precision": a.fast_precision, "fast_coarse_so3": a.fast_coarse,
                    "errors": "against the generating poses, over pairs whose plain grid hit is within 20 degrees"}}
     print(json.dumps(line), flush=True)
 
 
-def compare_forms(ds, P, iterations, peaks, precision, fast_only=False):
+def compare_forms(ds, P, iterations, peaks, precision, fast_only=False, coarse=FAST_COARSE):
     """Plain and fast form on the first P particles of ds against its reference: per form (result rows,
     alignments/s, the library's profile), timed after one warm-up call at full size."""
     import torch
@@ -345,7 +348,8 @@ def compare_forms(ds, P, iterations, peaks, precision, fast_only=False):
     out = {}
     forms = (("fast", precision),) if fast_only else (("plain", 0), ("fast", precision))
     for form, prec in forms:
-        m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec))
+        m = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=prec,
+                                            fast_coarse_so3=coarse if form == "fast" else 0))
         m.set_references([ref])
         m.set_particles(vols)
 
@@ -560,7 +564,8 @@ def main():
     ms_e2e = timed(step_e2e, a.steps)
     D_plain = step_device()
     # the fast form on the same pairs: split-BF16 Wigner contraction, half-grid candidate screening, local refinement
-    mf = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=FAST_PRECISION), device=local)
+    mf = ProjectionRotationMetric3D(dict(ds.params, wigner_precision=FAST_PRECISION, fast_coarse_so3=FAST_COARSE),
+                                    device=local)
     mf.set_references([WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})])
     fstream = torch.cuda.ExternalStream(mf.stream())
 

@@ -43,6 +43,7 @@ class Params(ctypes.Structure):
         ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
         ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
         ("mutual_correlation", ctypes.c_int), ("max_batch", ctypes.c_int), ("wigner_precision", ctypes.c_int),
+        ("fast_coarse_so3", ctypes.c_int),
     ]
 
 
@@ -142,7 +143,7 @@ def make_params(p):
         candidate_peaks=int(p["candidate_peaks"]), number_of_candidates=int(p["number_of_candidates"]),
         wedge_compensation=int(bool(p["wedge_compensation"])), overlap_normalized=int(bool(p["overlap_normalized"])),
         mutual_correlation=int(bool(p.get("mutual_correlation", False))), max_batch=int(p.get("max_batch", 0)),
-        wigner_precision=int(p.get("wigner_precision", 0)))
+        wigner_precision=int(p.get("wigner_precision", 0)), fast_coarse_so3=int(p.get("fast_coarse_so3", 0)))
 
 
 _META_DTYPE = np.dtype({"names": [f[0] for f in VolumeMeta._fields_],

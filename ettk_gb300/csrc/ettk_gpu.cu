@@ -677,6 +677,11 @@ struct ettk_ctx {
         streamed = true;
       }
     }
+    if constexpr (has_line_base<Pre>::value)
+      if (pre.real_only) {
+        if ((pre.N % (2 * L)) != 0) throw CudaError(ETTK_ERR_ARG, "real-line tiles must divide the box");
+        tiles = pre.real_tiles(lines, 2 * L);
+      }
     if (!streamed) k_r2c_reg<NN, L, Pre><<<(unsigned)tiles, 256, 0, st>>>(pre, out, lines);
     post_launch();
   }
@@ -815,6 +820,7 @@ struct ettk_ctx {
     OpPaddedMagnitude<N2> last{sp_F.p, sp_M.p};
     last.kz0 = N2 / 2;
     last.mutual = p.mutual_correlation ? 1 : 0;
+    if (N2 == 128) last.padc = sp_padc.p;  // the z pass skipped the padding lines (PrePadded::real_only)
     fft2d_t<N2>(last, P, "sphere_fft", 16.0, 1);
   }
   // |F| spherical projections of the items into Pp_out[out_index[i] * nn] (device; out_index null: [i * nn])
@@ -888,6 +894,7 @@ struct ettk_ctx {
   // set-up only, the child's stream waits for dec_ev before its first kernel
   cudaEvent_t dec_ev = nullptr;
   void half_particles(const std::vector<int> &pp);
+  void merge_child_profile();
   // best CCF candidate per pair scored on the decimated volumes: full-grid transform (translation doubled)
   void half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
                    const std::vector<int> &owner, std::vector<EvalReq> &finals);
@@ -1913,6 +1920,9 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   post_launch();
   PrePadded pre{sp_v.p, mask.p, sp_acc.p, 4, N};
   pre.nyquist_only = N2 <= 128;  // k_fft2d_padded consumes the spectra (larger boxes transform every plane)
+  // at 2N = 128 the z pass transforms the N^2 lines of the windowed box alone (tiles of 32 lines divide N = 64) and
+  // the last plane's magnitude pass supplies the padding lines' Nyquist entries from the padding constant
+  pre.real_only = N2 == 128;
   k_pad_constant<<<nblocks<int>(P, 128), 128, 0, st>>>(pre, (int)P, sp_padc.p);
   post_launch();
   r2c_z(N2, pre, sp_F.p, P * N2 * N2, "sphere_fft");
@@ -2710,7 +2720,7 @@ void ettk_ctx::half_setup() {
   if (!half) {
     ettk_params hp = p;
     hp.N = N / 2;
-    hp.B = 8;  // the child runs no SO(3) search
+    hp.B = p.fast_coarse_so3 ? std::max(8, p.B / 2) : 8;  // B/2 when the child runs the coarse SO(3) search
     hp.mask_radius = 0.5f * p.mask_radius;
     hp.mask_sigma = 0.5f * p.mask_sigma;
     hp.square_mask_size = 0.5f * p.square_mask_size;
@@ -2721,7 +2731,8 @@ void ettk_ctx::half_setup() {
     hp.bp_high_sigma = 2.f * p.bp_high_sigma;
     hp.bfactor = 0.25f * p.bfactor;
     hp.restrict_translation = 0.5f * p.restrict_translation;
-    hp.wigner_precision = 0;
+    hp.wigner_precision = p.fast_coarse_so3 ? p.wigner_precision : 0;
+    hp.fast_coarse_so3 = 0;
     ettk_ctx *h = nullptr;
     const int rc = ettk_gpu_create(device, &hp, &h);
     if (rc != ETTK_OK) throw CudaError(rc, "half-grid screening context could not be created");
@@ -2743,6 +2754,18 @@ void ettk_ctx::half_setup() {
     if (rc != ETTK_OK) throw CudaError(rc, "half-grid references: " + half->err);
     half_refs_ok = true;
   }
+}
+
+// The child's kernel families, reported under "half:" (when profiling).
+void ettk_ctx::merge_child_profile() {
+  if (!prof || !half) return;
+  for (auto &kv : half->prof_agg) {
+    ProfAgg &g = prof_agg["half:" + kv.first];
+    g.n += kv.second.n;
+    g.ms += kv.second.ms;
+    g.bytes += kv.second.bytes;
+  }
+  half->prof_agg.clear();
 }
 
 void ettk_ctx::half_particles(const std::vector<int> &pp) {
@@ -2768,15 +2791,7 @@ void ettk_ctx::half_screen(const std::vector<int> &pr, const std::vector<int> &p
   half->prof = prof;
   std::vector<EvalRes> res;
   half->eval_batch(hreq, res);
-  if (prof) {  // the child's kernel families, reported under "half:"
-    for (auto &kv : half->prof_agg) {
-      ProfAgg &g = prof_agg["half:" + kv.first];
-      g.n += kv.second.n;
-      g.ms += kv.second.ms;
-      g.bytes += kv.second.bytes;
-    }
-    half->prof_agg.clear();
-  }
+  merge_child_profile();
   std::vector<int> best(P, -1);
   for (size_t k = 0; k < cand.size(); ++k) {
     const int i = owner[k];
@@ -2868,7 +2883,16 @@ void ettk_ctx::align_refined(int npairs, const int *pairs, float *D, int cols, i
     }
     std::vector<PairPlan> plans;
     std::vector<PQ> q1, q2;
-    {
+    if (use_half && p.fast_coarse_so3) {
+      // the SO(3) search of the child on the half grid at B/2 (its particles are the batch's crops, slot order)
+      HostScope hs_so3(this, "stage_so3");
+      CK(cudaStreamWaitEvent(half->st, dec_ev, 0));
+      std::vector<int> pc(P);
+      for (int i = 0; i < P; ++i) pc[i] = lr_slot[pp[i]];
+      half->prof = prof;
+      half->so3_queues(P, pr, pc, plans, q1, q2);
+      merge_child_profile();
+    } else {
       HostScope hs_so3(this, "stage_so3");
       so3_queues(P, pr, pp, plans, q1, q2);
     }

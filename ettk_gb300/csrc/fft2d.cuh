@@ -149,6 +149,9 @@ struct OpPaddedMagnitude {
   int sign = -1;
   int kz0 = 0;  // plane of blockIdx.x = 0 (the launch for the last plane alone uses kz0 = N2 / 2)
   int mutual = 0;  // store |F|^(1/2) (mutual correlation)
+  // with padc (the padding constant c of each item), the entries (x, y) of the last plane with x >= N2/2 or
+  // y >= N2/2 are those of padding lines whose z pass was skipped: N2 c (-1)^(x+y)
+  const float *padc = nullptr;
   ETTK_DEV void begin() {}
   ETTK_DEV void rows(int kz, int &r0, int &r1) const {
     if (kz + kz0 < KXY<N2>::H - 1) {
@@ -156,7 +159,16 @@ struct OpPaddedMagnitude {
       r1 = N2 / 2;
     }
   }
-  ETTK_DEV float2 load(int e, int kz, int i) const { return d[KXY<N2>::at(e, kz + kz0, i)]; }
+  ETTK_DEV float2 load(int e, int kz, int i) const {
+    if (padc && kz + kz0 == KXY<N2>::H - 1) {
+      const int x = i / N2, y = i - x * N2;
+      if (x >= N2 / 2 || y >= N2 / 2) {
+        const float v = (float)N2 * padc[e];
+        return make_float2(((x + y) & 1) ? -v : v, 0.f);
+      }
+    }
+    return d[KXY<N2>::at(e, kz + kz0, i)];
+  }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
     mag[KXY<N2>::at(e, kz + kz0, i)] = spectrum_magnitude(v, mutual);
   }

@@ -180,6 +180,18 @@ template <class T, class = void>
 struct has_pad_lines : std::false_type {};
 template <class T>
 struct has_pad_lines<T, std::void_t<decltype(T::kPadLines)>> : std::true_type {};
+// Input functors that can restrict the pass to a subset of the lines declare kLineBase and map tile t to its first
+// line with line_base(t, RL) when real_only is set (the grid then has real_tiles(lines, RL) tiles).
+template <class T, class = void>
+struct has_line_base : std::false_type {};
+template <class T>
+struct has_line_base<T, std::void_t<decltype(T::kLineBase)>> : std::true_type {};
+template <class Pre>
+ETTK_DEV long tile_first_line(const Pre &pre, long tile, int RL) {
+  if constexpr (has_line_base<Pre>::value)
+    if (pre.real_only) return pre.line_base(tile, RL);
+  return tile * RL;
+}
 
 // Real-to-complex pass along the contiguous axis: two real lines (2c, 2c+1) packed into one complex
 // FFT; Pre(line, k) supplies the real inputs (line = item*N*N + x*N + y). The half spectra are written
@@ -193,7 +205,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   constexpr long NN = (long)N * N;
   __shared__ float2 tw[N];
   __shared__ float2 ex[ex_size<N, LINES, true>()];
-  const long l_base = (long)blockIdx.x * RL;
+  const long l_base = tile_first_line(pre, (long)blockIdx.x, RL);
   if constexpr (has_pad_lines<Pre>::value) {
     // a CTA whose lines are all padding lines writes their spectra directly: the N-point transform of
     // c (-1)^(x+y+z) is N c (-1)^(x+y) at k = N/2 and zero elsewhere
@@ -217,8 +229,7 @@ __global__ void __launch_bounds__(LINES * ((Split<N>::A > Split<N>::B) ? Split<N
   load_full_twiddles<N>(tw);
   int line, lane;
   thread_map<N, LINES, true>(line, lane);
-  const long c = (long)blockIdx.x * LINES + line;  // complex line = real lines 2c, 2c+1
-  const long l0 = 2 * c;
+  const long l0 = l_base + 2 * line;  // complex line = real lines l0, l0 + 1
   const bool ok0 = l0 < n_lines, ok1 = l0 + 1 < n_lines;
   float2 v[A], o[B];
   pre.begin();

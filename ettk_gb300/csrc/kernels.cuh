@@ -1202,6 +1202,21 @@ struct PrePadded {
   // the z pass of a padding line writes only its kz = N2/2 entry (the padded magnitude pass of k_fft2d_padded
   // reads no other plane of such a line)
   bool nyquist_only = false;
+  // the z pass runs over the lines x < N, y < N alone, in tiles of RL consecutive y (RL divides N); the padding
+  // lines' only nonzero entry, N2 c (-1)^(x+y) at kz = N2/2, is supplied by the magnitude pass of that plane
+  bool real_only = false;
+  static constexpr bool kLineBase = true;
+  ETTK_DEV long line_base(long tile, int RL) const {
+    const int N2 = 2 * N, per_row = N / RL;
+    const long per_item = (long)N * per_row;
+    const long e = tile / per_item, r = tile - e * per_item;
+    const int x = (int)(r / per_row), yb = (int)(r - (long)x * per_row);
+    return e * N2 * N2 + (long)x * N2 + (long)yb * RL;
+  }
+  ETTK_HD long real_tiles(long lines, int RL) const {
+    const long N2 = 2 * N;
+    return lines / (N2 * N2) * N * (N / RL);
+  }
   // line (x, y) with x >= N or y >= N lies wholly in the padding: r[z] = c (-1)^(x+y+z)
   ETTK_DEV bool pad_line(long line, float &c, float &sign_xy) {
     const int N2 = 2 * N;

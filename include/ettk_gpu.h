@@ -56,6 +56,9 @@ typedef struct {
   int wigner_precision;         /* Wigner-d contraction of the SO(3) correlation (no reference setting; the
                                    reference contracts in FP64): 0 FP32 (default, parity), 1 BF16 tensor cores,
                                    2 split-BF16 tensor cores, 3 TF32 tensor cores, 4 FP64 (precision reference) */
+  int fast_coarse_so3;          /* fast form only (ettk_gpu_align_pairs_refined; no reference setting): 1 runs its
+                                   SO(3) search on the volumes Fourier-cropped to half the edge at bandwidth B/2, the
+                                   grid the candidate screening already uses; 0 searches at the full edge and B */
 } ettk_params;
 
 /* Per-volume metadata: the columns of the reference's 33-column volume list
