@@ -6,9 +6,10 @@ translational CCF candidates, alignment_mode 3) through the library's getDistanc
   value : pairs/s with the particle volumes already resident in HBM (set_particles_device + align)
   e2e   : pairs/s through the host-buffer API: pinned host volumes copied in every step
           (ettk_gpu_set_particles) and the result rows read back (ettk_gpu_align_pairs)
-  fast_form : the same pairs through the fast form (ettk_gpu_align_pairs_refined: split-BF16 Wigner contraction,
-          half-grid candidate screening, local refinement): alignments/s, speed-up over the plain form, e2e, and
-          both forms' rotation/shift errors against the generating poses
+  fast_form : the same pairs through the fast form (ettk_gpu_align_pairs_refined: coarse SO(3) search on the half
+          grid at B/2 with the split-BF16 Wigner contraction, half-grid candidate screening, local refinement):
+          alignments/s, speed-up over the plain form, e2e, and both forms' rotation/shift errors against the
+          generating poses
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank aligns its own batch on its own GPU (independent replicas, no collective
@@ -29,8 +30,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "align64_b32"
 FAST_PRECISION = 2   # split-BF16 Wigner-d contraction on the tensor cores
-FAST_ITERATIONS = 6  # local refinement steps of the fast form
-FAST_COARSE = 0  # 1: the fast form's SO(3) search on the half grid at B/2
+FAST_ITERATIONS = 9  # local refinement steps of the fast form
+FAST_COARSE = 1  # the fast form's SO(3) search on the half grid at B/2 (0: at the full edge and B)
 METRIC = "alignments/s at 64^3 bw=32: plain GPU vs batched+adjoint form at <=0.5deg/0.1 vox"
 
 
@@ -53,7 +54,7 @@ def parse():
     ap.add_argument("--fast-study", action="store_true",
                     help="plain form against the fast form (coarse SO(3) hit, one CCF per kept peak, local refinement) "
                          "on the 64^3 B=32 workload: alignments/s, stage times and errors against the generating poses")
-    ap.add_argument("--fast-iterations", type=int, default=6)
+    ap.add_argument("--fast-iterations", type=int, default=FAST_ITERATIONS)
     ap.add_argument("--workload", default=WORKLOAD, help="workload of the studies (align64_b32, refine64_b32)")
     ap.add_argument("--fast-peaks", type=int, default=0, help="0: the metric's candidate_peaks")
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
@@ -642,9 +643,10 @@ def main():
             "e2e": {"value": world * P * a.steps / (ms_fast_e2e * 1e-3), "unit": "alignments/s",
                     "h2d_bytes_per_step": P * N ** 3 * 4, "d2h_bytes_per_step": P * 17 * 4},
             "gpu_launches": fast_launches,
-            "method": "SO(3) grid with split-BF16 tcgen05 Wigner contraction, CCF of the candidatePeaks + 1 best "
-                      "candidates on half-grid Fourier crops, %d steps of local 6-DOF refinement by the analytic "
-                      "gradient of the masked normalised correlation" % FAST_ITERATIONS,
+            "method": "SO(3) grid on the %s with split-BF16 tcgen05 Wigner contraction, CCF of the candidatePeaks + "
+                      "1 best candidates on half-grid Fourier crops, %d steps of local 6-DOF refinement by the "
+                      "analytic gradient of the masked normalised correlation"
+                      % ("half grid at B/2" if FAST_COARSE else "full grid", FAST_ITERATIONS),
             "errors": {"plain": error_summary(rp, sp, hit), "fast": dict(error_summary(rf, sf, hit),
                                                                          basin_hits_fast=int((rf < 20.0).sum())),
                        "note": "against the generating poses; medians and means over the pairs whose plain grid hit "

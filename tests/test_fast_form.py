@@ -26,8 +26,8 @@ def vol(img, meta):
     return WedgedSubImage3D(img, **{k: meta[k] for k in KW})
 
 
-def metric(ds, n):
-    m = ProjectionRotationMetric3D(ds.params)
+def metric(ds, n, **extra):
+    m = ProjectionRotationMetric3D(dict(ds.params, **extra))
     m.set_references([vol(ds.references[0], ds.ref_meta[0])])
     m.set_particles([vol(ds.particles[i], ds.meta[i]) for i in range(n)])
     return m
@@ -107,16 +107,22 @@ def ds64():
     return synthetic.generate("align64_b32", n_particles=24)
 
 
-def test_fast_form_against_plain_form(ds64):
+@pytest.mark.parametrize("coarse", [0, 1])
+def test_fast_form_against_plain_form(ds64, coarse):
+    """The fast form (coarse = 1: its SO(3) search on the half grid at B/2, split-BF16 Wigner contraction) against
+    the plain form on the same pairs: refined rows score at least their coarse start, and the median errors against
+    the generating poses are no worse than the plain grid's over the pairs the grid puts in the right basin."""
     n = 24
     pairs = [(0, i) for i in range(n)]
     m = metric(ds64, n)
+    mf = metric(ds64, n, fast_coarse_so3=coarse, wigner_precision=2 if coarse else 0)
     try:
         Dp = m.getDistances(pairs)
-        D0 = m.getDistancesRefined(pairs, iterations=0)
-        Df = m.getDistancesRefined(pairs, cols=19, ncand=2, iterations=16)
+        D0 = mf.getDistancesRefined(pairs, iterations=0)
+        Df = mf.getDistancesRefined(pairs, cols=19, ncand=2, iterations=16)
     finally:
         m.close()
+        mf.close()
     assert np.all(Df[:, 0, 1] == np.finfo(np.float32).max)
     assert np.all(Df[:, 1, 0] == 1.0)
     assert np.all((Df[:, 2, 0] > 0) & (Df[:, 2, 0] <= 1.0))
