@@ -1307,28 +1307,63 @@ __global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__
       xm[t] = ((N2 - x) & MSK) * N2;
     }
     float v = 0.f;
+    // Taps with 1 <= y <= 2N - 1 on all four rows (every sample inside the band): each row of four consecutive y
+    // (or, mirrored, four consecutive 2N - y) is read as one or two aligned 16-byte quads, a quarter to half of
+    // the per-tap load instructions; the sum keeps the order of the per-tap path below, so the values agree bit
+    // for bit.
+    const int y0 = iy - 1;
+    if (y0 >= 1 && y0 + 3 <= MSK) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int z = (iz - 1 + k) & MSK;
-      const bool mir = z > N;
-      const int zo = (mir ? N2 - z : z) * N2 * N2;
+      for (int k = 0; k < 4; ++k) {
+        const int z = (iz - 1 + k) & MSK;
+        const bool mir = z > N;
+        const int zo = (mir ? N2 - z : z) * N2 * N2;
+        const int ys = mir ? N2 - y0 - 3 : y0;  // first y of the row's run in memory
+        const int s = ys & 3;
+        float g[4][4];                          // [j][t]
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int y = (iy - 1 + j) & MSK;
-        float g[4];
-        if (!mir) {
-          const int base = zo + y;
+        for (int t = 0; t < 4; ++t) {
+          const float *row = M + zo + (mir ? xm[t] : xo[t]) + (ys - s);
+          const float4 a = __ldg(reinterpret_cast<const float4 *>(row));
+          const float4 b = s ? __ldg(reinterpret_cast<const float4 *>(row + 4)) : make_float4(0.f, 0.f, 0.f, 0.f);
+          float r[4];
+          switch (s) {
+            case 0: r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w; break;
+            case 1: r[0] = a.y; r[1] = a.z; r[2] = a.w; r[3] = b.x; break;
+            case 2: r[0] = a.z; r[1] = a.w; r[2] = b.x; r[3] = b.y; break;
+            default: r[0] = a.w; r[1] = b.x; r[2] = b.y; r[3] = b.z; break;
+          }
 #pragma unroll
-          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xo[t]);
-        } else if (y == 0) {
-#pragma unroll
-          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : pc;
-        } else {
-          const int base = zo + (N2 - y);
-#pragma unroll
-          for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xm[t]);
+          for (int j = 0; j < 4; ++j) g[j][t] = x0[t] ? 0.f : (mir ? r[3 - j] : r[j]);
         }
-        v += (wz[k] * wy[j]) * (wx[0] * g[0] + wx[1] * g[1] + wx[2] * g[2] + wx[3] * g[3]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          v += (wz[k] * wy[j]) * (wx[0] * g[j][0] + wx[1] * g[j][1] + wx[2] * g[j][2] + wx[3] * g[j][3]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int z = (iz - 1 + k) & MSK;
+        const bool mir = z > N;
+        const int zo = (mir ? N2 - z : z) * N2 * N2;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int y = (iy - 1 + j) & MSK;
+          float g[4];
+          if (!mir) {
+            const int base = zo + y;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xo[t]);
+          } else if (y == 0) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : pc;
+          } else {
+            const int base = zo + (N2 - y);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) g[t] = x0[t] ? 0.f : __ldg(M + base + xm[t]);
+          }
+          v += (wz[k] * wy[j]) * (wx[0] * g[0] + wx[1] * g[1] + wx[2] * g[2] + wx[3] * g[3]);
+        }
       }
     }
     acc += v;

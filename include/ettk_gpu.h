@@ -263,7 +263,8 @@ int ettk_gpu_score_pairs(ettk_ctx *ctx, int npairs, const int *pairs, float *D, 
 /* Fast alignment form (no counterpart in the reference; it takes the place of getDistances with typeOfMetric 0,
    whose Powell refinement, inc/em/nbfFourierImageMetric.h:1701-1809, and whose mirror and candidate CCF loop,
    inc/em/nbfProjectionRotationMetric3D.h:678-901, it replaces): the same spherical projections, SO(3) correlations
-   (in the context's wigner_precision) and candidate queues as ettk_gpu_align_pairs, then per pair one CCF
+   (in the context's wigner_precision) and candidate queues as ettk_gpu_align_pairs — or, with fast_coarse_so3, the
+   same on the volumes Fourier-cropped to half the edge at bandwidth B/2 — then per pair one CCF
    (executeFourierNewHalf) of each of the `peaks` best candidates of the windowed queue and of the peaks / 3 (at
    least one) best of the unwindowed one, no mirror evaluations, computed for boxes of edge 32 and more on the
    volumes Fourier-cropped to half the edge (the band-pass keeps little above half the Nyquist frequency), and the
