@@ -866,6 +866,8 @@ struct ettk_ctx {
   void lr_filter_particles(const std::vector<int> &parts, bool with_half = false);
   DevBuf<double> lr_acc;
   double lr_C0 = 0, lr_C1 = 0;  // sum m, sum m^2 of the spherical mask
+  DevBuf<int> lr_in;             // indices of the voxels with m != 0 (ascending)
+  long lr_nin = 0;
   double lr_radius() const { return 0.6 * (p.mask_radius > 0 ? p.mask_radius : 0.5 * N); }
   // zm of every request (reference filtered with the wedges at the request's pose, times the mask), the
   // refinement states at the requests' poses and their index maps
@@ -874,9 +876,10 @@ struct ettk_ctx {
   void lr_run(long P, int iterations);
   template <int NN>
   void lr_eval_t(long E) {
-    constexpr int SLAB = NN >= 64 ? 4 : (NN >= 32 ? 8 : 16);
-    Scope sc(this, "local_refine", 4.0 * E * (double)n3 * 2);
-    k_lr_eval<NN, SLAB><<<dim3(NN / SLAB, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, mask.p, lr_acc.p);
+    Scope sc(this, "local_refine", 4.0 * E * (double)lr_nin * 3);
+    const unsigned chunks = (unsigned)std::max<long>(1, (lr_nin + LR_CHUNK - 1) / LR_CHUNK);
+    k_lr_eval<NN><<<dim3(chunks, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, mask.p, lr_in.p,
+                                                            (int)lr_nin, lr_acc.p);
     post_launch();
   }
   void lr_eval(long E) { with_n(N, [&](auto nn) { lr_eval_t<decltype(nn)::value>(E); }); }
@@ -1780,9 +1783,16 @@ void ettk_ctx::init_tables() {
   filter.ensure(h3);
   h2d(mask.p, m.data(), n3 * 4);
   lr_C0 = lr_C1 = 0;
-  for (long i = 0; i < n3; ++i) {
-    lr_C0 += (double)m[i];
-    lr_C1 += (double)m[i] * (double)m[i];
+  {
+    std::vector<int> ids;  // the voxels inside the mask, in index order: the only ones the refinement's sums see
+    for (long i = 0; i < n3; ++i) {
+      lr_C0 += (double)m[i];
+      lr_C1 += (double)m[i] * (double)m[i];
+      if (m[i] != 0.f) ids.push_back((int)i);
+    }
+    lr_nin = (long)ids.size();
+    lr_in.ensure(std::max<long>(1, lr_nin));
+    if (lr_nin) h2d(lr_in.p, ids.data(), lr_nin * sizeof(int));
   }
   h2d(maskfft.p, mf.data(), n3 * 4);
   {
@@ -3352,6 +3362,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_jobs.release();
   c->w_sjobs.release();
   c->repr_idx_dev.release();
+  c->lr_in.release();
   c->real_idx_dev.release();
   c->w_plans.release();
   if (c->st) cudaStreamDestroy(c->st);

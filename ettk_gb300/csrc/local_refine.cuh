@@ -40,13 +40,16 @@ struct LRState {
   int done, accepted;
 };
 
+constexpr int LR_CHUNK = 8192;  // in-mask voxels per CTA of k_lr_eval
+
 // Sums of pair e (acc[e][0..27]): S1 = sum m I, S2 = sum m^2 I, S3 = sum m^2 I^2, S4 = sum zm I, then for each
-// derivative k (w0..w2, d0..d2): sum m D_k, sum m^2 D_k, sum m^2 I D_k, sum zm D_k. FP32 per-thread partials,
-// FP64 across the CTA and across CTAs.
-template <int N, int SLAB>
+// derivative k (w0..w2, d0..d2): sum m D_k, sum m^2 D_k, sum m^2 I D_k, sum zm D_k. Every term carries m or zm = m y1,
+// so only the nin voxels inside the mask (their indices in `in`, ascending) are visited: CTA (x, e) takes the chunk
+// [x LR_CHUNK, (x + 1) LR_CHUNK) of them. FP32 per-thread partials, FP64 across the CTA and across CTAs.
+template <int N>
 __global__ void __launch_bounds__(256) k_lr_eval(const LRItem *__restrict__ items, const float *__restrict__ maps,
                                                  const float *__restrict__ zm, const float *__restrict__ mask,
-                                                 double *__restrict__ acc) {
+                                                 const int *__restrict__ in, int nin, double *__restrict__ acc) {
   constexpr long n3 = (long)N * N * N;
   __shared__ float red[8][LR_NACC];
   const int e = blockIdx.y;
@@ -63,12 +66,11 @@ __global__ void __launch_bounds__(256) k_lr_eval(const LRItem *__restrict__ item
   float s[LR_NACC];
 #pragma unroll
   for (int k = 0; k < LR_NACC; ++k) s[k] = 0.f;
-  const int a0 = blockIdx.x * SLAB;
-  for (int v = threadIdx.x; v < SLAB * N * N; v += blockDim.x) {
-    const int a = a0 + v / (N * N), b = (v / N) % N, c = v % N;
-    const long id = ((long)a * N + b) * N + c;
+  const int v1 = min(nin, (int)(blockIdx.x + 1) * LR_CHUNK);
+  for (int v = blockIdx.x * LR_CHUNK + threadIdx.x; v < v1; v += blockDim.x) {
+    const int id = __ldg(in + v);
+    const int a = id / (N * N), b = (id / N) % N, c = id % N;
     const float mv = __ldg(mask + id);
-    if (mv == 0.f) continue;
     const float zv = __ldg(Z + id);
     const float px = M[0] + a * M[3] + b * M[6] + c * M[9];
     const float py = M[1] + a * M[4] + b * M[7] + c * M[10];
