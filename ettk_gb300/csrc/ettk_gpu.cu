@@ -898,6 +898,23 @@ struct ettk_ctx {
   cudaEvent_t dec_ev = nullptr;
   void half_particles(const std::vector<int> &pp);
   void merge_child_profile();
+  // NaN / infinity check of an upload on the device, queued behind its copy; finite_or_throw after the next sync
+  // (a failed upload leaves the context without particles)
+  DevBuf<int> nf_flag;
+  void check_finite(const float *v, long n) {
+    nf_flag.ensure(1);
+    CK(cudaMemsetAsync(nf_flag.p, 0, sizeof(int), st));
+    k_nonfinite<<<nblocks<int>((n + 3) / 4, 256, 4096), 256, 0, st>>>(v, n, nf_flag.p);
+    post_launch();
+  }
+  void finite_or_throw(const char *what) {
+    int bad = 0;
+    d2h(&bad, nf_flag.p, sizeof(int));
+    if (bad) {
+      V = 0;
+      throw CudaError(ETTK_ERR_NAN, what);
+    }
+  }
   // best CCF candidate per pair scored on the decimated volumes: full-grid transform (translation doubled)
   void half_screen(const std::vector<int> &pr, const std::vector<int> &pp, const std::vector<EvalReq> &cand,
                    const std::vector<int> &owner, std::vector<EvalReq> &finals);
@@ -3363,6 +3380,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   c->w_sjobs.release();
   c->repr_idx_dev.release();
   c->lr_in.release();
+  c->nf_flag.release();
   c->real_idx_dev.release();
   c->w_plans.release();
   if (c->st) cudaStreamDestroy(c->st);
@@ -3432,7 +3450,6 @@ static void particle_tables(ettk_ctx *c, const ettk_volume_meta *meta);
 
 static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_volume_meta *meta, bool device) {
   if (!c || V <= 0 || !vols || !meta) return fail(c, ETTK_ERR_ARG, "invalid particle arguments");
-  if (!device && !finite_volume(vols, (long)V * c->n3)) return fail(c, ETTK_ERR_NAN, "non-finite particle volume");
   return guarded(c, [&] {
     long n3 = c->n3;
     c->V = V;
@@ -3447,9 +3464,11 @@ static int set_particles_impl(ettk_ctx *c, int V, const float *vols, const ettk_
       CK(cudaMemcpyAsync(c->partvol.p, vols, V * n3 * 4, cudaMemcpyHostToDevice, c->st));
       c->partptr = c->partvol.p;
     }
-    particle_tables(c, meta);  // host work overlaps the volume upload
+    c->check_finite(c->partptr, (long)V * n3);  // on the device, behind the upload
+    particle_tables(c, meta);                   // host work overlaps the volume upload
     c->upload_maps(c->partptr, V, c->tm_part, c->tm_part_ok);
     c->sync();
+    c->finite_or_throw("non-finite particle volume");
   });
 }
 
@@ -3475,7 +3494,6 @@ int ettk_gpu_set_particles_tomogram(ettk_ctx *c, int nx, int ny, int nz, const f
   if (!c || nx < 1 || ny < 1 || nz < 1 || !tomogram || V <= 0 || !meta)
     return fail(c, ETTK_ERR_ARG, "invalid tomogram arguments");
   const long nt = (long)nx * ny * nz;
-  if (!finite_volume(tomogram, nt)) return fail(c, ETTK_ERR_NAN, "non-finite tomogram");
   return guarded(c, [&] {
     c->V = V;
     c->partg.resize(V);
@@ -3483,6 +3501,7 @@ int ettk_gpu_set_particles_tomogram(ettk_ctx *c, int nx, int ny, int nz, const f
     c->pp2_ready.assign(V, 0);
     c->tomo.ensure(nt);
     CK(cudaMemcpyAsync(c->tomo.p, tomogram, nt * 4, cudaMemcpyHostToDevice, c->st));
+    c->check_finite(c->tomo.p, nt);
     c->tomo_dims[0] = nx;
     c->tomo_dims[1] = ny;
     c->tomo_dims[2] = nz;
@@ -3491,6 +3510,7 @@ int ettk_gpu_set_particles_tomogram(ettk_ctx *c, int nx, int ny, int nz, const f
     c->upload_maps(c->tomo.p, 1, c->tm_part, c->tm_part_ok, c->tomo_dims);
     particle_tables(c, meta);
     c->sync();
+    c->finite_or_throw("non-finite tomogram");
   });
 }
 

@@ -1371,6 +1371,21 @@ __global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__
   Pp[(long)(out_index ? out_index[e] : e) * n_dirs + d] = acc;
 }
 
+// *flag |= 1 when v[0..n) holds a NaN or an infinity (exponent field all ones); 16-byte loads, grid-stride.
+static __global__ void k_nonfinite(const float *__restrict__ v, long n, int *flag) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(v);
+  const long n4 = n >> 2;
+  uint32_t any = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long)gridDim.x * blockDim.x) {
+    const uint4 u = __ldg(q + i);
+    any |= ((u.x & 0x7f800000u) == 0x7f800000u) | ((u.y & 0x7f800000u) == 0x7f800000u) |
+           ((u.z & 0x7f800000u) == 0x7f800000u) | ((u.w & 0x7f800000u) == 0x7f800000u);
+  }
+  for (long i = (n4 << 2) + (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    any |= (__float_as_uint(v[i]) & 0x7f800000u) == 0x7f800000u;
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 // Corner value of the windowed image (the pad constant).
 static __global__ void k_pad_constant(PrePadded pre, int n_items, float *padc) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;

@@ -80,7 +80,9 @@ int ettk_gpu_destroy(ettk_ctx *ctx);
  * R reference volumes (R*N^3 floats) and their metadata. */
 int ettk_gpu_set_references(ettk_ctx *ctx, int R, const float *volumes, const ettk_volume_meta *meta);
 
-/* Replaces the list2 side: V particle volumes and metadata (host memory). */
+/* Replaces the list2 side: V particle volumes and metadata (host memory). A volume holding a NaN or an infinity
+ * (checked on the device after the copy, as for the _device and _tomogram variants) fails the call with
+ * ETTK_ERR_NAN and leaves the context without particles. */
 int ettk_gpu_set_particles(ettk_ctx *ctx, int V, const float *volumes, const ettk_volume_meta *meta);
 
 /* As ettk_gpu_set_particles with `volumes` already in device memory of the context's GPU. The buffer is
