@@ -190,3 +190,29 @@ def test_class_average(ds32, metric32):
     o = o.transpose(2, 1, 0)
     err = np.sqrt(np.mean((g - o) ** 2)) / np.sqrt(np.mean(o ** 2))
     assert err <= 1e-5, err
+
+
+def test_nonfinite_particles_rejected_and_context_recovers(ds32):
+    """A particle volume with a NaN or an infinity fails the upload with ETTK_ERR_NAN (checked on the device behind
+    the copy); the context then has no particles, and a valid upload afterwards aligns as before."""
+    from ettk_gb300 import _lib
+    from ettk_gb300.metric import EttkError
+    m = ProjectionRotationMetric3D(ds32.params)
+    try:
+        m.set_references([vol(ds32.references[0], ds32.ref_meta[0])])
+        good = [vol(ds32.particles[i], ds32.meta[i]) for i in range(2)]
+        m.set_particles(good)
+        D0 = m.getDistances([(0, 0), (0, 1)])
+        for value in (np.nan, np.inf, -np.inf):
+            img = ds32.particles[1].copy()
+            img[5, 6, 7] = value
+            with pytest.raises(EttkError) as ex:
+                m.set_particles([good[0], vol(img, ds32.meta[1])])
+            assert ex.value.code == _lib.ETTK_ERR_NAN
+            with pytest.raises(EttkError) as ex:
+                m.getDistances([(0, 0)])
+            assert ex.value.code == _lib.ETTK_ERR_STATE
+        m.set_particles(good)
+        assert np.array_equal(m.getDistances([(0, 0), (0, 1)]), D0)
+    finally:
+        m.close()
