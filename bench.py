@@ -62,6 +62,8 @@ def parse():
                     help="1: the fast form's SO(3) search on the half grid at B/2")
     ap.add_argument("--fast-only", action="store_true",
                     help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")
+    ap.add_argument("--tune-study", action="store_true",
+                    help="plain-form rate under the default launch shapes, the autotuner's trials, the tuned rate")
     ap.add_argument("--config-table", action="store_true",
                     help="plain and fast form on every alignment configuration, the oracle beside each, one "
                          "classification pass (--study-pairs particles x 10 references)")
@@ -373,6 +375,46 @@ def compare_forms(ds, P, iterations, peaks, precision, fast_only=False, coarse=F
     return out
 
 
+def tune_study(a):
+    """The launch-shape autotuner on the headline workload: plain-form alignments/s of P pairs (particles resident,
+    CUDA-synchronised wall time of three steps after one warm-up) under the default shapes, the autotuner's trials on a
+    64-pair sample, and the same rate under the chosen shapes (result rows compared bit for bit)."""
+    import numpy as np
+    import torch
+    from ettk_gb300 import synthetic
+    from ettk_gb300.metric import ProjectionRotationMetric3D, WedgedSubImage3D
+    P = a.pairs
+    ds = synthetic.generate(WORKLOAD, n_particles=P)
+    kw = ("lwedge", "uwedge", "normal", "matrix", "position", "cut_offset")
+    metas = [{k: m[k] for k in kw} for m in ds.meta]
+    m = ProjectionRotationMetric3D(ds.params)
+    m.set_references([WedgedSubImage3D(ds.references[0], **{k: ds.ref_meta[0][k] for k in kw})])
+    parts = torch.from_numpy(ds.particles).to("cuda")
+    pairs = [(0, i) for i in range(P)]
+
+    def rate():
+        def step():
+            m.set_particles_device(parts.data_ptr(), metas)
+            return m.getDistances(pairs)
+        step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            D = step()
+        torch.cuda.synchronize()
+        return 3 * P / (time.perf_counter() - t0), D
+
+    r0, D0 = rate()
+    m.set_particles_device(parts.data_ptr(), metas)
+    best, trials = m.autotune(pairs[:64], repeats=3)
+    r1, D1 = rate()
+    m.close()
+    print(json.dumps({"tune_study": {"default_alignments_per_s": r0, "tuned_alignments_per_s": r1,
+                                     "tuned": best, "identical_rows": bool(np.array_equal(D0, D1)),
+                                     "trials": trials},
+                      "config": {"workload": WORKLOAD, "pairs": P, "sample_pairs": 64}}), flush=True)
+
+
 def config_table(a):
     """The results table of the configurations: per alignment configuration the plain and the fast form
     (alignments/s, errors against the generating poses) and the oracle on the host cores on a bounded sample;
@@ -467,6 +509,9 @@ def main():
         return
     if a.config_table:
         config_table(a)
+        return
+    if a.tune_study:
+        tune_study(a)
         return
     if a.adjoint_study:
         adjoint_study(a)

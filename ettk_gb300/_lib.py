@@ -47,6 +47,11 @@ class Params(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("synth_job_blocks", ctypes.c_int), ("eval_chunk", ctypes.c_int), ("zpass_oversub", ctypes.c_int),
+                ("sample_block", ctypes.c_int)]
+
+
 class VolumeMeta(ctypes.Structure):
     _fields_ = [
         ("lwedge", ctypes.c_float), ("uwedge", ctypes.c_float), ("normal", ctypes.c_float * 3),
@@ -63,7 +68,7 @@ SYMBOLS = [
     "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
     "ettk_gpu_representation_distances", "ettk_gpu_representations", "ettk_gpu_representations_real",
-    "ettk_gpu_mean_images",
+    "ettk_gpu_mean_images", "ettk_gpu_get_tuning", "ettk_gpu_set_tuning", "ettk_gpu_autotune",
     "ettk_gpu_mra_assign",
     "ettk_gpu_align_pairs_refined", "ettk_gpu_refined_objective", "ettk_gpu_score_pairs",
     "ettk_gpu_average_partial", "ettk_gpu_average_finish", "ettk_gpu_wait_probe",
@@ -117,6 +122,9 @@ def load(path=None):
     L.ettk_gpu_set_reference_spherical_wedge.argtypes = [vp, ctypes.c_int, vp]
     L.ettk_gpu_representations.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, P(ctypes.c_int), vp]
     L.ettk_gpu_mean_images.argtypes = [vp, vp, ctypes.c_int, vp, vp]
+    L.ettk_gpu_get_tuning.argtypes = [vp, P(Tuning)]
+    L.ettk_gpu_set_tuning.argtypes = [vp, P(Tuning)]
+    L.ettk_gpu_autotune.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, P(Tuning), ctypes.c_char_p, ctypes.c_int]
     L.ettk_gpu_representations_real.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int), vp]
     L.ettk_gpu_representation_distances.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                                     vp]

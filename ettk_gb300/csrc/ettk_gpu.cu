@@ -383,6 +383,8 @@ void wedge_half_host(const VolumeGeom &g, int N, std::vector<float> &W);
 struct ettk_ctx {
   int device = 0;
   ettk_params p{};
+  // launch shapes chosen by ettk_gpu_autotune or ettk_gpu_set_tuning; none of them changes a result
+  ettk_tuning tune{64, 4096, 1, 128};
   cudaStream_t st = nullptr;
   int N = 0, H = 0, B = 0, n = 0;
   long n3 = 0, h3 = 0, nn = 0, nso3 = 0;
@@ -416,7 +418,7 @@ struct ettk_ctx {
                               256, 0, st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab64.p, doff.p, w_S.p);
         break;
       default:
-        k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(64, (NJ + 7) / 8)), 256, 0,
+        k_so3_synth<BB><<<dim3((2 * BB - 1) * (2 * BB - 1), (unsigned)std::min<long>(tune.synth_job_blocks, (NJ + 7) / 8)), 256, 0,
                           st>>>(w_coef.p, w_jobs.p, (int)NJ, dtab.p, doff.p, w_S.p);
     }
     post_launch();
@@ -667,11 +669,11 @@ struct ettk_ctx {
       if ((sa & 15) == 0 && (aa & 15) == 0) {
         if (aa) {
           constexpr size_t smem = r2c_stream_smem<NN, true>();
-          const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre, true>, smem));
+          const int grid = (int)std::min<long>(tiles, tune.zpass_oversub * resident_grid(k_r2c_stream<NN, L, Pre, true>, smem));
           k_r2c_stream<NN, L, Pre, true><<<grid, 256, smem, st>>>(pre, out, lines);
         } else {
           constexpr size_t smem = r2c_stream_smem<NN, false>();
-          const int grid = (int)std::min<long>(tiles, resident_grid(k_r2c_stream<NN, L, Pre, false>, smem));
+          const int grid = (int)std::min<long>(tiles, tune.zpass_oversub * resident_grid(k_r2c_stream<NN, L, Pre, false>, smem));
           k_r2c_stream<NN, L, Pre, false><<<grid, 256, smem, st>>>(pre, out, lines);
         }
         streamed = true;
@@ -721,7 +723,7 @@ struct ettk_ctx {
     Scope sc(this, "fft_c2r_z", 4.0 * lines * NN + 8.0 * lines * (NN / 2 + 1));
     if (lines % (2 * L) == 0 && (((unsigned long long)in) & 15) == 0) {
       constexpr size_t smem = c2r_stream_smem<NN>();
-      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_stream<NN, L, Post>, smem));
+      const int grid = (int)std::min<long>(tiles, tune.zpass_oversub * resident_grid(k_c2r_stream<NN, L, Post>, smem));
       k_c2r_stream<NN, L, Post><<<grid, 256, smem, st>>>(in, post, lines);
     } else {
       k_c2r_reg<NN, L, Post><<<(unsigned)tiles, 256, 0, st>>>(in, post, lines);
@@ -748,11 +750,11 @@ struct ettk_ctx {
       throw CudaError(ETTK_ERR_ARG, "fused z pass: lines must fill whole tiles of 16-byte aligned data");
     if (mid.aux) {
       constexpr size_t smem = c2r_r2c_stream_smem<NN, true>();
-      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_r2c_stream<NN, L, Mid, true>, smem));
+      const int grid = (int)std::min<long>(tiles, tune.zpass_oversub * resident_grid(k_c2r_r2c_stream<NN, L, Mid, true>, smem));
       k_c2r_r2c_stream<NN, L, Mid, true><<<grid, 256, smem, st>>>(data, mid, lines);
     } else {
       constexpr size_t smem = c2r_r2c_stream_smem<NN, false>();
-      const int grid = (int)std::min<long>(tiles, resident_grid(k_c2r_r2c_stream<NN, L, Mid, false>, smem));
+      const int grid = (int)std::min<long>(tiles, tune.zpass_oversub * resident_grid(k_c2r_r2c_stream<NN, L, Mid, false>, smem));
       k_c2r_r2c_stream<NN, L, Mid, false><<<grid, 256, smem, st>>>(data, mid, lines);
     }
     post_launch();
@@ -831,7 +833,7 @@ struct ettk_ctx {
   // fewer host round trips and larger grids
   void eval_batch(const std::vector<EvalReq> &req, std::vector<EvalRes> &res) {
     res.resize(req.size());
-    const size_t chunk = (size_t)std::min(8192L, std::max(256L, 4096L * 64 * 64 * 64 / n3));
+    const size_t chunk = (size_t)std::min(16384L, std::max(256L, (long)tune.eval_chunk * 64 * 64 * 64 / n3));
     for (size_t c0 = 0; c0 < req.size(); c0 += chunk) {
       size_t c1 = std::min(req.size(), c0 + chunk);
       std::vector<EvalReq> sub(req.begin() + c0, req.begin() + c1);
@@ -1969,8 +1971,8 @@ void ettk_ctx::spherical_projection(const std::vector<ResliceItem> &items, float
   switch (N) {
 #define SS_CASE(NN)                                                                                              \
   case NN:                                                                                                       \
-    k_sphere_sample<NN><<<dim3(nblocks<int>(nn, 128), P), 128, 0, st>>>(sp_M.p, dirs.p, (int)nn, bandL, bandU,   \
-                                                                        sp_padc.p, Pp_out, out_index);          \
+    k_sphere_sample<NN><<<dim3(nblocks<int>(nn, tune.sample_block), P), tune.sample_block, 0, st>>>(            \
+        sp_M.p, dirs.p, (int)nn, bandL, bandU, sp_padc.p, Pp_out, out_index);                                    \
     break;
     SS_CASE(16)
     SS_CASE(32)
@@ -3552,6 +3554,98 @@ int ettk_gpu_refined_objective(ettk_ctx *c, int npairs, const int *pairs, const 
   if (!c || npairs <= 0 || !pairs || !poses || !theta || !rho) return fail(c, ETTK_ERR_ARG, "invalid arguments");
   if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
   return guarded(c, [&] { c->refined_objective(npairs, pairs, poses, theta, rho, grad); });
+}
+
+// ---- launch-shape tuning ---------------------------------------------------------------------
+
+static const int kTuneSynth[] = {16, 32, 64, 128}, kTuneChunk[] = {1024, 2048, 4096, 8192}, kTuneOver[] = {1, 2},
+                 kTuneSample[] = {64, 128, 256};
+static bool tune_in(int v, const int *list, int n) { return std::find(list, list + n, v) != list + n; }
+static bool tuning_valid(const ettk_tuning &t) {
+  return tune_in(t.synth_job_blocks, kTuneSynth, 4) && tune_in(t.eval_chunk, kTuneChunk, 4) &&
+         tune_in(t.zpass_oversub, kTuneOver, 2) && tune_in(t.sample_block, kTuneSample, 3);
+}
+
+int ettk_gpu_get_tuning(ettk_ctx *c, ettk_tuning *t) {
+  if (!c || !t) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  *t = c->tune;
+  return ETTK_OK;
+}
+
+int ettk_gpu_set_tuning(ettk_ctx *c, const ettk_tuning *t) {
+  if (!c || !t || !tuning_valid(*t)) return fail(c, ETTK_ERR_ARG, "invalid launch shapes");
+  c->tune = *t;
+  return ETTK_OK;
+}
+
+int ettk_gpu_autotune(ettk_ctx *c, int npairs, const int *pairs, int repeats, ettk_tuning *best, char *report,
+                      int report_size) {
+  if (!c || npairs < 1 || !pairs || repeats < 1 || repeats > 20 || (report && report_size < 1))
+    return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  if (!c->R || !c->V) return fail(c, ETTK_ERR_STATE, "references or particles not set");
+  for (int i = 0; i < npairs; ++i)
+    if (pairs[2 * i] < 0 || pairs[2 * i] >= c->R || pairs[2 * i + 1] < 0 || pairs[2 * i + 1] >= c->V)
+      return fail(c, ETTK_ERR_ARG, "pair index out of range");
+  return guarded(c, [&] {
+    const ettk_tuning start = c->tune;
+    std::string js = "[";
+    std::vector<float> ref;
+    // median wall time of `repeats` synchronous alignments of the sample under t (after one warm-up), and whether
+    // the rows equal the first trial's bit for bit
+    auto trial = [&](const ettk_tuning &t, bool &same) -> double {
+      c->tune = t;
+      std::vector<double> ms;
+      std::vector<float> D;
+      for (int r = 0; r <= repeats; ++r) {
+        std::fill(c->pp2_ready.begin(), c->pp2_ready.end(), 0);  // time the spherical projections too
+        D.assign((size_t)npairs * 17, -1.f);
+        const auto t0 = std::chrono::steady_clock::now();
+        c->align(npairs, pairs, D.data(), 17, 1);
+        const auto t1 = std::chrono::steady_clock::now();
+        if (r > 0) ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+      }
+      std::sort(ms.begin(), ms.end());
+      if (ref.empty()) ref = D;
+      same = memcmp(D.data(), ref.data(), D.size() * sizeof(float)) == 0;
+      const double med = ms[ms.size() / 2];
+      char buf[256];
+      snprintf(buf, sizeof buf,
+               "%s{\"synth_job_blocks\": %d, \"eval_chunk\": %d, \"zpass_oversub\": %d, \"sample_block\": %d, "
+               "\"ms\": %.4f, \"identical\": %s}",
+               js.size() > 1 ? ", " : "", t.synth_job_blocks, t.eval_chunk, t.zpass_oversub, t.sample_block, med,
+               same ? "true" : "false");
+      js += buf;
+      return med;
+    };
+    ettk_tuning cur = tuning_valid(start) ? start : ettk_tuning{64, 4096, 1, 128};
+    bool same = true;
+    double cur_ms = trial(cur, same);
+    auto search = [&](int ettk_tuning::*field, const int *vals, int nv) {
+      for (int k = 0; k < nv; ++k) {
+        if (vals[k] == cur.*field) continue;
+        ettk_tuning t = cur;
+        t.*field = vals[k];
+        bool ok = true;
+        const double ms = trial(t, ok);
+        if (ok && ms < cur_ms) {
+          cur = t;
+          cur_ms = ms;
+        }
+      }
+    };
+    search(&ettk_tuning::synth_job_blocks, kTuneSynth, 4);
+    search(&ettk_tuning::eval_chunk, kTuneChunk, 4);
+    search(&ettk_tuning::zpass_oversub, kTuneOver, 2);
+    search(&ettk_tuning::sample_block, kTuneSample, 3);
+    c->tune = cur;
+    if (best) *best = cur;
+    js += "]";
+    if (report) {
+      const size_t n = std::min<size_t>(js.size(), (size_t)report_size - 1);
+      memcpy(report, js.data(), n);
+      report[n] = 0;
+    }
+  });
 }
 
 int ettk_gpu_wait_probe(ettk_ctx *c, int max_iter) {

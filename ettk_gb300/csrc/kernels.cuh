@@ -1275,7 +1275,7 @@ static __global__ void k_mutual_scale(float2 *__restrict__ F, long n) {
 // real-space value (the corner value).
 // 2N is a power of two, so the wrap of the tap indices is a mask; the mirror offsets are hoisted per axis.
 template <int N>
-__global__ void __launch_bounds__(128) k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs,
+__global__ void __launch_bounds__(256) k_sphere_sample(const float *__restrict__ Mh, const float4 *__restrict__ dirs,
                                                        int n_dirs, int bandL, int bandU, const float *__restrict__ padc,
                                                        float *__restrict__ Pp, const int *__restrict__ out_index) {
   constexpr int N2 = 2 * N, H = N + 1, MSK = N2 - 1;

@@ -385,6 +385,27 @@ class ProjectionRotationMetric3D:
         self._check(self.L.ettk_gpu_soft(self._ctx, a.ctypes.data, b.ctypes.data, int(scaled), C.ctypes.data), "soft")
         return C
 
+    # -- launch shapes (no counterpart in the reference) ---------------------------------------
+    def get_tuning(self):
+        t = _lib.Tuning()
+        self._check(self.L.ettk_gpu_get_tuning(self._ctx, ctypes.byref(t)), "get_tuning")
+        return {f[0]: getattr(t, f[0]) for f in _lib.Tuning._fields_}
+
+    def set_tuning(self, tuning):
+        t = _lib.Tuning(**{f[0]: int(tuning[f[0]]) for f in _lib.Tuning._fields_})
+        self._check(self.L.ettk_gpu_set_tuning(self._ctx, ctypes.byref(t)), "set_tuning")
+
+    def autotune(self, indexes, repeats=3):
+        """Chooses the launch shapes on the sample pairs (ettk_gpu_autotune) and applies them; returns
+        (tuning dict, list of trials)."""
+        import json
+        idx = np.ascontiguousarray(np.asarray(indexes, np.int32).reshape(-1, 2))
+        t = _lib.Tuning()
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self.L.ettk_gpu_autotune(self._ctx, idx.shape[0], idx.ctypes.data, int(repeats), ctypes.byref(t),
+                                             buf, len(buf)), "autotune")
+        return {f[0]: getattr(t, f[0]) for f in _lib.Tuning._fields_}, json.loads(buf.value.decode())
+
     def stream(self):
         """cudaStream_t of this context (for CUDA-event timing)."""
         return int(self.L.ettk_gpu_stream(self._ctx) or 0)

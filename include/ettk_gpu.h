@@ -61,6 +61,17 @@ typedef struct {
                                    grid the candidate screening already uses; 0 searches at the full edge and B */
 } ettk_params;
 
+/* Launch shapes of the library's kernels (no reference setting). None of them changes a result; they trade
+ * parallelism against scheduling overhead, and ettk_gpu_autotune chooses them per GPU and box size.
+ *   synth_job_blocks  job blocks per (m1, m2) cell of the FP32 Wigner-d synthesis: 16, 32, 64 (default) or 128
+ *   eval_chunk        CCF evaluations per device chunk at 64^3 (scaled by 64^3 / N^3): 1024, 2048, 4096 (default)
+ *                     or 8192
+ *   zpass_oversub     CTAs of the persistent z passes per resident CTA slot: 1 (default) or 2
+ *   sample_block      threads per CTA of the spherical sampling: 64, 128 (default) or 256 */
+typedef struct {
+  int synth_job_blocks, eval_chunk, zpass_oversub, sample_block;
+} ettk_tuning;
+
 /* Per-volume metadata: the columns of the reference's 33-column volume list
  * (nbfWedgedSubImage3D::serialize, inc/em/nbfWedgedSubImage3D.h:387-421). */
 typedef struct {
@@ -297,6 +308,20 @@ int ettk_gpu_refine_objective(ettk_ctx *ctx, int npairs, const int *pairs, const
  * nothing arrives at max_iter times (1 .. 2^24), gives up and flags it; the call returns ETTK_ERR_TIMEOUT, as any
  * call whose bulk copy or tensor-core commit never completes does, and the context stays usable. */
 int ettk_gpu_wait_probe(ettk_ctx *ctx, int max_iter);
+
+/* The context's launch shapes (ettk_tuning); set rejects values outside the lists above with ETTK_ERR_ARG. */
+int ettk_gpu_get_tuning(ettk_ctx *ctx, ettk_tuning *t);
+int ettk_gpu_set_tuning(ettk_ctx *ctx, const ettk_tuning *t);
+
+/* Chooses the launch shapes for the context's references and particles (no reference counterpart): aligns the
+ * npairs sample pairs (as ettk_gpu_align_pairs, 17 columns, one candidate, the particles' spherical projections
+ * recomputed every time) under candidate shapes, one field at a time with the others at their best so far
+ * (coordinate search over the values listed at ettk_tuning), each trial one warm-up and `repeats` timed runs
+ * (median wall time of the synchronous call). A shape whose result rows differ from the first trial's in any bit
+ * is rejected. The fastest shapes are applied to the context and written to *best (optional); report (optional,
+ * report_size bytes) receives a JSON array with one object per trial. repeats 1..20. */
+int ettk_gpu_autotune(ettk_ctx *ctx, int npairs, const int *pairs, int repeats, ettk_tuning *best, char *report,
+                      int report_size);
 
 /* Diagnostics (staged parity checks; no counterpart in the reference API):
  * one executeFourierNewHalf call (inc/em/nbfFourierImageMetric.h:1077-1323) of particle p against
