@@ -3621,8 +3621,9 @@ int ettk_gpu_autotune(ettk_ctx *c, int npairs, const int *pairs, int repeats, et
     bool same = true;
     double cur_ms = trial(cur, same);
     auto search = [&](int ettk_tuning::*field, const int *vals, int nv) {
+      const int timed = cur.*field;  // the field's value in the best shapes so far, already timed
       for (int k = 0; k < nv; ++k) {
-        if (vals[k] == cur.*field) continue;
+        if (vals[k] == timed) continue;
         ettk_tuning t = cur;
         t.*field = vals[k];
         bool ok = true;
