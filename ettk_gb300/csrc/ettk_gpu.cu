@@ -922,10 +922,6 @@ struct ettk_ctx {
                    const std::vector<int> &owner, std::vector<EvalReq> &finals);
   void refined_objective(int npairs, const int *pairs, const double *poses, const double *theta, double *rho,
                          double *grad);
-  // Euler matrix of every SO(3) grid cell (a, b, g) as the queues build it (B <= 32: 32 MB at B = 32), filled on
-  // the host threads at the first search
-  std::vector<Mat4> cell_mats;
-  void build_cell_mats();
   void so3_queues(int P, const std::vector<int> &pr, const std::vector<int> &pp, std::vector<PairPlan> &plans,
                   std::vector<PQ> &q1, std::vector<PQ> &q2);
   // nbfCorrelationImageMetric::getWedgeOverlap(T) of each request: sum(w1 w2 filter) / sum(filter) over the
@@ -2466,7 +2462,6 @@ case BB: {                                                                      
   }
   q1.assign(P, PQ());
   q2.assign(P, PQ());
-  if (B <= 32 && cell_mats.empty()) build_cell_mats();
   {
   HostScope hs_q(this, "host_queues");
   // queues are independent: build them on the host cores
@@ -2483,7 +2478,7 @@ case BB: {                                                                      
       float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
       if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
       float gamma = (float)(g / (double)B * 180.0);
-      const Mat4 m = cell_mats.empty() ? euler_candidate(alpha, beta, gamma) : cell_mats[e.x];
+      const Mat4 m = euler_candidate(alpha, beta, gamma);
       if (transform_valid(p, m)) {
         pos.push_back({{alpha, beta, gamma, -val}, -1});
         mats.push_back(m);
@@ -2493,24 +2488,6 @@ case BB: {                                                                      
   };
   parallel_for(2 * P, build_queue);
   }
-}
-
-// The candidate angles of cell (a, b, g) exactly as the queue builder derives them (the reference's float angles,
-// getTrueLocalMaximaPositions, inc/em/nbfProjectionRotationMetric3D.h:1593-1640) and their Euler matrices.
-void ettk_ctx::build_cell_mats() {
-  const int n = 2 * B;
-  cell_mats.resize((size_t)n * n * n);
-  parallel_for(n, [&](int a) {
-    const float alpha = (float)(a / (double)B * 180.0);
-    for (int bb = 0; bb < n; ++bb) {
-      float beta = (float)((2 * bb + 1.0) / (4. * B) * 180.0);
-      if ((float)B <= 32) beta = (float)((2 * bb + 0.0) / (4. * B) * 180.0);
-      for (int g = 0; g < n; ++g) {
-        const float gamma = (float)(g / (double)B * 180.0);
-        cell_mats[((size_t)a * n + bb) * n + g] = euler_candidate(alpha, beta, gamma);
-      }
-    }
-  });
 }
 
 void ettk_ctx::align(int npairs, const int *pairs, float *D, int cols, int ncand) {
