@@ -23,6 +23,9 @@
 #include <algorithm>
 #include <atomic>
 #include <thread>
+#include <condition_variable>
+#include <functional>
+#include <unistd.h>
 #include <type_traits>
 #include <array>
 #include <chrono>
@@ -2212,22 +2215,79 @@ bool transform_valid(const ettk_params &p, const Mat4 &t) {
   return ang <= p.restrict_rotation;
 }
 
-// Runs f(0..n-1) on up to 16 host threads (independent items; f must not throw).
+// Host worker threads shared by every context: up to 15 persistent workers plus the calling thread (thread creation
+// costs more than most of the host work it would carry). One job at a time; a call from inside a job, from a
+// process forked after the workers started, or with a single item runs serially on the caller. The pool is never
+// destroyed: its idle workers block on a condition variable until the process exits.
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool *pool = new HostPool;
+    return *pool;
+  }
+  void run(int n, const std::function<void(int)> &f) {
+    if (n <= 1 || inside || workers.empty() || getpid() != owner) {
+      for (int i = 0; i < n; ++i) f(i);
+      return;
+    }
+    std::lock_guard<std::mutex> one(submit);
+    {
+      std::lock_guard<std::mutex> lk(m);
+      job = &f;
+      count = n;
+      next.store(0);
+      busy = (int)workers.size();
+      ++gen;
+    }
+    cv.notify_all();
+    inside = true;
+    for (int i; (i = next.fetch_add(1)) < n;) f(i);
+    inside = false;
+    std::unique_lock<std::mutex> lk(m);
+    done.wait(lk, [&] { return busy == 0; });
+    job = nullptr;
+  }
+ private:
+  HostPool() : owner(getpid()) {
+    const int nt = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+    for (int t = 1; t < nt; ++t) workers.emplace_back([this] { loop(); });
+  }
+  void loop() {
+    unsigned long long seen = 0;
+    for (;;) {
+      const std::function<void(int)> *f;
+      int n;
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return gen != seen; });
+        seen = gen;
+        f = job;
+        n = count;
+      }
+      inside = true;
+      for (int i; (i = next.fetch_add(1)) < n;) (*f)(i);
+      inside = false;
+      std::lock_guard<std::mutex> lk(m);
+      if (--busy == 0) done.notify_one();
+    }
+  }
+  std::mutex submit, m;
+  std::condition_variable cv, done;
+  const std::function<void(int)> *job = nullptr;
+  int count = 0, busy = 0;
+  std::atomic<int> next{0};
+  unsigned long long gen = 0;
+  pid_t owner;
+  std::vector<std::thread> workers;
+  static thread_local bool inside;
+};
+thread_local bool HostPool::inside = false;
+
+// Runs f(0..n-1) on the host workers (independent items; f must not throw).
 template <class F>
 void parallel_for(int n, F f) {
-  int nt = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
-  nt = std::min(nt, n);
-  if (nt <= 1) {
-    for (int i = 0; i < n; ++i) f(i);
-    return;
-  }
-  std::atomic<int> next{0};
-  std::vector<std::thread> th;
-  for (int t = 0; t < nt; ++t)
-    th.emplace_back([&] {
-      for (int i; (i = next.fetch_add(1)) < n;) f(i);
-    });
-  for (auto &x : th) x.join();
+  const std::function<void(int)> g = [&](int i) { f(i); };
+  HostPool::get().run(n, g);
 }
 
 // eliminateEquivalentAngles (inc/em/nbfProjectionRotationMetric3D.h:1636-1702). Only pairs whose rotation
