@@ -388,6 +388,9 @@ struct ettk_ctx {
   ettk_params p{};
   // launch shapes chosen by ettk_gpu_autotune or ettk_gpu_set_tuning; none of them changes a result
   ettk_tuning tune{64, 4096, 1, 128};
+  // trilinear reslices in the CCF evaluations (set on the fast form's half-grid screening context only, with
+  // fast_coarse_so3 = 2; never on the reference path)
+  bool linear_reslice = false;
   cudaStream_t st = nullptr;
   int N = 0, H = 0, B = 0, n = 0;
   long n3 = 0, h3 = 0, nn = 0, nso3 = 0;
@@ -596,11 +599,14 @@ struct ettk_ctx {
   // Tricubic reslice of n_items items (device array `items_dev`, optionally through item_index) into
   // out[item][a][b][c], with the valid-value sums into acc (k_reslice_brick, one 8^3 brick per CTA)
   void reslice(const ResliceItem *items_dev, float *out, double *acc_, int acc_stride, const int *item_index,
-               long n_items, bool clamp_all = false) {
+               long n_items, bool clamp_all = false, bool linear = false) {
     if (n_items <= 0) return;
     const dim3 grid((N / RB) * (N / RB) * (N / RB), (unsigned)n_items);
     if (clamp_all)
       k_reslice_brick<false, true><<<grid, 256, RS_SMEM, st>>>(items_dev, N, out, acc_, acc_stride, status.p, item_index);
+    else if (linear)
+      k_reslice_brick<false, false, true><<<grid, 256, RS_SMEM, st>>>(items_dev, N, out, acc_, acc_stride, status.p,
+                                                                      item_index);
     else
       k_reslice_brick<false><<<grid, 256, RS_SMEM, st>>>(items_dev, N, out, acc_, acc_stride, status.p, item_index);
     post_launch();
@@ -1731,6 +1737,9 @@ void ettk_ctx::init_tables() {
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
   CK(cudaFuncSetAttribute(k_reslice_brick<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CK(cudaFuncSetAttribute(k_reslice_brick<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_reslice_brick<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)RS_SMEM));
+  CK(cudaFuncSetAttribute(k_reslice_brick<false, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CK(cudaFuncSetAttribute(k_reslice_brick<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CK(cudaFuncSetAttribute(k_reslice_brick<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   N = p.N;
@@ -2135,7 +2144,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   }
   {
     Scope sc(this, "reslice", 8.0 * direct.size() * n3);
-    reslice(w_items.p, w_v.p, acc2, ACC, w_ridx.p, (long)direct.size());
+    reslice(w_items.p, w_v.p, acc2, ACC, w_ridx.p, (long)direct.size(), false, linear_reslice);
   }
   if (!mirrors.empty()) {
     Scope sc(this, "reslice_mirror", 8.0 * mirrors.size() * n3);
@@ -2826,6 +2835,7 @@ void ettk_ctx::half_setup() {
     const int rc = ettk_gpu_create(device, &hp, &h);
     if (rc != ETTK_OK) throw CudaError(rc, "half-grid screening context could not be created");
     half = h;
+    half->linear_reslice = p.fast_coarse_so3 >= 2;
     half_refs_ok = false;
   }
   if (!half_refs_ok) {
@@ -3376,7 +3386,7 @@ int ettk_gpu_create(int device, const ettk_params *params, ettk_ctx **out) {
   const ettk_params &p = *params;
   if (!pow2(p.N) || p.N < 16 || p.N > 128 || !(p.B == 8 || p.B == 16 || p.B == 32 || p.B == 64) ||
       p.candidate_peaks < 1 || p.number_of_candidates < 1 || p.wigner_precision < 0 ||
-      p.wigner_precision > WIG_FP64)
+      p.wigner_precision > WIG_FP64 || p.fast_coarse_so3 < 0 || p.fast_coarse_so3 > 2)
     return ETTK_ERR_ARG;
   ettk_ctx *c = new (std::nothrow) ettk_ctx;
   if (!c) return ETTK_ERR_OOM;

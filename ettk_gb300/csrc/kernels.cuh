@@ -76,7 +76,7 @@ struct ResliceTap {
 // Voxel (a, b, cz) of the output. PRECISE: the voxel coordinate follows the reference's FP64 sequence
 // ((origin + c*z) + b*y) + a*x without FMA contraction and is rounded to the 2^-16 grid in FP64 (used where 1e-5
 // output parity matters); otherwise the same sequence runs in FP32. CLAMP_ALL: every position is inside.
-template <bool PRECISE, bool CLAMP_ALL>
+template <bool PRECISE, bool CLAMP_ALL, bool LINEAR = false>
 ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, int b, int cz, ResliceTap &t) {
   float fx, fy, fz;
   if (PRECISE) {
@@ -109,6 +109,16 @@ ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, 
     t.iy = vtk_floor(p1, fy);
     t.iz = vtk_floor(p2, fz);
   }
+  if (LINEAR) {  // trilinear weights on the middle two taps of each axis
+    t.wx[0] = t.wx[3] = t.wy[0] = t.wy[3] = t.wz[0] = t.wz[3] = 0.f;
+    t.wx[1] = 1.f - fx;
+    t.wx[2] = fx;
+    t.wy[1] = 1.f - fy;
+    t.wy[2] = fy;
+    t.wz[1] = 1.f - fz;
+    t.wz[2] = fz;
+    return;
+  }
   cubic_weights(t.wx, fx);
   cubic_weights(t.wy, fy);
   cubic_weights(t.wz, fz);
@@ -116,6 +126,33 @@ ETTK_DEV void reslice_tap(const ResliceItem &it, int dx, int dy, int dz, int a, 
   // (0, 1, 0, 0) weights it forces there adds exact zeros, so the result is unchanged.
   if (!((dy > 1) && (fy != 0.f))) { t.wy[0] = 0.f; t.wy[1] = 1.f; t.wy[2] = 0.f; t.wy[3] = 0.f; }
   if (!((dz > 1) && (fz != 0.f))) { t.wz[0] = 0.f; t.wz[1] = 1.f; t.wz[2] = 0.f; t.wz[3] = 0.f; }
+}
+
+// Trilinear sums (taps 1 and 2 of each axis, as reslice_tap<..., true> weights them) from the staged box at
+// unclamped positions and at clamped positions.
+ETTK_DEV float tap_sum_box_lin(const float *b0, int P, int PE, const ResliceTap &t) {
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 1; k < 3; ++k)
+#pragma unroll
+    for (int j = 1; j < 3; ++j) {
+      const float *r = b0 + k * PE + j * P;
+      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), __fmaf_rn(t.wx[2], r[2], __fmul_rn(t.wx[1], r[1])), acc);
+    }
+  return acc;
+}
+ETTK_DEV float tap_sum_clamped_lin(const float *box, int x0, int o1, int o2, int P, int PE, int dx, int dy, int dz,
+                                   const ResliceTap &t) {
+  float acc = 0.f;
+  const int xa = min(max(t.ix, 0), dx - 1) - x0, xb = min(max(t.ix + 1, 0), dx - 1) - x0;
+#pragma unroll
+  for (int k = 1; k < 3; ++k)
+#pragma unroll
+    for (int j = 1; j < 3; ++j) {
+      const float *r = box + (min(max(t.iz - 1 + k, 0), dz - 1) - o2) * PE + (min(max(t.iy - 1 + j, 0), dy - 1) - o1) * P;
+      acc = __fmaf_rn(__fmul_rn(t.wz[k], t.wy[j]), __fmaf_rn(t.wx[2], r[xb], __fmul_rn(t.wx[1], r[xa])), acc);
+    }
+  return acc;
 }
 
 // The tricubic sum of every path below, in one fixed order: per row (z plane k, y row j)
@@ -190,8 +227,9 @@ static __device__ __noinline__ float tricubic_global(const float *__restrict__ v
 }
 
 // PRECISE: FP64 voxel coordinates (reslice_tap). CLAMP_ALL: every voxel takes the clamped tricubic value (no -max
-// background), for the continuous refinement.
-template <bool PRECISE, bool CLAMP_ALL = false>
+// background), for the continuous refinement. LINEAR: trilinear instead of tricubic interpolation (8 taps), for the
+// candidate screening of the fast form (no reference counterpart: the reference always resamples tricubically).
+template <bool PRECISE, bool CLAMP_ALL = false, bool LINEAR = false>
 __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_reslice_brick(const ResliceItem *__restrict__ items, int N,
                                                           float *__restrict__ out, double *acc, int acc_stride,
                                                           int *status, const int *__restrict__ item_index) {
@@ -328,6 +366,12 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
       return tricubic_global(vol, dx, dy, dz, t.ix, t.iy, t.iz, t.wx[0], t.wx[1], t.wx[2], t.wx[3], t.wy[0], t.wy[1],
                              t.wy[2], t.wy[3], t.wz[0], t.wz[1], t.wz[2], t.wz[3]);
     const int off = ((t.iz - 1 - o2) * E1 + (t.iy - 1 - o1)) * P + (t.ix - 1 - x0);
+    if (LINEAR) {
+      if (!use_tma) return tap_sum_box_lin(box + off, P, PE, t);
+      if ((unsigned)t.ix <= (unsigned)(dx - 2) && (unsigned)t.iy <= (unsigned)(dy - 2) && (unsigned)t.iz <= (unsigned)(dz - 2))
+        return tap_sum_box_lin(box + off, RT_X, RT_X * RT_Y, t);
+      return tap_sum_clamped_lin(box, x0, o1, o2, P, PE, dx, dy, dz, t);
+    }
     if (!use_tma) return tap_sum_box(box + off, P, PE, t);
     if ((unsigned)(t.ix - 1) <= (unsigned)(dx - 4) && (unsigned)(t.iy - 1) <= (unsigned)(dy - 4) &&
         (unsigned)(t.iz - 1) <= (unsigned)(dz - 4))
@@ -340,7 +384,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
     const int w = v >> 5, ln = v & 31;
     const int la = 4 * (w >> 3) + (ln >> 3), lb = 4 * ((w >> 2) & 1) + ((ln >> 1) & 3), lc = 2 * (w & 3) + (ln & 1);
     ResliceTap t;
-    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, bx * RB + la, by * RB + lb, bz * RB + lc, t);
+    reslice_tap<PRECISE, CLAMP_ALL, LINEAR>(it, dx, dy, dz, bx * RB + la, by * RB + lb, bz * RB + lc, t);
     const float val = value(t);
     if (t.inside) {
       s += val;
@@ -359,7 +403,7 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
     if (fa < RB && fb < RB && fc < RB) continue;
     ResliceTap t;
     const int a = bx * RB + fa, b = by * RB + fb, cz = bz * RB + fc;
-    reslice_tap<PRECISE, CLAMP_ALL>(it, dx, dy, dz, a, b, cz, t);
+    reslice_tap<PRECISE, CLAMP_ALL, LINEAR>(it, dx, dy, dz, a, b, cz, t);
     it.faces[face_index(a, b, cz, N)] = value(t);
   }
   if (acc) {

@@ -58,7 +58,8 @@ typedef struct {
                                    2 split-BF16 tensor cores, 3 TF32 tensor cores, 4 FP64 (precision reference) */
   int fast_coarse_so3;          /* fast form only (ettk_gpu_align_pairs_refined; no reference setting): 1 runs its
                                    SO(3) search on the volumes Fourier-cropped to half the edge at bandwidth B/2, the
-                                   grid the candidate screening already uses; 0 searches at the full edge and B */
+                                   grid the candidate screening already uses; 2 also resamples the screened candidates
+                                   trilinearly instead of tricubically; 0 searches at the full edge and B */
 } ettk_params;
 
 /* Launch shapes of the library's kernels (no reference setting). None of them changes a result; they trade
