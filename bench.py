@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "align64_b32"
 FAST_PRECISION = 2   # split-BF16 Wigner-d contraction on the tensor cores
 FAST_ITERATIONS = 9  # local refinement steps of the fast form
-FAST_COARSE = 1  # the fast form's SO(3) search on the half grid at B/2 (0: at the full edge and B)
+FAST_COARSE = 2  # the fast form's SO(3) search on the half grid at B/2, trilinear screening (1: tricubic; 0: full grid)
 METRIC = "alignments/s at 64^3 bw=32: plain GPU vs batched+adjoint form at <=0.5deg/0.1 vox"
 
 
@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--fast-peaks", type=int, default=0, help="0: the metric's candidate_peaks")
     ap.add_argument("--fast-precision", type=int, default=2, help="Wigner-d contraction of the fast form")
     ap.add_argument("--fast-coarse", type=int, default=FAST_COARSE,
-                    help="1: the fast form's SO(3) search on the half grid at B/2")
+                    help="the fast form's SO(3) search: 0 full grid, 1 half grid at B/2, 2 also trilinear screening")
     ap.add_argument("--fast-only", action="store_true",
                     help="--fast-study without the plain form (the fast form run twice on all pairs, the second timed)")
     ap.add_argument("--tune-study", action="store_true",
@@ -689,9 +689,10 @@ def main():
                     "h2d_bytes_per_step": P * N ** 3 * 4, "d2h_bytes_per_step": P * 17 * 4},
             "gpu_launches": fast_launches,
             "method": "SO(3) grid on the %s with split-BF16 tcgen05 Wigner contraction, CCF of the candidatePeaks + "
-                      "1 best candidates on half-grid Fourier crops, %d steps of local 6-DOF refinement by the "
-                      "analytic gradient of the masked normalised correlation"
-                      % ("half grid at B/2" if FAST_COARSE else "full grid", FAST_ITERATIONS),
+                      "1 best candidates on half-grid Fourier crops (%s resampling), %d steps of local 6-DOF "
+                      "refinement by the analytic gradient of the masked normalised correlation"
+                      % ("half grid at B/2" if FAST_COARSE else "full grid",
+                         "trilinear" if FAST_COARSE >= 2 else "tricubic", FAST_ITERATIONS),
             "errors": {"plain": error_summary(rp, sp, hit), "fast": dict(error_summary(rf, sf, hit),
                                                                          basin_hits_fast=int((rf < 20.0).sum())),
                        "note": "against the generating poses; medians and means over the pairs whose plain grid hit "

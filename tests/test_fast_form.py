@@ -107,9 +107,10 @@ def ds64():
     return synthetic.generate("align64_b32", n_particles=24)
 
 
-@pytest.mark.parametrize("coarse", [0, 1])
+@pytest.mark.parametrize("coarse", [0, 1, 2])
 def test_fast_form_against_plain_form(ds64, coarse):
-    """The fast form (coarse = 1: its SO(3) search on the half grid at B/2, split-BF16 Wigner contraction) against
+    """The fast form (coarse = 1: its SO(3) search on the half grid at B/2, split-BF16 Wigner contraction; 2: the
+    screened candidates also resampled trilinearly) against
     the plain form on the same pairs: refined rows score at least their coarse start, and the median errors against
     the generating poses are no worse than the plain grid's over the pairs the grid puts in the right basin."""
     n = 24
