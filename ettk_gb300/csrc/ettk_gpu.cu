@@ -869,6 +869,7 @@ struct ettk_ctx {
   // ---------------------------------------------------------------- fast form: coarse SO(3) hit + local refinement
   DevBuf<LRItem> lr_items;
   DevBuf<LRState> lr_state;
+  bool lr_skip_done = false;  // inside lr_run: converged pairs are not evaluated again
   DevBuf<float> lr_zm, lr_maps, lr_ip;
   DevBuf<int> lr_src;
   std::vector<int> lr_slot;  // particle -> slot of its band-passed copy in lr_ip (-1: none)
@@ -890,7 +891,8 @@ struct ettk_ctx {
     Scope sc(this, "local_refine", 4.0 * E * (double)lr_nin * 3);
     const unsigned chunks = (unsigned)std::max<long>(1, (lr_nin + LR_CHUNK - 1) / LR_CHUNK);
     k_lr_eval<NN><<<dim3(chunks, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, mask.p, lr_in.p,
-                                                            (int)lr_nin, lr_acc.p);
+                                                            (int)lr_nin, lr_skip_done ? lr_state.p : nullptr,
+                                                            lr_acc.p);
     post_launch();
   }
   void lr_eval(long E) { with_n(N, [&](auto nn) { lr_eval_t<decltype(nn)::value>(E); }); }
@@ -2944,6 +2946,11 @@ void ettk_ctx::lr_filter_particles(const std::vector<int> &parts, bool with_half
 }
 
 void ettk_ctx::lr_run(long P, int iterations) {
+  struct Skip {
+    bool &f;
+    Skip(bool &f_) : f(f_) { f = true; }
+    ~Skip() { f = false; }
+  } skip(lr_skip_done);
   for (int it = 0; it <= iterations; ++it) {
     CK(cudaMemsetAsync(lr_acc.p, 0, P * LR_NACC * sizeof(double), st));
     lr_eval(P);

@@ -49,10 +49,12 @@ constexpr int LR_CHUNK = 8192;  // in-mask voxels per CTA of k_lr_eval
 template <int N>
 __global__ void __launch_bounds__(256) k_lr_eval(const LRItem *__restrict__ items, const float *__restrict__ maps,
                                                  const float *__restrict__ zm, const float *__restrict__ mask,
-                                                 const int *__restrict__ in, int nin, double *__restrict__ acc) {
+                                                 const int *__restrict__ in, int nin, const LRState *__restrict__ state,
+                                                 double *__restrict__ acc) {
   constexpr long n3 = (long)N * N * N;
   __shared__ float red[8][LR_NACC];
   const int e = blockIdx.y;
+  if (state && state[e].done) return;  // a converged pair's sums are not read again
   const LRItem it = items[e];
   float M[12];
 #pragma unroll
