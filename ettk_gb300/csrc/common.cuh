@@ -58,6 +58,54 @@ ETTK_DEV double block_sum(double v, double *sh) {
   return r;
 }
 
+// Block-wide sums without FP64 arithmetic in the tree (on GB300 a warp-wide FP64 add occupies the SM's FP64 pipe
+// for about as long as dozens of FP32 instructions, which made the FP64 tree the largest cost of short CTAs).
+// FP32 values: each partial sum is carried as an unevaluated pair hi + lo, every addition split exactly into sum
+// and rounding error (Knuth's TwoSum, rounded intrinsics so that no FMA contraction disturbs it), about 48
+// significant bits; thread 0 gets hi + lo as a double. Agrees with an FP64 tree except in the last bits of the
+// double. `sh` needs blockDim/32 float2.
+ETTK_DEV float2 ff_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  const float h = __fadd_rn(s, e);
+  return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+ETTK_DEV float2 warp_sum_ff(float2 v) {
+  for (int o = 16; o > 0; o >>= 1)
+    v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+  return v;
+}
+ETTK_DEV double block_sum_f(float v, float2 *sh) {
+  float2 p = warp_sum_ff(make_float2(v, 0.f));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = p;
+  __syncthreads();
+  double r = 0;
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    p = warp_sum_ff(lane < nw ? sh[lane] : make_float2(0.f, 0.f));
+    if (lane == 0) r = (double)p.x + (double)p.y;
+  }
+  __syncthreads();
+  return r;
+}
+// Integer counts: exact. `sh` needs blockDim/32 ints.
+ETTK_DEV int block_sum_i(int v, int *sh) {
+  v = __reduce_add_sync(0xffffffffu, v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  int r = 0;
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    r = __reduce_add_sync(0xffffffffu, lane < nw ? sh[lane] : 0);
+  }
+  __syncthreads();
+  return r;
+}
+
 ETTK_DEV unsigned long long warp_max_u64(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);

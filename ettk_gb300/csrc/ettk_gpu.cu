@@ -642,6 +642,44 @@ struct ettk_ctx {
     }
   }
 
+  // x and y stages of the window in one pass per (kz plane, item) (k_pruned_xy), when the plane's W window rows fit
+  // in shared memory with three CTAs per SM; otherwise the two stages above through the [item][X][kz][ky]
+  // intermediate
+  template <int NN>
+  static size_t pruned_xy_smem(int W) {
+    return (size_t)W * (NN / 2 + 8) * sizeof(float2);
+  }
+  template <int NN>
+  static bool pruned_xy_fits(int W) {
+    return pruned_xy_smem<NN>(W) + (NN + pruned_xy_ex<NN, reg_lines<NN>()>()) * sizeof(float2) <= 75 * 1024;
+  }
+  bool pruned_xy_used() const {
+    switch (2 * N) {
+      case 32: return pruned_xy_fits<32>(W);
+      case 64: return pruned_xy_fits<64>(W);
+      case 128: return pruned_xy_fits<128>(W);
+      case 256: return pruned_xy_fits<256>(W);
+      default: return false;
+    }
+  }
+  template <int NN>
+  void pruned_xy_t(const float2 *in, float2 *out, long E, int off) {
+    constexpr int L = reg_lines<NN>();
+    const size_t dyn = pruned_xy_smem<NN>(W);
+    if (dyn > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_xy<NN, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    k_pruned_xy<NN, L><<<dim3(NN / 4 + 1, (unsigned)E), L * MaxAB<NN>::v, dyn, st>>>(in, out, W, lo, off);
+    post_launch();
+  }
+  void pruned_xy(const float2 *in, float2 *out, long E, int off) {
+    switch (2 * N) {
+      case 32: pruned_xy_t<32>(in, out, E, off); break;
+      case 64: pruned_xy_t<64>(in, out, E, off); break;
+      case 128: pruned_xy_t<128>(in, out, E, off); break;
+      case 256: pruned_xy_t<256>(in, out, E, off); break;
+      default: throw CudaError(ETTK_ERR_ARG, "unsupported volume size");
+    }
+  }
+
   // ---------------------------------------------------------------- FFT drivers
   // CTA shape of the register FFT kernels: 256 threads = LINES x max(A, B)
   template <int NN>
@@ -2017,7 +2055,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   w_norm2.ensure(E);
   w_peak.ensure(E);
   w_out.ensure(E);
-  w_p1.ensure(E * W * N * H);
+  if (!pruned_xy_used()) w_p1.ensure(E * W * N * H);
   w_p2.ensure(E * W * W * H);
   // Reference branch sharing: the wedge * filter, F1, y1 and FFT1re of an evaluation depend only on its
   // reference and its wedge planes; the binary wedge tests the product of two plane distances, so planes
@@ -2178,12 +2216,16 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   int o0 = N - (int)floor(N / 2.0), o2 = H - 1;
   {
   Scope sc_p(this, "pruned_dft", 8.0 * E * ((double)N * N * H + 2.0 * W * N * H + 2.0 * W * W * H));
-  // x: lines (item, kz, ky) of the kz-major spectrum, stride N, into q1[item][X][kz][ky];
-  // y: lines (item, X, kz), contiguous, into q2[item][X][kz][Y]
-  pruned_fft<false>(w_cB.p, w_p1.p,
-                    PrunedLines{E * H * N, (long)H * N, (long)H * N * N, (long)N, (long)N * N, (long)N,
-                                (long)W * H * N, (long)H * N}, o0);
-  pruned_fft<true>(w_p1.p, w_p2.p, PrunedLines{E * W * H, 1, (long)N, 1, 0, 1, (long)W, 1}, o0);
+  if (pruned_xy_used()) {
+    pruned_xy(w_cB.p, w_p2.p, E, o0);
+  } else {
+    // x: lines (item, kz, ky) of the kz-major spectrum, stride N, into q1[item][X][kz][ky];
+    // y: lines (item, X, kz), contiguous, into q2[item][X][kz][Y]
+    pruned_fft<false>(w_cB.p, w_p1.p,
+                      PrunedLines{E * H * N, (long)H * N, (long)H * N * N, (long)N, (long)N * N, (long)N,
+                                  (long)W * H * N, (long)H * N}, o0);
+    pruned_fft<true>(w_p1.p, w_p2.p, PrunedLines{E * W * H, 1, (long)N, 1, 0, 1, (long)W, 1}, o0);
+  }
   size_t smz = 2 * (size_t)H * (4 * ((W + 3) / 4)) * sizeof(float2);
   if (smz > 48 * 1024) CK(cudaFuncSetAttribute(k_pruned_z_peak, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
   k_pruned_z_peak<<<dim3(W, E), 128, smz, st>>>(w_p2.p, N, W, lo, o2, rr2, w_peak.p);

@@ -238,7 +238,8 @@ __global__ void __launch_bounds__(256, 2) k_fft2d_padded(const float2 *__restric
 }
 
 // Sums of |v|^2 of a normalizeFourierHalf (inc/em/nbfCorrelationImageMetric.h:497-530): kz < H-1 into
-// acc[e][slot], the kz = H-1 plane into acc[e][slot+1]; per-thread FP32 partials, FP64 across threads.
+// acc[e][slot], the kz = H-1 plane into acc[e][slot+1]; per-thread FP32 partials, a float-pair tree across
+// threads (block_sum_f).
 template <int N>
 struct HalfSums {
   double *acc;
@@ -246,8 +247,8 @@ struct HalfSums {
   float s = 0.f;
   ETTK_DEV void add(float2 v) { s += v.x * v.x + v.y * v.y; }
   ETTK_DEV void flush(int e, int kz) {
-    __shared__ double shm[32];
-    const double b = block_sum((double)s, shm);
+    __shared__ float2 shm[32];
+    const double b = block_sum_f(s, shm);
     if (threadIdx.x == 0) atomicAdd(&acc[(long)e * acc_stride + slot + (kz == KXY<N>::H - 1 ? 1 : 0)], b);
   }
 };

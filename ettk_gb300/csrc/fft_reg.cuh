@@ -688,4 +688,87 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
   }
 }
 
+// The x and y axes of the same windowed transform in one pass per (kz plane, item), for the kz-major spectrum
+// [item][kz][kx][ky] (n = N/2 = NN/2, H = n/2 + 1): the plane's n x lines (stride n) are read from global memory
+// LINES at a time and their W window outputs kept in shared memory, T[X][ky] (row pitch n + 8 complex: the x
+// stores and y loads of a warp touch distinct banks); then the W y lines of T are transformed and written to
+// q2[item][X][kz][Y]. Each line takes the zero-padded NN-point inverse and the output twiddle of k_pruned_fft, in
+// the same order, so q2 equals that of the two separate passes; the intermediate [item][X][kz][ky] array (and its
+// round trip through HBM) is gone. Dynamic shared memory: W * (n + 8) complex.
+template <int NN, int LINES>
+__host__ __device__ constexpr int pruned_xy_ex() {
+  return ex_size<NN, LINES, false>() > ex_size<NN, LINES, true>() ? ex_size<NN, LINES, false>()
+                                                                  : ex_size<NN, LINES, true>();
+}
+template <int NN, int LINES>
+__global__ void __launch_bounds__(LINES * MaxAB<NN>::v, NN >= 256 ? 2 : 4)
+    k_pruned_xy(const float2 *__restrict__ in, float2 *__restrict__ q2, int W, int lo, int off) {
+  constexpr int A = Split<NN>::A, B = Split<NN>::B, n = NN / 2, H = n / 2 + 1, TP = n + 8;
+  __shared__ float2 tw[NN];
+  __shared__ float2 ex[pruned_xy_ex<NN, LINES>()];
+  extern __shared__ float4 pxy_dyn[];
+  float2 *T = reinterpret_cast<float2 *>(pxy_dyn);
+  load_full_twiddles<NN>(tw);
+  const int kz = blockIdx.x;
+  const long item = blockIdx.y;
+  float2 v[A], o[B];
+  {
+    // x: line ky of the plane, elements kx at stride n; adjacent threads are adjacent lines (coalesced rows)
+    int line, lane;
+    thread_map<NN, LINES, false>(line, lane);
+    const float2 *plane = in + (item * H + kz) * (long)n * n;
+#pragma unroll 1
+    for (int ky0 = 0; ky0 < n; ky0 += LINES) {
+      const int ky = ky0 + line;
+      const bool ok = ky < n;
+      if (lane < B) {
+#pragma unroll
+        for (int j1 = 0; j1 < A; ++j1) {
+          const int kx = B * j1 + lane;
+          v[j1] = (ok && kx < n) ? plane[(long)kx * n + ky] : make_float2(0.f, 0.f);
+        }
+      }
+      __syncthreads();  // twiddles loaded; the previous round's exchange reads done
+      four_step<NN, LINES, false>(v, o, line, lane, +1, tw, ex);
+      if (lane < A && ok) {
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) {
+          const int m = lane + A * k2;
+          const int X = (m - lo) & (NN - 1);
+          if (X < W) T[X * TP + ky] = cmul(o[k2], twid<NN>(tw, off * m, +1));
+        }
+      }
+    }
+  }
+  __syncthreads();
+  {
+    // y: line X of T (contiguous), adjacent threads are adjacent elements of a line
+    int line, lane;
+    thread_map<NN, LINES, true>(line, lane);
+#pragma unroll 1
+    for (int X0 = 0; X0 < W; X0 += LINES) {
+      const int X = X0 + line;
+      const bool ok = X < W;
+      if (lane < B) {
+#pragma unroll
+        for (int j1 = 0; j1 < A; ++j1) {
+          const int ky = B * j1 + lane;
+          v[j1] = (ok && ky < n) ? T[X * TP + ky] : make_float2(0.f, 0.f);
+        }
+      }
+      __syncthreads();
+      four_step<NN, LINES, true>(v, o, line, lane, +1, tw, ex);
+      if (lane < A && ok) {
+        float2 *dst = q2 + ((item * W + X) * H + kz) * (long)W;
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) {
+          const int m = lane + A * k2;
+          const int Y = (m - lo) & (NN - 1);
+          if (Y < W) dst[Y] = cmul(o[k2], twid<NN>(tw, off * m, +1));
+        }
+      }
+    }
+  }
+}
+
 }  // namespace ettk

@@ -407,10 +407,11 @@ __global__ void __launch_bounds__(256, PRECISE ? 3 : ETTK_RESLICE_MIN_BLOCKS) k_
     it.faces[face_index(a, b, cz, N)] = value(t);
   }
   if (acc) {
-    double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
+    const double bs = block_sum_f(s, reinterpret_cast<float2 *>(sh));
+    const int bc = block_sum_i(cnt, reinterpret_cast<int *>(sh));
     if (threadIdx.x == 0) {
       atomicAdd(&acc[(long)eidx * acc_stride + 0], bs);
-      atomicAdd(&acc[(long)eidx * acc_stride + 1], bc);
+      atomicAdd(&acc[(long)eidx * acc_stride + 1], (double)bc);
     }
   }
 }
@@ -466,10 +467,11 @@ static __global__ void __launch_bounds__(256) k_reslice_mirror(const ResliceItem
     }
     reinterpret_cast<float4 *>(dst)[qd] = make_float4(v[0], v[1], v[2], v[3]);
   }
-  const double bs = block_sum((double)s, sh), bc = block_sum((double)cnt, sh);
+  const double bs = block_sum_f(s, reinterpret_cast<float2 *>(sh));
+  const int bc = block_sum_i(cnt, reinterpret_cast<int *>(sh));
   if (threadIdx.x == 0) {
     atomicAdd(&acc[(long)em * acc_stride + 0], bs);
-    atomicAdd(&acc[(long)em * acc_stride + 1], bc);
+    atomicAdd(&acc[(long)em * acc_stride + 1], (double)bc);
   }
 }
 
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(256, 3) k_wedge_roll(const WedgeVecs *__restri
     if (p - 1 >= i0) emit(p - 1);
   }
   if (pend == N - 1 && N - 1 < i0 + SLAB) emit(N - 1);
-  const double b = block_sum((double)s, sh);
+  const double b = block_sum_f(s, reinterpret_cast<float2 *>(sh));
   if (threadIdx.x == 0) atomicAdd(&acc[(long)e * acc_stride + acc_slot], b);
 }
 template <int N>
