@@ -607,6 +607,8 @@ def main():
     launches = m.kernel_launches() - launches0
     prof = m.profile_read()
     m.profile(False)
+    for _ in range(a.warmup):  # the host-buffer path's own first use (its device buffer) outside the timed steps
+        step_e2e()
     ms_e2e = timed(step_e2e, a.steps)
     D_plain = step_device()
     # the fast form on the same pairs: split-BF16 Wigner contraction, half-grid candidate screening, local refinement
@@ -628,6 +630,8 @@ def main():
     fl0 = mf.kernel_launches()
     ms_fast = timed(step_fast, a.steps, fstream)
     fast_launches = mf.kernel_launches() - fl0
+    for _ in range(a.warmup):
+        step_fast_e2e()
     ms_fast_e2e = timed(step_fast_e2e, a.steps, fstream)
     D_fast = step_fast()
     mf.close()
