@@ -68,7 +68,7 @@ SYMBOLS = [
     "ettk_gpu_symmetrize", "ettk_gpu_symmetrize_rotational", "ettk_gpu_outlier_cutoff", "ettk_gpu_soft_weights",
     "ettk_gpu_average_spherical_wedge", "ettk_gpu_set_reference_spherical_wedge",
     "ettk_gpu_representation_distances", "ettk_gpu_representations", "ettk_gpu_representations_real",
-    "ettk_gpu_mean_images", "ettk_gpu_get_tuning", "ettk_gpu_set_tuning", "ettk_gpu_autotune",
+    "ettk_gpu_mean_images", "ettk_gpu_set_reference_mask", "ettk_gpu_get_reference_mask", "ettk_gpu_get_tuning", "ettk_gpu_set_tuning", "ettk_gpu_autotune",
     "ettk_gpu_mra_assign",
     "ettk_gpu_align_pairs_refined", "ettk_gpu_refined_objective", "ettk_gpu_score_pairs",
     "ettk_gpu_average_partial", "ettk_gpu_average_finish", "ettk_gpu_wait_probe",
@@ -122,6 +122,8 @@ def load(path=None):
     L.ettk_gpu_set_reference_spherical_wedge.argtypes = [vp, ctypes.c_int, vp]
     L.ettk_gpu_representations.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, P(ctypes.c_int), vp]
     L.ettk_gpu_mean_images.argtypes = [vp, vp, ctypes.c_int, vp, vp]
+    L.ettk_gpu_set_reference_mask.argtypes = [vp, ctypes.c_int, vp, ctypes.c_float]
+    L.ettk_gpu_get_reference_mask.argtypes = [vp, vp]
     L.ettk_gpu_get_tuning.argtypes = [vp, P(Tuning)]
     L.ettk_gpu_set_tuning.argtypes = [vp, P(Tuning)]
     L.ettk_gpu_autotune.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, P(Tuning), ctypes.c_char_p, ctypes.c_int]

@@ -398,6 +398,12 @@ struct ettk_ctx {
   long long launches = 0;
   // constant tables
   DevBuf<float> mask, maskfft, filter, lw, plm, dtab, sinth;
+  // m1 of the translational CCF (nbfFourierImageMetric::referenceMask): the spherical mask, or the external mask
+  // set by ettk_gpu_set_reference_mask; [x][y][z], z fastest. `mask` stays the image filter's (spherical
+  // projection, representations).
+  DevBuf<float> refmask;
+  bool refmask_external = false;
+  void apply_reference_mask(const std::vector<float> &m1);
   DevBuf<int> doff;
   DevBuf<double> dtab64;  // FP64 Wigner-d table (wigner_precision 4 only)
   // Wigner-d synthesis of NJ correlation jobs into w_S (zeroed by the caller) in the configured precision
@@ -928,7 +934,7 @@ struct ettk_ctx {
   void lr_eval_t(long E) {
     Scope sc(this, "local_refine", 4.0 * E * (double)lr_nin * 3);
     const unsigned chunks = (unsigned)std::max<long>(1, (lr_nin + LR_CHUNK - 1) / LR_CHUNK);
-    k_lr_eval<NN><<<dim3(chunks, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, mask.p, lr_in.p,
+    k_lr_eval<NN><<<dim3(chunks, (unsigned)E), 256, 0, st>>>(lr_items.p, lr_maps.p, lr_zm.p, refmask.p, lr_in.p,
                                                             (int)lr_nin, lr_skip_done ? lr_state.p : nullptr,
                                                             lr_acc.p);
     post_launch();
@@ -1672,17 +1678,17 @@ void ettk_ctx::refine_eval(const std::vector<std::array<double, 12>> &maps, cons
   };
   const dim3 gn(nblocks<int>(n3, 256, 64), E);
   CK(cudaMemsetAsync(w_acc.p, 0, E * 2 * sizeof(double), st));
-  k_masked_mean<<<gn, 256, 0, st>>>(w_v.p, mask.p, (int)n3, w_acc.p);  // window: the spherical mask m1
+  k_masked_mean<<<gn, 256, 0, st>>>(w_v.p, refmask.p, (int)n3, w_acc.p);  // window: the CCF's mask m1
   post_launch();
-  filtered(PreMaskedParticle{w_v.p, mask.p, w_acc.p, N});
-  k_ncc_sums<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, mask.p, (int)n3, rf_acc.p);
+  filtered(PreMaskedParticle{w_v.p, refmask.p, w_acc.p, N});
+  k_ncc_sums<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, refmask.p, (int)n3, rf_acc.p);
   post_launch();
   if (grad) {
-    k_ncc_adjoint<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, mask.p, (int)n3, rf_acc.p, rf_a.p);
+    k_ncc_adjoint<<<gn, 256, 0, st>>>(rf_y1.p, rf_pair.p, w_r.p, refmask.p, (int)n3, rf_acc.p, rf_a.p);
     post_launch();
     filtered(PreCopy{rf_a.p, N});  // K a into w_r
     Scope sc(this, "refine_grad", 8.0 * E * n3);
-    k_reslice_grad<<<dim3(nblocks<int>(n3, 256, 64), E), 256, 0, st>>>(w_items.p, N, w_v.p, w_r.p, mask.p,
+    k_reslice_grad<<<dim3(nblocks<int>(n3, 256, 64), E), 256, 0, st>>>(w_items.p, N, w_v.p, w_r.p, refmask.p,
                                                                         rf_acc.p + E * 4);
     post_launch();
   }
@@ -1853,18 +1859,6 @@ void ettk_ctx::init_tables() {
   maskfft.ensure(n3);
   filter.ensure(h3);
   h2d(mask.p, m.data(), n3 * 4);
-  lr_C0 = lr_C1 = 0;
-  {
-    std::vector<int> ids;  // the voxels inside the mask, in index order: the only ones the refinement's sums see
-    for (long i = 0; i < n3; ++i) {
-      lr_C0 += (double)m[i];
-      lr_C1 += (double)m[i] * (double)m[i];
-      if (m[i] != 0.f) ids.push_back((int)i);
-    }
-    lr_nin = (long)ids.size();
-    lr_in.ensure(std::max<long>(1, lr_nin));
-    if (lr_nin) h2d(lr_in.p, ids.data(), lr_nin * sizeof(int));
-  }
   h2d(maskfft.p, mf.data(), n3 * 4);
   {
     std::vector<float> fk = to_kz_major(f.data(), N);
@@ -1969,11 +1963,29 @@ void ettk_ctx::init_tables() {
   double rs = floor((double)(p.restrict_rotation * (float)B) / 90.0 - 1.0);
   rstart = (int)std::max(1.0, std::min(rs, (double)(n - 1)));
   set_window(p.restrict_translation);
+  apply_reference_mask(m);
+}
+
+// m1 of the CCF and what depends on it: the device copy, F(m1 * shift) of the cross term, and the in-mask voxel list
+// and sums of the fast form's refinement (which correlates under the same mask)
+void ettk_ctx::apply_reference_mask(const std::vector<float> &m1) {
+  refmask.ensure(n3);
+  h2d(refmask.p, m1.data(), n3 * 4);
+  lr_C0 = lr_C1 = 0;
+  std::vector<int> ids;  // the voxels inside the mask, in index order: the only ones the refinement's sums see
+  for (long i = 0; i < n3; ++i) {
+    lr_C0 += (double)m1[i];
+    lr_C1 += (double)m1[i] * (double)m1[i];
+    if (m1[i] != 0.f) ids.push_back((int)i);
+  }
+  lr_nin = (long)ids.size();
+  lr_in.ensure(std::max<long>(1, lr_nin));
+  if (lr_nin) h2d(lr_in.p, ids.data(), lr_nin * sizeof(int));
   // F(m1*shift)
   Fm1.ensure(h3);
-  PreProductShift pre{mask.p, nullptr, N};
+  PreProductShift pre{refmask.p, nullptr, N};
   pre.src = nullptr;
-  pre.aux = mask.p;
+  pre.aux = refmask.p;
   r2c_z(N, pre, Fm1.p, (long)N * N);
   xy_kxy(N, Fm1.p, 1, -1);
   sync();
@@ -2171,7 +2183,7 @@ void ettk_ctx::eval_chunk(const std::vector<EvalReq> &req, std::vector<EvalRes> 
   });
   k_norms<<<nblocks<int>(Dn, 128), 128, 0, st>>>(acc, ACC, 2, N, (int)Dn, w_norm.p, nullptr);
   post_launch();
-  c2r_r2c_z(N, w_cA.p, MidScaleY1M1{w_norm.p, ilog2((long)N * N), mask.p, acc, ACC, 4, N}, Dn * N * N);
+  c2r_r2c_z(N, w_cA.p, MidScaleY1M1{w_norm.p, ilog2((long)N * N), refmask.p, acc, ACC, 4, N}, Dn * N * N);
   xy_kxy(N, w_cA.p, Dn, -1);
   // I2 branch: reslice under T, R2C((I2-mean) maskfft shift), forward (x, y) passes then * fw with the
   // normalisation sums
@@ -2820,7 +2832,7 @@ void ettk_ctx::lr_setup(const std::vector<EvalReq> &req) {
     fft2d_t<NN>(OpFilterInv<NN>{FI1.p, w_idx.p, w_fw.p, w_cA.p, HalfSums<NN>{w_acc.p, ACC, 2}}, P, "local_refine_setup",
                 20.0);
   });
-  c2r_z(N, w_cA.p, PostStoreZm{lr_zm.p, mask.p, N}, P * N * N);
+  c2r_z(N, w_cA.p, PostStoreZm{lr_zm.p, refmask.p, N}, P * N * N);
   k_lr_consts<<<(unsigned)P, 256, 0, st>>>(lr_zm.p, n3, lr_state.p);
   post_launch();
 }
@@ -3461,7 +3473,7 @@ int ettk_gpu_destroy(ettk_ctx *c) {
   cudaSetDevice(c->device);
   if (c->dec_ev) cudaEventDestroy(c->dec_ev);
   if (c->st) cudaStreamSynchronize(c->st);
-  DevBuf<float> *fb[] = {&c->mask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
+  DevBuf<float> *fb[] = {&c->mask, &c->refmask, &c->maskfft, &c->filter, &c->lw, &c->plm, &c->dtab, &c->sinth, &c->refvol,
                          &c->W1half, &c->Pp1, &c->W1sph, &c->partvol, &c->W2sph, &c->Pp2, &c->w_r, &c->w_v,
                          &c->w_fw, &c->w_tmp, &c->w_C, &c->w_sig, &c->w_norm,
                          &c->w_norm2, &c->sp_v, &c->sp_M, &c->sp_padc};
@@ -4081,6 +4093,70 @@ int ettk_gpu_representations(ettk_ctx *c, int M, const int *particles, int fold,
     for (int i = 0; i < M; ++i)
       if (particles[i] < 0 || particles[i] >= c->V) throw CudaError(ETTK_ERR_ARG, "particle index out of range");
     c->representations(M, particles, fold, R);
+  });
+}
+
+// nbfImageFilter::buildMaskFromFile + softenMask (inc/em/nbfImageFilter.h:319-381, 474-494) on a mask volume of
+// edge M (x fastest, as its MRC file holds it): centred into a zero N^3 box or cropped from its centre with the
+// reference's integer offsets, binarised (> threshold), softened (Gaussian std sigma, radius factor 0.75 sigma,
+// sigma = the filter's mask sigma); returned [x][y][z], z fastest (the Blitz order of the reference's arrays).
+static std::vector<float> external_mask(int N, float sigma, int M, const float *mask, float threshold) {
+  const long n3 = (long)N * N * N;
+  std::vector<float> out(n3, 0.0f);
+  auto at = [&](int x, int y, int z) { return mask[x + (long)M * (y + (long)M * z)]; };
+  if (M == N) {
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) out[((long)x * N + y) * N + z] = at(x, y, z);
+  } else if ((int)((N - M) / 2.0) > 0) {  // smaller mask: centred into the box
+    const int o = N / 2 - M / 2;
+    for (int x = 0; x < M; ++x)
+      for (int y = 0; y < M; ++y)
+        for (int z = 0; z < M; ++z) out[((long)(o + x) * N + (o + y)) * N + (o + z)] = at(x, y, z);
+  } else {  // larger mask: the centre of it
+    const int o = M / 2 - N / 2;
+    if (o < 0 || o + N > M) throw CudaError(ETTK_ERR_ARG, "mask edge does not fit the box");
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) out[((long)x * N + y) * N + z] = at(o + x, o + y, o + z);
+  }
+  for (float &v : out) v = v > threshold ? 1.0f : 0.0f;
+  if (sigma > 0) {
+    std::vector<float> t(n3);  // VTK order (x fastest) for the smoothing
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) t[x + (long)N * (y + (long)N * z)] = out[((long)x * N + y) * N + z];
+    const int dims[3] = {N, N, N};
+    gaussian_smooth(t, dims, (double)sigma, (double)sigma * .75);
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) out[((long)x * N + y) * N + z] = t[x + (long)N * (y + (long)N * z)];
+  }
+  return out;
+}
+
+int ettk_gpu_set_reference_mask(ettk_ctx *c, int M, const float *mask, float threshold) {
+  if (!c || M < 0 || M > 2048 || (M > 0 && !mask)) return fail(c, ETTK_ERR_ARG, "invalid mask arguments");
+  return guarded(c, [&] {
+    if (c->mask.p == nullptr) throw CudaError(ETTK_ERR_STATE, "context not initialised");
+    std::vector<float> m1(c->n3);
+    if (M == 0) c->d2h(m1.data(), c->mask.p, c->n3 * sizeof(float));  // back to the spherical mask
+    else m1 = external_mask(c->N, c->p.mask_sigma, M, mask, threshold);
+    c->apply_reference_mask(m1);
+    c->refmask_external = M > 0;
+  });
+}
+
+int ettk_gpu_get_reference_mask(ettk_ctx *c, float *out) {
+  if (!c || !out) return fail(c, ETTK_ERR_ARG, "invalid arguments");
+  return guarded(c, [&] {
+    if (c->refmask.p == nullptr) throw CudaError(ETTK_ERR_STATE, "context not initialised");
+    const int N = c->N;
+    std::vector<float> m1(c->n3);
+    c->d2h(m1.data(), c->refmask.p, c->n3 * sizeof(float));
+    for (int x = 0; x < N; ++x)
+      for (int y = 0; y < N; ++y)
+        for (int z = 0; z < N; ++z) out[x + (long)N * (y + (long)N * z)] = m1[((long)x * N + y) * N + z];
   });
 }
 

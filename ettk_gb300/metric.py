@@ -226,6 +226,27 @@ class ProjectionRotationMetric3D:
                     "mean_images")
         return out
 
+    def setMaskFile(self, mask, threshold):
+        """nbfImageFilter::setMaskFile as the alignment uses it: `mask` is the mask file's volume ((M, M, M) in
+        [z][y][x] order, x fastest; None restores the spherical mask), binarised at `threshold` and softened; it
+        becomes the CCF's reference mask m1."""
+        if mask is None:
+            self._check(self.L.ettk_gpu_set_reference_mask(self._ctx, 0, None, 0.0), "set_reference_mask")
+            return
+        m = np.ascontiguousarray(mask, np.float32)
+        M = m.shape[0]
+        if m.shape != (M, M, M):
+            raise ValueError("the mask must be a cube")
+        self._check(self.L.ettk_gpu_set_reference_mask(self._ctx, M, m.ctypes.data, float(threshold)),
+                    "set_reference_mask")
+
+    def reference_mask(self):
+        """The CCF's reference mask m1 in use, (N, N, N) in [z][y][x] order."""
+        N = self.params["N"]
+        out = np.zeros((N, N, N), np.float32)
+        self._check(self.L.ettk_gpu_get_reference_mask(self._ctx, out.ctypes.data), "get_reference_mask")
+        return out
+
     def representations(self, particles, fold=1):
         """getLowDimensionRepresentationHalf of the given particles (n-fold symmetrised about z when fold > 1):
         (M, K, 3) float32 (re, im, wedge bit)."""

@@ -155,6 +155,20 @@ int ettk_gpu_symmetrize(ettk_ctx *ctx, const float *vol, int fold, float *out);
    vol and out: N^3 floats, x fastest. n 1..4096. */
 int ettk_gpu_mean_images(ettk_ctx *ctx, const float *vol, int n, const double *transforms, float *out);
 
+/* The external mask of the alignment (nbfImageFilter::setMaskFile(file, threshold), src/MPI_Classification.cpp:554-555,
+   as nbfFourierImageMetric::reinitializeHalf uses it, inc/em/nbfFourierImageMetric.h:667-676): it becomes the reference
+   mask m1 of the translational CCF (the k1_m and I1'.m1 sums and F(m1) of the cross term), and of the fast form's
+   refinement. mask: M^3 floats, x fastest, the mask file's volume; processed as nbfImageFilter::buildMaskFromFile
+   (inc/em/nbfImageFilter.h:319-381): centred into a zero N^3 box (M < N - 1) or cropped from its centre (M > N),
+   binarised (value > threshold), softened (softenMask: Gaussian, std = mask_sigma, radius factor 0.75 mask_sigma).
+   M = 0 restores the spherical mask. The spherical projection and the representations keep the spherical mask, as the
+   reference's image filter does; the fast form's half-grid screening keeps its own spherical mask. M = N - 1 fails
+   with ETTK_ERR_ARG (the reference indexes outside the mask there). */
+int ettk_gpu_set_reference_mask(ettk_ctx *ctx, int M, const float *mask, float threshold);
+
+/* The reference mask m1 in use (spherical or external): N^3 floats, x fastest. */
+int ettk_gpu_get_reference_mask(ettk_ctx *ctx, float *out);
+
 /* Low-dimensional representations of particles (nbfFourierImageMetric::getLowDimensionRepresentationHalf,
    inc/em/nbfFourierImageMetric.h:1967-2034, as nbfCorrelationImageMetric::getRepresentations collects them,
    inc/em/nbfCorrelationImageMetric.h:1323-1372; padding 1): per particle its image (own geometry, mean of

@@ -45,6 +45,8 @@ typedef struct {
   int wedge_compensation;     /* useMissingWedgeCompensation */
   int overlap_normalized;     /* overlapNormalizedDistances */
   int mutual_correlation;     /* useMutualCorrelation */
+  const float *reference_mask; /* referenceMask of the CCF when an external mask is set (oracle_file_mask's output,
+                                  N^3 [x][y][z], z fastest), or NULL for the spherical mask */
 } OracleParams;
 
 typedef struct {
@@ -184,6 +186,16 @@ void build_mask(const OracleParams &P, std::vector<float> &mask) {
         if (m > r1 && m <= r2) m = (float)((1 + cosf(kappa * (m - r1))) / 2.0);
         mask[((long)i * N + j) * N + k] = m;
       }
+}
+
+/* m1 of the CCF: nbfFourierImageMetric::reinitializeHalf's referenceMask (inc/em/nbfFourierImageMetric.h:667-676),
+ * the external mask when one is set, else the spherical mask of buildMask. */
+void build_reference_mask(const OracleParams &P, std::vector<float> &mask) {
+  if (P.reference_mask == nullptr) {
+    build_mask(P, mask);
+    return;
+  }
+  mask.assign(P.reference_mask, P.reference_mask + (long)P.N * P.N * P.N);
 }
 
 /* Gaussian-smooth a float array stored [x][y][z] (z fastest) with VTK semantics. */
@@ -524,7 +536,7 @@ struct CCF {
   int ncalls = 0;
 
   CCF(const OracleParams &p, const OracleVolume &r, const OracleVolume &q) : P(p), ref(r), part(q) {
-    build_mask(P, mask);
+    build_reference_mask(P, mask);
     build_maskfft(P, maskfft);
     build_filter(P, filter);
     for (float f : filter) sumFilter += f;
@@ -923,6 +935,42 @@ int oracle_wedge_half(const OracleParams *P, const OracleVolume *v, const double
   if (t16) memcpy(t.e, t16, sizeof(t.e));
   wedge_half(*v, P->N, t16 ? &t : nullptr, w);
   memcpy(W, w.data(), sizeof(float) * w.size());
+  return 0;
+}
+
+/* nbfImageFilter::buildMaskFromFile (inc/em/nbfImageFilter.h:319-381) on a mask volume already read from its file:
+ * M^3 floats, x fastest (the MRC reader's VTK order, x = first Blitz index). A mask of another edge is centred into
+ * a zero N^3 box (N > M + 1) or cropped from its centre (the reference's integer offsets); then binarised
+ * (> threshold) and softened (softenMask with the filter's sigma: Gaussian std sigma, radius factor 0.75 sigma).
+ * out: N^3 [x][y][z]. Returns 0, or -1 where the reference would index outside the mask (M = N - 1). */
+int oracle_file_mask(const OracleParams *P, int M, const float *mask, float threshold, float *out) {
+  const int N = P->N;
+  std::vector<float> A((long)M * M * M);
+  for (int x = 0; x < M; ++x)
+    for (int y = 0; y < M; ++y)
+      for (int z = 0; z < M; ++z) A[((long)x * M + y) * M + z] = mask[x + (long)M * (y + (long)M * z)];
+  std::vector<float> Bx((long)N * N * N, 0.0f);
+  if (M == N) {
+    Bx = A;
+  } else {
+    const int diff = (int)((N - M) / 2.0);
+    if (diff > 0) {
+      const int o = N / 2 + 1 - M / 2 - 1;
+      for (int x = 0; x < M; ++x)
+        for (int y = 0; y < M; ++y)
+          for (int z = 0; z < M; ++z) Bx[((long)(o + x) * N + (o + y)) * N + (o + z)] = A[((long)x * M + y) * M + z];
+    } else {
+      const int o = M / 2 + 1 - N / 2 - 1;
+      if (o < 0 || o + N > M) return -1;
+      for (int x = 0; x < N; ++x)
+        for (int y = 0; y < N; ++y)
+          for (int z = 0; z < N; ++z) Bx[((long)x * N + y) * N + z] = A[((long)(o + x) * M + (o + y)) * M + (o + z)];
+    }
+  }
+  for (float &v : Bx) v = v > threshold ? 1.0f : 0.0f;
+  const float s = P->mask_sigma;
+  if (s > 0) smooth_xyz(Bx, N, N, N, (double)s, (double)s * .75);
+  memcpy(out, Bx.data(), sizeof(float) * Bx.size());
   return 0;
 }
 

@@ -28,6 +28,7 @@ class OracleParams(ctypes.Structure):
         ("candidate_peaks", ctypes.c_int), ("number_of_candidates", ctypes.c_int),
         ("wedge_compensation", ctypes.c_int), ("overlap_normalized", ctypes.c_int),
         ("mutual_correlation", ctypes.c_int),
+        ("reference_mask", ctypes.POINTER(ctypes.c_float)),
     ]
 
 
@@ -79,6 +80,7 @@ def lib():
         L.oracle_spherical_wedge.argtypes = [P, V, fp]
         L.oracle_wedge_half.argtypes = [P, V, ctypes.c_void_p, fp]
         L.oracle_masks.argtypes = [P, fp, fp, fp]
+        L.oracle_file_mask.argtypes = [P, ctypes.c_int, fp, ctypes.c_float, fp]
         L.oracle_soft.argtypes = [ctypes.c_int, dp, dp, dp]
         L.oracle_soft_scaled.argtypes = [ctypes.c_int, dp, dp, dp]
         L.oracle_rotate.argtypes = [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
@@ -112,8 +114,9 @@ def lib():
 
 
 def make_params(p):
-    """OracleParams from the alignment parameter dict used across the repo."""
-    return OracleParams(
+    """OracleParams from the alignment parameter dict used across the repo. p["reference_mask"] (optional): the
+    CCF's reference mask m1 as file_mask returns it ([x][y][z], N^3)."""
+    P = OracleParams(
         N=p["N"], B=p["B"], mask_x=p["mask_radius"], mask_y=p["mask_radius"], mask_z=p["mask_radius"],
         mask_sigma=p["mask_sigma"], square_mask_size=p["square_mask_size"],
         bp_low=p["bp_low"], bp_high=p["bp_high"], bp_low_sigma=p["bp_low_sigma"],
@@ -122,6 +125,27 @@ def make_params(p):
         candidate_peaks=p["candidate_peaks"], number_of_candidates=p["number_of_candidates"],
         wedge_compensation=int(p["wedge_compensation"]), overlap_normalized=int(p["overlap_normalized"]),
         mutual_correlation=int(bool(p.get("mutual_correlation", False))))
+    rm = p.get("reference_mask")
+    if rm is not None:
+        rm = np.ascontiguousarray(rm, dtype=np.float32)
+        assert rm.size == p["N"] ** 3
+        P.reference_mask = rm.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        P._keep = rm
+    return P
+
+
+def file_mask(params, mask, threshold):
+    """nbfImageFilter::buildMaskFromFile + softenMask on a mask volume (M, M, M) in [z][y][x] order (x fastest, as
+    read from its MRC file): the N^3 reference mask in [x][y][z] order, for params["reference_mask"]."""
+    m = np.ascontiguousarray(mask, dtype=np.float32)
+    M = m.shape[0]
+    assert m.shape == (M, M, M)
+    N = params["N"]
+    out = np.zeros((N, N, N), np.float32)
+    P = make_params(params)
+    if lib().oracle_file_mask(ctypes.byref(P), M, m, float(threshold), out) != 0:
+        raise ValueError("mask edge %d cannot be centred into %d" % (M, N))
+    return out
 
 
 def make_volume(data, meta):

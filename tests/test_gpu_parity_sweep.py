@@ -200,3 +200,42 @@ def test_sweep_resume_rule(ds32):
     orc = oracle_all(params, ds32, todo)
     bad = check_rows("resume_rule", D[todo], orc)
     assert not bad, bad
+
+
+def _ellipsoid(M, a, b, c):
+    """A binary ellipsoid in a cube of edge M, [z][y][x] (x fastest, as a mask file holds it), values 0 / 1.5."""
+    z, y, x = np.mgrid[0:M, 0:M, 0:M] - M / 2.0
+    return np.where((x / a) ** 2 + (y / b) ** 2 + (z / c) ** 2 <= 1.0, 1.5, 0.0).astype(np.float32)
+
+
+@pytest.mark.parametrize("offset", [8, -8])
+def test_sweep_external_mask(ds32, offset):
+    """An external mask (nbfImageFilter::setMaskFile, used as the CCF's referenceMask by
+    nbfFourierImageMetric::reinitializeHalf, inc/em/nbfFourierImageMetric.h:667-676) of edge N + 8 (centre cropped)
+    and N - 8 (centred into the box): the library's processed mask equals the oracle's, 24 alignments match the
+    oracle's with the same mask, and clearing the mask gives the spherical-mask results again."""
+    params = dict(ds32.params)
+    N = params["N"]
+    mask = _ellipsoid(N + offset, 0.34 * (N + offset), 0.28 * (N + offset), 0.38 * (N + offset))
+    m1 = pyoracle.file_mask(params, mask, 0.5)
+    idx = list(range(24))
+    m = ProjectionRotationMetric3D(params)
+    try:
+        m.setMaskFile(mask, 0.5)
+        got = m.reference_mask().transpose(2, 1, 0)
+        err = float(np.abs(got - m1).max())
+        assert err <= 1e-6, err
+        m.set_references([vol(ds32.references[0], ds32.ref_meta[0])])
+        m.set_particles([vol(ds32.particles[i], ds32.meta[i]) for i in idx])
+        pairs = [(0, k) for k in range(len(idx))]
+        D = m.getDistances(pairs)
+        m.setMaskFile(None, 0.0)
+        D0 = m.getDistances(pairs)
+    finally:
+        m.close()
+    orc = oracle_all(dict(params, reference_mask=m1), ds32, idx)
+    bad = check_rows("external_mask_%d" % (N + offset), D, orc)
+    SUMMARY["external_mask_%d" % (N + offset)]["mask_max_abs_err"] = err
+    assert not bad, bad
+    assert np.array_equal(D0, gpu_all(params, ds32, idx))
+    assert not np.allclose(D[:, 0, 0], D0[:, 0, 0])

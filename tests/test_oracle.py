@@ -109,3 +109,40 @@ def test_ccf_restriction_zero_scores_the_pose():
     assert np.abs(t0[:3, 3] - T[:3, 3]).max() <= 0.5
     assert t6[0, 3] - T[0, 3] < -1.5
     assert d6 < d0
+
+
+def _ellipsoid(M, a, b, c):
+    """A binary ellipsoid in a cube of edge M, [z][y][x] (x fastest, as a mask file holds it), values 0 / 1.5."""
+    z, y, x = np.mgrid[0:M, 0:M, 0:M] - M / 2.0
+    return np.where((x / a) ** 2 + (y / b) ** 2 + (z / c) ** 2 <= 1.0, 1.5, 0.0).astype(np.float32)
+
+
+def test_file_mask_centring_binarising_softening():
+    """buildMaskFromFile + softenMask (inc/em/nbfImageFilter.h:319-381, 474-494) as the oracle restates them: a
+    larger mask gives the same m1 as its centred crop, a smaller one the same as its zero-padded centring, values
+    above the threshold only count (binarised), the result is softened with the mask sigma, and M = N - 1 (where the
+    reference indexes outside the mask) is refused."""
+    params = {"N": 32, "B": 16, "mask_radius": 11.0, "mask_sigma": 2.0, "square_mask_size": 2.0, "bp_low": .01,
+              "bp_high": .5, "bp_low_sigma": .01, "bp_high_sigma": .05, "restrict_translation": 6.0,
+              "restrict_rotation": 180.0, "candidate_peaks": 5, "number_of_candidates": 1,
+              "wedge_compensation": True, "overlap_normalized": True}
+    N = params["N"]
+    big = _ellipsoid(N + 8, 11.0, 9.0, 12.0)
+    m_big = pyoracle.file_mask(params, big, 0.5)
+    m_crop = pyoracle.file_mask(params, big[4:4 + N, 4:4 + N, 4:4 + N], 0.5)
+    assert np.array_equal(m_big, m_crop)
+    small = _ellipsoid(N - 8, 8.0, 7.0, 9.0)
+    padded = np.zeros((N, N, N), np.float32)
+    padded[4:4 + N - 8, 4:4 + N - 8, 4:4 + N - 8] = small
+    assert np.array_equal(pyoracle.file_mask(params, small, 0.5), pyoracle.file_mask(params, padded, 0.5))
+    # binarised: scaling the values above the threshold changes nothing; a threshold above them empties the mask
+    assert np.array_equal(pyoracle.file_mask(params, 7.0 * big, 0.5), m_big)
+    assert not pyoracle.file_mask(params, big, 2.0).any()
+    # softened: without the Gaussian the mask is the binary ellipsoid itself ([x][y][z] order)
+    hard = pyoracle.file_mask(dict(params, mask_sigma=0.0), big[4:4 + N, 4:4 + N, 4:4 + N], 0.5)
+    assert np.array_equal(hard, (big[4:4 + N, 4:4 + N, 4:4 + N] > 0.5).astype(np.float32).transpose(2, 1, 0))
+    assert m_big.min() >= 0.0 and m_big.max() <= 1.0 + 1e-6
+    assert ((m_big > 0.01) & (m_big < 0.99)).any()  # a soft edge
+    assert np.abs(m_big.sum() - hard.sum()) < 1e-3 * hard.sum()  # the smoothing keeps the mass (interior mask)
+    with pytest.raises(ValueError):
+        pyoracle.file_mask(params, _ellipsoid(N - 1, 8.0, 7.0, 9.0), 0.5)
