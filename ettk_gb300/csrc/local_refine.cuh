@@ -69,8 +69,13 @@ __global__ void __launch_bounds__(256) k_lr_eval(const LRItem *__restrict__ item
 #pragma unroll
   for (int k = 0; k < LR_NACC; ++k) s[k] = 0.f;
   const int v1 = min(nin, (int)(blockIdx.x + 1) * LR_CHUNK);
-  for (int v = blockIdx.x * LR_CHUNK + threadIdx.x; v < v1; v += blockDim.x) {
-    const int id = __ldg(in + v);
+  // the next voxel's index is loaded one iteration ahead, so that its mask, operand and particle loads do not wait
+  // behind the index load
+  int v = blockIdx.x * LR_CHUNK + threadIdx.x;
+  int id_next = v < v1 ? __ldg(in + v) : 0;
+  for (; v < v1; v += blockDim.x) {
+    const int id = id_next;
+    if (v + (int)blockDim.x < v1) id_next = __ldg(in + v + blockDim.x);
     const int a = id / (N * N), b = (id / N) % N, c = id % N;
     const float mv = __ldg(mask + id);
     const float zv = __ldg(Z + id);
