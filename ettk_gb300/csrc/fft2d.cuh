@@ -289,7 +289,7 @@ struct OpFwdFilter {
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) {
     const long g = KXY<N>::at(e, kz, i);
     if (mutual) v = mutual_scale(v);
-    v = cscale(v, fw[fw_index ? KXY<N>::at(fw_index[e], kz, i) : g]);
+    v = cscale(v, __ldg(fw + (fw_index ? KXY<N>::at(__ldg(fw_index + e), kz, i) : g)));
     if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
     sums.add(v);
     d[g] = v;
@@ -311,10 +311,10 @@ struct OpFft2reInv {
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) {
     const long g = KXY<N>::at(e, kz, i);
-    const float sc = inv_norm2[e];
+    const float sc = __ldg(inv_norm2 + e);
     const float2 bb = b[g];
     const float2 bs = cscale(bb, sc * (float)((long)N * N * N));
-    const float2 f1 = a[a_index ? KXY<N>::at(a_index[e], kz, i) : g];
+    const float2 f1 = __ldg(a + (a_index ? KXY<N>::at(__ldg(a_index + e), kz, i) : g));
     fft2re[g] = cscale(cmul(f1, cconj(bs)), 2.0f);
     return cscale(bb, sc);
   }
@@ -335,7 +335,7 @@ struct OpFwdCross {
   ETTK_DEV float2 load(int e, int kz, int i) const { return q[KXY<N>::at(e, kz, i)]; }
   ETTK_DEV void store(int e, int kz, int i, int x, int y, float2 v) {
     const long g = KXY<N>::at(e, kz, i);
-    const float2 w = cadd(cscale(cmul(fm1[KXY<N>::at(0, kz, i)], cconj(v)), -1.f), fft2re[g]);
+    const float2 w = cadd(cscale(cmul(__ldg(fm1 + KXY<N>::at(0, kz, i)), cconj(v)), -1.f), __ldg(fft2re + g));
     q[g] = cscale(w, parity_sign(x, y, kz) * factor);
   }
   ETTK_DEV void end(int, int) {}
