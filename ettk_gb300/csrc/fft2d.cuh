@@ -131,7 +131,7 @@ struct OpFilterShared {
   int sign = +1;
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) const {
-    return cscale(d[KXY<N>::at(e, kz, i)], filter[KXY<N>::at(0, kz, i)]);
+    return cscale(d[KXY<N>::at(e, kz, i)], __ldg(filter + KXY<N>::at(0, kz, i)));
   }
   ETTK_DEV void store(int e, int kz, int i, int, int, float2 v) { d[KXY<N>::at(e, kz, i)] = v; }
   ETTK_DEV void end(int, int) {}
@@ -266,7 +266,7 @@ struct OpFilterInv {
   ETTK_DEV void begin() {}
   ETTK_DEV float2 load(int e, int kz, int i) {
     const long g = KXY<N>::at(e, kz, i);
-    float2 v = cscale(src[KXY<N>::at(src_index[e], kz, i)], fw[g]);
+    float2 v = cscale(__ldg(src + KXY<N>::at(__ldg(src_index + e), kz, i)), __ldg(fw + g));
     if (kz == KXY<N>::H - 1 && i == KXY<N>::dc_xy) v = make_float2(0.f, 0.f);
     sums.add(v);
     return v;
