@@ -689,8 +689,8 @@ __global__ void __launch_bounds__(LINES * ((Split<NN>::A > Split<NN>::B) ? Split
 }
 
 // The x and y axes of the same windowed transform in one pass per (kz plane, item), for the kz-major spectrum
-// [item][kz][kx][ky] (n = N/2 = NN/2, H = n/2 + 1): the plane's n x lines (stride n) are read from global memory
-// LINES at a time and their W window outputs kept in shared memory, T[X][ky] (row pitch n + 8 complex: the x
+// [item][kz][kx][ky] (n = NN / 2 the box edge, H = n/2 + 1): the plane's n x lines (stride n) are read from global
+// memory LINES at a time and their W window outputs kept in shared memory, T[X][ky] (row pitch n + 8 complex: the x
 // stores and y loads of a warp touch distinct banks); then the W y lines of T are transformed and written to
 // q2[item][X][kz][Y]. Each line takes the zero-padded NN-point inverse and the output twiddle of k_pruned_fft, in
 // the same order, so q2 equals that of the two separate passes; the intermediate [item][X][kz][ky] array (and its
